@@ -1,0 +1,228 @@
+"""Host-side API of the crmsd engine, mirroring the Rust interface the engine
+is bound to in ``bioshell_pdb::calc``:
+
+* ``crmsd(a, b)``                      -- one pair, ``&[T: HasCartesians]`` inputs
+  (bioshell-core/src/has_cartesians.rs:6-8), like
+  ``SubstructureAxis::from_3d_points`` (bioshell-pdb/src/calc/substructures.rs:17);
+* ``crmsd_all_vs_all(models, opts)``   -- the distance matrix consumed by
+  ``hierarchical_clustering`` (bioshell-clustering/src/hierarchical/
+  hierarchical.rs:22) through ``HierarchicalClusteringMatrix::new``
+  (clustering_matrix.rs:11-22), returned as a ``CrmsdMatrix``;
+* ``CrmsdMatrix.get(i, j)`` / ``as_f32_closure()`` -- the ``Fn(usize, usize) -> f32``
+  distance closure the clustering takes.
+
+Everything computes on the GPU through the C ABI; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import weakref
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import lib as _l
+
+
+@dataclass
+class CrmsdOptions:
+    """Mirrors ``bs_opts``: precision ``"mixed"`` (tensor cores, default) or
+    ``"plain64"``; layout ``"triangle"`` (packed upper triangle) or
+    ``"square"``; element type ``"f64"`` or ``"f32"``; tolerance in Angstrom
+    (None = engine default)."""
+
+    precision: str = "mixed"
+    layout: str = "triangle"
+    out_type: str = "f64"
+    tolerance: Optional[float] = None
+
+    def to_c(self) -> _l.bs_opts:
+        o = _l.bs_opts()
+        _l.load().bs_opts_init(ctypes.byref(o))
+        o.precision = _l.PRECISION[self.precision]
+        o.layout = _l.LAYOUT[self.layout]
+        o.out_type = _l.OUT_TYPE[self.out_type]
+        o.tolerance = float(self.tolerance or 0.0)
+        return o
+
+
+def tri_index(n: int, i, j):
+    """Index of pair (i, j), i < j, in the packed row-major upper triangle."""
+    return i * n - i * (i + 1) // 2 + (j - i - 1)
+
+
+class CrmsdMatrix:
+    """All-vs-all crmsd values of n structures (packed triangle or square)."""
+
+    def __init__(self, n: int, values, layout: str = "triangle"):
+        self.n = n
+        self.values = values
+        self.layout = layout
+
+    def get(self, i: int, j: int) -> float:
+        if i == j:
+            return 0.0
+        if self.layout == "square":
+            return float(self.values[i * self.n + j])
+        if i > j:
+            i, j = j, i
+        return float(self.values[tri_index(self.n, i, j)])
+
+    def as_f32_closure(self):
+        """``Fn(usize, usize) -> f32`` for hierarchical_clustering."""
+        v = self.values
+        n = self.n
+        if self.layout == "square":
+            return lambda i, j: np.float32(v[i * n + j])
+        return lambda i, j: np.float32(0.0) if i == j else np.float32(
+            v[tri_index(n, min(i, j), max(i, j))])
+
+    def to_square(self) -> np.ndarray:
+        vals = np.asarray(self.values)
+        if self.layout == "square":
+            return vals.reshape(self.n, self.n)
+        out = np.zeros((self.n, self.n), dtype=vals.dtype)
+        iu = np.triu_indices(self.n, 1)
+        out[iu] = vals
+        out[(iu[1], iu[0])] = vals
+        return out
+
+
+def _ptr(x):
+    """(address, keepalive) of a numpy array or a CUDA tensor."""
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return x.ctypes.data, x
+    if hasattr(x, "data_ptr") and hasattr(x, "is_cuda"):
+        if not x.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return x.data_ptr(), x
+    raise TypeError(f"unsupported buffer type {type(x)!r}")
+
+
+class Engine:
+    """A context on one GPU (``bs_ctx``): owns the stream and device workspaces."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._lib = _l.load()
+        h = ctypes.c_void_p()
+        st = self._lib.bs_ctx_create(ctypes.byref(h), int(device), int(hbm_budget))
+        if st != _l.BS_OK:
+            raise _l.CrmsdError(st, "bs_ctx_create: " + self._lib.bs_status_string(st).decode())
+        self._h = h
+        self._fin = weakref.finalize(self, self._lib.bs_ctx_destroy, h)
+
+    def close(self):
+        self._fin()
+
+    def _check(self, st: int):
+        if st != _l.BS_OK:
+            raise _l.CrmsdError(st, self._lib.bs_last_error(self._h).decode())
+
+    # -- metrics -------------------------------------------------------
+    def metrics(self) -> dict:
+        m = _l.bs_metrics()
+        self._check(self._lib.bs_get_metrics(self._h, ctypes.byref(m)))
+        return m.as_dict()
+
+    # -- pinned host memory ----------------------------------------------
+    def host_empty(self, shape, dtype=np.float64) -> np.ndarray:
+        """numpy array backed by page-locked host memory."""
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        p = ctypes.c_void_p()
+        self._check(self._lib.bs_host_alloc(max(nbytes, 1), ctypes.byref(p)))
+        buf = (ctypes.c_char * max(nbytes, 1)).from_address(p.value)
+        arr = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+        weakref.finalize(buf, self._lib.bs_host_free, ctypes.c_void_p(p.value))
+        return arr
+
+    # -- crmsd -------------------------------------------------------------
+    def crmsd(self, a, b) -> float:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if a.ndim != 2 or a.shape[1] != 3 or a.shape != b.shape:
+            raise ValueError("crmsd: both inputs must be [L][3] with the same L")
+        r = ctypes.c_double()
+        self._check(self._lib.bs_crmsd(self._h, a.ctypes.data, b.ctypes.data, a.shape[0], ctypes.byref(r)))
+        return r.value
+
+    def all_vs_all(self, xyz, opts: Optional[CrmsdOptions] = None, out=None) -> CrmsdMatrix:
+        opts = opts or CrmsdOptions()
+        if isinstance(xyz, np.ndarray):
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        if len(xyz.shape) != 3 or xyz.shape[2] != 3:
+            raise ValueError("coordinates must be [n][L][3]")
+        n, L = int(xyz.shape[0]), int(xyz.shape[1])
+        count = n * (n - 1) // 2 if opts.layout == "triangle" else n * n
+        dt = np.float64 if opts.out_type == "f64" else np.float32
+        if out is None:
+            out = np.empty(count, dtype=dt)
+        xp, _k1 = _ptr(xyz)
+        op, _k2 = _ptr(out)
+        o = opts.to_c()
+        self._check(self._lib.bs_all_vs_all(self._h, xp, n, L, ctypes.byref(o), op))
+        return CrmsdMatrix(n, out, opts.layout)
+
+    def pairs(self, xyz, ii, jj, opts: Optional[CrmsdOptions] = None, out=None):
+        opts = opts or CrmsdOptions()
+        if isinstance(xyz, np.ndarray):
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        n, L = int(xyz.shape[0]), int(xyz.shape[1])
+        if isinstance(ii, np.ndarray) or not hasattr(ii, "data_ptr"):
+            ii = np.ascontiguousarray(ii, dtype=np.int64)
+            jj = np.ascontiguousarray(jj, dtype=np.int64)
+        npairs = int(ii.shape[0])
+        if out is None:
+            out = np.empty(npairs, dtype=np.float64)
+        xp, _k1 = _ptr(xyz)
+        ip, _k2 = _ptr(ii)
+        jp, _k3 = _ptr(jj)
+        op, _k4 = _ptr(out)
+        o = opts.to_c()
+        self._check(self._lib.bs_pairs(self._h, xp, n, L, ip, jp, npairs, ctypes.byref(o), op))
+        return out
+
+    # -- diagnostics ---------------------------------------------------------
+    def debug_tile_levels(self, xyz) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        out = np.zeros((4, 128, 128), dtype=np.float32)
+        self._check(self._lib.bs_debug_tile_levels(self._h, xyz.ctypes.data, xyz.shape[0], xyz.shape[1],
+                                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def debug_pair_levels(self, xyz, ii, jj):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        ii = np.ascontiguousarray(ii, dtype=np.int64)
+        jj = np.ascontiguousarray(jj, dtype=np.int64)
+        lv = np.zeros((ii.shape[0], 4, 9), dtype=np.float32)
+        r = np.zeros(ii.shape[0])
+        self._check(self._lib.bs_debug_pair_levels(self._h, xyz.ctypes.data, xyz.shape[0], xyz.shape[1],
+                                                   ii.ctypes.data, jj.ctypes.data, ii.shape[0],
+                                                   lv.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                   r.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return lv, r
+
+
+_default: Optional[Engine] = None
+
+
+def default_engine() -> Engine:
+    global _default
+    if _default is None:
+        _default = Engine(0)
+    return _default
+
+
+def crmsd(a, b) -> float:
+    """crmsd of two index-matched [L][3] coordinate sets (on the GPU)."""
+    return default_engine().crmsd(a, b)
+
+
+def crmsd_all_vs_all(models, opts: Optional[CrmsdOptions] = None) -> CrmsdMatrix:
+    """All-vs-all crmsd of ``models`` ([n][L][3], or a list of [L][3])."""
+    if isinstance(models, (list, tuple)):
+        models = np.stack([np.asarray(m, dtype=np.float64) for m in models])
+    return default_engine().all_vs_all(models, opts)

@@ -1,0 +1,459 @@
+// crmsd_math.cuh -- per-pair arithmetic of the crmsd engine, shared by the
+// GPU kernels and the host-side self-test hooks (same source, __host__
+// __device__).
+//
+// Notation (one pair of structures a, b with L index-matched atoms):
+//   centred coordinates are quantised to integers n = rint(y / 2^e);
+//   n = d0 * 2^16 + d1 * 2^8 + d2 with balanced digits |d1|,|d2| <= 128,
+//   |d0| <= 128; every digit is exact in bf16.
+//   S_l[x][y]  level sums of digit products, l = i + j:
+//     S0 = sum d0a d0b                    S1 = sum d0a d1b + d1a d0b
+//     S2 = sum d0a d2b + d1a d1b + d2a d0b S3 = sum d1a d2b + d2a d1b
+//   (the level-4 term sum d2a d2b is dropped; its effect on E is bounded
+//   by 2 sqrt(3) sqrt(N2a N2b), N2 = sum of squared lowest digits).
+//   Mhat = 2^32 S0 + 2^24 S1 + 2^16 S2 + 2^8 S3          (units u = 2^(2e))
+//   Ghat = sum n^2 (exact)                               (units u)
+//   K(S) 4x4 quaternion key matrix, lambda0 = (Ga + Gb)/2,
+//   E = Ga + Gb - 2 lambda_max(K) = 2 min_q q'(lambda0 I - K)q / |q|^2,
+//   RMSD = sqrt(E / L).
+// With the row-major convention S[3x+y] = sum a_x b_y used here,
+//   q' K(S) q = sum_xy T(q)_xy S_xy,  T(q) = R(q)^T (transposed rotation).
+//
+// The level sums are exact: the host picks e so that every partial sum of
+// every level stays below 2^24 in magnitude, which FP32 accumulation
+// represents exactly.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define BS_HD __host__ __device__ __forceinline__
+#else
+#define BS_HD static inline
+#endif
+
+namespace bsm {
+
+// ---------------------------------------------------------------- FP32 QCP
+struct Key {
+  float k00, k01, k02, k03, k11, k12, k13, k22, k23, k33;
+};
+
+BS_HD Key key_from_s(const float s[9]) {
+  Key k;
+  const float sxx = s[0], sxy = s[1], sxz = s[2];
+  const float syx = s[3], syy = s[4], syz = s[5];
+  const float szx = s[6], szy = s[7], szz = s[8];
+  k.k00 = sxx + syy + szz;
+  k.k01 = syz - szy;
+  k.k02 = szx - sxz;
+  k.k03 = sxy - syx;
+  k.k11 = sxx - syy - szz;
+  k.k12 = sxy + syx;
+  k.k13 = szx + sxz;
+  k.k22 = -sxx + syy - szz;
+  k.k23 = syz + szy;
+  k.k33 = -sxx - syy + szz;
+  return k;
+}
+
+BS_HD float det3f(const float m[9]) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// det of the symmetric 4x4 with entries b_ij; Laplace over 2x2 minors of
+// rows (0,1) and their complements in rows (2,3).
+BS_HD float det4_sym(float b00, float b01, float b02, float b03, float b11, float b12, float b13, float b22,
+                     float b23, float b33) {
+  // rows 0,1
+  const float s01 = b00 * b11 - b01 * b01;
+  const float s02 = b00 * b12 - b02 * b01;
+  const float s03 = b00 * b13 - b03 * b01;
+  const float s12 = b01 * b12 - b02 * b11;
+  const float s13 = b01 * b13 - b03 * b11;
+  const float s23 = b02 * b13 - b03 * b12;
+  // rows 2,3 (row2 = b02 b12 b22 b23, row3 = b03 b13 b23 b33)
+  const float c23 = b22 * b33 - b23 * b23;
+  const float c13 = b12 * b33 - b23 * b13;
+  const float c12 = b12 * b23 - b22 * b13;
+  const float c03 = b02 * b33 - b23 * b03;
+  const float c02 = b02 * b23 - b22 * b03;
+  const float c01 = b02 * b13 - b12 * b03;
+  return s01 * c23 - s02 * c13 + s03 * c12 + s12 * c03 - s13 * c02 + s23 * c01;
+}
+
+// 4-D generalised cross product of three row vectors (null vector of the
+// 3x4 matrix they form).
+BS_HD void gcross4(const float a[4], const float b[4], const float c[4], float v[4]) {
+  const float m01 = b[0] * c[1] - b[1] * c[0];
+  const float m02 = b[0] * c[2] - b[2] * c[0];
+  const float m03 = b[0] * c[3] - b[3] * c[0];
+  const float m12 = b[1] * c[2] - b[2] * c[1];
+  const float m13 = b[1] * c[3] - b[3] * c[1];
+  const float m23 = b[2] * c[3] - b[3] * c[2];
+  v[0] = a[1] * m23 - a[2] * m13 + a[3] * m12;
+  v[1] = -(a[0] * m23 - a[2] * m03 + a[3] * m02);
+  v[2] = a[0] * m13 - a[1] * m03 + a[3] * m01;
+  v[3] = -(a[0] * m12 - a[1] * m02 + a[2] * m01);
+}
+
+// Largest eigenvalue x and an eigenvector q (unnormalised) of K(s), for s
+// scaled so that (Ga+Gb)/2 == 1 (then x <= 1).  Newton on the QCP quartic
+// from x = 1, then the adjugate column of K - xI with the largest diagonal
+// cofactor.  Returns |q|^2 relative to the scale of the cofactors; a tiny
+// value means the top eigenvalue is (nearly) degenerate.
+BS_HD float qcp_top_eig(const float s[9], float &xout, float q[4]) {
+  const Key k = key_from_s(s);
+  float fro2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fro2 = fmaf(s[i], s[i], fro2);
+  const float c2 = -2.f * fro2;
+  const float c1 = -8.f * det3f(s);
+  const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
+  float x = 1.0f;
+  for (int it = 0; it < 32; ++it) {
+    const float x2 = x * x;
+    const float p = fmaf(fmaf(x2 + c2, x, c1), x, c0);  // ((x^2+c2)x + c1)x + c0
+    const float dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
+    if (!(dp > 0.f)) break;  // guards 0 and NaN
+    const float dx = p / dp;
+    x -= dx;
+    if (fabsf(dx) <= 3e-7f * fabsf(x) + 1e-30f) break;
+  }
+  xout = x;
+  const float b00 = k.k00 - x, b11 = k.k11 - x, b22 = k.k22 - x, b33 = k.k33 - x;
+  const float r0[4] = {b00, k.k01, k.k02, k.k03};
+  const float r1[4] = {k.k01, b11, k.k12, k.k13};
+  const float r2[4] = {k.k02, k.k12, b22, k.k23};
+  const float r3[4] = {k.k03, k.k13, k.k23, b33};
+  // diagonal cofactors
+  const float C0 = b11 * (b22 * b33 - k.k23 * k.k23) - k.k12 * (k.k12 * b33 - k.k23 * k.k13) +
+                   k.k13 * (k.k12 * k.k23 - b22 * k.k13);
+  const float C1 = b00 * (b22 * b33 - k.k23 * k.k23) - k.k02 * (k.k02 * b33 - k.k23 * k.k03) +
+                   k.k03 * (k.k02 * k.k23 - b22 * k.k03);
+  const float C2 = b00 * (b11 * b33 - k.k13 * k.k13) - k.k01 * (k.k01 * b33 - k.k13 * k.k03) +
+                   k.k03 * (k.k01 * k.k13 - b11 * k.k03);
+  const float C3 = b00 * (b11 * b22 - k.k12 * k.k12) - k.k01 * (k.k01 * b22 - k.k12 * k.k02) +
+                   k.k02 * (k.k01 * k.k12 - b11 * k.k02);
+  const float a0 = fabsf(C0), a1 = fabsf(C1), a2 = fabsf(C2), a3 = fabsf(C3);
+  int j = 0;
+  float best = a0;
+  if (a1 > best) { best = a1; j = 1; }
+  if (a2 > best) { best = a2; j = 2; }
+  if (a3 > best) { best = a3; j = 3; }
+  float sa[4], sb[4], sc[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    sa[i] = (j == 0) ? r1[i] : r0[i];
+    sb[i] = (j <= 1) ? r2[i] : r1[i];
+    sc[i] = (j <= 2) ? r3[i] : r2[i];
+  }
+  gcross4(sa, sb, sc, q);
+  return best;
+}
+
+// ------------------------------------------------- quaternion -> T = R^T
+// T(q) with q = (w, x, y, z); quadratic, homogeneous.
+template <typename V>
+BS_HD void t_of_q(const V q[4], V t[9]) {
+  const V w = q[0], x = q[1], y = q[2], z = q[3];
+  const V ww = w * w, xx = x * x, yy = y * y, zz = z * z;
+  const V wx = w * x, wy = w * y, wz = w * z, xy = x * y, xz = x * z, yz = y * z;
+  t[0] = ww + xx - yy - zz;
+  t[1] = 2 * (xy + wz);
+  t[2] = 2 * (xz - wy);
+  t[3] = 2 * (xy - wz);
+  t[4] = ww - xx + yy - zz;
+  t[5] = 2 * (yz + wx);
+  t[6] = 2 * (xz + wy);
+  t[7] = 2 * (yz - wx);
+  t[8] = ww - xx - yy + zz;
+}
+
+// Symmetric bilinear form T(q, p):  T(q+p) = T(q) + 2 T(q,p) + T(p).
+BS_HD void t_bilinear(const float q[4], const float p[4], float t[9]) {
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  const float W = p[0], X = p[1], Y = p[2], Z = p[3];
+  const float ww = w * W, xx = x * X, yy = y * Y, zz = z * Z;
+  const float xy = x * Y + y * X, wz = w * Z + z * W, xz = x * Z + z * X;
+  const float wy = w * Y + y * W, yz = y * Z + z * Y, wx = w * X + x * W;
+  t[0] = ww + xx - yy - zz;
+  t[1] = xy + wz;
+  t[2] = xz - wy;
+  t[3] = xy - wz;
+  t[4] = ww - xx + yy - zz;
+  t[5] = yz + wx;
+  t[6] = xz + wy;
+  t[7] = yz - wx;
+  t[8] = ww - xx - yy + zz;
+}
+
+// int128 -> float (round-to-nearest of the high part, then add the low part)
+BS_HD float i128_to_f32(__int128 v) {
+  const long long hi = (long long)(v >> 64);
+  const unsigned long long lo = (unsigned long long)v;
+  return (float)hi * 18446744073709551616.0f + (float)lo;
+}
+
+// ----------------------------------------------------- fast-path epilogue
+// The fast path runs in three phases so that the tensor-core epilogue can
+// stream one TMEM level accumulator at a time:
+//   1. fast_begin: FP32 covariance m (from all levels) -> FP32 QCP eigenpair,
+//      split of the eigenvector q = q_h + q_l with q_h on the 2^-11 grid,
+//      exact integer T(Q_h), and the small FP32 terms 4 B(q_h,q_l) + 2 F(q_l);
+//   2. fast_level (l = 0..3): U_l += sum_xy T_xy S_l,xy, exactly in int64 for
+//      l = 0, 1, 2 and in FP32 for l = 3;
+//   3. fast_finish: 2 F(q_h) exactly in int128, E = 2 F(q) / |q|^2, RMSD and
+//      the error bound that decides whether the pair is recomputed.
+// m is the covariance in units of 2^32 u:  m = S0 + 2^-8 S1 + 2^-16 S2 + 2^-24 S3.
+BS_HD float m_from_levels(float s0, float s1, float s2, float s3) {
+  return fmaf(s3, 5.9604644775390625e-8f, fmaf(s2, 1.52587890625e-5f, fmaf(s1, 0.00390625f, s0)));
+}
+
+struct FastState {
+  int T[9];
+  long long U0, U1, U2;
+  float U3;
+  float rest;  // 4 B(q_h,q_l) + 2 F(q_l), units 2^32 u
+  float qq;    // |q|^2 of the normalised eigenvector (max component 1)
+  int q2;      // |Q_h|^2
+  int flag;    // 1: degenerate eigenvector, recompute exactly
+};
+
+BS_HD void fast_begin(const float m[9], long long gsum, FastState &st) {
+  st.U0 = st.U1 = st.U2 = 0;
+  st.U3 = 0.f;
+  st.flag = 0;
+  st.rest = 0.f;
+  st.qq = 1.f;
+  st.q2 = 0;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) st.T[i] = 0;
+  if (gsum <= 0) return;  // both structures collapse onto one point: E = 0
+  const float lam0 = (float)gsum * 1.16415321826934814453125e-10f;  // 2^-33
+  const float inv = 1.0f / lam0;
+  float sn[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
+  float x, q[4];
+  const float cof = qcp_top_eig(sn, x, q);
+  const float qa = fmaxf(fmaxf(fabsf(q[0]), fabsf(q[1])), fmaxf(fabsf(q[2]), fabsf(q[3])));
+  if (!(qa > 1e-30f) || !(cof > 1e-6f)) {
+    st.flag = 1;
+    return;
+  }
+  const float qs = 1.0f / qa;
+  float qn[4], qh[4], ql[4];
+  int Q[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qn[i] = q[i] * qs;
+    const float h = rintf(qn[i] * 2048.f);
+    Q[i] = (int)h;
+    qh[i] = h * 4.8828125e-4f;  // 2^-11
+    ql[i] = qn[i] - qh[i];
+  }
+  t_of_q<int>(Q, st.T);
+  st.q2 = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3];
+  float tb[9], tl[9];
+  t_bilinear(qh, ql, tb);
+  t_of_q<float>(ql, tl);
+  const float dot_hl = qh[0] * ql[0] + qh[1] * ql[1] + qh[2] * ql[2] + qh[3] * ql[3];
+  const float dot_ll = ql[0] * ql[0] + ql[1] * ql[1] + ql[2] * ql[2] + ql[3] * ql[3];
+  float sb = 0.f, sl = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    sb = fmaf(tb[i], m[i], sb);
+    sl = fmaf(tl[i], m[i], sl);
+  }
+  st.rest = 4.f * (lam0 * dot_hl - sb) + 2.f * (lam0 * dot_ll - sl);
+  float qq = 0.f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) qq = fmaf(qn[i], qn[i], qq);
+  st.qq = qq;
+}
+
+BS_HD void fast_level(FastState &st, int level, const float s[9]) {
+  if (level < 3) {
+    long long u = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) u += (long long)st.T[i] * (long long)(int)s[i];
+    if (level == 0) st.U0 += u;
+    else if (level == 1) st.U1 += u;
+    else st.U2 += u;
+  } else {
+    float u = st.U3;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) u = fmaf((float)st.T[i], s[i], u);
+    st.U3 = u;
+  }
+}
+
+BS_HD float fast_finish(const FastState &st, long long gsum, float low_a, float low_b, int scale_exp, int L,
+                        float tol, int &flag) {
+  flag = st.flag;
+  if (gsum <= 0 || st.flag) return 0.f;
+  // 2 F(q_h) 2^22 in units u = gsum |Q_h|^2 - 2 (2^32 U0 + 2^24 U1 + 2^16 U2 + 2^8 U3)
+  __int128 c = (__int128)gsum * (__int128)st.q2;
+  c -= ((__int128)st.U0 << 33) + ((__int128)st.U1 << 25) + ((__int128)st.U2 << 17);
+  const float twoFh = (i128_to_f32(c) - 512.f * st.U3) * 2.384185791015625e-7f;  // 2^-22 -> u
+  const float twoF = twoFh + st.rest * 4294967296.0f;                             // 2^32 -> u
+  const float e_u = twoF / st.qq;
+  const float u = ldexpf(1.0f, 2 * scale_exp);  // Angstrom^2 per unit
+  const float e_a2 = fmaxf(e_u, 0.f) * u;
+  const float rmsd = sqrtf(e_a2 / (float)L);
+  // error bound on E: dropped level 4 (Weyl: 2 sqrt(3) sqrt(N2a N2b)) plus
+  // the FP32 arithmetic of the fast path (<= 2^-28 lambda0)
+  const float d4 = 3.4641016f * low_a * low_b;
+  const float darith = (float)gsum * 1.862645149230957e-9f;  // 2^-29 (Ga+Gb)
+  const float de_a2 = (d4 + darith) * u;
+  const float elo = fmaxf(e_a2 - de_a2, 0.f);
+  // |dRMSD| <= dE / (sqrt(L) sqrt(E_lo)): recompute when dE^2 > tol^2 L E_lo
+  if (de_a2 * de_a2 > tol * tol * (float)L * elo) flag = 1;
+  return rmsd;
+}
+
+// All three phases for one pair whose level sums are at hand.
+struct EpilogueIn {
+  float s0[9], s1[9], s2[9], s3[9];
+  long long ga, gb;
+  float low_a, low_b;  // sqrt(sum d2^2) of each structure
+};
+
+BS_HD float pair_rmsd_fast(const EpilogueIn &in, int scale_exp, int L, float tol, int &flag) {
+  const long long gsum = in.ga + in.gb;
+  float m[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) m[i] = m_from_levels(in.s0[i], in.s1[i], in.s2[i], in.s3[i]);
+  FastState st;
+  fast_begin(m, gsum, st);
+  fast_level(st, 0, in.s0);
+  fast_level(st, 1, in.s1);
+  fast_level(st, 2, in.s2);
+  fast_level(st, 3, in.s3);
+  return fast_finish(st, gsum, in.low_a, in.low_b, scale_exp, L, tol, flag);
+}
+
+// ------------------------------------------------------------ FP64 QCP
+// Largest eigenvalue of K(sn) for sn = S / lambda0 (so the root is <= 1),
+// by Newton on the quartic from 1; returns the deficit 1 - x.  Then
+// E = (Ga + Gb) (1 - x).
+BS_HD double qcp_deficit_f64(const double sn[9]) {
+  const double sxx = sn[0], sxy = sn[1], sxz = sn[2], syx = sn[3], syy = sn[4], syz = sn[5], szx = sn[6],
+               szy = sn[7], szz = sn[8];
+  const double k00 = sxx + syy + szz, k01 = syz - szy, k02 = szx - sxz, k03 = sxy - syx;
+  const double k11 = sxx - syy - szz, k12 = sxy + syx, k13 = szx + sxz;
+  const double k22 = -sxx + syy - szz, k23 = syz + szy, k33 = -sxx - syy + szz;
+  double fro2 = 0.0;
+  for (int i = 0; i < 9; ++i) fro2 += sn[i] * sn[i];
+  const double c2 = -2.0 * fro2;
+  const double det3 = sxx * (syy * szz - syz * szy) - sxy * (syx * szz - syz * szx) + sxz * (syx * szy - syy * szx);
+  const double c1 = -8.0 * det3;
+  const double s01 = k00 * k11 - k01 * k01, s02 = k00 * k12 - k02 * k01, s03 = k00 * k13 - k03 * k01;
+  const double s12 = k01 * k12 - k02 * k11, s13 = k01 * k13 - k03 * k11, s23 = k02 * k13 - k03 * k12;
+  const double t23 = k22 * k33 - k23 * k23, t13 = k12 * k33 - k23 * k13, t12 = k12 * k23 - k22 * k13;
+  const double t03 = k02 * k33 - k23 * k03, t02 = k02 * k23 - k22 * k03, t01 = k02 * k13 - k12 * k03;
+  const double c0 = s01 * t23 - s02 * t13 + s03 * t12 + s12 * t03 - s13 * t02 + s23 * t01;
+  double x = 1.0;
+  for (int it = 0; it < 60; ++it) {
+    const double x2 = x * x;
+    const double p = ((x2 + c2) * x + c1) * x + c0;
+    const double dp = (4.0 * x2 + 2.0 * c2) * x + c1;
+    if (!(dp > 0.0)) break;
+    const double dx = p / dp;
+    x -= dx;
+    if (fabs(dx) <= 1e-16 * fabs(x)) break;
+  }
+  return 1.0 - x;
+}
+
+// RMSD from an FP64 covariance S (S[3x+y] = sum a_x b_y) and G_a + G_b.
+BS_HD double qcp_rmsd_f64(const double s[9], double gsum, int L) {
+  if (!(gsum > 0.0)) return 0.0;
+  const double inv = 2.0 / gsum;
+  double sn[9];
+  for (int i = 0; i < 9; ++i) sn[i] = s[i] * inv;
+  const double e = gsum * qcp_deficit_f64(sn);
+  return e > 0.0 ? sqrt(e / (double)L) : 0.0;
+}
+
+// ------------------------------------------------------- exact recompute
+// FP64 eigenvector of K(sn) for the eigenvalue x: adjugate column of
+// K - xI with the largest diagonal cofactor.  Returns that cofactor's size.
+BS_HD double top_vec_f64(const double sn[9], double x, double q[4]) {
+  const double sxx = sn[0], sxy = sn[1], sxz = sn[2], syx = sn[3], syy = sn[4], syz = sn[5], szx = sn[6],
+               szy = sn[7], szz = sn[8];
+  const double k01 = syz - szy, k02 = szx - sxz, k03 = sxy - syx;
+  const double k12 = sxy + syx, k13 = szx + sxz, k23 = syz + szy;
+  const double b00 = sxx + syy + szz - x, b11 = sxx - syy - szz - x, b22 = -sxx + syy - szz - x,
+               b33 = -sxx - syy + szz - x;
+  const double r[4][4] = {{b00, k01, k02, k03}, {k01, b11, k12, k13}, {k02, k12, b22, k23}, {k03, k13, k23, b33}};
+  double best = -1.0;
+  int jb = 0;
+  for (int j = 0; j < 4; ++j) {
+    int id[3], c = 0;
+    for (int t = 0; t < 4; ++t)
+      if (t != j) id[c++] = t;
+    const double m00 = r[id[0]][id[0]], m01 = r[id[0]][id[1]], m02 = r[id[0]][id[2]];
+    const double m11 = r[id[1]][id[1]], m12 = r[id[1]][id[2]], m22 = r[id[2]][id[2]];
+    const double cof = m00 * (m11 * m22 - m12 * m12) - m01 * (m01 * m22 - m12 * m02) + m02 * (m01 * m12 - m11 * m02);
+    if (fabs(cof) > best) {
+      best = fabs(cof);
+      jb = j;
+    }
+  }
+  int id[3], c = 0;
+  for (int t = 0; t < 4; ++t)
+    if (t != jb) id[c++] = t;
+  const double *A = r[id[0]], *B = r[id[1]], *C = r[id[2]];
+  const double m01 = B[0] * C[1] - B[1] * C[0], m02 = B[0] * C[2] - B[2] * C[0], m03 = B[0] * C[3] - B[3] * C[0];
+  const double m12 = B[1] * C[2] - B[2] * C[1], m13 = B[1] * C[3] - B[3] * C[1], m23 = B[2] * C[3] - B[3] * C[2];
+  q[0] = A[1] * m23 - A[2] * m13 + A[3] * m12;
+  q[1] = -(A[0] * m23 - A[2] * m03 + A[3] * m02);
+  q[2] = A[0] * m13 - A[1] * m03 + A[3] * m01;
+  q[3] = -(A[0] * m12 - A[1] * m02 + A[2] * m01);
+  return best;
+}
+
+// Exact recomputation from the integer covariance Mhat of the quantised
+// coordinates (units u = 2^(2e)).  Mhat and Ghat are exact integers below
+// 2^53, so they are exact in FP64.  The FP64 QCP root gives the eigenvector
+// q, and E is its Rayleigh quotient against the exact matrix:
+//   E = 2 (lambda0 |q|^2 - sum_xy T(q)_xy Mhat_xy) / |q|^2,
+// whose error is second order in the eigenvector error plus FP64 rounding
+// of terms of size lambda0.  A degenerate top eigenvalue falls back to
+// E = (Ga + Gb)(1 - x).  Used for the (rare) pairs the fast path flags.
+BS_HD double pair_rmsd_exact(const long long mh[9], long long ga, long long gb, int scale_exp, int L) {
+  const long long gsum = ga + gb;
+  if (gsum <= 0) return 0.0;
+  const double g = (double)gsum;
+  const double inv = 2.0 / g;
+  double sn[9];
+  for (int i = 0; i < 9; ++i) sn[i] = (double)mh[i] * inv;
+  const double deficit = qcp_deficit_f64(sn);
+  double e_u = g * deficit;
+  double q[4];
+  const double cof = top_vec_f64(sn, 1.0 - deficit, q);
+  if (cof > 1e-12) {
+    double t[9];
+    t_of_q<double>(q, t);
+    const double qq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    double acc = 0.5 * g * qq;
+    for (int i = 0; i < 9; ++i) acc -= t[i] * (double)mh[i];
+    e_u = 2.0 * acc / qq;
+  }
+  const double e_a2 = (e_u > 0.0 ? e_u : 0.0) * ldexp(1.0, 2 * scale_exp);
+  return sqrt(e_a2 / (double)L);
+}
+
+// ------------------------------------------------------------- digits
+// Balanced base-256 digits of a quantised coordinate |n| < 2^23.
+BS_HD void split_digits(int n, int &d0, int &d1, int &d2) {
+  d2 = ((n + 128) & 255) - 128;
+  const int n1 = (n - d2) >> 8;
+  d1 = ((n1 + 128) & 255) - 128;
+  d0 = (n1 - d1) >> 8;
+}
+
+}  // namespace bsm

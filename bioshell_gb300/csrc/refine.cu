@@ -1,0 +1,235 @@
+// refine.cu -- exact recomputation of flagged pairs, and the CUDA-core
+// mixed path for explicit pair lists.
+//
+// Exact path: the quantised coordinates n = d0 2^16 + d1 2^8 + d2 are
+// rebuilt from the digit matrices, the covariance Mhat = sum n_a n_b is
+// accumulated in int64 (exact), and the FP64 QCP of crmsd_math.cuh finishes
+// the pair.  One warp per pair, lanes striding over atoms.
+#include "crmsd_math.cuh"
+#include "kernels.h"
+
+namespace bs {
+namespace {
+
+__device__ __forceinline__ int64_t tri_index(int64_t n, int64_t i, int64_t j) {
+  return i * n - i * (i + 1) / 2 + (j - i - 1);
+}
+
+__device__ __forceinline__ void tri_pair(int64_t n, int64_t t, int64_t &i, int64_t &j) {
+  // inverse of tri_index: row i holds n-1-i pairs
+  const double b = 2.0 * (double)n - 1.0;
+  int64_t r = (int64_t)floor((b - sqrt(b * b - 8.0 * (double)t)) * 0.5);
+  if (r < 0) r = 0;
+  while (r > 0 && r * n - r * (r + 1) / 2 > t) --r;
+  while ((r + 1) * n - (r + 1) * (r + 2) / 2 <= t) ++r;
+  i = r;
+  j = t - (r * n - r * (r + 1) / 2) + r + 1;
+}
+
+__device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t j, double v) {
+  if (o.layout == 0) {
+    const int64_t idx = tri_index(o.n, i, j);
+    if (o.out_type == 0) static_cast<double *>(o.ptr)[idx] = v;
+    else static_cast<float *>(o.ptr)[idx] = (float)v;
+  } else {
+    if (o.out_type == 0) {
+      static_cast<double *>(o.ptr)[i * o.n + j] = v;
+      static_cast<double *>(o.ptr)[j * o.n + i] = v;
+    } else {
+      static_cast<float *>(o.ptr)[i * o.n + j] = (float)v;
+      static_cast<float *>(o.ptr)[j * o.n + i] = (float)v;
+    }
+  }
+}
+
+struct Digits {
+  const __nv_bfloat16 *d0, *d1, *d2;
+  int lp;
+  __device__ __forceinline__ int coord(int64_t s, int c, int k) const {
+    const int64_t off = digit_row(s, c) * lp + k;
+    const int a = (int)__bfloat162float(d0[off]);
+    const int b = (int)__bfloat162float(d1[off]);
+    const int d = (int)__bfloat162float(d2[off]);
+    return a * 65536 + b * 256 + d;
+  }
+};
+
+// Exact int64 covariance of pair (i, j), partial over atoms k = k0, k0+ks, ...
+__device__ __forceinline__ void exact_cov_partial(const Digits &dg, int64_t i, int64_t j, int L, int k0, int ks,
+                                                  long long mh[9]) {
+#pragma unroll
+  for (int e = 0; e < 9; ++e) mh[e] = 0;
+  for (int k = k0; k < L; k += ks) {
+    const int a0 = dg.coord(i, 0, k), a1 = dg.coord(i, 1, k), a2 = dg.coord(i, 2, k);
+    const int b0 = dg.coord(j, 0, k), b1 = dg.coord(j, 1, k), b2 = dg.coord(j, 2, k);
+    mh[0] += (long long)a0 * b0;
+    mh[1] += (long long)a0 * b1;
+    mh[2] += (long long)a0 * b2;
+    mh[3] += (long long)a1 * b0;
+    mh[4] += (long long)a1 * b1;
+    mh[5] += (long long)a1 * b2;
+    mh[6] += (long long)a2 * b0;
+    mh[7] += (long long)a2 * b1;
+    mh[8] += (long long)a2 * b2;
+  }
+}
+
+__device__ __forceinline__ double exact_pair_warp(const Digits &dg, int64_t i, int64_t j, int L,
+                                                  const long long *ghat, int scale_exp, int lane) {
+  long long mh[9];
+  exact_cov_partial(dg, i, j, L, lane, 32, mh);
+#pragma unroll
+  for (int e = 0; e < 9; ++e)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mh[e] += __shfl_xor_sync(0xffffffffu, mh[e], o);
+  return bsm::pair_rmsd_exact(mh, ghat[i], ghat[j], scale_exp, L);
+}
+
+__global__ void k_refine_list(Digits dg, int L, const long long *__restrict__ ghat, DevScalars *sc,
+                              const unsigned long long *__restrict__ flags, unsigned long long cap, OutDesc out) {
+  const unsigned long long cnt = sc->flag_count < cap ? sc->flag_count : cap;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int scale_exp = sc->scale_exp;
+  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)cnt; w += warps) {
+    const unsigned long long f = flags[w];
+    const int64_t i = (int64_t)(f >> 32), j = (int64_t)(f & 0xffffffffull);
+    const double r = exact_pair_warp(dg, i, j, L, ghat, scale_exp, lane);
+    if (lane == 0) store_pair(out, i, j, r);
+  }
+}
+
+// Fallback when the flag list overflowed: every negative (sentinel) entry of
+// the output is recomputed.
+__global__ void k_refine_scan(Digits dg, int L, const long long *__restrict__ ghat, DevScalars *sc, OutDesc out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n = out.n;
+  const int64_t total = n * (n - 1) / 2;
+  const int scale_exp = sc->scale_exp;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t base = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < total;
+       base += warps * 32) {
+    const int64_t t = base + lane;
+    int64_t i = 0, j = 0;
+    bool sent = false;
+    if (t < total) {
+      tri_pair(n, t, i, j);
+      double v;
+      if (out.layout == 0) v = out.out_type == 0 ? static_cast<double *>(out.ptr)[t] : static_cast<float *>(out.ptr)[t];
+      else v = out.out_type == 0 ? static_cast<double *>(out.ptr)[i * n + j] : static_cast<float *>(out.ptr)[i * n + j];
+      sent = v < 0.0;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, sent);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const int64_t si = __shfl_sync(0xffffffffu, i, src);
+      const int64_t sj = __shfl_sync(0xffffffffu, j, src);
+      const double r = exact_pair_warp(dg, si, sj, L, ghat, scale_exp, lane);
+      if (lane == 0) store_pair(out, si, sj, r);
+    }
+  }
+}
+
+// Thread per pair: exact level sums on CUDA cores, the fast epilogue, and
+// the exact path when the pair is flagged.
+__global__ void k_mixed_pairs(Digits dg, int L, const long long *__restrict__ ghat, const float *__restrict__ low,
+                              DevScalars *sc, float tol, const int64_t *__restrict__ ii, const int64_t *__restrict__ jj,
+                              int64_t np, double *__restrict__ out, float *__restrict__ levels_out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const int64_t i = ii[t], j = jj[t];
+  if (i == j) {
+    out[t] = 0.0;
+    return;
+  }
+  int S[4][9];
+#pragma unroll
+  for (int l = 0; l < 4; ++l)
+#pragma unroll
+    for (int e = 0; e < 9; ++e) S[l][e] = 0;
+  const int lp = dg.lp;
+  for (int k = 0; k < L; ++k) {
+    int a[3][3], b[3][3];  // [coord][digit]
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t oa = digit_row(i, c) * lp + k, ob = digit_row(j, c) * lp + k;
+      a[c][0] = (int)__bfloat162float(dg.d0[oa]);
+      a[c][1] = (int)__bfloat162float(dg.d1[oa]);
+      a[c][2] = (int)__bfloat162float(dg.d2[oa]);
+      b[c][0] = (int)__bfloat162float(dg.d0[ob]);
+      b[c][1] = (int)__bfloat162float(dg.d1[ob]);
+      b[c][2] = (int)__bfloat162float(dg.d2[ob]);
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+      for (int y = 0; y < 3; ++y) {
+        const int e = 3 * x + y;
+        S[0][e] += a[x][0] * b[y][0];
+        S[1][e] += a[x][0] * b[y][1] + a[x][1] * b[y][0];
+        S[2][e] += a[x][0] * b[y][2] + a[x][1] * b[y][1] + a[x][2] * b[y][0];
+        S[3][e] += a[x][1] * b[y][2] + a[x][2] * b[y][1];
+      }
+  }
+  bsm::EpilogueIn in;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) {
+    in.s0[e] = (float)S[0][e];
+    in.s1[e] = (float)S[1][e];
+    in.s2[e] = (float)S[2][e];
+    in.s3[e] = (float)S[3][e];
+  }
+  in.ga = ghat[i];
+  in.gb = ghat[j];
+  in.low_a = low[i];
+  in.low_b = low[j];
+  if (levels_out) {
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) levels_out[t * 36 + l * 9 + e] = (float)S[l][e];
+  }
+  const int scale_exp = sc->scale_exp;
+  int flag = 0;
+  const float r = bsm::pair_rmsd_fast(in, scale_exp, L, tol, flag);
+  if (!flag) {
+    out[t] = (double)r;
+    return;
+  }
+  long long mh[9];
+  exact_cov_partial(dg, i, j, L, 0, 1, mh);
+  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, scale_exp, L);
+}
+
+}  // namespace
+
+cudaError_t launch_refine_list(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
+                               int L, const long long *ghat, DevScalars *sc, const unsigned long long *flags,
+                               unsigned long long cap, OutDesc out, int num_sms, cudaStream_t st) {
+  Digits dg{d0, d1, d2, lp};
+  k_refine_list<<<num_sms * 4, 256, 0, st>>>(dg, L, ghat, sc, flags, cap, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine_scan(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
+                               int L, const long long *ghat, DevScalars *sc, OutDesc out, int num_sms,
+                               cudaStream_t st) {
+  Digits dg{d0, d1, d2, lp};
+  k_refine_scan<<<num_sms * 4, 256, 0, st>>>(dg, L, ghat, sc, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_pairs(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
+                               int L, const long long *ghat, const float *low, DevScalars *sc, float tol,
+                               const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
+                               cudaStream_t st) {
+  if (np <= 0) return cudaSuccess;
+  Digits dg{d0, d1, d2, lp};
+  const int th = 128;
+  k_mixed_pairs<<<(unsigned)((np + th - 1) / th), th, 0, st>>>(dg, L, ghat, low, sc, tol, ii, jj, np, out,
+                                                               levels_out);
+  return cudaGetLastError();
+}
+
+}  // namespace bs

@@ -1,0 +1,103 @@
+"""ctypes binding of ``libbioshell_crmsd.so`` (declarations in
+``include/bioshell_crmsd.h``).
+
+The library is loaded from the package's ``lib/`` directory.  There is no
+fallback: if the shared library is missing or cannot be loaded, importing the
+binding raises, and every compute call needs a usable sm_103 GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libbioshell_crmsd.so")
+
+BS_OK = 0
+STATUS_NAMES = {
+    0: "BS_OK", 1: "BS_ERR_INVALID_ARG", 2: "BS_ERR_CUDA", 3: "BS_ERR_OOM", 4: "BS_ERR_TIMEOUT",
+    5: "BS_ERR_UNSUPPORTED", 6: "BS_ERR_NONFINITE", 7: "BS_ERR_BUDGET", 8: "BS_ERR_NO_DEVICE",
+    9: "BS_ERR_INTERNAL",
+}
+PRECISION = {"plain64": 0, "mixed": 1}
+LAYOUT = {"triangle": 0, "square": 1}
+OUT_TYPE = {"f64": 0, "f32": 1}
+
+
+class bs_opts(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_uint32), ("precision", ctypes.c_int32), ("layout", ctypes.c_int32),
+                ("out_type", ctypes.c_int32), ("tolerance", ctypes.c_double),
+                ("reserved", ctypes.c_int32 * 8)]
+
+
+class bs_metrics(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_int64), ("pairs_refined", ctypes.c_int64), ("ms_total", ctypes.c_double),
+                ("ms_h2d", ctypes.c_double), ("ms_prep", ctypes.c_double), ("ms_main", ctypes.c_double),
+                ("ms_refine", ctypes.c_double), ("ms_d2h", ctypes.c_double), ("scale_exp", ctypes.c_int32),
+                ("main_launches", ctypes.c_int32), ("quant_bound", ctypes.c_double),
+                ("bytes_h2d", ctypes.c_int64), ("bytes_d2h", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+# (name, restype, argtypes) for every function the header declares
+SIGNATURES = [
+    ("bs_abi_version", ctypes.c_int32, []),
+    ("bs_status_string", ctypes.c_char_p, [ctypes.c_int32]),
+    ("bs_last_error", ctypes.c_char_p, [_vp]),
+    ("bs_ctx_create", ctypes.c_int32, [ctypes.POINTER(_vp), ctypes.c_int32, ctypes.c_size_t]),
+    ("bs_ctx_destroy", None, [_vp]),
+    ("bs_opts_init", None, [ctypes.POINTER(bs_opts)]),
+    ("bs_get_metrics", ctypes.c_int32, [_vp, ctypes.POINTER(bs_metrics)]),
+    ("bs_ctx_trim", ctypes.c_int32, [_vp]),
+    ("bs_crmsd", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _dp]),
+    ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
+    ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
+                                  ctypes.POINTER(bs_opts), _vp]),
+    ("bs_host_alloc", ctypes.c_int32, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    ("bs_host_free", ctypes.c_int32, [_vp]),
+    ("bs_selftest_digits", ctypes.c_int32, [_dp, ctypes.c_int32, ctypes.c_int32, _i32p, _i64p, _i64p]),
+    ("bs_selftest_epilogue", ctypes.c_int32, [_fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp, _i32p]),
+    ("bs_selftest_exact", ctypes.c_int32, [_i32p, _i32p, ctypes.c_int32, ctypes.c_int32, _dp]),
+    ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
+    ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
+                                              _fp, _dp]),
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load():
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m bioshell_gb300._build` "
+                              "(the engine has no CPU fallback)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+class CrmsdError(RuntimeError):
+    """A non-zero bs_status from the engine."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")

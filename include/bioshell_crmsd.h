@@ -1,0 +1,190 @@
+/*
+ * bioshell_crmsd.h -- C ABI of the GB300-native all-vs-all crmsd engine.
+ *
+ * This is the drop-in boundary for the crmsd path of bioshell-pdb.  The
+ * reference (BioShell 4.0.0-dev, Rust) has no crmsd routine yet -- the only
+ * trace is the dependency comment at bioshell-pdb/Cargo.toml:27 -- so the
+ * entry points below are the ones the crate's calc module would bind through
+ * an `extern "C"` block built from build.rs.  Each declaration names the
+ * reference interface it serves:
+ *
+ *   crmsd of one pair            -> bioshell-pdb/src/calc/mod.rs:1-10 (new fn
+ *                                   beside SubstructureAxis::from_3d_points,
+ *                                   calc/substructures.rs:17, same
+ *                                   `&[T: HasCartesians]` inputs,
+ *                                   bioshell-core/src/has_cartesians.rs:6-8)
+ *   all-vs-all distance matrix   -> fills the matrix that
+ *                                   HierarchicalClusteringMatrix::new builds
+ *                                   from n(n-1)/2 closure calls
+ *                                   (bioshell-clustering/src/hierarchical/
+ *                                   clustering_matrix.rs:11-22)
+ *
+ * Conventions
+ *   - Coordinates are f64 AoS xyz triples, `[n][L][3]`, the layout of
+ *     bioshell_core::Vec3 (bioshell-core/src/vec3.rs:44-51); every atom has
+ *     the same weight and each structure is centred on its arithmetic mean.
+ *   - Pointers may be host memory (pageable or pinned) or device memory of
+ *     the context's GPU; the library detects which.
+ *   - The caller owns inputs and outputs; the context owns device workspaces.
+ *   - Every call returns a bs_status; 0 is success.  No C++ exception and no
+ *     abort crosses this boundary.  bs_last_error() describes the last
+ *     failure of a context.
+ *   - A context is used by one host thread at a time.  All work runs on the
+ *     context's CUDA stream; calls return after their results are in `out`.
+ *   - No CPU fallback exists: without a usable sm_103 GPU every compute call
+ *     fails with BS_ERR_NO_DEVICE.
+ */
+#ifndef BIOSHELL_CRMSD_H
+#define BIOSHELL_CRMSD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BS_API __attribute__((visibility("default")))
+
+#define BS_ABI_VERSION 1
+#define BS_OPTS_VERSION 1
+
+typedef int32_t bs_status;
+enum {
+  BS_OK = 0,
+  BS_ERR_INVALID_ARG = 1,  /* null pointer, n < 0, L < 1, bad option value  */
+  BS_ERR_CUDA = 2,         /* a CUDA runtime/driver call failed              */
+  BS_ERR_OOM = 3,          /* device or pinned allocation failed             */
+  BS_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up             */
+  BS_ERR_UNSUPPORTED = 5,  /* shape outside what this path supports          */
+  BS_ERR_NONFINITE = 6,    /* NaN or Inf in the input coordinates            */
+  BS_ERR_BUDGET = 7,       /* request exceeds the context's HBM budget       */
+  BS_ERR_NO_DEVICE = 8,    /* no usable GPU (or not an sm_103 device)        */
+  BS_ERR_INTERNAL = 9      /* invariant violated inside the library          */
+};
+
+typedef struct bs_ctx bs_ctx;
+
+/* Arithmetic of the all-vs-all fill. */
+enum {
+  /* FP64 centring, FP64 CUDA-core covariance, FP64 QCP: the plain method. */
+  BS_PRECISION_PLAIN64 = 0,
+  /* Exact fixed-point digits on tcgen05 tensor cores + FP32/integer QCP with
+   * an exact Rayleigh-quotient cancellation step; pairs whose error bound is
+   * not below the tolerance are recomputed with exact integer covariances. */
+  BS_PRECISION_MIXED = 1
+};
+
+/* Layout of the result buffer. */
+enum {
+  BS_LAYOUT_TRIANGLE = 0, /* n(n-1)/2 values, row-major upper triangle:
+                             index(i,j) = i*n - i*(i+1)/2 + (j-i-1), i<j   */
+  BS_LAYOUT_SQUARE = 1    /* n*n values, symmetric, zero diagonal          */
+};
+
+/* Element type of the result buffer. */
+enum { BS_OUT_F64 = 0, BS_OUT_F32 = 1 };
+
+typedef struct {
+  uint32_t version;   /* must be BS_OPTS_VERSION (bs_opts_init sets it)   */
+  int32_t precision;  /* BS_PRECISION_*                                    */
+  int32_t layout;     /* BS_LAYOUT_*                                       */
+  int32_t out_type;   /* BS_OUT_*                                          */
+  double tolerance;   /* mixed path: per-pair |dRMSD| bound in Angstrom
+                         that a pair must meet without recomputation;
+                         <= 0 selects the default (2.5e-5)                */
+  int32_t reserved[8];
+} bs_opts;
+
+/* Per-call counters of the last compute call on a context. */
+typedef struct {
+  int64_t pairs;           /* pairs written                                  */
+  int64_t pairs_refined;   /* mixed path: pairs recomputed exactly           */
+  double ms_total;         /* device time of the whole call (CUDA events)    */
+  double ms_h2d;           /* host -> device copy of the coordinates         */
+  double ms_prep;          /* centring / quantisation pass                   */
+  double ms_main;          /* covariance + QCP kernel                        */
+  double ms_refine;        /* exact recomputation of flagged pairs           */
+  double ms_d2h;           /* device -> host copy of the result              */
+  int32_t scale_exp;       /* mixed path: coordinate grid is 2^scale_exp A   */
+  int32_t main_launches;   /* kernels launched by the call                   */
+  double quant_bound;      /* mixed path: worst RMSD change from the grid    */
+  int64_t bytes_h2d;
+  int64_t bytes_d2h;
+} bs_metrics;
+
+/* ---- version / errors -------------------------------------------------- */
+BS_API int32_t bs_abi_version(void);
+BS_API const char *bs_status_string(bs_status s);
+/* Last error message of `ctx` (never NULL; "" when none). */
+BS_API const char *bs_last_error(const bs_ctx *ctx);
+
+/* ---- context ----------------------------------------------------------- */
+/* Creates a context on CUDA device `device`.  `hbm_budget_bytes` caps the
+ * device workspace the context may hold (0 = 90% of free memory). */
+BS_API bs_status bs_ctx_create(bs_ctx **out, int32_t device, size_t hbm_budget_bytes);
+BS_API void bs_ctx_destroy(bs_ctx *ctx);
+BS_API void bs_opts_init(bs_opts *opts);
+BS_API bs_status bs_get_metrics(const bs_ctx *ctx, bs_metrics *out);
+/* Releases cached device workspaces (they regrow on demand). */
+BS_API bs_status bs_ctx_trim(bs_ctx *ctx);
+
+/* ---- crmsd ------------------------------------------------------------- */
+/* crmsd of one pair of index-matched point sets a[L][3], b[L][3]
+ * (new bioshell_pdb::calc::crmsd; runs on the GPU as a batch of one). */
+BS_API bs_status bs_crmsd(bs_ctx *ctx, const double *a, const double *b, int32_t L, double *out_rmsd);
+
+/* All-vs-all crmsd of n structures xyz[n][L][3] into `out` (layout and
+ * element type from `opts`, NULL = defaults: mixed precision, packed f64
+ * triangle).  Replaces the n(n-1)/2 distance-closure calls of
+ * HierarchicalClusteringMatrix::new (clustering_matrix.rs:11-22). */
+BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const bs_opts *opts,
+                               void *out);
+
+/* crmsd of an explicit pair list: out[t] = crmsd(xyz[ii[t]], xyz[jj[t]]),
+ * f64.  Used for sampled checks and for sparse consumers. */
+BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
+                          const int64_t *jj, int64_t npairs, const bs_opts *opts, double *out);
+
+/* ---- pinned host memory ------------------------------------------------- */
+/* Page-locked host buffers for fast host<->device staging (cudaHostAlloc);
+ * free with bs_host_free.  Pageable memory is accepted everywhere too. */
+BS_API bs_status bs_host_alloc(size_t bytes, void **out);
+BS_API bs_status bs_host_free(void *p);
+
+/* ---- test hooks (no reference counterpart) ------------------------------
+ * These run the engine's fixed-point epilogue arithmetic on the HOST, so the
+ * CPU test-suite can check the exact-digit algebra without a GPU.  They are
+ * never used by the compute entry points above. */
+
+/* Digits of one structure's centred coordinates at grid 2^scale_exp:
+ * digits[3][3][L] (digit-major, then coordinate, then atom), plus the exact
+ * squared norm (int64) and the sum of squared lowest digits. */
+BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_exp, int32_t *digits,
+                                    int64_t *g_exact, int64_t *low_norm2);
+/* The mixed-path epilogue for one pair from its four level sums
+ * levels[4][9] (exact integers stored as float) and exact squared norms;
+ * returns rmsd and whether the pair would be recomputed (flag = 1). */
+BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double low_a,
+                                      double low_b, int32_t scale_exp, int32_t L, double tolerance,
+                                      double *rmsd, int32_t *flag);
+/* The exact recomputation from integer coordinates n_a[3][L], n_b[3][L]. */
+BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t L, int32_t scale_exp,
+                                   double *rmsd);
+
+/* GPU diagnostics of the mixed path.  bs_debug_tile_levels returns the raw
+ * tensor-core level sums of the first tile (structures 0..39 against
+ * 0..39) as levels[4][128][128] (level, row, column; rows and columns in the
+ * digit-matrix order of the engine: structure s, coordinate c at
+ * 32*(s/10) + 3*(s%10) + c).  bs_debug_pair_levels returns, for each listed
+ * pair, the level sums computed with integer CUDA-core arithmetic
+ * (levels[npairs][4][9]) and that path's crmsd. */
+BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels);
+BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
+                                      const int64_t *jj, int64_t npairs, float *levels, double *rmsd);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BIOSHELL_CRMSD_H */
