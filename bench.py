@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 crmsd engine: all-vs-all crmsd pairs/s.
+
+Workload (default): 50,000 synthetic decoys x 300 CA atoms, 5% near-duplicates
+(noise sigma 0.01 A), every one of the 1,249,975,000 pairs per step, mixed
+precision (exact bf16 digit products on tcgen05 tensor cores + FP32/integer
+QCP epilogue), f64 packed-triangle output.
+
+One JSON line on stdout (rank 0):
+  value     pairs/s with coordinates and result resident in HBM, CUDA events
+            on the engine's stream around K steps;
+  e2e       the same through the C ABI with pinned HOST buffers: every step
+            copies the coordinates in and the whole f64 triangle out;
+  roofline  the tensor-core kernel: algorithmic 18*L flops/pair over its
+            event-timed duration, against the measured bf16 peak;
+  plain64   the plain FP64 GPU path on the same workload (the denominator);
+  accuracy  |dRMSD| vs the FP64 oracle on 1e6 seeded pairs + all
+            near-duplicate pairs;
+  cpu_baseline  the oracle on this host's cores on a bounded sample.
+``--impl reference`` times the CPU oracle alone (the reference has no crmsd
+implementation of its own; see the oracle's header).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from bioshell_gb300 import synth  # noqa: E402
+
+METRIC = "crmsd pairs/s (all-vs-all, mixed precision)"
+UNIT = "pairs/s"
+
+
+def args_():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=None, help="override the number of decoys (debug only)")
+    p.add_argument("--L", type=int, default=None, help="override the chain length (debug only)")
+    p.add_argument("--skip-plain", action="store_true")
+    p.add_argument("--skip-accuracy", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    return p.parse_args()
+
+
+def workload(a):
+    w = synth.MIXED_50K
+    if a.n or a.L:
+        w = synth.Workload(f"decoys-{a.n or w.n}x{a.L or w.L}-neardup5", n=a.n or w.n, L=a.L or w.L,
+                           near_dup_frac=w.near_dup_frac, near_dup_sigma=w.near_dup_sigma, seed=w.seed)
+    return w
+
+
+def tri_pairs(n, t):
+    t = np.asarray(t, dtype=np.int64)
+    i = np.floor((2 * n - 1 - np.sqrt((2 * n - 1) ** 2 - 8 * t.astype(np.float64))) / 2).astype(np.int64)
+    i = np.where(i * n - i * (i + 1) // 2 > t, i - 1, i)
+    i = np.where((i + 1) * n - (i + 1) * (i + 2) // 2 <= t, i + 1, i)
+    j = t - (i * n - i * (i + 1) // 2) + i + 1
+    return i, j
+
+
+def issued_flops(n, L):
+    """Tensor-core flops the mixed kernel issues per call: every upper-
+    triangle tile of 40 x 40 structures (128 x 128 rows) runs 8 digit
+    products over the 16-padded chain length."""
+    nb = (n + 39) // 40
+    lp = ((L + 15) // 16) * 16
+    return nb * (nb + 1) // 2 * 2.0 * 128 * 128 * lp * 8
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(x, seconds, seed=99):
+    """The FP64 oracle on this host's cores, on a bounded random sample."""
+    from oracle import oracle
+    oracle.build()
+    n = x.shape[0]
+    rng = np.random.default_rng(seed)
+    threads = host_threads()
+    npairs = n * (n - 1) // 2
+    probe = min(npairs, 20000)
+    t = rng.choice(npairs, probe, replace=False)
+    i, j = tri_pairs(n, t)
+    t0 = time.perf_counter()
+    oracle.crmsd_pairs(x, i, j, nthreads=threads)
+    dt = time.perf_counter() - t0
+    size = int(min(npairs, max(probe, probe * seconds / max(dt, 1e-6))))
+    t = rng.choice(npairs, size, replace=False) if size < npairs else np.arange(npairs)
+    i, j = tri_pairs(n, t)
+    t0 = time.perf_counter()
+    oracle.crmsd_pairs(x, i, j, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": size / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{size} seeded random pairs of the same {n}x{x.shape[1]} set, {dt:.1f} s"}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+        self.f.flush()
+
+    def summary(self):
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(rows[0][2]),
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profiled_traffic(name):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh).get(name)
+    except (OSError, ValueError):
+        return None
+
+
+def run_reference(a, rank):
+    if rank != 0:
+        return
+    w = workload(a)
+    x = w.generate()
+    samples = []
+    for s in range(a.warmup + a.steps):
+        cb = cpu_baseline(x, a.cpu_seconds / 2, seed=1000 + s)
+        if s >= a.warmup:
+            samples.append(cb)
+    v = statistics.median([c["value"] for c in samples])
+    cb = dict(samples[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "n": w.n, "L": w.L, "pairs": w.pairs},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a, rank, world, local_rank):
+    import torch
+    from bioshell_gb300.crmsd import CrmsdOptions, Engine
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("nccl")
+    w = workload(a)
+    x, sig = w.generate(return_sigma=True)
+    n, L = x.shape[0], x.shape[1]
+    npairs = n * (n - 1) // 2
+    eng = Engine(local_rank)
+    stream = torch.cuda.ExternalStream(eng.stream_handle())
+    xd = torch.from_numpy(x).cuda()
+    outd = torch.empty(npairs, dtype=torch.float64, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def step(xin, out, opts=None):
+        eng.all_vs_all(xin, opts, out=out)
+        return eng.metrics()
+
+    # ---- device-resident timed region
+    for _ in range(a.warmup):
+        step(xd, outd)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    mets = []
+    with Clocks(local_rank) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            mets.append(step(xd, outd))
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * npairs * a.steps / (ms * 1e-3)
+    clocks = clk.summary()
+    ms_main = statistics.mean(m["ms_main"] for m in mets)
+    launches = int(sum(m["main_launches"] for m in mets))
+    refined = mets[-1]["pairs_refined"]
+
+    # ---- end to end through the C ABI with pinned host buffers
+    xh = eng.host_empty(x.shape, np.float64)
+    xh[...] = x
+    oh = eng.host_empty((npairs,), np.float64)
+    step(xh, oh)
+    barrier()
+    e_steps = max(1, min(a.steps, 3))
+    ev0.record(stream)
+    for _ in range(e_steps):
+        step(xh, oh)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms_e2e = ev0.elapsed_time(ev1)
+    e2e = {"value": world * npairs * e_steps / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes),
+           "d2h_bytes_per_step": int(npairs * 8), "steps": e_steps, "ms_per_step": ms_e2e / e_steps}
+    np.testing.assert_array_equal(oh[:1000], outd[:1000].cpu().numpy())
+
+    # ---- plain FP64 denominator on the same workload
+    plain = None
+    if not a.skip_plain:
+        step(xd, outd, CrmsdOptions(precision="plain64"))
+        m = step(xd, outd, CrmsdOptions(precision="plain64"))
+        plain = {"value": npairs / (m["ms_total"] * 1e-3), "unit": UNIT, "ms_per_step": m["ms_total"],
+                 "kernel_ms": m["ms_main"]}
+        step(xd, outd)  # leave the mixed result in outd
+
+    # ---- accuracy against the FP64 oracle
+    acc = None
+    if not a.skip_accuracy and rank == 0:
+        from oracle import oracle
+        oracle.build()
+        rng = np.random.default_rng(2024)
+        sel = rng.choice(npairs, min(npairs, 1_000_000), replace=False)
+        i, j = tri_pairs(n, sel)
+        ref = oracle.crmsd_pairs(x, i, j, nthreads=host_threads())
+        got = outd[torch.from_numpy(sel).cuda()].cpu().numpy()
+        d = np.abs(got - ref)
+        nd = np.flatnonzero(sig == w.near_dup_sigma)
+        ia, ja = np.triu_indices(len(nd), 1)
+        ni, nj = nd[ia], nd[ja]
+        tsel = ni * n - ni * (ni + 1) // 2 + (nj - ni - 1)
+        ref2 = oracle.crmsd_pairs(x, ni, nj, nthreads=host_threads())
+        got2 = outd[torch.from_numpy(tsel).cuda()].cpu().numpy()
+        d2 = np.abs(got2 - ref2)
+        acc = {"random_pairs": int(len(sel)), "max_abs": float(d.max()), "p99_abs": float(np.percentile(d, 99)),
+               "near_dup_pairs": int(len(tsel)), "near_dup_max_abs": float(d2.max()) if len(d2) else None,
+               "near_dup_p99_abs": float(np.percentile(d2, 99)) if len(d2) else None,
+               "tolerance": 1e-4, "pass": bool(d.max() <= 1e-4 and (len(d2) == 0 or d2.max() <= 1e-4))}
+
+    pk, pk_kind = peaks()
+    achieved = 18.0 * L * npairs / (ms_main * 1e-3) / 1e12
+    peak = pk["bf16_tflops_sustained"]
+    traffic = profiled_traffic("mixed_tc")
+    roof = {"kernel": "k_mixed_tc", "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": f"{pk_kind} bf16 sustained",
+            "issued_tflops": issued_flops(n, L) / (ms_main * 1e-3) / 1e12,
+            "kernel_ms": ms_main, "traffic": traffic}
+    cb = cpu_baseline(x, a.cpu_seconds) if rank == 0 else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": w.name, "n": n, "L": L, "pairs": npairs, "precision": "mixed",
+                       "output": "f64 packed triangle", "l2": "no flush: inputs (360 MB) and output (10 GB) exceed L2",
+                       "replicas": world},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+            "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
+            "accuracy": acc, "pairs_refined": int(refined)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = args_()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank)
+        return
+    run_ours(a, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

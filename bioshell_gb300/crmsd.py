@@ -121,6 +121,10 @@ class Engine:
         if st != _l.BS_OK:
             raise _l.CrmsdError(st, self._lib.bs_last_error(self._h).decode())
 
+    def stream_handle(self) -> int:
+        """The engine's cudaStream_t as an integer handle."""
+        return int(self._lib.bs_ctx_stream(self._h) or 0)
+
     # -- metrics -------------------------------------------------------
     def metrics(self) -> dict:
         m = _l.bs_metrics()

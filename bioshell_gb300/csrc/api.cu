@@ -509,6 +509,8 @@ BS_API bs_status bs_ctx_trim(bs_ctx *ctx) {
   return BS_OK;
 }
 
+BS_API void *bs_ctx_stream(const bs_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
 BS_API bs_status bs_get_metrics(const bs_ctx *ctx, bs_metrics *out) {
   if (!ctx || !out) return BS_ERR_INVALID_ARG;
   *out = ctx->metrics;

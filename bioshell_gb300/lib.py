@@ -58,6 +58,7 @@ SIGNATURES = [
     ("bs_opts_init", None, [ctypes.POINTER(bs_opts)]),
     ("bs_get_metrics", ctypes.c_int32, [_vp, ctypes.POINTER(bs_metrics)]),
     ("bs_ctx_trim", ctypes.c_int32, [_vp]),
+    ("bs_ctx_stream", ctypes.c_void_p, [_vp]),
     ("bs_crmsd", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _dp]),
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,

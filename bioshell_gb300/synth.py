@@ -87,8 +87,9 @@ def random_rotations(n: int, rng: np.random.Generator) -> np.ndarray:
 
 def decoys(base: np.ndarray, n: int, rng: np.random.Generator, sigma=(0.5, 4.0),
            near_dup_frac: float = 0.0, near_dup_sigma: float = 0.01,
-           chunk: int = 8192) -> np.ndarray:
-    """n noisy, randomly placed copies of ``base`` -> [n][L][3] float64."""
+           chunk: int = 8192, return_sigma: bool = False):
+    """n noisy, randomly placed copies of ``base`` -> [n][L][3] float64
+    (and the per-decoy noise sigma when ``return_sigma``)."""
     L = base.shape[0]
     sig = rng.uniform(sigma[0], sigma[1], size=n)
     if near_dup_frac > 0.0:
@@ -103,7 +104,7 @@ def decoys(base: np.ndarray, n: int, rng: np.random.Generator, sigma=(0.5, 4.0),
         rot = random_rotations(m, rng)
         shift = rng.uniform(-50.0, 50.0, size=(m, 1, 3))
         out[s:e] = np.einsum("nkj,nij->nki", noisy, rot) + shift
-    return out
+    return (out, sig) if return_sigma else out
 
 
 @dataclass(frozen=True)
@@ -120,10 +121,11 @@ class Workload:
     def pairs(self) -> int:
         return self.n * (self.n - 1) // 2
 
-    def generate(self) -> np.ndarray:
+    def generate(self, return_sigma: bool = False):
         rng = np.random.Generator(np.random.PCG64(self.seed))
         base = base_chain(self.L, rng)
-        return decoys(base, self.n, rng, self.sigma, self.near_dup_frac, self.near_dup_sigma)
+        return decoys(base, self.n, rng, self.sigma, self.near_dup_frac, self.near_dup_sigma,
+                      return_sigma=return_sigma)
 
 
 # The workloads the crmsd engine is measured on (sizes from the project spec).

@@ -128,6 +128,9 @@ BS_API void bs_opts_init(bs_opts *opts);
 BS_API bs_status bs_get_metrics(const bs_ctx *ctx, bs_metrics *out);
 /* Releases cached device workspaces (they regrow on demand). */
 BS_API bs_status bs_ctx_trim(bs_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), so callers can order or time
+ * their own work against the engine's. */
+BS_API void *bs_ctx_stream(const bs_ctx *ctx);
 
 /* ---- crmsd ------------------------------------------------------------- */
 /* crmsd of one pair of index-matched point sets a[L][3], b[L][3]

@@ -1,0 +1,130 @@
+"""CPU checks of the mixed path's fixed-point algebra, through the library's
+host-side self-test hooks (the same crmsd_math.cuh code the kernels run).
+
+Level sums are formed here exactly (numpy int64), exactly as the tensor-core
+accumulators hold them; the fast epilogue and the exact recomputation must
+then reproduce the FP64 oracle within the engine's error budget: quantisation
+(<= sqrt(3) 2^e) plus the fast path's certified tolerance.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from bioshell_gb300 import synth
+
+TOL_FAST = 2.5e-5  # fast-path certified |dRMSD| (Angstrom)
+
+
+def _grid_exp(xs):
+    m = max(np.abs(x - x.mean(0)).max() for x in xs)
+    e = int(np.ceil(np.log2(m / (2 ** 23 - 1))))
+    while np.ldexp(2 ** 23 - 1, e) < m:
+        e += 1
+    while np.ldexp(2 ** 23 - 1, e - 1) >= m:
+        e -= 1
+    return e
+
+
+class Hooks:
+    def __init__(self, lib):
+        self.lib = lib
+
+    def digits(self, x, e):
+        L = x.shape[0]
+        d = np.zeros((3, 3, L), dtype=np.int32)
+        g, low = ctypes.c_int64(), ctypes.c_int64()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        st = self.lib.bs_selftest_digits(x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), L, e,
+                                         d.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(g),
+                                         ctypes.byref(low))
+        assert st == 0
+        return d.astype(np.int64), g.value, low.value
+
+    @staticmethod
+    def levels(da, db):
+        s = np.zeros((4, 3, 3), dtype=np.int64)
+        for x in range(3):
+            for y in range(3):
+                a, b = da[:, x, :], db[:, y, :]
+                s[0, x, y] = (a[0] * b[0]).sum()
+                s[1, x, y] = (a[0] * b[1] + a[1] * b[0]).sum()
+                s[2, x, y] = (a[0] * b[2] + a[1] * b[1] + a[2] * b[0]).sum()
+                s[3, x, y] = (a[1] * b[2] + a[2] * b[1]).sum()
+        return s
+
+    def fast(self, s, ga, gb, la, lb, e, L, tol=TOL_FAST):
+        lv = np.ascontiguousarray(s.reshape(4, 9), dtype=np.float32)
+        r, f = ctypes.c_double(), ctypes.c_int32()
+        st = self.lib.bs_selftest_epilogue(lv.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ga, gb,
+                                           float(np.sqrt(la)), float(np.sqrt(lb)), e, L, tol, ctypes.byref(r),
+                                           ctypes.byref(f))
+        assert st == 0
+        return r.value, f.value
+
+    def exact(self, da, db, e):
+        na = np.ascontiguousarray((da[0] * 65536 + da[1] * 256 + da[2]).astype(np.int32))
+        nb = np.ascontiguousarray((db[0] * 65536 + db[1] * 256 + db[2]).astype(np.int32))
+        r = ctypes.c_double()
+        p = ctypes.POINTER(ctypes.c_int32)
+        st = self.lib.bs_selftest_exact(na.ctypes.data_as(p), nb.ctypes.data_as(p), na.shape[1], e, ctypes.byref(r))
+        assert st == 0
+        return r.value
+
+
+@pytest.fixture(scope="module")
+def hooks(enginelib):
+    return Hooks(enginelib)
+
+
+def test_digits_reconstruct(hooks):
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(50, 3)) * 20
+    e = _grid_exp([x])
+    d, g, low = hooks.digits(x, e)
+    assert np.abs(d[1:]).max() <= 128 and np.abs(d[0]).max() <= 128
+    n = d[0] * 65536 + d[1] * 256 + d[2]
+    y = x - x.mean(0)
+    assert np.abs(n.T * 2.0 ** e - y).max() <= 2.0 ** (e - 1) * (1 + 1e-9)
+    assert g == int((n.astype(np.int64) ** 2).sum())
+    assert low == int((d[2] ** 2).sum())
+
+
+@pytest.mark.parametrize("L", [5, 47, 300])
+def test_fast_and_exact_paths_match_oracle(hooks, oracle_mod, L):
+    rng = np.random.default_rng(L)
+    base = synth.base_chain(L, rng)
+    xs = synth.decoys(base, 14, rng, near_dup_frac=0.25)
+    rot = synth.random_rotations(1, rng)[0]
+    xs = np.concatenate([xs, np.stack([xs[0].copy(), xs[1] @ rot.T + 3.0, xs[2] + rng.normal(size=(L, 3)) * 1e-4])])
+    e = _grid_exp(xs)
+    quant = np.sqrt(3.0) * 2.0 ** e
+    n = xs.shape[0]
+    dig = [hooks.digits(x, e) for x in xs]
+    flagged = 0
+    for i in range(n):
+        for j in range(i + 1, n):
+            ref = oracle_mod.crmsd(xs[i], xs[j])
+            da, ga, la = dig[i]
+            db, gb, lb = dig[j]
+            s = hooks.levels(da, db)
+            assert np.abs(s).max() < 2 ** 24
+            r, f = hooks.fast(s, ga, gb, la, lb, e, L)
+            rx = hooks.exact(da, db, e)
+            assert abs(rx - ref) <= quant + 1e-6, (i, j, rx, ref)
+            if f:
+                flagged += 1
+            else:
+                assert abs(r - ref) <= quant + TOL_FAST, (i, j, r, ref)
+    # exact copies and near-duplicates must be caught by the error bound
+    assert flagged >= 1
+
+
+def test_identical_structures_exact_zero(hooks):
+    rng = np.random.default_rng(9)
+    x = synth.base_chain(64, rng)
+    e = _grid_exp([x])
+    d, g, low = hooks.digits(x, e)
+    assert hooks.exact(d, d, e) == pytest.approx(0.0, abs=1e-9)
+    r, f = hooks.fast(hooks.levels(d, d), g, g, low, low, e, 64)
+    assert f == 1 or r <= 1e-4
