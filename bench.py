@@ -74,12 +74,13 @@ def tri_pairs(n, t):
 
 
 def issued_flops(n, L):
-    """Tensor-core flops the mixed kernel issues per call: every upper-
-    triangle tile of 40 x 40 structures (128 x 128 rows) runs 8 digit
-    products over the 16-padded chain length."""
-    nb = (n + 39) // 40
+    """Tensor-core flops the mixed kernel issues per call: every tile of 40 x
+    20 structures (128 x 64 rows) holding a pair i < j (column block J >= 2I)
+    runs 8 digit products over the 16-padded chain length."""
+    nba, nbb = (n + 39) // 40, (n + 19) // 20
+    tiles = sum(max(0, nbb - 2 * i) for i in range(nba))
     lp = ((L + 15) // 16) * 16
-    return nb * (nb + 1) // 2 * 2.0 * 128 * 128 * lp * 8
+    return tiles * 2.0 * 128 * 64 * lp * 8
 
 
 def host_threads():

@@ -20,7 +20,7 @@ using namespace bs;
 
 namespace {
 
-constexpr double kDefaultTol = 2.5e-5;        // Angstrom, fast-path |dRMSD| bound
+constexpr double kDefaultTol = 1e-4;  // Angstrom, certified total |dRMSD| per pair
 constexpr unsigned long long kFlagCap = 1ull << 24;  // queued exact recomputations
 
 struct DevBuf {
@@ -184,16 +184,19 @@ bs_status prep_mixed(bs_ctx *ctx, const double *dxyz, int64_t n, int L, int lp, 
                  "chain length %d too long for exact 3-digit level sums (bound not met after 8 coarsenings)", L);
 }
 
-// Upper-triangle block tiles (I <= J) in super-block order, so that the
-// tiles in flight at any time touch a working set that stays in L2.
-void build_tiles(int64_t nb, std::vector<int2> &t) {
-  const int64_t SB = 32;
+// Tensor-core tiles: row blocks I of 40 structures against column blocks J
+// of 20 structures, kept when some pair i < j falls in the tile (J >= 2I),
+// in super-block order so that the tiles in flight at any time touch a
+// working set that stays in L2.
+void build_tiles(int64_t n, std::vector<int2> &t) {
+  const int64_t nba = blocks_for(n), nbb = (n + 19) / 20;
+  const int64_t SA = 32, SBB = 64;
   t.clear();
-  t.reserve((size_t)(nb * (nb + 1) / 2));
-  for (int64_t si = 0; si < nb; si += SB)
-    for (int64_t sj = si; sj < nb; sj += SB)
-      for (int64_t I = si; I < std::min(si + SB, nb); ++I)
-        for (int64_t J = std::max(sj, I); J < std::min(sj + SB, nb); ++J) t.push_back(make_int2((int)I, (int)J));
+  for (int64_t sa = 0; sa < nba; sa += SA)
+    for (int64_t sb = 2 * sa; sb < nbb; sb += SBB)
+      for (int64_t I = sa; I < std::min(sa + SA, nba); ++I)
+        for (int64_t J = std::max(sb, 2 * I); J < std::min(sb + SBB, nbb); ++J)
+          t.push_back(make_int2((int)I, (int)J));
 }
 
 bs_status encode_maps(bs_ctx *ctx, int64_t rows, int lp, CUtensorMap *tm) {
@@ -206,12 +209,14 @@ bs_status encode_maps(bs_ctx *ctx, int64_t rows, int lp, CUtensorMap *tm) {
       return set_err(ctx, BS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable in the driver");
     ctx->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
-  for (int d = 0; d < 3; ++d) {
+  // maps 0-2: A operand boxes (64 atoms x 128 rows); 3-5: B boxes (64 x 64)
+  for (int m = 0; m < 6; ++m) {
+    const int d = m % 3;
     cuuint64_t gdim[2] = {(cuuint64_t)lp, (cuuint64_t)rows};
     cuuint64_t gstride[1] = {(cuuint64_t)lp * 2};
-    cuuint32_t box[2] = {64, 128};
+    cuuint32_t box[2] = {64, m < 3 ? 128u : 64u};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = ctx->encode(&tm[d], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ctx->dig[d].p, gdim, gstride, box, estr,
+    CUresult r = ctx->encode(&tm[m], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ctx->dig[d].p, gdim, gstride, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_err(ctx, BS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -221,6 +226,16 @@ bs_status encode_maps(bs_ctx *ctx, int64_t rows, int lp, CUtensorMap *tm) {
 
 size_t out_elems(int64_t n, int layout) {
   return layout == BS_LAYOUT_TRIANGLE ? (size_t)(n * (n - 1) / 2) : (size_t)n * (size_t)n;
+}
+
+// The quantisation grid 2^e moves each centred coordinate by <= 2^(e-1), so
+// the RMSD of the quantised pair is within sqrt(3) 2^e of the exact one; the
+// fast path gets the rest of the requested tolerance (at least 1e-6).
+double grid_bound(int scale_exp) { return sqrt(3.0) * ldexp(1.0, scale_exp); }
+float fast_tolerance(const bs_opts &o, int scale_exp) {
+  const double total = o.tolerance > 0 ? o.tolerance : kDefaultTol;
+  const double t = total - grid_bound(scale_exp);
+  return (float)(t > 1e-6 ? t : 1e-6);
 }
 
 bs_status check_device_errors(bs_ctx *ctx, DevScalars *hs) {
@@ -280,16 +295,16 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
     if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
     const int64_t nb = blocks_for(n);
-    if (ctx->tiles_nb != nb) {
+    if (ctx->tiles_nb != n) {
       std::vector<int2> t;
-      build_tiles(nb, t);
+      build_tiles(n, t);
       if ((s = ensure(ctx, ctx->tiles, t.size() * sizeof(int2), "tile table"))) return s;
       CK(cudaMemcpy(ctx->tiles.p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice), "upload tile table");
-      ctx->tiles_nb = nb;
+      ctx->tiles_nb = n;
       ctx->tiles_count = (int64_t)t.size();
     }
     if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
-    CUtensorMap tm[3];
+    CUtensorMap tm[6];
     if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
     TcArgs a{};
     a.tiles = static_cast<const int2 *>(ctx->tiles.p);
@@ -300,7 +315,7 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
     a.ghat = static_cast<const long long *>(ctx->ghat.p);
     a.low = static_cast<const float *>(ctx->low.p);
     a.sc = static_cast<DevScalars *>(ctx->scal.p);
-    a.tol = (float)(o.tolerance > 0 ? o.tolerance : kDefaultTol);
+    a.tol = fast_tolerance(o, hs.scale_exp);
     a.out = od;
     a.flags = static_cast<unsigned long long *>(ctx->flags.p);
     a.flag_cap = kFlagCap;
@@ -325,7 +340,7 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
     CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
     ctx->metrics.pairs_refined = (int64_t)hs.flag_count;
     ctx->metrics.scale_exp = hs.scale_exp;
-    ctx->metrics.quant_bound = sqrt(3.0) * ldexp(1.0, hs.scale_exp);
+    ctx->metrics.quant_bound = grid_bound(hs.scale_exp);  // |dRMSD| from the grid
     ctx->metrics.main_launches = 5 + (hs.flag_count > kFlagCap ? 1 : 0);
   }
   if (!out_dev) {
@@ -393,7 +408,7 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
                           static_cast<const __nv_bfloat16 *>(ctx->dig[1].p),
                           static_cast<const __nv_bfloat16 *>(ctx->dig[2].p), lp, L,
                           static_cast<const long long *>(ctx->ghat.p), static_cast<const float *>(ctx->low.p),
-                          static_cast<DevScalars *>(ctx->scal.p), (float)(o.tolerance > 0 ? o.tolerance : kDefaultTol),
+                          static_cast<DevScalars *>(ctx->scal.p), fast_tolerance(o, hs.scale_exp),
                           dii, djj, np, dout, levels_dbg, ctx->stream),
        "mixed pairs");
   }
@@ -407,6 +422,7 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
   if ((s = check_device_errors(ctx, &hs))) return s;
   ctx->metrics.pairs = np;
   ctx->metrics.scale_exp = hs.scale_exp;
+  if (o.precision == BS_PRECISION_MIXED) ctx->metrics.quant_bound = grid_bound(hs.scale_exp);
   ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
   ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
   ctx->metrics.ms_main = elapsed(ctx, 2, 3);
@@ -609,26 +625,29 @@ BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n,
   DevScalars hs{};
   if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
   const int64_t nb = blocks_for(n);
-  const int2 first = make_int2(0, 0);
-  if ((s = ensure(ctx, ctx->tiles, sizeof(int2), "tile table"))) return s;
-  CK(cudaMemcpy(ctx->tiles.p, &first, sizeof(int2), cudaMemcpyHostToDevice), "upload tile");
+  const int2 first[2] = {make_int2(0, 0), make_int2(0, 1)};
+  if ((s = ensure(ctx, ctx->tiles, sizeof(first), "tile table"))) return s;
+  CK(cudaMemcpy(ctx->tiles.p, first, sizeof(first), cudaMemcpyHostToDevice), "upload tiles");
   ctx->tiles_nb = -1;  // the cached table was replaced
   const size_t nout = (size_t)n * (size_t)(n > 1 ? n - 1 : 1) / 2 + 1;
   if ((s = ensure(ctx, ctx->out, nout * 8, "result buffer"))) return s;
   if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
   if ((s = ensure(ctx, ctx->pout, (size_t)4 * 128 * 128 * sizeof(float), "level dump"))) return s;
-  CUtensorMap tm[3];
+  CK(cudaMemsetAsync(ctx->pout.p, 0, (size_t)4 * 128 * 128 * sizeof(float), ctx->stream), "clear level dump");
+  CUtensorMap tm[6];
   if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
   TcArgs a{};
   a.tiles = static_cast<const int2 *>(ctx->tiles.p);
-  a.ntiles = 1;
+  a.ntiles = (n > 20) ? 2 : 1;
   a.n = n;
   a.L = L;
   a.lp = lp;
   a.ghat = static_cast<const long long *>(ctx->ghat.p);
   a.low = static_cast<const float *>(ctx->low.p);
   a.sc = static_cast<DevScalars *>(ctx->scal.p);
-  a.tol = (float)kDefaultTol;
+  bs_opts dflt;
+  bs_opts_init(&dflt);
+  a.tol = fast_tolerance(dflt, hs.scale_exp);
   a.out = OutDesc{ctx->out.p, n, BS_LAYOUT_TRIANGLE, BS_OUT_F64};
   a.flags = static_cast<unsigned long long *>(ctx->flags.p);
   a.flag_cap = kFlagCap;
@@ -673,7 +692,7 @@ BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_
     for (int d = 0; d < 3; ++d) {
       const double y = ldexp(xyz[3 * k + d] - c[d], -scale_exp);
       const double r = nearbyint(y);
-      if (!(fabs(r) < 8388608.0)) return BS_ERR_UNSUPPORTED;
+      if (!(fabs(r) < 4194304.0)) return BS_ERR_UNSUPPORTED;
       const int q = (int)r;
       int a, b, e;
       bsm::split_digits(q, a, b, e);
@@ -681,7 +700,7 @@ BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_
       digits[(1 * 3 + d) * L + k] = b;
       digits[(2 * 3 + d) * L + k] = e;
       g += (long long)q * q;
-      low += (long long)e * e;
+      low += (long long)(e / 16) * (e / 16);
     }
   *g_exact = g;
   *low_norm2 = low;
@@ -703,7 +722,7 @@ BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t g
   in.low_a = (float)low_a;
   in.low_b = (float)low_b;
   int f = 0;
-  const float r = bsm::pair_rmsd_fast(in, scale_exp, L, (float)(tolerance > 0 ? tolerance : kDefaultTol), f);
+  const float r = bsm::pair_rmsd_fast(in, scale_exp, L, (float)(tolerance > 0 ? tolerance : 2.5e-5), f);
   *rmsd = (double)r;
   *flag = f;
   return BS_OK;

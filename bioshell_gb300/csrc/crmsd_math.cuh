@@ -3,15 +3,17 @@
 // __device__).
 //
 // Notation (one pair of structures a, b with L index-matched atoms):
-//   centred coordinates are quantised to integers n = rint(y / 2^e);
-//   n = d0 * 2^16 + d1 * 2^8 + d2 with balanced digits |d1|,|d2| <= 128,
-//   |d0| <= 128; every digit is exact in bf16.
+//   centred coordinates are quantised to integers n = rint(y / 2^e),
+//   |n| < 2^22, and split into balanced digits
+//       n = d0 2^14 + d1 2^5 + d2,   |d0| <= 256, |d1| <= 256, |d2| <= 16,
+//   stored as the bf16 values e0 = d0, e1 = d1, e2 = 16 d2 (all exact in bf16),
+//   so that n = 2^14 (e0 + 2^-9 e1 + 2^-18 e2): three digits one 2^9 step apart.
 //   S_l[x][y]  level sums of digit products, l = i + j:
-//     S0 = sum d0a d0b                    S1 = sum d0a d1b + d1a d0b
-//     S2 = sum d0a d2b + d1a d1b + d2a d0b S3 = sum d1a d2b + d2a d1b
-//   (the level-4 term sum d2a d2b is dropped; its effect on E is bounded
-//   by 2 sqrt(3) sqrt(N2a N2b), N2 = sum of squared lowest digits).
-//   Mhat = 2^32 S0 + 2^24 S1 + 2^16 S2 + 2^8 S3          (units u = 2^(2e))
+//     S0 = sum e0a e0b                    S1 = sum e0a e1b + e1a e0b
+//     S2 = sum e0a e2b + e1a e1b + e2a e0b S3 = sum e1a e2b + e2a e1b
+//   (the level-4 term sum e2a e2b = 256 sum d2a d2b is dropped; its effect on
+//   E is bounded by 2 sqrt(3) sqrt(N2a N2b), N2 = sum of d2^2).
+//   Mhat = 2^28 S0 + 2^19 S1 + 2^10 S2 + 2 S3            (units u = 2^(2e))
 //   Ghat = sum n^2 (exact)                               (units u)
 //   K(S) 4x4 quaternion key matrix, lambda0 = (Ga + Gb)/2,
 //   E = Ga + Gb - 2 lambda_max(K) = 2 min_q q'(lambda0 I - K)q / |q|^2,
@@ -30,6 +32,14 @@
 #define BS_HD __host__ __device__ __forceinline__
 #else
 #define BS_HD static inline
+#endif
+
+// Division where a few ulps do not matter (Halley steps, normalisations):
+// the device uses the fast reciprocal-based divide, the host plain IEEE.
+#if defined(__CUDA_ARCH__)
+#define BS_FDIV(a, b) __fdividef((a), (b))
+#else
+#define BS_FDIV(a, b) ((a) / (b))
 #endif
 
 namespace bsm {
@@ -111,15 +121,19 @@ BS_HD float qcp_top_eig(const float s[9], float &xout, float q[4]) {
   const float c2 = -2.f * fro2;
   const float c1 = -8.f * det3f(s);
   const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
+  // Halley iterations from the upper bound x = 1 (the largest root is <= 1
+  // and P is convex above it); five steps reach FP32 precision for every
+  // root in (0, 1] met in practice, and a fixed count keeps warps converged.
   float x = 1.0f;
-  for (int it = 0; it < 32; ++it) {
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
     const float x2 = x * x;
     const float p = fmaf(fmaf(x2 + c2, x, c1), x, c0);  // ((x^2+c2)x + c1)x + c0
     const float dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
-    if (!(dp > 0.f)) break;  // guards 0 and NaN
-    const float dx = p / dp;
-    x -= dx;
-    if (fabsf(dx) <= 3e-7f * fabsf(x) + 1e-30f) break;
+    const float ddp = fmaf(12.f, x2, 2.f * c2);
+    const float den = fmaf(2.f * dp, dp, -p * ddp);
+    const float step = BS_FDIV(2.f * p * dp, den);
+    x = (den > 0.f) ? x - step : x;
   }
   xout = x;
   const float b00 = k.k00 - x, b11 = k.k11 - x, b22 = k.k22 - x, b33 = k.k33 - x;
@@ -200,23 +214,24 @@ BS_HD float i128_to_f32(__int128 v) {
 // The fast path runs in three phases so that the tensor-core epilogue can
 // stream one TMEM level accumulator at a time:
 //   1. fast_begin: FP32 covariance m (from all levels) -> FP32 QCP eigenpair,
-//      split of the eigenvector q = q_h + q_l with q_h on the 2^-11 grid,
-//      exact integer T(Q_h), and the small FP32 terms 4 B(q_h,q_l) + 2 F(q_l);
+//      unit eigenvector split q = q_h + q_l with q_h on the 2^-15 grid
+//      (Q_h = 2^15 q_h integers, |T(Q_h)| <= |Q_h|^2 <= 2^30), exact integer
+//      T(Q_h), and the small FP32 terms 4 B(q_h,q_l) + 2 F(q_l);
 //   2. fast_level (l = 0..3): U_l += sum_xy T_xy S_l,xy, exactly in int64 for
 //      l = 0, 1, 2 and in FP32 for l = 3;
 //   3. fast_finish: 2 F(q_h) exactly in int128, E = 2 F(q) / |q|^2, RMSD and
 //      the error bound that decides whether the pair is recomputed.
-// m is the covariance in units of 2^32 u:  m = S0 + 2^-8 S1 + 2^-16 S2 + 2^-24 S3.
+// m is the covariance in units of 2^28 u:  m = S0 + 2^-9 S1 + 2^-18 S2 + 2^-27 S3.
 BS_HD float m_from_levels(float s0, float s1, float s2, float s3) {
-  return fmaf(s3, 5.9604644775390625e-8f, fmaf(s2, 1.52587890625e-5f, fmaf(s1, 0.00390625f, s0)));
+  return fmaf(s3, 7.450580596923828125e-9f, fmaf(s2, 3.814697265625e-6f, fmaf(s1, 0.001953125f, s0)));
 }
 
 struct FastState {
   int T[9];
   long long U0, U1, U2;
   float U3;
-  float rest;  // 4 B(q_h,q_l) + 2 F(q_l), units 2^32 u
-  float qq;    // |q|^2 of the normalised eigenvector (max component 1)
+  float rest;  // 4 B(q_h,q_l) + 2 F(q_l), units 2^28 u
+  float qq;    // |q|^2 of the (unit) eigenvector as represented
   int q2;      // |Q_h|^2
   int flag;    // 1: degenerate eigenvector, recompute exactly
 };
@@ -231,27 +246,27 @@ BS_HD void fast_begin(const float m[9], long long gsum, FastState &st) {
 #pragma unroll
   for (int i = 0; i < 9; ++i) st.T[i] = 0;
   if (gsum <= 0) return;  // both structures collapse onto one point: E = 0
-  const float lam0 = (float)gsum * 1.16415321826934814453125e-10f;  // 2^-33
-  const float inv = 1.0f / lam0;
+  const float lam0 = (float)gsum * 1.862645149230957e-9f;  // gsum / 2 in units 2^28 u: 2^-29
+  const float inv = BS_FDIV(1.0f, lam0);
   float sn[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
   float x, q[4];
   const float cof = qcp_top_eig(sn, x, q);
-  const float qa = fmaxf(fmaxf(fabsf(q[0]), fabsf(q[1])), fmaxf(fabsf(q[2]), fabsf(q[3])));
-  if (!(qa > 1e-30f) || !(cof > 1e-6f)) {
+  const float qsq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  if (!(qsq > 1e-30f) || !(cof > 1e-6f)) {
     st.flag = 1;
     return;
   }
-  const float qs = 1.0f / qa;
+  const float qs = rsqrtf(qsq) * 0.99999f;  // unit length (a hair below, so |Q_h|^2 <= 2^30)
   float qn[4], qh[4], ql[4];
   int Q[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     qn[i] = q[i] * qs;
-    const float h = rintf(qn[i] * 2048.f);
+    const float h = rintf(qn[i] * 32768.f);
     Q[i] = (int)h;
-    qh[i] = h * 4.8828125e-4f;  // 2^-11
+    qh[i] = h * 3.0517578125e-5f;  // 2^-15
     ql[i] = qn[i] - qh[i];
   }
   t_of_q<int>(Q, st.T);
@@ -294,19 +309,20 @@ BS_HD float fast_finish(const FastState &st, long long gsum, float low_a, float 
                         float tol, int &flag) {
   flag = st.flag;
   if (gsum <= 0 || st.flag) return 0.f;
-  // 2 F(q_h) 2^22 in units u = gsum |Q_h|^2 - 2 (2^32 U0 + 2^24 U1 + 2^16 U2 + 2^8 U3)
+  // 2 F(q_h) 2^30 in units u = gsum |Q_h|^2 - 2 (2^28 U0 + 2^19 U1 + 2^10 U2 + 2 U3)
   __int128 c = (__int128)gsum * (__int128)st.q2;
-  c -= ((__int128)st.U0 << 33) + ((__int128)st.U1 << 25) + ((__int128)st.U2 << 17);
-  const float twoFh = (i128_to_f32(c) - 512.f * st.U3) * 2.384185791015625e-7f;  // 2^-22 -> u
-  const float twoF = twoFh + st.rest * 4294967296.0f;                             // 2^32 -> u
-  const float e_u = twoF / st.qq;
+  c -= ((__int128)st.U0 << 29) + ((__int128)st.U1 << 20) + ((__int128)st.U2 << 11);
+  const float twoFh = (i128_to_f32(c) - 4.f * st.U3) * 9.313225746154785e-10f;  // 2^-30 -> u
+  const float twoF = twoFh + st.rest * 268435456.0f;                              // 2^28 -> u
+  const float e_u = BS_FDIV(twoF, st.qq);
   const float u = ldexpf(1.0f, 2 * scale_exp);  // Angstrom^2 per unit
   const float e_a2 = fmaxf(e_u, 0.f) * u;
-  const float rmsd = sqrtf(e_a2 / (float)L);
+  const float rmsd = sqrtf(BS_FDIV(e_a2, (float)L));
   // error bound on E: dropped level 4 (Weyl: 2 sqrt(3) sqrt(N2a N2b)) plus
-  // the FP32 arithmetic of the fast path (<= 2^-28 lambda0)
+  // the FP32 arithmetic of the fast path: rounding of m and of the bilinear
+  // sum against |q_l| <= 2^-15 stays below 2^-32.8 (Ga+Gb); bounded by 2^-32
   const float d4 = 3.4641016f * low_a * low_b;
-  const float darith = (float)gsum * 1.862645149230957e-9f;  // 2^-29 (Ga+Gb)
+  const float darith = (float)gsum * 2.3283064365386963e-10f;  // 2^-32 (Ga+Gb)
   const float de_a2 = (d4 + darith) * u;
   const float elo = fmaxf(e_a2 - de_a2, 0.f);
   // |dRMSD| <= dE / (sqrt(L) sqrt(E_lo)): recompute when dE^2 > tol^2 L E_lo
@@ -448,12 +464,18 @@ BS_HD double pair_rmsd_exact(const long long mh[9], long long ga, long long gb, 
 }
 
 // ------------------------------------------------------------- digits
-// Balanced base-256 digits of a quantised coordinate |n| < 2^23.
-BS_HD void split_digits(int n, int &d0, int &d1, int &d2) {
-  d2 = ((n + 128) & 255) - 128;
-  const int n1 = (n - d2) >> 8;
-  d1 = ((n1 + 128) & 255) - 128;
-  d0 = (n1 - d1) >> 8;
+// Balanced digits of a quantised coordinate |n| < 2^22:
+//   n = d0 2^14 + d1 2^5 + d2,  d2 in [-16, 15], d1 in [-256, 255], |d0| <= 256;
+// returned as the stored values e0 = d0, e1 = d1, e2 = 16 d2.
+BS_HD void split_digits(int n, int &e0, int &e1, int &e2) {
+  const int d2 = ((n + 16) & 31) - 16;
+  const int n1 = (n - d2) >> 5;
+  e1 = ((n1 + 256) & 511) - 256;
+  e0 = (n1 - e1) >> 9;
+  e2 = 16 * d2;
 }
+
+// The quantised coordinate back from its stored digits.
+BS_HD int join_digits(int e0, int e1, int e2) { return e0 * 16384 + e1 * 32 + (e2 >> 4); }
 
 }  // namespace bsm

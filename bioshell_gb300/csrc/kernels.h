@@ -12,8 +12,9 @@ namespace bs {
 // Digit matrices: one row per (structure, coordinate), `lp` bf16 columns
 // (atoms, zero padded to a multiple of 16).  Structures are packed ten to a
 // 32-row group (rows 30 and 31 of each group are zero), four groups to a
-// 128-row block, so that a tensor-core tile of 128 rows holds 40 whole
-// structures and each structure's three rows sit in one warp's TMEM lanes.
+// 128-row block, so that a tensor-core A tile of 128 rows holds 40 whole
+// structures (B tiles: 64 rows, 20 structures) and each structure's three
+// rows sit in one warp's TMEM lanes.
 constexpr int kGroupRows = 32;
 constexpr int kGroupStructs = 10;
 constexpr int kBlockRows = 128;
@@ -81,7 +82,8 @@ struct TcArgs {
   float *dbg;  // optional dump of the first tile's raw level sums
   int num_sms;
 };
-cudaError_t launch_mixed_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t st);
+cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [6]: A digits 0-2, B digits 0-2 */, const TcArgs &a,
+                            cudaStream_t st);
 size_t mixed_tc_smem_bytes();
 
 // refine.cu

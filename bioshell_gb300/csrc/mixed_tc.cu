@@ -1,29 +1,30 @@
 // mixed_tc.cu -- all-vs-all crmsd on tcgen05 tensor cores (sm_103a).
 //
-// The per-pair 3x3 covariances of a 40 x 40 block of structures are the
-// 3x3 blocks of one 128 x 128 tile of X X^T, where X holds a row per
+// The per-pair 3x3 covariances of a 40 x 20 block of structures are the
+// 3x3 blocks of one 128 x 64 tile of X X^T, where X holds a row per
 // (structure, coordinate) and a column per atom (layout in kernels.h).  X is
 // split into three exact bf16 digit matrices D0, D1, D2 (prep.cu); per
 // 16-atom step the kernel issues the eight digit products of levels 0..3
 //     L0 += D0 D0'   L1 += D0 D1' + D1 D0'
 //     L2 += D0 D2' + D1 D1' + D2 D0'   L3 += D1 D2' + D2 D1'
-// into four FP32 accumulators in TMEM (4 x 128 columns).  Every partial sum
-// is an integer below 2^24, so the accumulation is exact.
+// into four FP32 accumulators of 128 lanes x 64 columns in TMEM.  Every
+// partial sum is an integer below 2^24, so the accumulation is exact.  TMEM
+// holds two such accumulator sets, so the epilogue of one tile overlaps the
+// MMAs of the next.
 //
-// Roles (one persistent CTA per SM, 256 threads):
-//   warp 0  TMA producer: 6 boxes (A and B digits, 128 rows x 64 atoms,
-//           128-byte swizzle) per stage, 2 stages;
-//   warp 1  MMA issuer (one thread), tcgen05.mma kind::f16, M = N = 128;
-//   warp 2  TMEM allocation;
-//   warps 4-7  epilogue: each warp owns 32 TMEM lanes = 10 row structures;
-//           per 10-structure column group it stages one level at a time in
-//           shared memory, the thread of coordinate x of structure i finishes
-//           pairs (i, j) with j = x mod 3 through the three phases of
-//           crmsd_math.cuh, and writes the result.
+// Roles (one persistent CTA per SM, 384 threads):
+//   warp 0  TMA producer: A digits (128 rows x 64 atoms) and B digits (64
+//           rows x 64 atoms), 128-byte swizzle, 2 stages;
+//   warp 1  MMA issuer (one thread), tcgen05.mma kind::f16, M = 128, N = 64;
+//   warp 2  TMEM allocation (512 columns);
+//   warps 4-11  epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 (10 row
+//           structures) and column group (w - 4) / 4 (10 column structures);
+//           it stages one level at a time in shared memory, the thread of
+//           coordinate x of structure i finishes pairs (i, j) with
+//           j = x mod 3 through the three phases of crmsd_math.cuh, and
+//           writes the result.
 // Every mbarrier wait is bounded; a timeout sets an error bit and all roles
 // leave their loops so the block always reaches TMEM deallocation.
-#include <stdio.h>
-
 #include "crmsd_math.cuh"
 #include "kernels.h"
 #include "ptx.cuh"
@@ -32,24 +33,27 @@ namespace bs {
 namespace {
 
 constexpr int kStages = 2;
-constexpr int kKChunk = 64;                         // atoms per 128-byte swizzle row
-constexpr int kOpBytes = kBlockRows * kKChunk * 2;  // one operand box: 16 KB
-constexpr int kStageBytes = 6 * kOpBytes;           // A0 A1 A2 B0 B1 B2
-constexpr int kThreads = 256;
+constexpr int kKChunk = 64;                              // atoms per 128-byte swizzle row
+constexpr int kBRows = 64;                               // B tile rows = 20 structures
+constexpr int kAOpBytes = kBlockRows * kKChunk * 2;      // 16 KB
+constexpr int kBOpBytes = kBRows * kKChunk * 2;          // 8 KB
+constexpr int kStageBytes = 3 * kAOpBytes + 3 * kBOpBytes;
+constexpr int kThreads = 384;
 constexpr int kEpiWarp0 = 4;
-constexpr int kTmemCols = 512;
-constexpr int kPitch = 33;  // epilogue staging pitch in floats (bank-conflict free row writes)
-constexpr int kEpiStageBytes = 4 * 32 * kPitch * 4;
+constexpr int kEpiWarps = 8;
+constexpr int kTmemCols = 512;                           // 2 buffers x 4 levels x 64 columns
+constexpr int kPitch = 33;                               // staging pitch in floats
+constexpr int kEpiStageBytes = kEpiWarps * 32 * kPitch * 4;
 constexpr int kBarBytes = 256;
 constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kBarBytes;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
-constexpr uint32_t kIdesc = ptx::idesc_bf16_f32(128, 128);
+constexpr uint32_t kIdesc = ptx::idesc_bf16_f32(128, kBRows);
 
 struct Shared {
   uint64_t full[kStages];
   uint64_t empty[kStages];
-  uint64_t tfull;
-  uint64_t tempty;
+  uint64_t tfull[2];
+  uint64_t tempty[2];
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -81,8 +85,9 @@ __device__ __forceinline__ void fail(Shared *sh, DevScalars *sc) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    k_mixed_tc(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
-               const __grid_constant__ CUtensorMap tm2, TcArgs a) {
+    k_mixed_tc(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
+               const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
+               const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2, TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   float *stage_epi = reinterpret_cast<float *>(smem + (size_t)kStages * kStageBytes);
@@ -97,14 +102,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       ptx::mbar_init(&sh->full[s], 1);
       ptx::mbar_init(&sh->empty[s], 1);
     }
-    ptx::mbar_init(&sh->tfull, 1);
-    ptx::mbar_init(&sh->tempty, 128);
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&sh->tfull[b], 1);
+      ptx::mbar_init(&sh->tempty[b], kEpiWarps * 32);
+    }
     ptx::mbar_init(&sh->drain, 1);
     sh->abort = 0;
     ptx::fence_mbar_init();
-    ptx::prefetch_tmap(&tm0);
-    ptx::prefetch_tmap(&tm1);
-    ptx::prefetch_tmap(&tm2);
+    ptx::prefetch_tmap(&ta0);
+    ptx::prefetch_tmap(&ta1);
+    ptx::prefetch_tmap(&ta2);
+    ptx::prefetch_tmap(&tb0);
+    ptx::prefetch_tmap(&tb1);
+    ptx::prefetch_tmap(&tb2);
   }
   if (warp == 2) {
     ptx::tmem_alloc(&sh->tmem_base, kTmemCols);
@@ -122,7 +132,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t it = 0;
       for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
         const int2 tile = a.tiles[t];
-        const int rowA = tile.x * kBlockRows, rowB = tile.y * kBlockRows;
+        const int rowA = tile.x * kBlockRows, rowB = tile.y * kBRows;
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
@@ -133,12 +143,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           ptx::mbar_arrive_expect_tx(&sh->full[s], kStageBytes);
           uint8_t *st = smem + (size_t)s * kStageBytes;
           const int k0 = kc * kKChunk;
-          ptx::tma_load_2d(st + 0 * kOpBytes, &tm0, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 1 * kOpBytes, &tm1, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 2 * kOpBytes, &tm2, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 3 * kOpBytes, &tm0, k0, rowB, &sh->full[s]);
-          ptx::tma_load_2d(st + 4 * kOpBytes, &tm1, k0, rowB, &sh->full[s]);
-          ptx::tma_load_2d(st + 5 * kOpBytes, &tm2, k0, rowB, &sh->full[s]);
+          ptx::tma_load_2d(st + 0 * kAOpBytes, &ta0, k0, rowA, &sh->full[s]);
+          ptx::tma_load_2d(st + 1 * kAOpBytes, &ta1, k0, rowA, &sh->full[s]);
+          ptx::tma_load_2d(st + 2 * kAOpBytes, &ta2, k0, rowA, &sh->full[s]);
+          ptx::tma_load_2d(st + 3 * kAOpBytes + 0 * kBOpBytes, &tb0, k0, rowB, &sh->full[s]);
+          ptx::tma_load_2d(st + 3 * kAOpBytes + 1 * kBOpBytes, &tb1, k0, rowB, &sh->full[s]);
+          ptx::tma_load_2d(st + 3 * kAOpBytes + 2 * kBOpBytes, &tb2, k0, rowB, &sh->full[s]);
         }
       }
       // let the stages still in flight land before the block can retire
@@ -153,11 +163,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       // ------------------------------------------------------- MMA issuer
       uint32_t it = 0, tt = 0;
       for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
-        if (!ptx::mbar_wait(&sh->tempty, (tt & 1u) ^ 1u, abort, kTimeoutNs)) {
+        const uint32_t buf = tt & 1u, use = tt >> 1;
+        if (!ptx::mbar_wait(&sh->tempty[buf], (use & 1u) ^ 1u, abort, kTimeoutNs)) {
           fail(sh, a.sc);
           break;
         }
         ptx::tc_fence_after();
+        const uint32_t acc0 = tmem + buf * 256u;
         bool ok = true;
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
@@ -169,29 +181,30 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           ptx::tc_fence_after();
           const uint32_t base = ptx::smem_u32(smem + (size_t)s * kStageBytes);
+          const uint32_t bbase = base + 3 * kAOpBytes;
           const int ksteps = min(4, nk16 - kc * 4);
           for (int kk = 0; kk < ksteps; ++kk) {
             const uint32_t off = (uint32_t)kk * 32u;
-            const uint64_t da0 = ptx::smem_desc_sw128(base + 0 * kOpBytes + off);
-            const uint64_t da1 = ptx::smem_desc_sw128(base + 1 * kOpBytes + off);
-            const uint64_t da2 = ptx::smem_desc_sw128(base + 2 * kOpBytes + off);
-            const uint64_t db0 = ptx::smem_desc_sw128(base + 3 * kOpBytes + off);
-            const uint64_t db1 = ptx::smem_desc_sw128(base + 4 * kOpBytes + off);
-            const uint64_t db2 = ptx::smem_desc_sw128(base + 5 * kOpBytes + off);
+            const uint64_t da0 = ptx::smem_desc_sw128(base + 0 * kAOpBytes + off);
+            const uint64_t da1 = ptx::smem_desc_sw128(base + 1 * kAOpBytes + off);
+            const uint64_t da2 = ptx::smem_desc_sw128(base + 2 * kAOpBytes + off);
+            const uint64_t db0 = ptx::smem_desc_sw128(bbase + 0 * kBOpBytes + off);
+            const uint64_t db1 = ptx::smem_desc_sw128(bbase + 1 * kBOpBytes + off);
+            const uint64_t db2 = ptx::smem_desc_sw128(bbase + 2 * kBOpBytes + off);
             const uint32_t acc = (kc | kk) ? 1u : 0u;
-            ptx::tc_mma_f16(tmem + 0 * 128, da0, db0, kIdesc, acc);
-            ptx::tc_mma_f16(tmem + 1 * 128, da0, db1, kIdesc, acc);
-            ptx::tc_mma_f16(tmem + 1 * 128, da1, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(tmem + 2 * 128, da0, db2, kIdesc, acc);
-            ptx::tc_mma_f16(tmem + 2 * 128, da1, db1, kIdesc, 1u);
-            ptx::tc_mma_f16(tmem + 2 * 128, da2, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(tmem + 3 * 128, da1, db2, kIdesc, acc);
-            ptx::tc_mma_f16(tmem + 3 * 128, da2, db1, kIdesc, 1u);
+            ptx::tc_mma_f16(acc0 + 0 * 64, da0, db0, kIdesc, acc);
+            ptx::tc_mma_f16(acc0 + 1 * 64, da0, db1, kIdesc, acc);
+            ptx::tc_mma_f16(acc0 + 1 * 64, da1, db0, kIdesc, 1u);
+            ptx::tc_mma_f16(acc0 + 2 * 64, da0, db2, kIdesc, acc);
+            ptx::tc_mma_f16(acc0 + 2 * 64, da1, db1, kIdesc, 1u);
+            ptx::tc_mma_f16(acc0 + 2 * 64, da2, db0, kIdesc, 1u);
+            ptx::tc_mma_f16(acc0 + 3 * 64, da1, db2, kIdesc, acc);
+            ptx::tc_mma_f16(acc0 + 3 * 64, da2, db1, kIdesc, 1u);
           }
           ptx::tc_commit(&sh->empty[s]);
         }
         if (!ok) break;
-        ptx::tc_commit(&sh->tfull);
+        ptx::tc_commit(&sh->tfull[buf]);
       }
       // all MMAs of this thread complete before teardown
       ptx::tc_commit(&sh->drain);
@@ -201,105 +214,106 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
   } else if (warp >= kEpiWarp0) {
     // ---------------------------------------------------------- epilogue
-    const int qd = warp & 3;  // TMEM lane quarter of this warp
-    float *stg = stage_epi + qd * 32 * kPitch;
+    const int qd = warp & 3;                // TMEM lane quarter of this warp
+    const int g = (warp - kEpiWarp0) >> 2;  // column group (10 structures)
+    float *stg = stage_epi + (warp - kEpiWarp0) * 32 * kPitch;
     const int il = lane / 3, x = lane - 3 * (lane / 3);
     const int ilr = il < kGroupStructs ? il : kGroupStructs - 1;  // pad lanes read a valid row
-    const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * g;
     const int scale_exp = a.sc->scale_exp;
     uint32_t tt = 0;
     for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++tt) {
-      if (!ptx::mbar_wait(&sh->tfull, tt & 1u, abort, kTimeoutNs)) {
+      const uint32_t buf = tt & 1u, use = tt >> 1;
+      if (!ptx::mbar_wait(&sh->tfull[buf], use & 1u, abort, kTimeoutNs)) {
         fail(sh, a.sc);
         break;
       }
       ptx::tc_fence_after();
       const int2 tile = a.tiles[t];
+      const uint32_t col0 = lane_base + buf * 256u;
       const int64_t i = (int64_t)tile.x * kBlockStructs + qd * kGroupStructs + il;
       const bool row_ok = (lane < 30) && (i < a.n);
       const long long ga = row_ok ? a.ghat[i] : 0;
       const float lowa = row_ok ? a.low[i] : 0.f;
-      const bool dump = (a.dbg != nullptr) && (t == 0);
-#pragma unroll 1
-      for (int g = 0; g < 4; ++g) {
-        // ---- pass A: FP32 covariance rows of this group, staged per lane
-        {
-          float m[32], v[32];
-          ptx::tmem_ld_32x32b_x32(lane_base + 0 * 128 + 32 * g, m);
-          ptx::tmem_ld_32x32b_x32(lane_base + 1 * 128 + 32 * g, v);
+      const bool dump = (a.dbg != nullptr) && (tile.x == 0) && (tile.y < 2);
+      // ---- pass A: FP32 covariance rows of this group, staged per lane
+      {
+        float m[32], v[32];
+        ptx::tmem_ld_32x32b_x32(col0 + 0 * 64, m);
+        ptx::tmem_ld_32x32b_x32(col0 + 1 * 64, v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.00390625f, m[c]);
-          ptx::tmem_ld_32x32b_x32(lane_base + 2 * 128 + 32 * g, v);
+        for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);  // 2^-9
+        ptx::tmem_ld_32x32b_x32(col0 + 2 * 64, v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 1.52587890625e-5f, m[c]);
-          ptx::tmem_ld_32x32b_x32(lane_base + 3 * 128 + 32 * g, v);
+        for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 3.814697265625e-6f, m[c]);  // 2^-18
+        ptx::tmem_ld_32x32b_x32(col0 + 3 * 64, v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 5.9604644775390625e-8f, m[c]);
+        for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 7.450580596923828125e-9f, m[c]);  // 2^-27
 #pragma unroll
-          for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = m[c];
+        for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = m[c];
+      }
+      __syncwarp();
+      bsm::FastState st[4];
+      int64_t jj[4];
+      bool valid[4];
+#pragma unroll
+      for (int sl = 0; sl < 4; ++sl) {
+        const int jl = 3 * sl + x;  // owned column structure (0..11, valid < 10)
+        const int jc = jl < 10 ? jl : 9;
+        jj[sl] = (int64_t)tile.y * 20 + g * kGroupStructs + jl;
+        valid[sl] = row_ok && (jl < 10) && (jj[sl] < a.n) && (jj[sl] > i);
+        float m9[9];
+#pragma unroll
+        for (int xr = 0; xr < 3; ++xr)
+#pragma unroll
+          for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+        bsm::fast_begin(m9, valid[sl] ? ga + a.ghat[jj[sl]] : 0, st[sl]);
+      }
+      __syncwarp();
+      // ---- pass B: exact level sums, one level at a time
+#pragma unroll
+      for (int lv = 0; lv < 4; ++lv) {
+        float v[32];
+        ptx::tmem_ld_32x32b_x32(col0 + lv * 64, v);
+        if (dump) {
+          float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * tile.y + 32 * g;
+#pragma unroll
+          for (int c = 0; c < 32; ++c) drow[c] = v[c];
         }
+#pragma unroll
+        for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = v[c];
         __syncwarp();
-        bsm::FastState st[4];
-        int64_t jj[4];
-        bool valid[4];
 #pragma unroll
         for (int sl = 0; sl < 4; ++sl) {
-          const int jl = 3 * sl + x;  // owned column structure (0..11, valid < 10)
+          const int jl = 3 * sl + x;
           const int jc = jl < 10 ? jl : 9;
-          jj[sl] = (int64_t)tile.y * kBlockStructs + g * kGroupStructs + jl;
-          valid[sl] = row_ok && (jl < 10) && (jj[sl] < a.n) && (jj[sl] > i);
-          float m9[9];
+          float s9[9];
 #pragma unroll
           for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
-          bsm::fast_begin(m9, valid[sl] ? ga + a.ghat[jj[sl]] : 0, st[sl]);
+            for (int y = 0; y < 3; ++y) s9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+          bsm::fast_level(st[sl], lv, s9);
         }
         __syncwarp();
-        // ---- pass B: exact level sums, one level at a time
+      }
+      // all TMEM reads of this buffer are done: hand it back to the MMA warp
+      ptx::tc_fence_before();
+      ptx::mbar_arrive(&sh->tempty[buf]);
+      // ---- finish and store
 #pragma unroll
-        for (int lv = 0; lv < 4; ++lv) {
-          float v[32];
-          ptx::tmem_ld_32x32b_x32(lane_base + lv * 128 + 32 * g, v);
-          if (dump) {
-            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 32 * g;
-#pragma unroll
-            for (int c = 0; c < 32; ++c) drow[c] = v[c];
-          }
-#pragma unroll
-          for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = v[c];
-          __syncwarp();
-#pragma unroll
-          for (int sl = 0; sl < 4; ++sl) {
-            const int jl = 3 * sl + x;
-            const int jc = jl < 10 ? jl : 9;
-            float s9[9];
-#pragma unroll
-            for (int xr = 0; xr < 3; ++xr)
-#pragma unroll
-              for (int y = 0; y < 3; ++y) s9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
-            bsm::fast_level(st[sl], lv, s9);
-          }
-          __syncwarp();
-        }
-        // ---- finish and store
-#pragma unroll
-        for (int sl = 0; sl < 4; ++sl) {
-          if (!valid[sl]) continue;
-          const int64_t j = jj[sl];
-          int flag = 0;
-          const float r = bsm::fast_finish(st[sl], ga + a.ghat[j], lowa, a.low[j], scale_exp, a.L, a.tol, flag);
-          if (flag) {
-            store_pair(a.out, i, j, -1.0f);
-            const unsigned long long slot = atomicAdd(&a.sc->flag_count, 1ull);
-            if (slot < a.flag_cap) a.flags[slot] = ((unsigned long long)i << 32) | (unsigned long long)j;
-          } else {
-            store_pair(a.out, i, j, r);
-          }
+      for (int sl = 0; sl < 4; ++sl) {
+        if (!valid[sl]) continue;
+        const int64_t j = jj[sl];
+        int flag = 0;
+        const float r = bsm::fast_finish(st[sl], ga + a.ghat[j], lowa, a.low[j], scale_exp, a.L, a.tol, flag);
+        if (flag) {
+          store_pair(a.out, i, j, -1.0f);
+          const unsigned long long slot = atomicAdd(&a.sc->flag_count, 1ull);
+          if (slot < a.flag_cap) a.flags[slot] = ((unsigned long long)i << 32) | (unsigned long long)j;
+        } else {
+          store_pair(a.out, i, j, r);
         }
       }
-      ptx::tc_fence_before();
-      ptx::mbar_arrive(&sh->tempty);
     }
   }
   __syncthreads();
@@ -322,7 +336,7 @@ cudaError_t launch_mixed_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t
     attr_set = true;
   }
   const int64_t grid = a.ntiles < a.num_sms ? a.ntiles : a.num_sms;
-  k_mixed_tc<<<(unsigned)grid, kThreads, kSmemBytes, st>>>(tm[0], tm[1], tm[2], a);
+  k_mixed_tc<<<(unsigned)grid, kThreads, kSmemBytes, st>>>(tm[0], tm[1], tm[2], tm[3], tm[4], tm[5], a);
   return cudaGetLastError();
 }
 

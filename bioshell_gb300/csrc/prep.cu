@@ -3,8 +3,8 @@
 // Per structure: centroid (arithmetic mean, as bioshell-pdb's
 // SubstructureAxis centres, calc/substructures.rs:26-31), largest centred
 // coordinate, then either
-//   - mixed path: quantisation onto the grid 2^e, balanced base-256 digits
-//     written as bf16 rows of the digit matrices, exact squared norm Ghat
+//   - mixed path: quantisation onto the grid 2^e, balanced digits (9, 9 and
+//     5 bits) written as bf16 rows of the digit matrices, exact squared norm Ghat
 //     (int64) and digit norms for the exactness bound; or
 //   - plain path: the centred f64 coordinates in K-major [n][3][lp] and G.
 // One block per structure; the [L][3] AoS input of a structure is one
@@ -94,11 +94,11 @@ __global__ void __launch_bounds__(kPrepThreads) k_prep_stats(const double *__res
   }
 }
 
-// Smallest e >= scale_min with max|y| <= (2^23 - 1) 2^e, so that every
+// Smallest e >= scale_min with max|y| <= (2^22 - 1) 2^e, so that every
 // quantised coordinate fits the three balanced digits.
 __global__ void k_prep_scale(DevScalars *sc) {
   const double maxabs = __longlong_as_double((long long)sc->maxabs_bits);
-  const double lim = 8388607.0;  // 2^23 - 1
+  const double lim = 4194303.0;  // 2^22 - 1
   int e = -40;
   if (maxabs > 0.0) {
     e = (int)ceil(log2(maxabs / lim));
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kPrepThreads)
   int64_t row[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) row[c] = digit_row(s, c) * lp;
-  // acc[0] = Ghat, acc[1 + 3*i + c] = sum of d_i^2 for coordinate c
+  // acc[0] = Ghat, acc[1 + 3*i + c] = sum of e_i^2 for coordinate c
   long long acc[10];
 #pragma unroll
   for (int i = 0; i < 10; ++i) acc[i] = 0;
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kPrepThreads)
   block_sum<long long, 10>(acc, red);
   if (threadIdx.x == 0) {
     ghat[s] = acc[0];
-    low[s] = (float)sqrt((double)(acc[7] + acc[8] + acc[9]));
+    low[s] = (float)(sqrt((double)(acc[7] + acc[8] + acc[9])) * 0.0625);  // sqrt(sum d2^2), e2 = 16 d2
     for (int i = 0; i < 3; ++i) {
       long long mx = acc[1 + 3 * i];
       mx = acc[2 + 3 * i] > mx ? acc[2 + 3 * i] : mx;

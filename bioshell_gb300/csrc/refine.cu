@@ -1,7 +1,7 @@
 // refine.cu -- exact recomputation of flagged pairs, and the CUDA-core
 // mixed path for explicit pair lists.
 //
-// Exact path: the quantised coordinates n = d0 2^16 + d1 2^8 + d2 are
+// Exact path: the quantised coordinates n = 2^14 e0 + 2^5 e1 + e2 / 16 are
 // rebuilt from the digit matrices, the covariance Mhat = sum n_a n_b is
 // accumulated in int64 (exact), and the FP64 QCP of crmsd_math.cuh finishes
 // the pair.  One warp per pair, lanes striding over atoms.
@@ -47,10 +47,8 @@ struct Digits {
   int lp;
   __device__ __forceinline__ int coord(int64_t s, int c, int k) const {
     const int64_t off = digit_row(s, c) * lp + k;
-    const int a = (int)__bfloat162float(d0[off]);
-    const int b = (int)__bfloat162float(d1[off]);
-    const int d = (int)__bfloat162float(d2[off]);
-    return a * 65536 + b * 256 + d;
+    return bsm::join_digits((int)__bfloat162float(d0[off]), (int)__bfloat162float(d1[off]),
+                            (int)__bfloat162float(d2[off]));
   }
 };
 

@@ -90,9 +90,12 @@ typedef struct {
   int32_t precision;  /* BS_PRECISION_*                                    */
   int32_t layout;     /* BS_LAYOUT_*                                       */
   int32_t out_type;   /* BS_OUT_*                                          */
-  double tolerance;   /* mixed path: per-pair |dRMSD| bound in Angstrom
-                         that a pair must meet without recomputation;
-                         <= 0 selects the default (2.5e-5)                */
+  double tolerance;   /* mixed path: certified per-pair |dRMSD| bound in
+                         Angstrom against exact arithmetic on the input
+                         coordinates (grid quantisation + fast-path
+                         arithmetic); pairs whose fast-path bound does not
+                         meet it are recomputed exactly.  <= 0 selects the
+                         default, 1e-4                                    */
   int32_t reserved[8];
 } bs_opts;
 
@@ -161,8 +164,9 @@ BS_API bs_status bs_host_free(void *p);
  * never used by the compute entry points above. */
 
 /* Digits of one structure's centred coordinates at grid 2^scale_exp:
- * digits[3][3][L] (digit-major, then coordinate, then atom), plus the exact
- * squared norm (int64) and the sum of squared lowest digits. */
+ * digits[3][3][L] (digit-major, then coordinate, then atom) as stored, i.e.
+ * e0, e1 and e2 = 16 d2 with n = 2^14 e0 + 2^5 e1 + d2, plus the exact
+ * squared norm of n (int64) and the sum of d2^2. */
 BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_exp, int32_t *digits,
                                     int64_t *g_exact, int64_t *low_norm2);
 /* The mixed-path epilogue for one pair from its four level sums
@@ -176,10 +180,10 @@ BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t
                                    double *rmsd);
 
 /* GPU diagnostics of the mixed path.  bs_debug_tile_levels returns the raw
- * tensor-core level sums of the first tile (structures 0..39 against
- * 0..39) as levels[4][128][128] (level, row, column; rows and columns in the
- * digit-matrix order of the engine: structure s, coordinate c at
- * 32*(s/10) + 3*(s%10) + c).  bs_debug_pair_levels returns, for each listed
+ * tensor-core level sums of the first two tiles (structures 0..39 against
+ * 0..19 and 20..39) as levels[4][128][128] (level, row, column; rows and
+ * columns in the digit-matrix order of the engine: structure s, coordinate c
+ * at 32*(s/10) + 3*(s%10) + c).  bs_debug_pair_levels returns, for each listed
  * pair, the level sums computed with integer CUDA-core arithmetic
  * (levels[npairs][4][9]) and that path's crmsd. */
 BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels);

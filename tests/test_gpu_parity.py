@@ -2,9 +2,10 @@
 
 Tolerances (Angstrom, |RMSD_gpu - RMSD_oracle|):
   * plain FP64 path: 1e-9 (same method, FP64 throughout);
-  * mixed path: 1e-4, the project's accuracy bar.  The engine certifies
-    quantisation (sqrt(3) 2^e) + 2.5e-5 per pair; the tests also report the
-    observed maximum.
+  * mixed path: 1e-4, the project's accuracy bar.  By default the engine
+    certifies 1e-4 per pair: grid quantisation (sqrt(3) 2^e) plus the
+    fast path's arithmetic bound, with exact recomputation of any pair whose
+    bound does not fit.
 Tensor-core exactness is checked bit for bit: the raw TMEM level sums of a
 tile must equal the CUDA-core integer sums.
 """
@@ -18,6 +19,14 @@ pytestmark = pytest.mark.gpu
 
 TOL_MIXED = 1e-4
 TOL_PLAIN = 1e-9
+# FP64 cancellation floor of G_a + G_b - 2 lambda for (near-)identical pairs:
+# ~sqrt(eps (G_a + G_b) / L), about 1e-6 A; the CPU oracle has the same floor
+PLAIN_FLOOR = 2e-6
+
+
+def plain_close(got, ref):
+    d = np.abs(np.asarray(got) - ref)
+    return bool(np.all(np.where(ref > 1e-3, d <= TOL_PLAIN, d <= PLAIN_FLOOR)))
 
 
 def _tri_pairs(n, t):
@@ -32,7 +41,7 @@ def _tri_pairs(n, t):
 def test_tensor_core_level_sums_are_exact(engine):
     rng = np.random.default_rng(11)
     x = synth.decoys(synth.base_chain(77, rng), 40, rng, near_dup_frac=0.1)
-    tl = engine.debug_tile_levels(x)
+    tl = engine.debug_tile_levels(x)  # tiles (rows 0..39) x (columns 0..19, 20..39)
     ia, ja = np.meshgrid(np.arange(40), np.arange(40), indexing="ij")
     ia, ja = ia.ravel(), ja.ravel()
     pl, _ = engine.debug_pair_levels(x, ia, ja)
@@ -58,9 +67,9 @@ def test_config_500x64_all_pairs(engine, oracle_mod):
     print(f"mixed 500x64: max {d.max():.3e} p99 {np.percentile(d, 99):.3e}")
     assert d.max() <= TOL_MIXED
     m = engine.metrics()
-    assert d.max() <= m["quant_bound"] + 2.5e-5
+    assert 0.0 < m["quant_bound"] < TOL_MIXED
     plain = engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values
-    assert np.abs(plain - ref).max() <= TOL_PLAIN
+    assert plain_close(plain, ref)
 
 
 def test_golden_fixtures(engine, golden_small, golden_2jqb):
@@ -68,7 +77,7 @@ def test_golden_fixtures(engine, golden_small, golden_2jqb):
                    (golden_2jqb["all_atoms"], golden_2jqb["rmsd_all"]),
                    (golden_2jqb["ca"], golden_2jqb["rmsd_ca"])):
         assert np.abs(engine.all_vs_all(x).values - ref).max() <= TOL_MIXED
-        assert np.abs(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values - ref).max() <= TOL_PLAIN
+        assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
 
 
 @pytest.mark.parametrize("n,L", [(2, 3), (3, 4), (39, 5), (40, 17), (41, 64), (81, 129), (123, 255), (47, 301)])
@@ -77,7 +86,7 @@ def test_ragged_shapes(engine, oracle_mod, n, L):
     x = synth.decoys(synth.base_chain(L, rng), n, rng, near_dup_frac=0.1)
     ref = oracle_mod.crmsd_all_vs_all(x)
     assert np.abs(engine.all_vs_all(x).values - ref).max() <= TOL_MIXED
-    assert np.abs(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values - ref).max() <= TOL_PLAIN
+    assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
 
 
 def test_duplicates_and_rigid_copies(engine, oracle_mod):
@@ -114,9 +123,9 @@ def test_pairs_api_and_single_pair(engine, oracle_mod):
     ii = rng.integers(0, 900, 20000)
     jj = rng.integers(0, 900, 20000)
     ref = oracle_mod.crmsd_pairs(x, ii, jj)
-    for prec, tol in (("mixed", TOL_MIXED), ("plain64", TOL_PLAIN)):
-        got = engine.pairs(x, ii, jj, CrmsdOptions(precision=prec))
-        assert np.abs(got - ref).max() <= max(tol, 1e-6 if prec == "plain64" else tol)
+    got = engine.pairs(x, ii, jj, CrmsdOptions(precision="mixed"))
+    assert np.abs(got - ref).max() <= TOL_MIXED
+    assert plain_close(engine.pairs(x, ii, jj, CrmsdOptions(precision="plain64")), ref)
     assert abs(engine.crmsd(x[0], x[1]) - oracle_mod.crmsd(x[0], x[1])) <= TOL_MIXED
     assert engine.crmsd(x[3], x[3]) <= TOL_MIXED
 
@@ -132,7 +141,7 @@ def test_subsample_20000x150(engine, oracle_mod):
     mixed = engine.all_vs_all(x).values
     assert np.abs(mixed[sel] - ref).max() <= TOL_MIXED
     plain = engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values
-    assert np.abs(plain[sel] - ref).max() <= TOL_PLAIN
+    assert plain_close(plain[sel], ref)
     # size-independent properties of the full matrix
     assert np.all(np.isfinite(mixed)) and mixed.min() >= 0.0
     assert np.abs(mixed - plain).max() <= TOL_MIXED

@@ -18,12 +18,17 @@ TOL_FAST = 2.5e-5  # fast-path certified |dRMSD| (Angstrom)
 
 def _grid_exp(xs):
     m = max(np.abs(x - x.mean(0)).max() for x in xs)
-    e = int(np.ceil(np.log2(m / (2 ** 23 - 1))))
-    while np.ldexp(2 ** 23 - 1, e) < m:
+    e = int(np.ceil(np.log2(m / (2 ** 22 - 1))))
+    while np.ldexp(2 ** 22 - 1, e) < m:
         e += 1
-    while np.ldexp(2 ** 23 - 1, e - 1) >= m:
+    while np.ldexp(2 ** 22 - 1, e - 1) >= m:
         e -= 1
     return e
+
+
+def join(d):
+    """Quantised coordinates from stored digits: n = 2^14 e0 + 2^5 e1 + e2 / 16."""
+    return d[0] * 16384 + d[1] * 32 + d[2] // 16
 
 
 class Hooks:
@@ -63,8 +68,8 @@ class Hooks:
         return r.value, f.value
 
     def exact(self, da, db, e):
-        na = np.ascontiguousarray((da[0] * 65536 + da[1] * 256 + da[2]).astype(np.int32))
-        nb = np.ascontiguousarray((db[0] * 65536 + db[1] * 256 + db[2]).astype(np.int32))
+        na = np.ascontiguousarray(join(da).astype(np.int32))
+        nb = np.ascontiguousarray(join(db).astype(np.int32))
         r = ctypes.c_double()
         p = ctypes.POINTER(ctypes.c_int32)
         st = self.lib.bs_selftest_exact(na.ctypes.data_as(p), nb.ctypes.data_as(p), na.shape[1], e, ctypes.byref(r))
@@ -82,12 +87,12 @@ def test_digits_reconstruct(hooks):
     x = rng.normal(size=(50, 3)) * 20
     e = _grid_exp([x])
     d, g, low = hooks.digits(x, e)
-    assert np.abs(d[1:]).max() <= 128 and np.abs(d[0]).max() <= 128
-    n = d[0] * 65536 + d[1] * 256 + d[2]
+    assert np.abs(d).max() <= 256 and np.all(d[2] % 16 == 0) and np.abs(d[2]).max() <= 256
+    n = join(d)
     y = x - x.mean(0)
     assert np.abs(n.T * 2.0 ** e - y).max() <= 2.0 ** (e - 1) * (1 + 1e-9)
     assert g == int((n.astype(np.int64) ** 2).sum())
-    assert low == int((d[2] ** 2).sum())
+    assert low == int(((d[2] // 16) ** 2).sum())
 
 
 @pytest.mark.parametrize("L", [5, 47, 300])
