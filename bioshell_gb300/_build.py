@@ -1,7 +1,8 @@
 """Builds the engine's shared library in-tree for sm_103a.
 
 Every ``csrc/*.cu`` translation unit is compiled in parallel with
-``-gencode arch=compute_103a,code=sm_103a`` and linked into
+``-gencode arch=compute_103a,code=sm_103a`` (host-only ``csrc/*.cpp`` with the
+host compiler, no FMA contraction) and linked into
 ``bioshell_gb300/lib/libbioshell_crmsd.so`` (CUDA runtime linked
 statically; the driver's tensor-map encoder is resolved at run time, so no
 libcuda is needed at link time).
@@ -33,8 +34,11 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build the engine")
 
 
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I" + INCLUDE]
+
+
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _headers_mtime() -> float:
@@ -44,10 +48,13 @@ def _headers_mtime() -> float:
 
 
 def _compile(src: str, extra) -> str:
-    obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
+    obj = os.path.join(OBJ, os.path.splitext(os.path.basename(src))[0] + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _headers_mtime()) and not extra:
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+    if src.endswith(".cpp"):
+        cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-c", src, "-o", obj]
+    else:
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")

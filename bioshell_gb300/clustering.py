@@ -1,0 +1,93 @@
+"""Clustering of a crmsd matrix through the engine's C ABI (host code in
+``csrc/cluster.cpp``), mirroring bioshell-clustering's consumers:
+
+* ``hierarchical_clustering(matrix, rule)``  -- hierarchical.rs:22-80
+* ``cut_tree(tree, cutoff)``                   -- labels of retrieve_clusters, hierarchical.rs:136-169
+* ``optics(matrix, eps, min_points)``          -- optics.rs:51-148
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import lib as _l
+from .crmsd import CrmsdMatrix
+
+
+@dataclass
+class ClusteringTree:
+    """n-1 merges: merges[s] = (left id, right id, new id, size), dist[s]."""
+
+    n: int
+    merges: np.ndarray
+    dist: np.ndarray
+
+    def leaves_preorder(self):
+        """Leaf ids in depth-first preorder (the order retrieve_data returns)."""
+        if self.n == 0:
+            return []
+        kids = {int(m[2]): (int(m[0]), int(m[1])) for m in self.merges}
+        out, stack = [], [2 * self.n - 2 if self.n > 1 else 0]
+        while stack:
+            v = stack.pop()
+            if v < self.n:
+                out.append(v)
+            else:
+                a, b = kids[v]
+                stack.append(b)
+                stack.append(a)
+        return out
+
+
+def _tri(matrix: CrmsdMatrix):
+    if matrix.layout != "triangle":
+        raise ValueError("clustering takes the packed-triangle layout")
+    v = np.ascontiguousarray(matrix.values)
+    if v.dtype == np.float64:
+        return v, _l.OUT_TYPE["f64"]
+    if v.dtype == np.float32:
+        return v, _l.OUT_TYPE["f32"]
+    raise TypeError("matrix values must be float64 or float32")
+
+
+def _check(st, what):
+    if st != _l.BS_OK:
+        raise _l.CrmsdError(st, what)
+
+
+def hierarchical_clustering(matrix: CrmsdMatrix, rule: str = "single") -> ClusteringTree:
+    v, ot = _tri(matrix)
+    n = matrix.n
+    merges = np.zeros((max(n - 1, 0), 4), dtype=np.int64)
+    dist = np.zeros(max(n - 1, 0), dtype=np.float32)
+    st = _l.load().bs_hierarchical(v.ctypes.data, n, ot, _l.LINK[rule],
+                                   merges.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                   dist.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    _check(st, "bs_hierarchical")
+    return ClusteringTree(n, merges, dist)
+
+
+def cut_tree(tree: ClusteringTree, cutoff: float) -> np.ndarray:
+    labels = np.zeros(tree.n, dtype=np.int64)
+    st = _l.load().bs_cut_tree(tree.merges.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                               tree.dist.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), tree.n, float(cutoff),
+                               labels.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _check(st, "bs_cut_tree")
+    return labels
+
+
+def optics(matrix: CrmsdMatrix, eps: float, min_points: int):
+    """(clustering order, reachability in that order, cluster index per item)."""
+    v, ot = _tri(matrix)
+    n = matrix.n
+    order = np.zeros(n, dtype=np.int64)
+    reach = np.zeros(n, dtype=np.float64)
+    cl = np.zeros(n, dtype=np.int64)
+    st = _l.load().bs_optics(v.ctypes.data, n, ot, float(eps), int(min_points),
+                             order.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                             reach.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                             cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _check(st, "bs_optics")
+    return order, reach, cl

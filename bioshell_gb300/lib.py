@@ -23,6 +23,7 @@ STATUS_NAMES = {
 PRECISION = {"plain64": 0, "mixed": 1}
 LAYOUT = {"triangle": 0, "square": 1}
 OUT_TYPE = {"f64": 0, "f32": 1}
+LINK = {"single": 0, "complete": 1, "average": 2, "median": 3, "centroid": 4, "ward": 5}
 
 
 class bs_opts(ctypes.Structure):
@@ -63,6 +64,10 @@ SIGNATURES = [
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                   ctypes.POINTER(bs_opts), _vp]),
+    ("bs_hierarchical", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _i64p, _fp]),
+    ("bs_cut_tree", ctypes.c_int32, [_i64p, _fp, ctypes.c_int64, ctypes.c_float, _i64p]),
+    ("bs_optics", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _i64p,
+                                   _dp, _i64p]),
     ("bs_host_alloc", ctypes.c_int32, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     ("bs_host_free", ctypes.c_int32, [_vp]),
     ("bs_selftest_digits", ctypes.c_int32, [_dp, ctypes.c_int32, ctypes.c_int32, _i32p, _i64p, _i64p]),

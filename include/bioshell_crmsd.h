@@ -152,6 +152,38 @@ BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_
 BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
                           const int64_t *jj, int64_t npairs, const bs_opts *opts, double *out);
 
+/* ---- clustering of a crmsd matrix --------------------------------------- */
+/* Merge rules of bioshell-clustering/src/hierarchical/strategies/mod.rs. */
+enum {
+  BS_LINK_SINGLE = 0,
+  BS_LINK_COMPLETE = 1,
+  BS_LINK_AVERAGE = 2,
+  BS_LINK_MEDIAN = 3,
+  BS_LINK_CENTROID = 4,
+  BS_LINK_WARD = 5
+};
+
+/* Hierarchical agglomerative clustering of the n items of a packed-triangle
+ * crmsd matrix (`tri` as written by bs_all_vs_all, element type out_type),
+ * with the semantics of hierarchical_clustering
+ * (bioshell-clustering/src/hierarchical/hierarchical.rs:22-80): f32
+ * distances, first-minimum tie-breaking, the reference's size bookkeeping.
+ * Writes the n-1 merges in order: merges[s] = {left id, right id, new id,
+ * size}, merge_dist[s] = merging distance; leaves are 0..n-1 and merged
+ * clusters n, n+1, ... (the root is 2n-2).  Runs on the host. */
+BS_API bs_status bs_hierarchical(const void *tri, int64_t n, int32_t out_type, int32_t rule, int64_t *merges,
+                                 float *merge_dist);
+/* Cluster label of every item at a distance cutoff, as retrieve_clusters
+ * (hierarchical.rs:136-169) splits the tree; labels number the clusters in
+ * the order that function returns them. */
+BS_API bs_status bs_cut_tree(const int64_t *merges, const float *merge_dist, int64_t n, float cutoff,
+                             int64_t *labels);
+/* OPTICS (bioshell-clustering/src/optics.rs:51-148) over the matrix:
+ * clustering order, reachability in that order, and the cluster index of
+ * every item (clusters split where reachability is undefined = 10 eps). */
+BS_API bs_status bs_optics(const void *tri, int64_t n, int32_t out_type, double eps, int32_t min_points,
+                           int64_t *order, double *reach, int64_t *cluster_of);
+
 /* ---- pinned host memory ------------------------------------------------- */
 /* Page-locked host buffers for fast host<->device staging (cudaHostAlloc);
  * free with bs_host_free.  Pageable memory is accepted everywhere too. */
