@@ -260,6 +260,9 @@ def run_ours(a, rank, world, local_rank):
     ms_main = statistics.mean(m["ms_main"] for m in mets)
     launches = int(sum(m["main_launches"] for m in mets))
     refined = mets[-1]["pairs_refined"]
+    phases = {k: statistics.mean(m[k] for m in mets) for k in ("ms_prep", "ms_main", "ms_refine", "ms_total")}
+    phases["quant_bound"] = mets[-1]["quant_bound"]
+    phases["scale_exp"] = mets[-1]["scale_exp"]
 
     # ---- end to end through the C ABI with pinned host buffers
     xh = eng.host_empty(x.shape, np.float64)
@@ -327,7 +330,7 @@ def run_ours(a, rank, world, local_rank):
                        "replicas": world},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
-            "accuracy": acc, "pairs_refined": int(refined)}
+            "accuracy": acc, "pairs_refined": int(refined), "phases": phases}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

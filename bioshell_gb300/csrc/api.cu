@@ -40,7 +40,8 @@ struct bs_ctx {
   std::string err;
   bs_metrics metrics{};
   // workspaces
-  DevBuf xyz, ctr, ghat, low, dig[3], y, g, out, tiles, flags, scal, pairs_i, pairs_j, pout;
+  DevBuf xyz, ctr, info, dig[4], y, g, out, tiles, flags, scal, pairs_i, pairs_j, pout;
+  double d34 = 0.0;  // level-3 rounding bound of the last preparation (units u)
   int64_t tiles_nb = -1;
   int64_t tiles_count = 0;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
@@ -144,40 +145,50 @@ bs_status read_scalars(bs_ctx *ctx, DevScalars *host) {
 }
 
 // Mixed path preparation: centring, grid choice, digits, and the exactness
-// bound: every level sum must stay below 2^24 in magnitude.  With
-// n_i = max over (structure, coordinate) of sqrt(sum d_i^2), Cauchy-Schwarz
-// bounds |S_l| by sum_{i+j=l} n_i n_j; when that reaches 2^24 the grid is
-// coarsened by one bit and the digits are recomputed.
+// bound: levels 0-2 must stay below 2^24 in magnitude.  With n_i = max over
+// (structure, coordinate) of sqrt(sum e_i^2), Cauchy-Schwarz bounds |S_l| by
+// sum_{i+j=l} n_i n_j; when that reaches 2^24 the grid is coarsened by one bit
+// and the digits are recomputed.  Level 3 (S3 + S4/512) is exact below 2^23;
+// above, its FP32 rounding is bounded here and charged to the error budget.
 bs_status prep_mixed(bs_ctx *ctx, const double *dxyz, int64_t n, int L, int lp, DevScalars *hs) {
   const int64_t rows = blocks_for(n) * kBlockRows;
   const size_t dbytes = (size_t)rows * lp * sizeof(__nv_bfloat16);
   bs_status s;
   if ((s = ensure(ctx, ctx->ctr, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
-  if ((s = ensure(ctx, ctx->ghat, (size_t)n * sizeof(long long), "norms"))) return s;
-  if ((s = ensure(ctx, ctx->low, (size_t)n * sizeof(float), "digit norms"))) return s;
-  for (int d = 0; d < 3; ++d)
+  if ((s = ensure(ctx, ctx->info, (size_t)n * sizeof(SInfo), "structure data"))) return s;
+  for (int d = 0; d < 4; ++d)
     if ((s = ensure(ctx, ctx->dig[d], dbytes, "digit matrices"))) return s;
+  __nv_bfloat16 *digs[4];
+  for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
   DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
   int scale_min = -1000;
   for (int attempt = 0; attempt < 8; ++attempt) {
     DevScalars init{};
     init.scale_min = scale_min;
     CK(cudaMemcpyAsync(sc, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream), "init scalars");
-    for (int d = 0; d < 3; ++d) CK(cudaMemsetAsync(ctx->dig[d].p, 0, dbytes, ctx->stream), "clear digits");
+    for (int d = 0; d < 4; ++d) CK(cudaMemsetAsync(digs[d], 0, dbytes, ctx->stream), "clear digits");
     CK(launch_prep_stats(dxyz, n, L, static_cast<double *>(ctx->ctr.p), sc, ctx->stream), "prep stats");
     CK(launch_prep_scale(sc, ctx->stream), "prep scale");
-    CK(launch_prep_digits(dxyz, static_cast<const double *>(ctx->ctr.p), n, L, lp,
-                          static_cast<__nv_bfloat16 *>(ctx->dig[0].p), static_cast<__nv_bfloat16 *>(ctx->dig[1].p),
-                          static_cast<__nv_bfloat16 *>(ctx->dig[2].p), static_cast<long long *>(ctx->ghat.p),
-                          static_cast<float *>(ctx->low.p), sc, ctx->stream),
+    CK(launch_prep_digits(dxyz, static_cast<const double *>(ctx->ctr.p), n, L, lp, digs,
+                          static_cast<SInfo *>(ctx->info.p), sc, ctx->stream),
        "prep digits");
     if ((s = read_scalars(ctx, hs))) return s;
     if (hs->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
     const double n0 = sqrt((double)hs->norm_max[0]), n1 = sqrt((double)hs->norm_max[1]),
                  n2 = sqrt((double)hs->norm_max[2]);
-    const double b0 = n0 * n0, b1 = 2 * n0 * n1, b2 = 2 * n0 * n2 + n1 * n1, b3 = 2 * n1 * n2;
+    const double b0 = n0 * n0, b1 = 2 * n0 * n1, b2 = 2 * n0 * n2 + n1 * n1;
     const double lim = 16777216.0;  // 2^24
-    if (b0 < lim && b1 < lim && b2 < lim && b3 < lim) return BS_OK;
+    if (b0 < lim && b1 < lim && b2 < lim) {
+      const double b34 = 2 * n1 * n2 + n2 * n2 / 512.0;
+      double err3 = 0.0;  // level-3 units
+      if (b34 >= 8388608.0) {  // 2^23: half-integers no longer exact
+        const int k = (int)floor(log2(b34));
+        err3 = 3.0 * (double)L * ldexp(1.0, k - 24);
+      }
+      // Mhat carries 2 S3' -> |dM| <= 2 err3 u per entry; |dE| <= 2 sqrt(3) ||dM||_F
+      ctx->d34 = 12.0 * sqrt(3.0) * err3;
+      return BS_OK;
+    }
     scale_min = hs->scale_exp + 1;
   }
   return set_err(ctx, BS_ERR_UNSUPPORTED,
@@ -209,12 +220,13 @@ bs_status encode_maps(bs_ctx *ctx, int64_t rows, int lp, CUtensorMap *tm) {
       return set_err(ctx, BS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable in the driver");
     ctx->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
-  // maps 0-2: A operand boxes (64 atoms x 128 rows); 3-5: B boxes (64 x 64)
-  for (int m = 0; m < 6; ++m) {
-    const int d = m % 3;
+  // maps 0-3: A operand boxes (64 atoms x 128 rows) of e0, e1, e2, d2/32;
+  // maps 4-6: B boxes (64 x 64) of e0, e1, e2
+  for (int m = 0; m < 7; ++m) {
+    const int d = m < 4 ? m : m - 4;
     cuuint64_t gdim[2] = {(cuuint64_t)lp, (cuuint64_t)rows};
     cuuint64_t gstride[1] = {(cuuint64_t)lp * 2};
-    cuuint32_t box[2] = {64, m < 3 ? 128u : 64u};
+    cuuint32_t box[2] = {64, m < 4 ? 128u : 64u};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = ctx->encode(&tm[m], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ctx->dig[d].p, gdim, gstride, box, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -228,14 +240,15 @@ size_t out_elems(int64_t n, int layout) {
   return layout == BS_LAYOUT_TRIANGLE ? (size_t)(n * (n - 1) / 2) : (size_t)n * (size_t)n;
 }
 
-// The quantisation grid 2^e moves each centred coordinate by <= 2^(e-1), so
-// the RMSD of the quantised pair is within sqrt(3) 2^e of the exact one; the
-// fast path gets the rest of the requested tolerance (at least 1e-6).
-double grid_bound(int scale_exp) { return sqrt(3.0) * ldexp(1.0, scale_exp); }
-float fast_tolerance(const bs_opts &o, int scale_exp) {
-  const double total = o.tolerance > 0 ? o.tolerance : kDefaultTol;
-  const double t = total - grid_bound(scale_exp);
-  return (float)(t > 1e-6 ? t : 1e-6);
+// Certified per-pair |dRMSD| budget: the kernels charge each pair its two
+// structures' quantisation residuals (Minkowski) and give the fast path the
+// rest (at least 1e-5 A).
+float total_tolerance(const bs_opts &o) { return (float)(o.tolerance > 0 ? o.tolerance : kDefaultTol); }
+float qres_max(const DevScalars &hs) {
+  float f;
+  const unsigned b = (unsigned)hs.qres_max_bits;
+  memcpy(&f, &b, 4);
+  return f;
 }
 
 bs_status check_device_errors(bs_ctx *ctx, DevScalars *hs) {
@@ -304,7 +317,7 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
       ctx->tiles_count = (int64_t)t.size();
     }
     if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
-    CUtensorMap tm[6];
+    CUtensorMap tm[7];
     if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
     TcArgs a{};
     a.tiles = static_cast<const int2 *>(ctx->tiles.p);
@@ -312,10 +325,11 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
     a.n = n;
     a.L = L;
     a.lp = lp;
-    a.ghat = static_cast<const long long *>(ctx->ghat.p);
-    a.low = static_cast<const float *>(ctx->low.p);
+    a.info = static_cast<const SInfo *>(ctx->info.p);
     a.sc = static_cast<DevScalars *>(ctx->scal.p);
-    a.tol = fast_tolerance(o, hs.scale_exp);
+    a.tol = total_tolerance(o);
+    a.u = ldexpf(1.0f, 2 * hs.scale_exp);
+    a.d34 = (float)ctx->d34;
     a.out = od;
     a.flags = static_cast<unsigned long long *>(ctx->flags.p);
     a.flag_cap = kFlagCap;
@@ -323,24 +337,18 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
     a.num_sms = ctx->num_sms;
     CK(launch_mixed_tc(tm, a, ctx->stream), "tensor-core all-vs-all");
     CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
-    CK(launch_refine_list(static_cast<const __nv_bfloat16 *>(ctx->dig[0].p),
-                          static_cast<const __nv_bfloat16 *>(ctx->dig[1].p),
-                          static_cast<const __nv_bfloat16 *>(ctx->dig[2].p), lp, L,
-                          static_cast<const long long *>(ctx->ghat.p), a.sc, a.flags, kFlagCap, od, ctx->num_sms,
-                          ctx->stream),
+    __nv_bfloat16 *digs[4];
+    for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
+    CK(launch_refine_list(digs, lp, L, a.info, a.sc, a.flags, kFlagCap, od, ctx->num_sms, ctx->stream),
        "exact recomputation");
     if ((s = check_device_errors(ctx, &hs))) return s;
     if (hs.flag_count > kFlagCap) {
-      CK(launch_refine_scan(static_cast<const __nv_bfloat16 *>(ctx->dig[0].p),
-                            static_cast<const __nv_bfloat16 *>(ctx->dig[1].p),
-                            static_cast<const __nv_bfloat16 *>(ctx->dig[2].p), lp, L,
-                            static_cast<const long long *>(ctx->ghat.p), a.sc, od, ctx->num_sms, ctx->stream),
-         "exact recomputation (scan)");
+      CK(launch_refine_scan(digs, lp, L, a.info, a.sc, od, ctx->num_sms, ctx->stream), "exact recomputation (scan)");
     }
     CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
     ctx->metrics.pairs_refined = (int64_t)hs.flag_count;
     ctx->metrics.scale_exp = hs.scale_exp;
-    ctx->metrics.quant_bound = grid_bound(hs.scale_exp);  // |dRMSD| from the grid
+    ctx->metrics.quant_bound = 2.0 * qres_max(hs);  // worst pair's |dRMSD| from the grid
     ctx->metrics.main_launches = 5 + (hs.flag_count > kFlagCap ? 1 : 0);
   }
   if (!out_dev) {
@@ -404,12 +412,11 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
   } else {
     if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
-    CK(launch_mixed_pairs(static_cast<const __nv_bfloat16 *>(ctx->dig[0].p),
-                          static_cast<const __nv_bfloat16 *>(ctx->dig[1].p),
-                          static_cast<const __nv_bfloat16 *>(ctx->dig[2].p), lp, L,
-                          static_cast<const long long *>(ctx->ghat.p), static_cast<const float *>(ctx->low.p),
-                          static_cast<DevScalars *>(ctx->scal.p), fast_tolerance(o, hs.scale_exp),
-                          dii, djj, np, dout, levels_dbg, ctx->stream),
+    __nv_bfloat16 *digs[4];
+    for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
+    CK(launch_mixed_pairs(digs, lp, L, static_cast<const SInfo *>(ctx->info.p), static_cast<DevScalars *>(ctx->scal.p),
+                          total_tolerance(o), ldexpf(1.0f, 2 * hs.scale_exp), (float)ctx->d34, dii, djj, np, dout,
+                          levels_dbg, ctx->stream),
        "mixed pairs");
   }
   CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
@@ -422,7 +429,7 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
   if ((s = check_device_errors(ctx, &hs))) return s;
   ctx->metrics.pairs = np;
   ctx->metrics.scale_exp = hs.scale_exp;
-  if (o.precision == BS_PRECISION_MIXED) ctx->metrics.quant_bound = grid_bound(hs.scale_exp);
+  if (o.precision == BS_PRECISION_MIXED) ctx->metrics.quant_bound = 2.0 * qres_max(hs);
   ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
   ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
   ctx->metrics.ms_main = elapsed(ctx, 2, 3);
@@ -504,7 +511,7 @@ BS_API void bs_ctx_destroy(bs_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->ghat, &ctx->low, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2],
+  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->info, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2], &ctx->dig[3],
                     &ctx->y, &ctx->g, &ctx->out, &ctx->tiles, &ctx->flags, &ctx->scal, &ctx->pairs_i,
                     &ctx->pairs_j, &ctx->pout};
   for (DevBuf *b : bufs) release(ctx, *b);
@@ -518,7 +525,7 @@ BS_API bs_status bs_ctx_trim(bs_ctx *ctx) {
   if (!ctx) return BS_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->ghat, &ctx->low, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2],
+  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->info, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2], &ctx->dig[3],
                     &ctx->y, &ctx->g, &ctx->out, &ctx->tiles, &ctx->flags, &ctx->pairs_i, &ctx->pairs_j, &ctx->pout};
   for (DevBuf *b : bufs) release(ctx, *b);
   ctx->tiles_nb = -1;
@@ -634,7 +641,7 @@ BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n,
   if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
   if ((s = ensure(ctx, ctx->pout, (size_t)4 * 128 * 128 * sizeof(float), "level dump"))) return s;
   CK(cudaMemsetAsync(ctx->pout.p, 0, (size_t)4 * 128 * 128 * sizeof(float), ctx->stream), "clear level dump");
-  CUtensorMap tm[6];
+  CUtensorMap tm[7];
   if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
   TcArgs a{};
   a.tiles = static_cast<const int2 *>(ctx->tiles.p);
@@ -642,12 +649,11 @@ BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n,
   a.n = n;
   a.L = L;
   a.lp = lp;
-  a.ghat = static_cast<const long long *>(ctx->ghat.p);
-  a.low = static_cast<const float *>(ctx->low.p);
+  a.info = static_cast<const SInfo *>(ctx->info.p);
   a.sc = static_cast<DevScalars *>(ctx->scal.p);
-  bs_opts dflt;
-  bs_opts_init(&dflt);
-  a.tol = fast_tolerance(dflt, hs.scale_exp);
+  a.tol = (float)kDefaultTol;
+  a.u = ldexpf(1.0f, 2 * hs.scale_exp);
+  a.d34 = (float)ctx->d34;
   a.out = OutDesc{ctx->out.p, n, BS_LAYOUT_TRIANGLE, BS_OUT_F64};
   a.flags = static_cast<unsigned long long *>(ctx->flags.p);
   a.flag_cap = kFlagCap;
@@ -681,33 +687,34 @@ BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n,
 
 // ------------------------------------------------------------ test hooks
 BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_exp, int32_t *digits,
-                                    int64_t *g_exact, int64_t *low_norm2) {
-  if (!xyz || !digits || !g_exact || !low_norm2 || L < 1) return BS_ERR_INVALID_ARG;
+                                    int64_t *g_exact, double *qres) {
+  if (!xyz || !digits || !g_exact || !qres || L < 1) return BS_ERR_INVALID_ARG;
   double c[3] = {0, 0, 0};
   for (int k = 0; k < L; ++k)
     for (int d = 0; d < 3; ++d) c[d] += xyz[3 * k + d];
   for (int d = 0; d < 3; ++d) c[d] /= (double)L;
-  long long g = 0, low = 0;
+  long long g = 0;
+  double res = 0.0;
   for (int k = 0; k < L; ++k)
     for (int d = 0; d < 3; ++d) {
-      const double y = ldexp(xyz[3 * k + d] - c[d], -scale_exp);
-      const double r = nearbyint(y);
+      const double y = xyz[3 * k + d] - c[d];
+      const double r = nearbyint(ldexp(y, -scale_exp));
       if (!(fabs(r) < 4194304.0)) return BS_ERR_UNSUPPORTED;
       const int q = (int)r;
+      res += (y - ldexp(r, scale_exp)) * (y - ldexp(r, scale_exp));
       int a, b, e;
       bsm::split_digits(q, a, b, e);
       digits[(0 * 3 + d) * L + k] = a;
       digits[(1 * 3 + d) * L + k] = b;
       digits[(2 * 3 + d) * L + k] = e;
       g += (long long)q * q;
-      low += (long long)(e / 16) * (e / 16);
     }
   *g_exact = g;
-  *low_norm2 = low;
+  *qres = sqrt(res / (double)L);
   return BS_OK;
 }
 
-BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double low_a, double low_b,
+BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double qa, double qb, double d34,
                                       int32_t scale_exp, int32_t L, double tolerance, double *rmsd, int32_t *flag) {
   if (!levels || !rmsd || !flag || L < 1) return BS_ERR_INVALID_ARG;
   bsm::EpilogueIn in;
@@ -719,10 +726,13 @@ BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t g
   }
   in.ga = ga;
   in.gb = gb;
-  in.low_a = (float)low_a;
-  in.low_b = (float)low_b;
+  in.gfa = (float)ga;
+  in.gfb = (float)gb;
+  in.qa = (float)qa;
+  in.qb = (float)qb;
   int f = 0;
-  const float r = bsm::pair_rmsd_fast(in, scale_exp, L, (float)(tolerance > 0 ? tolerance : 2.5e-5), f);
+  const float r = bsm::pair_rmsd_fast(in, ldexpf(1.0f, 2 * scale_exp), (float)d34, L,
+                                      (float)(tolerance > 0 ? tolerance : kDefaultTol), f);
   *rmsd = (double)r;
   *flag = f;
   return BS_OK;

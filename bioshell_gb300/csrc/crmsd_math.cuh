@@ -11,9 +11,12 @@
 //   S_l[x][y]  level sums of digit products, l = i + j:
 //     S0 = sum e0a e0b                    S1 = sum e0a e1b + e1a e0b
 //     S2 = sum e0a e2b + e1a e1b + e2a e0b S3 = sum e1a e2b + e2a e1b
-//   (the level-4 term sum e2a e2b = 256 sum d2a d2b is dropped; its effect on
-//   E is bounded by 2 sqrt(3) sqrt(N2a N2b), N2 = sum of d2^2).
-//   Mhat = 2^28 S0 + 2^19 S1 + 2^10 S2 + 2 S3            (units u = 2^(2e))
+//   The level-4 term sum e2a e2b = 256 sum d2a d2b rides in the level-3
+//   accumulator as sum (d2a/32) e2b, i.e. the accumulator holds
+//     S3' = S3 + S4 / 512,
+//   which is exact while its partial sums stay below 2^23 (half-integers) and
+//   otherwise carries a small, bounded FP32 rounding error.
+//   Mhat = 2^28 S0 + 2^19 S1 + 2^10 S2 + 2 S3'           (units u = 2^(2e))
 //   Ghat = sum n^2 (exact)                               (units u)
 //   K(S) 4x4 quaternion key matrix, lambda0 = (Ga + Gb)/2,
 //   E = Ga + Gb - 2 lambda_max(K) = 2 min_q q'(lambda0 I - K)q / |q|^2,
@@ -21,12 +24,13 @@
 // With the row-major convention S[3x+y] = sum a_x b_y used here,
 //   q' K(S) q = sum_xy T(q)_xy S_xy,  T(q) = R(q)^T (transposed rotation).
 //
-// The level sums are exact: the host picks e so that every partial sum of
-// every level stays below 2^24 in magnitude, which FP32 accumulation
-// represents exactly.
+// Levels 0-2 are exact: the host picks e so that every partial sum of those
+// levels stays below 2^24 in magnitude, which FP32 accumulation represents
+// exactly.
 #pragma once
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define BS_HD __host__ __device__ __forceinline__
@@ -203,19 +207,26 @@ BS_HD void t_bilinear(const float q[4], const float p[4], float t[9]) {
   t[8] = ww - xx - yy + zz;
 }
 
-// int128 -> float (round-to-nearest of the high part, then add the low part)
+// int128 -> float from three 32-bit pieces (|v| < 2^95); 32-bit integer
+// conversions avoid the 64-bit ones, which run on the slow FP64 pipe.
 BS_HD float i128_to_f32(__int128 v) {
-  const long long hi = (long long)(v >> 64);
-  const unsigned long long lo = (unsigned long long)v;
-  return (float)hi * 18446744073709551616.0f + (float)lo;
+  const int top = (int)(long long)(v >> 64);
+  const unsigned mid = (unsigned)((unsigned long long)v >> 32);
+  const unsigned low = (unsigned)(unsigned long long)v;
+  return fmaf((float)top, 18446744073709551616.0f, fmaf((float)mid, 4294967296.0f, (float)low));
+}
+
+// int64 -> float from two 32-bit pieces (|v| < 2^63).
+BS_HD float i64_to_f32(long long v) {
+  return fmaf((float)(int)(v >> 32), 4294967296.0f, (float)(unsigned)(unsigned long long)v);
 }
 
 // ----------------------------------------------------- fast-path epilogue
 // The fast path runs in three phases so that the tensor-core epilogue can
 // stream one TMEM level accumulator at a time:
 //   1. fast_begin: FP32 covariance m (from all levels) -> FP32 QCP eigenpair,
-//      unit eigenvector split q = q_h + q_l with q_h on the 2^-15 grid
-//      (Q_h = 2^15 q_h integers, |T(Q_h)| <= |Q_h|^2 <= 2^30), exact integer
+//      unit eigenvector split q = q_h + q_l with q_h on the 2^-17 grid
+//      (Q_h = 2^17 q_h integers, |T(Q_h)| <= |Q_h|^2 <= 2^34), exact int64
 //      T(Q_h), and the small FP32 terms 4 B(q_h,q_l) + 2 F(q_l);
 //   2. fast_level (l = 0..3): U_l += sum_xy T_xy S_l,xy, exactly in int64 for
 //      l = 0, 1, 2 and in FP32 for l = 3;
@@ -227,16 +238,17 @@ BS_HD float m_from_levels(float s0, float s1, float s2, float s3) {
 }
 
 struct FastState {
-  int T[9];
+  long long T[9];
   long long U0, U1, U2;
   float U3;
-  float rest;  // 4 B(q_h,q_l) + 2 F(q_l), units 2^28 u
-  float qq;    // |q|^2 of the (unit) eigenvector as represented
-  int q2;      // |Q_h|^2
-  int flag;    // 1: degenerate eigenvector, recompute exactly
+  float rest;    // 4 B(q_h,q_l) + 2 F(q_l), units 2^28 u
+  float qq;      // |q|^2 of the (unit) eigenvector as represented
+  long long q2;  // |Q_h|^2
+  float qh[4];   // q_h as floats (exact), for the level-3 term
+  int flag;      // 1: degenerate eigenvector, recompute exactly
 };
 
-BS_HD void fast_begin(const float m[9], long long gsum, FastState &st) {
+BS_HD void fast_begin(const float m[9], float gsum_f, FastState &st) {
   st.U0 = st.U1 = st.U2 = 0;
   st.U3 = 0.f;
   st.flag = 0;
@@ -245,8 +257,10 @@ BS_HD void fast_begin(const float m[9], long long gsum, FastState &st) {
   st.q2 = 0;
 #pragma unroll
   for (int i = 0; i < 9; ++i) st.T[i] = 0;
-  if (gsum <= 0) return;  // both structures collapse onto one point: E = 0
-  const float lam0 = (float)gsum * 1.862645149230957e-9f;  // gsum / 2 in units 2^28 u: 2^-29
+#pragma unroll
+  for (int i = 0; i < 4; ++i) st.qh[i] = 0.f;
+  if (!(gsum_f > 0.f)) return;  // both structures collapse onto one point: E = 0
+  const float lam0 = gsum_f * 1.862645149230957e-9f;  // (Ga+Gb)/2 in units 2^28 u: 2^-29
   const float inv = BS_FDIV(1.0f, lam0);
   float sn[9];
 #pragma unroll
@@ -258,19 +272,21 @@ BS_HD void fast_begin(const float m[9], long long gsum, FastState &st) {
     st.flag = 1;
     return;
   }
-  const float qs = rsqrtf(qsq) * 0.99999f;  // unit length (a hair below, so |Q_h|^2 <= 2^30)
+  const float qs = rsqrtf(qsq) * 0.99999f;  // unit length (a hair below, so |Q_h|^2 <= 2^34)
   float qn[4], qh[4], ql[4];
-  int Q[4];
+  long long Q[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     qn[i] = q[i] * qs;
-    const float h = rintf(qn[i] * 32768.f);
-    Q[i] = (int)h;
-    qh[i] = h * 3.0517578125e-5f;  // 2^-15
+    const float h = rintf(qn[i] * 131072.f);
+    Q[i] = (long long)(int)h;
+    qh[i] = h * 7.62939453125e-6f;  // 2^-17
     ql[i] = qn[i] - qh[i];
   }
-  t_of_q<int>(Q, st.T);
+  t_of_q<long long>(Q, st.T);
   st.q2 = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2] + Q[3] * Q[3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) st.qh[i] = qh[i];
   float tb[9], tl[9];
   t_bilinear(qh, ql, tb);
   t_of_q<float>(ql, tl);
@@ -293,62 +309,81 @@ BS_HD void fast_level(FastState &st, int level, const float s[9]) {
   if (level < 3) {
     long long u = 0;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) u += (long long)st.T[i] * (long long)(int)s[i];
+    for (int i = 0; i < 9; ++i) u += st.T[i] * (long long)(int)s[i];
     if (level == 0) st.U0 += u;
     else if (level == 1) st.U1 += u;
     else st.U2 += u;
   } else {
-    float u = st.U3;
+    // level 3 weighs 2^-27 of level 0: T(q_h) in FP32 is accurate enough
+    float t[9];
+    t_of_q<float>(st.qh, t);
+    float u = 0.f;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) u = fmaf((float)st.T[i], s[i], u);
-    st.U3 = u;
+    for (int i = 0; i < 9; ++i) u = fmaf(t[i], s[i], u);
+    st.U3 += u * 17179869184.0f;  // T(Q_h) = 2^34 T(q_h)
   }
 }
 
-BS_HD float fast_finish(const FastState &st, long long gsum, float low_a, float low_b, int scale_exp, int L,
+// gsum: exact Ga + Gb (units u); gsum_f: the same as float; qsum: the two
+// structures' quantisation residual RMS (Angstrom) -- by Minkowski, the
+// crmsd of the quantised pair is within qsum of the exact one; d34: bound on
+// the level-3 accumulator's rounding, as an error of E (units u); u:
+// Angstrom^2 per unit; tol: certified |dRMSD| budget per pair.
+BS_HD float fast_finish(const FastState &st, long long gsum, float gsum_f, float qsum, float d34, float u, int L,
                         float tol, int &flag) {
   flag = st.flag;
   if (gsum <= 0 || st.flag) return 0.f;
-  // 2 F(q_h) 2^30 in units u = gsum |Q_h|^2 - 2 (2^28 U0 + 2^19 U1 + 2^10 U2 + 2 U3)
+  // 2 F(q_h) 2^34 in units u = gsum |Q_h|^2 - 2 (2^28 U0 + 2^19 U1 + 2^10 U2 + 2 U3)
   __int128 c = (__int128)gsum * (__int128)st.q2;
   c -= ((__int128)st.U0 << 29) + ((__int128)st.U1 << 20) + ((__int128)st.U2 << 11);
-  const float twoFh = (i128_to_f32(c) - 4.f * st.U3) * 9.313225746154785e-10f;  // 2^-30 -> u
+  const float twoFh = (i128_to_f32(c) - 4.f * st.U3) * 5.820766091346741e-11f;  // 2^-34 -> u
   const float twoF = twoFh + st.rest * 268435456.0f;                              // 2^28 -> u
   const float e_u = BS_FDIV(twoF, st.qq);
-  const float u = ldexpf(1.0f, 2 * scale_exp);  // Angstrom^2 per unit
   const float e_a2 = fmaxf(e_u, 0.f) * u;
   const float rmsd = sqrtf(BS_FDIV(e_a2, (float)L));
-  // error bound on E: dropped level 4 (Weyl: 2 sqrt(3) sqrt(N2a N2b)) plus
-  // the FP32 arithmetic of the fast path: rounding of m and of the bilinear
-  // sum against |q_l| <= 2^-15 stays below 2^-32.8 (Ga+Gb); bounded by 2^-32
-  const float d4 = 3.4641016f * low_a * low_b;
-  const float darith = (float)gsum * 2.3283064365386963e-10f;  // 2^-32 (Ga+Gb)
-  const float de_a2 = (d4 + darith) * u;
+  // error bound on E: level-3 accumulator rounding plus the FP32 arithmetic
+  // of the fast path: the rounding of m and of the bilinear sum against
+  // |q_l| <= 2^-18 stays below 2^-34.8 (Ga+Gb); bounded by 2^-34
+  const float darith = gsum_f * 5.820766091346741e-11f;  // 2^-34 (Ga+Gb)
+  const float de_a2 = (d34 + darith) * u;
   const float elo = fmaxf(e_a2 - de_a2, 0.f);
-  // |dRMSD| <= dE / (sqrt(L) sqrt(E_lo)): recompute when dE^2 > tol^2 L E_lo
-  if (de_a2 * de_a2 > tol * tol * (float)L * elo) flag = 1;
+  // the fast path gets what quantisation leaves of the budget (at least 1e-5)
+  const float tf = fmaxf(tol - qsum, 1e-5f);
+  // |dRMSD| <= dE / (sqrt(L) sqrt(E_lo)): recompute when dE^2 > tf^2 L E_lo
+  if (de_a2 * de_a2 > tf * tf * (float)L * elo) flag = 1;
   return rmsd;
 }
 
 // All three phases for one pair whose level sums are at hand.
 struct EpilogueIn {
-  float s0[9], s1[9], s2[9], s3[9];
-  long long ga, gb;
-  float low_a, low_b;  // sqrt(sum d2^2) of each structure
+  float s0[9], s1[9], s2[9], s3[9];  // s3 holds S3 + S4/512
+  long long ga, gb;                  // exact Ghat
+  float gfa, gfb;                    // Ghat as float
+  float qa, qb;                      // quantisation residual RMS (Angstrom)
 };
 
-BS_HD float pair_rmsd_fast(const EpilogueIn &in, int scale_exp, int L, float tol, int &flag) {
-  const long long gsum = in.ga + in.gb;
+BS_HD float pair_rmsd_fast(const EpilogueIn &in, float u, float d34, int L, float tol, int &flag) {
+  const float gsum_f = in.gfa + in.gfb;
   float m[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) m[i] = m_from_levels(in.s0[i], in.s1[i], in.s2[i], in.s3[i]);
   FastState st;
-  fast_begin(m, gsum, st);
+  fast_begin(m, gsum_f, st);
   fast_level(st, 0, in.s0);
   fast_level(st, 1, in.s1);
   fast_level(st, 2, in.s2);
   fast_level(st, 3, in.s3);
-  return fast_finish(st, gsum, in.low_a, in.low_b, scale_exp, L, tol, flag);
+  return fast_finish(st, in.ga + in.gb, gsum_f, in.qa + in.qb, d34, u, L, tol, flag);
+}
+
+// Bits of the double nearest to a non-negative float, built with integer
+// operations (the float -> double conversion runs on the slow FP64 pipe).
+BS_HD unsigned long long f32_to_f64_bits(float f) {
+  unsigned b;
+  memcpy(&b, &f, 4);
+  if ((b & 0x7f800000u) == 0u) return (unsigned long long)(b & 0x80000000u) << 32;  // zero (flushes subnormals)
+  return ((unsigned long long)(b & 0x80000000u) << 32) | (((unsigned long long)(b & 0x7fffffffu) << 29) +
+                                                         ((unsigned long long)896 << 52));
 }
 
 // ------------------------------------------------------------ FP64 QCP
@@ -371,15 +406,19 @@ BS_HD double qcp_deficit_f64(const double sn[9]) {
   const double t23 = k22 * k33 - k23 * k23, t13 = k12 * k33 - k23 * k13, t12 = k12 * k23 - k22 * k13;
   const double t03 = k02 * k33 - k23 * k03, t02 = k02 * k23 - k22 * k03, t01 = k02 * k13 - k12 * k03;
   const double c0 = s01 * t23 - s02 * t13 + s03 * t12 + s12 * t03 - s13 * t02 + s23 * t01;
+  // Halley iterations from the upper bound 1 (cubic convergence; the
+  // largest root is simple and P is convex above it)
   double x = 1.0;
-  for (int it = 0; it < 60; ++it) {
+  for (int it = 0; it < 12; ++it) {
     const double x2 = x * x;
     const double p = ((x2 + c2) * x + c1) * x + c0;
     const double dp = (4.0 * x2 + 2.0 * c2) * x + c1;
-    if (!(dp > 0.0)) break;
-    const double dx = p / dp;
+    const double ddp = 12.0 * x2 + 2.0 * c2;
+    const double den = 2.0 * dp * dp - p * ddp;
+    if (!(den > 0.0)) break;
+    const double dx = 2.0 * p * dp / den;
     x -= dx;
-    if (fabs(dx) <= 1e-16 * fabs(x)) break;
+    if (fabs(dx) <= 1e-17) break;
   }
   return 1.0 - x;
 }
@@ -404,25 +443,24 @@ BS_HD double top_vec_f64(const double sn[9], double x, double q[4]) {
   const double k12 = sxy + syx, k13 = szx + sxz, k23 = syz + szy;
   const double b00 = sxx + syy + szz - x, b11 = sxx - syy - szz - x, b22 = -sxx + syy - szz - x,
                b33 = -sxx - syy + szz - x;
-  const double r[4][4] = {{b00, k01, k02, k03}, {k01, b11, k12, k13}, {k02, k12, b22, k23}, {k03, k13, k23, b33}};
-  double best = -1.0;
-  int jb = 0;
-  for (int j = 0; j < 4; ++j) {
-    int id[3], c = 0;
-    for (int t = 0; t < 4; ++t)
-      if (t != j) id[c++] = t;
-    const double m00 = r[id[0]][id[0]], m01 = r[id[0]][id[1]], m02 = r[id[0]][id[2]];
-    const double m11 = r[id[1]][id[1]], m12 = r[id[1]][id[2]], m22 = r[id[2]][id[2]];
-    const double cof = m00 * (m11 * m22 - m12 * m12) - m01 * (m01 * m22 - m12 * m02) + m02 * (m01 * m12 - m11 * m02);
-    if (fabs(cof) > best) {
-      best = fabs(cof);
-      jb = j;
-    }
+  const double C0 = b11 * (b22 * b33 - k23 * k23) - k12 * (k12 * b33 - k23 * k13) + k13 * (k12 * k23 - b22 * k13);
+  const double C1 = b00 * (b22 * b33 - k23 * k23) - k02 * (k02 * b33 - k23 * k03) + k03 * (k02 * k23 - b22 * k03);
+  const double C2 = b00 * (b11 * b33 - k13 * k13) - k01 * (k01 * b33 - k13 * k03) + k03 * (k01 * k13 - b11 * k03);
+  const double C3 = b00 * (b11 * b22 - k12 * k12) - k01 * (k01 * b22 - k12 * k02) + k02 * (k01 * k12 - b11 * k02);
+  const double a0 = fabs(C0), a1 = fabs(C1), a2 = fabs(C2), a3 = fabs(C3);
+  int j = 0;
+  double best = a0;
+  if (a1 > best) { best = a1; j = 1; }
+  if (a2 > best) { best = a2; j = 2; }
+  if (a3 > best) { best = a3; j = 3; }
+  const double r0[4] = {b00, k01, k02, k03}, r1[4] = {k01, b11, k12, k13};
+  const double r2[4] = {k02, k12, b22, k23}, r3[4] = {k03, k13, k23, b33};
+  double A[4], B[4], C[4];
+  for (int i = 0; i < 4; ++i) {
+    A[i] = (j == 0) ? r1[i] : r0[i];
+    B[i] = (j <= 1) ? r2[i] : r1[i];
+    C[i] = (j <= 2) ? r3[i] : r2[i];
   }
-  int id[3], c = 0;
-  for (int t = 0; t < 4; ++t)
-    if (t != jb) id[c++] = t;
-  const double *A = r[id[0]], *B = r[id[1]], *C = r[id[2]];
   const double m01 = B[0] * C[1] - B[1] * C[0], m02 = B[0] * C[2] - B[2] * C[0], m03 = B[0] * C[3] - B[3] * C[0];
   const double m12 = B[1] * C[2] - B[2] * C[1], m13 = B[1] * C[3] - B[3] * C[1], m23 = B[2] * C[3] - B[3] * C[2];
   q[0] = A[1] * m23 - A[2] * m13 + A[3] * m12;

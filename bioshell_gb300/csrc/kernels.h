@@ -26,11 +26,19 @@ __host__ __device__ inline int64_t digit_row(int64_t s, int c) {
 inline int64_t blocks_for(int64_t n) { return (n + kBlockStructs - 1) / kBlockStructs; }
 inline int lp_for(int L) { return ((L + 15) / 16) * 16; }
 
+// Per-structure data of the mixed path (one 16-byte load per structure).
+struct __align__(16) SInfo {
+  long long ghat;  // exact sum of squared quantised coordinates (units u)
+  float gf;        // ghat as float
+  float qres;      // RMS of the quantisation residual y - 2^e n (Angstrom, rounded up)
+};
+
 // Scalars the kernels exchange through device memory.
 struct DevScalars {
   unsigned long long maxabs_bits;   // max |centred coordinate| (double bits)
   unsigned long long norm_max[3];   // max over (structure, coord) of sum d_i^2
   unsigned long long flag_count;    // pairs queued for exact recomputation
+  unsigned long long qres_max_bits; // max per-structure quantisation residual RMS (float bits)
   int scale_exp;                    // grid exponent e (coordinates in units 2^e A)
   int err;                          // error bits (kErr*)
   int scale_min;                    // lower bound on e requested by the host
@@ -54,9 +62,9 @@ struct OutDesc {
 cudaError_t launch_prep_stats(const double *xyz, int64_t n, int L, double *ctr, DevScalars *sc,
                               cudaStream_t st);
 cudaError_t launch_prep_scale(DevScalars *sc, cudaStream_t st);
+// dig[0..3]: e0, e1, e2 = 16 d2, and d2 / 32 (the level-4 operand)
 cudaError_t launch_prep_digits(const double *xyz, const double *ctr, int64_t n, int L, int lp,
-                               __nv_bfloat16 *d0, __nv_bfloat16 *d1, __nv_bfloat16 *d2, long long *ghat,
-                               float *low, DevScalars *sc, cudaStream_t st);
+                               __nv_bfloat16 *const *dig, SInfo *info, DevScalars *sc, cudaStream_t st);
 cudaError_t launch_prep_plain(const double *xyz, const double *ctr, int64_t n, int L, int lp, double *y,
                               double *g, cudaStream_t st);
 
@@ -72,33 +80,31 @@ struct TcArgs {
   int64_t ntiles;
   int64_t n;
   int L, lp;
-  const long long *ghat;
-  const float *low;
+  const SInfo *info;
   DevScalars *sc;
-  float tol;
+  float tol;  // certified |dRMSD| budget per pair (Angstrom)
+  float u;    // Angstrom^2 per unit of the quantised products
+  float d34;  // level-3 accumulator rounding bound, as an error of E (units u)
   OutDesc out;
   unsigned long long *flags;
   unsigned long long flag_cap;
   float *dbg;  // optional dump of the first tile's raw level sums
   int num_sms;
 };
-cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [6]: A digits 0-2, B digits 0-2 */, const TcArgs &a,
-                            cudaStream_t st);
+cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [7]: A digits e0 e1 e2 d2/32, B digits e0 e1 e2 */,
+                            const TcArgs &a, cudaStream_t st);
 size_t mixed_tc_smem_bytes();
 
 // refine.cu
-cudaError_t launch_refine_list(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2,
-                               int lp, int L, const long long *ghat, DevScalars *sc,
-                               const unsigned long long *flags, unsigned long long cap, OutDesc out,
-                               int num_sms, cudaStream_t st);
-cudaError_t launch_refine_scan(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2,
-                               int lp, int L, const long long *ghat, DevScalars *sc, OutDesc out, int num_sms,
+cudaError_t launch_refine_list(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               const unsigned long long *flags, unsigned long long cap, OutDesc out, int num_sms,
                                cudaStream_t st);
+cudaError_t launch_refine_scan(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               OutDesc out, int num_sms, cudaStream_t st);
 // CUDA-core level sums + the same epilogue for an explicit pair list (used
 // for sparse pair lists and as the tensor-core path's independent check).
-cudaError_t launch_mixed_pairs(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
-                               int L, const long long *ghat, const float *low, DevScalars *sc, float tol,
-                               const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
-                               cudaStream_t st);
+cudaError_t launch_mixed_pairs(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               float tol, float u, float d34, const int64_t *ii, const int64_t *jj, int64_t np,
+                               double *out, float *levels_out, cudaStream_t st);
 
 }  // namespace bs

@@ -4,8 +4,10 @@
 // SubstructureAxis centres, calc/substructures.rs:26-31), largest centred
 // coordinate, then either
 //   - mixed path: quantisation onto the grid 2^e, balanced digits (9, 9 and
-//     5 bits) written as bf16 rows of the digit matrices, exact squared norm Ghat
-//     (int64) and digit norms for the exactness bound; or
+//     5 bits) written as bf16 rows of the digit matrices (plus the low digit
+//     scaled by 1/32, the operand of the level-4 product), exact squared norm
+//     Ghat, the RMS quantisation residual and digit norms for the exactness
+//     bound; or
 //   - plain path: the centred f64 coordinates in K-major [n][3][lp] and G.
 // One block per structure; the [L][3] AoS input of a structure is one
 // contiguous range, read coalesced.
@@ -112,11 +114,12 @@ __global__ void k_prep_scale(DevScalars *sc) {
 __global__ void __launch_bounds__(kPrepThreads)
     k_prep_digits(const double *__restrict__ xyz, const double *__restrict__ ctr, int L, int lp,
                   __nv_bfloat16 *__restrict__ d0, __nv_bfloat16 *__restrict__ d1, __nv_bfloat16 *__restrict__ d2,
-                  long long *__restrict__ ghat, float *__restrict__ low, DevScalars *sc) {
+                  __nv_bfloat16 *__restrict__ d2s, SInfo *__restrict__ info, DevScalars *sc) {
   __shared__ long long red[4 * 10];
+  __shared__ double redd[4];
   const int64_t s = blockIdx.x;
   const int e = sc->scale_exp;
-  const double inv_r = ldexp(1.0, -e);
+  const double r = ldexp(1.0, e), inv_r = ldexp(1.0, -e);
   const double *x = xyz + s * 3 * (int64_t)L;
   const double cc[3] = {ctr[3 * s], ctr[3 * s + 1], ctr[3 * s + 2]};
   int64_t row[3];
@@ -126,16 +129,20 @@ __global__ void __launch_bounds__(kPrepThreads)
   long long acc[10];
 #pragma unroll
   for (int i = 0; i < 10; ++i) acc[i] = 0;
+  double res[1] = {0.0};  // sum of squared quantisation residuals
   for (int k = threadIdx.x; k < L; k += kPrepThreads) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const double y = x[3 * k + c] - cc[c];
       const int q = __double2int_rn(y * inv_r);
+      const double dq = y - (double)q * r;
+      res[0] += dq * dq;
       int a, b, d;
       bsm::split_digits(q, a, b, d);
       d0[row[c] + k] = __float2bfloat16_rn((float)a);
       d1[row[c] + k] = __float2bfloat16_rn((float)b);
       d2[row[c] + k] = __float2bfloat16_rn((float)d);
+      d2s[row[c] + k] = __float2bfloat16_rn((float)d * (1.0f / 512.0f));  // d2 / 32 = e2 / 512
       acc[0] += (long long)q * q;
       acc[1 + c] += (long long)(a * a);
       acc[4 + c] += (long long)(b * b);
@@ -143,9 +150,15 @@ __global__ void __launch_bounds__(kPrepThreads)
     }
   }
   block_sum<long long, 10>(acc, red);
+  block_sum<double, 1>(res, redd);
   if (threadIdx.x == 0) {
-    ghat[s] = acc[0];
-    low[s] = (float)(sqrt((double)(acc[7] + acc[8] + acc[9])) * 0.0625);  // sqrt(sum d2^2), e2 = 16 d2
+    SInfo in;
+    in.ghat = acc[0];
+    in.gf = (float)acc[0];
+    // rounded up so that the Minkowski bound stays a bound
+    in.qres = (float)(sqrt(res[0] / (double)L) * (1.0 + 1e-6)) + 1e-12f;
+    info[s] = in;
+    atomicMax(&sc->qres_max_bits, (unsigned long long)__float_as_uint(in.qres));
     for (int i = 0; i < 3; ++i) {
       long long mx = acc[1 + 3 * i];
       mx = acc[2 + 3 * i] > mx ? acc[2 + 3 * i] : mx;
@@ -191,10 +204,9 @@ cudaError_t launch_prep_scale(DevScalars *sc, cudaStream_t st) {
 }
 
 cudaError_t launch_prep_digits(const double *xyz, const double *ctr, int64_t n, int L, int lp,
-                               __nv_bfloat16 *d0, __nv_bfloat16 *d1, __nv_bfloat16 *d2, long long *ghat,
-                               float *low, DevScalars *sc, cudaStream_t st) {
+                               __nv_bfloat16 *const *dig, SInfo *info, DevScalars *sc, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  k_prep_digits<<<(unsigned)n, kPrepThreads, 0, st>>>(xyz, ctr, L, lp, d0, d1, d2, ghat, low, sc);
+  k_prep_digits<<<(unsigned)n, kPrepThreads, 0, st>>>(xyz, ctr, L, lp, dig[0], dig[1], dig[2], dig[3], info, sc);
   return cudaGetLastError();
 }
 

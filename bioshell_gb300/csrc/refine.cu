@@ -73,17 +73,17 @@ __device__ __forceinline__ void exact_cov_partial(const Digits &dg, int64_t i, i
 }
 
 __device__ __forceinline__ double exact_pair_warp(const Digits &dg, int64_t i, int64_t j, int L,
-                                                  const long long *ghat, int scale_exp, int lane) {
+                                                  const SInfo *info, int scale_exp, int lane) {
   long long mh[9];
   exact_cov_partial(dg, i, j, L, lane, 32, mh);
 #pragma unroll
   for (int e = 0; e < 9; ++e)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mh[e] += __shfl_xor_sync(0xffffffffu, mh[e], o);
-  return bsm::pair_rmsd_exact(mh, ghat[i], ghat[j], scale_exp, L);
+  return bsm::pair_rmsd_exact(mh, info[i].ghat, info[j].ghat, scale_exp, L);
 }
 
-__global__ void k_refine_list(Digits dg, int L, const long long *__restrict__ ghat, DevScalars *sc,
+__global__ void k_refine_list(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc,
                               const unsigned long long *__restrict__ flags, unsigned long long cap, OutDesc out) {
   const unsigned long long cnt = sc->flag_count < cap ? sc->flag_count : cap;
   const int lane = threadIdx.x & 31;
@@ -92,14 +92,14 @@ __global__ void k_refine_list(Digits dg, int L, const long long *__restrict__ gh
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)cnt; w += warps) {
     const unsigned long long f = flags[w];
     const int64_t i = (int64_t)(f >> 32), j = (int64_t)(f & 0xffffffffull);
-    const double r = exact_pair_warp(dg, i, j, L, ghat, scale_exp, lane);
+    const double r = exact_pair_warp(dg, i, j, L, info, scale_exp, lane);
     if (lane == 0) store_pair(out, i, j, r);
   }
 }
 
 // Fallback when the flag list overflowed: every negative (sentinel) entry of
 // the output is recomputed.
-__global__ void k_refine_scan(Digits dg, int L, const long long *__restrict__ ghat, DevScalars *sc, OutDesc out) {
+__global__ void k_refine_scan(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc, OutDesc out) {
   const int lane = threadIdx.x & 31;
   const int64_t n = out.n;
   const int64_t total = n * (n - 1) / 2;
@@ -123,27 +123,30 @@ __global__ void k_refine_scan(Digits dg, int L, const long long *__restrict__ gh
       m &= m - 1;
       const int64_t si = __shfl_sync(0xffffffffu, i, src);
       const int64_t sj = __shfl_sync(0xffffffffu, j, src);
-      const double r = exact_pair_warp(dg, si, sj, L, ghat, scale_exp, lane);
+      const double r = exact_pair_warp(dg, si, sj, L, info, scale_exp, lane);
       if (lane == 0) store_pair(out, si, sj, r);
     }
   }
 }
 
 // Thread per pair: exact level sums on CUDA cores, the fast epilogue, and
-// the exact path when the pair is flagged.
-__global__ void k_mixed_pairs(Digits dg, int L, const long long *__restrict__ ghat, const float *__restrict__ low,
-                              DevScalars *sc, float tol, const int64_t *__restrict__ ii, const int64_t *__restrict__ jj,
-                              int64_t np, double *__restrict__ out, float *__restrict__ levels_out) {
+// the exact path when the pair is flagged.  Level 3 carries S3 + S4/512 as
+// the tensor cores accumulate it (here rounded once from the exact value).
+__global__ void k_mixed_pairs(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc, float tol, float u,
+                              float d34, const int64_t *__restrict__ ii, const int64_t *__restrict__ jj, int64_t np,
+                              double *__restrict__ out, float *__restrict__ levels_out) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= np) return;
   const int64_t i = ii[t], j = jj[t];
   if (i == j) {
     out[t] = 0.0;
+    if (levels_out)
+      for (int e = 0; e < 36; ++e) levels_out[t * 36 + e] = 0.f;
     return;
   }
-  int S[4][9];
+  int S[5][9];
 #pragma unroll
-  for (int l = 0; l < 4; ++l)
+  for (int l = 0; l < 5; ++l)
 #pragma unroll
     for (int e = 0; e < 9; ++e) S[l][e] = 0;
   const int lp = dg.lp;
@@ -168,64 +171,68 @@ __global__ void k_mixed_pairs(Digits dg, int L, const long long *__restrict__ gh
         S[1][e] += a[x][0] * b[y][1] + a[x][1] * b[y][0];
         S[2][e] += a[x][0] * b[y][2] + a[x][1] * b[y][1] + a[x][2] * b[y][0];
         S[3][e] += a[x][1] * b[y][2] + a[x][2] * b[y][1];
+        S[4][e] += (a[x][2] >> 4) * (b[y][2] >> 4);  // sum d2a d2b; S4/512 = (sum d2a d2b) / 2
       }
   }
+  const SInfo ia = info[i], ib = info[j];
   bsm::EpilogueIn in;
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
     in.s0[e] = (float)S[0][e];
     in.s1[e] = (float)S[1][e];
     in.s2[e] = (float)S[2][e];
-    in.s3[e] = (float)S[3][e];
+    in.s3[e] = (float)((double)S[3][e] + 0.5 * (double)S[4][e]);
   }
-  in.ga = ghat[i];
-  in.gb = ghat[j];
-  in.low_a = low[i];
-  in.low_b = low[j];
+  in.ga = ia.ghat;
+  in.gb = ib.ghat;
+  in.gfa = ia.gf;
+  in.gfb = ib.gf;
+  in.qa = ia.qres;
+  in.qb = ib.qres;
   if (levels_out) {
 #pragma unroll
-    for (int l = 0; l < 4; ++l)
-#pragma unroll
-      for (int e = 0; e < 9; ++e) levels_out[t * 36 + l * 9 + e] = (float)S[l][e];
+    for (int e = 0; e < 9; ++e) {
+      levels_out[t * 36 + e] = in.s0[e];
+      levels_out[t * 36 + 9 + e] = in.s1[e];
+      levels_out[t * 36 + 18 + e] = in.s2[e];
+      levels_out[t * 36 + 27 + e] = in.s3[e];
+    }
   }
-  const int scale_exp = sc->scale_exp;
   int flag = 0;
-  const float r = bsm::pair_rmsd_fast(in, scale_exp, L, tol, flag);
+  const float r = bsm::pair_rmsd_fast(in, u, d34, L, tol, flag);
   if (!flag) {
     out[t] = (double)r;
     return;
   }
   long long mh[9];
   exact_cov_partial(dg, i, j, L, 0, 1, mh);
-  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, scale_exp, L);
+  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, sc->scale_exp, L);
 }
 
 }  // namespace
 
-cudaError_t launch_refine_list(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
-                               int L, const long long *ghat, DevScalars *sc, const unsigned long long *flags,
-                               unsigned long long cap, OutDesc out, int num_sms, cudaStream_t st) {
-  Digits dg{d0, d1, d2, lp};
-  k_refine_list<<<num_sms * 4, 256, 0, st>>>(dg, L, ghat, sc, flags, cap, out);
+cudaError_t launch_refine_list(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               const unsigned long long *flags, unsigned long long cap, OutDesc out, int num_sms,
+                               cudaStream_t st) {
+  Digits dg{dig[0], dig[1], dig[2], lp};
+  k_refine_list<<<num_sms * 4, 256, 0, st>>>(dg, L, info, sc, flags, cap, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_refine_scan(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
-                               int L, const long long *ghat, DevScalars *sc, OutDesc out, int num_sms,
-                               cudaStream_t st) {
-  Digits dg{d0, d1, d2, lp};
-  k_refine_scan<<<num_sms * 4, 256, 0, st>>>(dg, L, ghat, sc, out);
+cudaError_t launch_refine_scan(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               OutDesc out, int num_sms, cudaStream_t st) {
+  Digits dg{dig[0], dig[1], dig[2], lp};
+  k_refine_scan<<<num_sms * 4, 256, 0, st>>>(dg, L, info, sc, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mixed_pairs(const __nv_bfloat16 *d0, const __nv_bfloat16 *d1, const __nv_bfloat16 *d2, int lp,
-                               int L, const long long *ghat, const float *low, DevScalars *sc, float tol,
-                               const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
-                               cudaStream_t st) {
+cudaError_t launch_mixed_pairs(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
+                               float tol, float u, float d34, const int64_t *ii, const int64_t *jj, int64_t np,
+                               double *out, float *levels_out, cudaStream_t st) {
   if (np <= 0) return cudaSuccess;
-  Digits dg{d0, d1, d2, lp};
+  Digits dg{dig[0], dig[1], dig[2], lp};
   const int th = 128;
-  k_mixed_pairs<<<(unsigned)((np + th - 1) / th), th, 0, st>>>(dg, L, ghat, low, sc, tol, ii, jj, np, out,
+  k_mixed_pairs<<<(unsigned)((np + th - 1) / th), th, 0, st>>>(dg, L, info, sc, tol, u, d34, ii, jj, np, out,
                                                                levels_out);
   return cudaGetLastError();
 }

@@ -70,9 +70,10 @@ SIGNATURES = [
                                    _dp, _i64p]),
     ("bs_host_alloc", ctypes.c_int32, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     ("bs_host_free", ctypes.c_int32, [_vp]),
-    ("bs_selftest_digits", ctypes.c_int32, [_dp, ctypes.c_int32, ctypes.c_int32, _i32p, _i64p, _i64p]),
+    ("bs_selftest_digits", ctypes.c_int32, [_dp, ctypes.c_int32, ctypes.c_int32, _i32p, _i64p, _dp]),
     ("bs_selftest_epilogue", ctypes.c_int32, [_fp, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
-                                              ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp, _i32p]),
+                                              ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp,
+                                              _i32p]),
     ("bs_selftest_exact", ctypes.c_int32, [_i32p, _i32p, ctypes.c_int32, ctypes.c_int32, _dp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,

@@ -198,15 +198,17 @@ BS_API bs_status bs_host_free(void *p);
 /* Digits of one structure's centred coordinates at grid 2^scale_exp:
  * digits[3][3][L] (digit-major, then coordinate, then atom) as stored, i.e.
  * e0, e1 and e2 = 16 d2 with n = 2^14 e0 + 2^5 e1 + d2, plus the exact
- * squared norm of n (int64) and the sum of d2^2. */
+ * squared norm of n (int64) and the RMS quantisation residual (Angstrom). */
 BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_exp, int32_t *digits,
-                                    int64_t *g_exact, int64_t *low_norm2);
-/* The mixed-path epilogue for one pair from its four level sums
- * levels[4][9] (exact integers stored as float) and exact squared norms;
- * returns rmsd and whether the pair would be recomputed (flag = 1). */
-BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double low_a,
-                                      double low_b, int32_t scale_exp, int32_t L, double tolerance,
-                                      double *rmsd, int32_t *flag);
+                                    int64_t *g_exact, double *qres);
+/* The mixed-path epilogue for one pair from its level sums levels[4][9]
+ * (levels 0-2 exact integers, level 3 = S3 + S4/512, stored as float), exact
+ * squared norms, quantisation residuals, the level-3 rounding bound d34
+ * (error of E, units 2^(2 scale_exp)) and the total tolerance; returns rmsd
+ * and whether the pair would be recomputed (flag = 1). */
+BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double qa, double qb,
+                                      double d34, int32_t scale_exp, int32_t L, double tolerance, double *rmsd,
+                                      int32_t *flag);
 /* The exact recomputation from integer coordinates n_a[3][L], n_b[3][L]. */
 BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t L, int32_t scale_exp,
                                    double *rmsd);
