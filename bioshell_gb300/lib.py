@@ -64,6 +64,7 @@ SIGNATURES = [
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                   ctypes.POINTER(bs_opts), _vp]),
+    ("bs_all_vs_all_static", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),
     ("bs_hierarchical", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _i64p, _fp]),
     ("bs_cut_tree", ctypes.c_int32, [_i64p, _fp, ctypes.c_int64, ctypes.c_float, _i64p]),
     ("bs_optics", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _i64p,

@@ -152,6 +152,26 @@ BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_
 BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
                           const int64_t *jj, int64_t npairs, const bs_opts *opts, double *out);
 
+/* All-vs-all crmsd without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc: code running inside
+ * another framework's memory pool, plugins that may only use the buffers they
+ * are given, or processes whose device footprint must stay fixed.  `xyz`
+ * ([n][L][3] f64) and `out` (packed f64 upper triangle, n(n-1)/2 values) must
+ * be device memory of the current device; the work runs on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) with the mixed-precision
+ * method of bs_all_vs_all and its default tolerance, and the call returns
+ * when `out` is complete.
+ *   - Limits: n <= 512 structures, L <= 512 atoms; larger sizes return
+ *     BS_ERR_UNSUPPORTED without touching the GPU.
+ *   - Scratch lives in static device arrays of the library (about 7.4 MB,
+ *     held by every GPU that loads the library until the process exits).
+ *   - The first call on a device looks up the arrays' device addresses; make
+ *     it before capturing the stream into a CUDA graph.
+ *   - All calls share the scratch: each call clears what must start at zero,
+ *     but calls whose work overlaps on the GPU (e.g. on two streams at once)
+ *     race and must not be issued. */
+BS_API bs_status bs_all_vs_all_static(const double *xyz, int64_t n, int32_t L, double *out, void *stream);
+
 /* ---- clustering of a crmsd matrix --------------------------------------- */
 /* Merge rules of bioshell-clustering/src/hierarchical/strategies/mod.rs. */
 enum {
