@@ -8,6 +8,8 @@ is bound to in ``bioshell_pdb::calc``:
   ``hierarchical_clustering`` (bioshell-clustering/src/hierarchical/
   hierarchical.rs:22) through ``HierarchicalClusteringMatrix::new``
   (clustering_matrix.rs:11-22), returned as a ``CrmsdMatrix``;
+* ``crmsd_batched(sets, opts)``        -- one matrix per decoy set, all sets in one
+  persistent tensor-core launch (the per-set clustering loop of a caller);
 * ``CrmsdMatrix.get(i, j)`` / ``as_f32_closure()`` -- the ``Fn(usize, usize) -> f32``
   distance closure the clustering takes.
 
@@ -36,6 +38,7 @@ class CrmsdOptions:
     layout: str = "triangle"
     out_type: str = "f64"
     tolerance: Optional[float] = None
+    graph: bool = True  # replay a captured CUDA graph for repeated shapes
 
     def to_c(self) -> _l.bs_opts:
         o = _l.bs_opts()
@@ -44,6 +47,7 @@ class CrmsdOptions:
         o.layout = _l.LAYOUT[self.layout]
         o.out_type = _l.OUT_TYPE[self.out_type]
         o.tolerance = float(self.tolerance or 0.0)
+        o.flags = 0 if self.graph else _l.FLAG_NO_GRAPH
         return o
 
 
@@ -170,6 +174,34 @@ class Engine:
         self._check(self._lib.bs_all_vs_all(self._h, xp, n, L, ctypes.byref(o), op))
         return CrmsdMatrix(n, out, opts.layout)
 
+    def batched(self, sets, opts: Optional[CrmsdOptions] = None, outs=None):
+        """All-vs-all of every set in ``sets`` (each [n][L][3], numpy or CUDA
+        tensor; n and L may differ) in one call; returns one CrmsdMatrix per set."""
+        opts = opts or CrmsdOptions()
+        dt = np.float64 if opts.out_type == "f64" else np.float32
+        descs = (_l.bs_set_desc * max(len(sets), 1))()
+        keep = []
+        mats = []
+        for k, x in enumerate(sets):
+            if isinstance(x, np.ndarray):
+                x = np.ascontiguousarray(x, dtype=np.float64)
+            if len(x.shape) != 3 or x.shape[2] != 3:
+                raise ValueError("each set must be [n][L][3]")
+            n, L = int(x.shape[0]), int(x.shape[1])
+            count = n * (n - 1) // 2 if opts.layout == "triangle" else n * n
+            out = outs[k] if outs is not None else np.empty(count, dtype=dt)
+            xp, k1 = _ptr(x)
+            op, k2 = _ptr(out)
+            keep += [k1, k2]
+            descs[k].xyz = xp
+            descs[k].n = n
+            descs[k].L = L
+            descs[k].out = op
+            mats.append(CrmsdMatrix(n, out, opts.layout))
+        o = opts.to_c()
+        self._check(self._lib.bs_batched(self._h, descs, len(sets), ctypes.byref(o)))
+        return mats
+
     def pairs(self, xyz, ii, jj, opts: Optional[CrmsdOptions] = None, out=None):
         opts = opts or CrmsdOptions()
         if isinstance(xyz, np.ndarray):
@@ -230,3 +262,8 @@ def crmsd_all_vs_all(models, opts: Optional[CrmsdOptions] = None) -> CrmsdMatrix
     if isinstance(models, (list, tuple)):
         models = np.stack([np.asarray(m, dtype=np.float64) for m in models])
     return default_engine().all_vs_all(models, opts)
+
+
+def crmsd_batched(sets, opts: Optional[CrmsdOptions] = None):
+    """All-vs-all crmsd of every decoy set in ``sets``: a list of CrmsdMatrix."""
+    return default_engine().batched(sets, opts)

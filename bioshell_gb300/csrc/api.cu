@@ -1,7 +1,7 @@
 // api.cu -- the C ABI (include/bioshell_crmsd.h): contexts, device
 // workspaces, host<->device staging, the call sequences of the plain and
-// mixed paths, metrics, and the host-side self-test hooks.
-#include <cudaTypedefs.h>
+// mixed paths (single set, batched sets, pair lists), the graph cache,
+// metrics, and the host-side self-test hooks.
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -12,42 +12,12 @@
 #include <string>
 #include <vector>
 
-#include "../../include/bioshell_crmsd.h"
 #include "crmsd_math.cuh"
-#include "kernels.h"
+#include "engine.h"
 
 using namespace bs;
 
-namespace {
-
-constexpr double kDefaultTol = 1e-4;  // Angstrom, certified total |dRMSD| per pair
-constexpr unsigned long long kFlagCap = 1ull << 24;  // queued exact recomputations
-
-struct DevBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-};
-
-}  // namespace
-
-struct bs_ctx {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[6] = {};
-  size_t budget = 0;
-  size_t used = 0;
-  std::string err;
-  bs_metrics metrics{};
-  // workspaces
-  DevBuf xyz, ctr, info, dig[4], y, g, out, tiles, flags, scal, pairs_i, pairs_j, pout;
-  double d34 = 0.0;  // level-3 rounding bound of the last preparation (units u)
-  int64_t tiles_nb = -1;
-  int64_t tiles_count = 0;
-  PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-};
-
-namespace {
+namespace bs {
 
 bs_status set_err(bs_ctx *ctx, bs_status s, const char *fmt, ...) {
   if (ctx) {
@@ -66,12 +36,6 @@ bs_status cuda_err(bs_ctx *ctx, cudaError_t e, const char *what) {
   return set_err(ctx, s, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CK(call, what)                                  \
-  do {                                                  \
-    cudaError_t _e = (call);                            \
-    if (_e != cudaSuccess) return cuda_err(ctx, _e, what); \
-  } while (0)
-
 bs_status ensure(bs_ctx *ctx, DevBuf &b, size_t bytes, const char *what) {
   if (bytes == 0) bytes = 16;
   if (b.cap >= bytes) return BS_OK;
@@ -81,6 +45,7 @@ bs_status ensure(bs_ctx *ctx, DevBuf &b, size_t bytes, const char *what) {
     b.p = nullptr;
     b.cap = 0;
   }
+  ++ctx->gen;
   if (ctx->used + bytes > ctx->budget)
     return set_err(ctx, BS_ERR_BUDGET, "%s: %zu bytes would exceed the context budget (%zu of %zu in use)", what,
                    bytes, ctx->used, ctx->budget);
@@ -98,6 +63,7 @@ void release(bs_ctx *ctx, DevBuf &b) {
   if (b.p) {
     cudaFree(b.p);
     ctx->used -= b.cap;
+    ++ctx->gen;
   }
   b.p = nullptr;
   b.cap = 0;
@@ -112,252 +78,317 @@ bool is_device_ptr(const void *p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+}  // namespace bs
+
+namespace {
+
+constexpr double kDefaultTol = 1e-4;                  // Angstrom, certified total |dRMSD| per pair
+constexpr unsigned long long kFlagCap = 1ull << 24;  // queued exact recomputations
+constexpr size_t kMaxGraphs = 16;
+
+#define CK(call, what)                                     \
+  do {                                                     \
+    cudaError_t _e = (call);                               \
+    if (_e != cudaSuccess) return cuda_err(ctx, _e, what); \
+  } while (0)
+
 bs_status check_opts(bs_ctx *ctx, const bs_opts *o) {
-  if (o->version != BS_OPTS_VERSION) return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.version %u != %d", o->version, BS_OPTS_VERSION);
+  if (o->version != BS_OPTS_VERSION)
+    return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.version %u != %d", o->version, BS_OPTS_VERSION);
   if (o->precision != BS_PRECISION_PLAIN64 && o->precision != BS_PRECISION_MIXED)
     return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.precision %d unknown", o->precision);
   if (o->layout != BS_LAYOUT_TRIANGLE && o->layout != BS_LAYOUT_SQUARE)
     return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.layout %d unknown", o->layout);
   if (o->out_type != BS_OUT_F64 && o->out_type != BS_OUT_F32)
     return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.out_type %d unknown", o->out_type);
+  if (o->flags & ~BS_FLAG_NO_GRAPH) return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.flags %d unknown", o->flags);
   return BS_OK;
-}
-
-// Coordinates on the device (copied from the host when needed).
-bs_status stage_coords(bs_ctx *ctx, const double *xyz, int64_t n, int L, const double **dev) {
-  const size_t bytes = (size_t)n * (size_t)L * 3 * sizeof(double);
-  if (is_device_ptr(xyz)) {
-    *dev = xyz;
-    return BS_OK;
-  }
-  bs_status s = ensure(ctx, ctx->xyz, bytes, "coordinates");
-  if (s) return s;
-  CK(cudaMemcpyAsync(ctx->xyz.p, xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
-  ctx->metrics.bytes_h2d += (int64_t)bytes;
-  *dev = static_cast<const double *>(ctx->xyz.p);
-  return BS_OK;
-}
-
-bs_status read_scalars(bs_ctx *ctx, DevScalars *host) {
-  CK(cudaMemcpyAsync(host, ctx->scal.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read scalars");
-  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
-  return BS_OK;
-}
-
-// Mixed path preparation: centring, grid choice, digits, and the exactness
-// bound: levels 0-2 must stay below 2^24 in magnitude.  With n_i = max over
-// (structure, coordinate) of sqrt(sum e_i^2), Cauchy-Schwarz bounds |S_l| by
-// sum_{i+j=l} n_i n_j; when that reaches 2^24 the grid is coarsened by one bit
-// and the digits are recomputed.  Level 3 (S3 + S4/512) is exact below 2^23;
-// above, its FP32 rounding is bounded here and charged to the error budget.
-bs_status prep_mixed(bs_ctx *ctx, const double *dxyz, int64_t n, int L, int lp, DevScalars *hs) {
-  const int64_t rows = blocks_for(n) * kBlockRows;
-  const size_t dbytes = (size_t)rows * lp * sizeof(__nv_bfloat16);
-  bs_status s;
-  if ((s = ensure(ctx, ctx->ctr, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
-  if ((s = ensure(ctx, ctx->info, (size_t)n * sizeof(SInfo), "structure data"))) return s;
-  for (int d = 0; d < 4; ++d)
-    if ((s = ensure(ctx, ctx->dig[d], dbytes, "digit matrices"))) return s;
-  __nv_bfloat16 *digs[4];
-  for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
-  DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
-  int scale_min = -1000;
-  for (int attempt = 0; attempt < 8; ++attempt) {
-    DevScalars init{};
-    init.scale_min = scale_min;
-    CK(cudaMemcpyAsync(sc, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream), "init scalars");
-    for (int d = 0; d < 4; ++d) CK(cudaMemsetAsync(digs[d], 0, dbytes, ctx->stream), "clear digits");
-    CK(launch_prep_stats(dxyz, n, L, static_cast<double *>(ctx->ctr.p), sc, ctx->stream), "prep stats");
-    CK(launch_prep_scale(sc, ctx->stream), "prep scale");
-    CK(launch_prep_digits(dxyz, static_cast<const double *>(ctx->ctr.p), n, L, lp, digs,
-                          static_cast<SInfo *>(ctx->info.p), sc, ctx->stream),
-       "prep digits");
-    if ((s = read_scalars(ctx, hs))) return s;
-    if (hs->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
-    const double n0 = sqrt((double)hs->norm_max[0]), n1 = sqrt((double)hs->norm_max[1]),
-                 n2 = sqrt((double)hs->norm_max[2]);
-    const double b0 = n0 * n0, b1 = 2 * n0 * n1, b2 = 2 * n0 * n2 + n1 * n1;
-    const double lim = 16777216.0;  // 2^24
-    if (b0 < lim && b1 < lim && b2 < lim) {
-      const double b34 = 2 * n1 * n2 + n2 * n2 / 512.0;
-      double err3 = 0.0;  // level-3 units
-      if (b34 >= 8388608.0) {  // 2^23: half-integers no longer exact
-        const int k = (int)floor(log2(b34));
-        err3 = 3.0 * (double)L * ldexp(1.0, k - 24);
-      }
-      // Mhat carries 2 S3' -> |dM| <= 2 err3 u per entry; |dE| <= 2 sqrt(3) ||dM||_F
-      ctx->d34 = 12.0 * sqrt(3.0) * err3;
-      return BS_OK;
-    }
-    scale_min = hs->scale_exp + 1;
-  }
-  return set_err(ctx, BS_ERR_UNSUPPORTED,
-                 "chain length %d too long for exact 3-digit level sums (bound not met after 8 coarsenings)", L);
-}
-
-// Tensor-core tiles: row blocks I of 40 structures against column blocks J
-// of 20 structures, kept when some pair i < j falls in the tile (J >= 2I),
-// in super-block order so that the tiles in flight at any time touch a
-// working set that stays in L2.
-void build_tiles(int64_t n, std::vector<int2> &t) {
-  const int64_t nba = blocks_for(n), nbb = (n + 19) / 20;
-  const int64_t SA = 32, SBB = 64;
-  t.clear();
-  for (int64_t sa = 0; sa < nba; sa += SA)
-    for (int64_t sb = 2 * sa; sb < nbb; sb += SBB)
-      for (int64_t I = sa; I < std::min(sa + SA, nba); ++I)
-        for (int64_t J = std::max(sb, 2 * I); J < std::min(sb + SBB, nbb); ++J)
-          t.push_back(make_int2((int)I, (int)J));
-}
-
-bs_status encode_maps(bs_ctx *ctx, int64_t rows, int lp, CUtensorMap *tm) {
-  if (!ctx->encode) {
-    cudaDriverEntryPointQueryResult q;
-    void *fn = nullptr;
-    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
-       "driver entry point cuTensorMapEncodeTiled");
-    if (q != cudaDriverEntryPointSuccess || !fn)
-      return set_err(ctx, BS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable in the driver");
-    ctx->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
-  // maps 0-3: A operand boxes (64 atoms x 128 rows) of e0, e1, e2, d2/32;
-  // maps 4-6: B boxes (64 x 64) of e0, e1, e2
-  for (int m = 0; m < 7; ++m) {
-    const int d = m < 4 ? m : m - 4;
-    cuuint64_t gdim[2] = {(cuuint64_t)lp, (cuuint64_t)rows};
-    cuuint64_t gstride[1] = {(cuuint64_t)lp * 2};
-    cuuint32_t box[2] = {64, m < 4 ? 128u : 64u};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = ctx->encode(&tm[m], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, ctx->dig[d].p, gdim, gstride, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return set_err(ctx, BS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-  }
-  return BS_OK;
-}
-
-size_t out_elems(int64_t n, int layout) {
-  return layout == BS_LAYOUT_TRIANGLE ? (size_t)(n * (n - 1) / 2) : (size_t)n * (size_t)n;
 }
 
 // Certified per-pair |dRMSD| budget: the kernels charge each pair its two
 // structures' quantisation residuals (Minkowski) and give the fast path the
 // rest (at least 1e-5 A).
 float total_tolerance(const bs_opts &o) { return (float)(o.tolerance > 0 ? o.tolerance : kDefaultTol); }
-float qres_max(const DevScalars &hs) {
-  float f;
-  const unsigned b = (unsigned)hs.qres_max_bits;
-  memcpy(&f, &b, 4);
-  return f;
-}
 
-bs_status check_device_errors(bs_ctx *ctx, DevScalars *hs) {
-  bs_status s = read_scalars(ctx, hs);
-  if (s) return s;
-  if (hs->err & kErrTimeout) return set_err(ctx, BS_ERR_TIMEOUT, "a device-side wait timed out");
-  if (hs->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
-  if (hs->err & kErrInternal) return set_err(ctx, BS_ERR_INTERNAL, "device-side invariant violated");
-  return BS_OK;
+size_t out_elems(int64_t n, int layout) {
+  return layout == BS_LAYOUT_TRIANGLE ? (size_t)(n * (n - 1) / 2) : (size_t)n * (size_t)n;
 }
 
 float elapsed(bs_ctx *ctx, int a, int b) {
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
+  if (cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.f;
+  }
   return ms;
 }
 
-bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const bs_opts &o, void *out) {
-  ctx->metrics = bs_metrics{};
-  const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
-  const size_t nout = out_elems(n, o.layout);
-  const bool out_dev = is_device_ptr(out);
+bs_status ensure_stage(bs_ctx *ctx, size_t njobs) {
+  const size_t bytes = std::max<size_t>(njobs, 1) * sizeof(Job);
+  if (ctx->job_stage_cap >= bytes) return BS_OK;
+  if (ctx->job_stage) cudaFreeHost(ctx->job_stage);
+  if (ctx->job_back) cudaFreeHost(ctx->job_back);
+  ctx->job_stage = ctx->job_back = nullptr;
+  ctx->job_stage_cap = 0;
+  ++ctx->gen;
+  CK(cudaHostAlloc(&ctx->job_stage, bytes, cudaHostAllocDefault), "pinned job table");
+  CK(cudaHostAlloc(&ctx->job_back, bytes, cudaHostAllocDefault), "pinned job table");
+  ctx->job_stage_cap = bytes;
+  return BS_OK;
+}
+
+void drop_graphs(bs_ctx *ctx) {
+  for (auto &g : ctx->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  ctx->graphs.clear();
+}
+
+// Device workspaces for a plan; fills `b` (symmetric jobs: B side = A side).
+bs_status prepare_buffers(bs_ctx *ctx, const Plan &plan, unsigned long long cap, MixedBuffers &b) {
+  const int64_t ns = plan.nblocks * kBlockStructs, rows = plan.nblocks * kBlockRows;
+  const int nj = (int)plan.jobs.size();
+  bs_status s;
+  if ((s = ensure(ctx, ctx->ctr, (size_t)ns * 3 * sizeof(long long), "centroids"))) return s;
+  if ((s = ensure(ctx, ctx->info, (size_t)ns * sizeof(SInfo), "structure data"))) return s;
+  for (int d = 0; d < 4; ++d)
+    if ((s = ensure(ctx, ctx->dig[d], (size_t)rows * plan.pitch * sizeof(__nv_bfloat16), "digit matrices"))) return s;
+  if ((s = ensure(ctx, ctx->jobs, (size_t)nj * sizeof(Job), "job table"))) return s;
+  if ((s = ensure(ctx, ctx->jobmap, (size_t)plan.nblocks * sizeof(int), "block map"))) return s;
+  if ((s = ensure(ctx, ctx->tiles, plan.tiles.size() * sizeof(Tile), "tile table"))) return s;
+  if ((s = ensure(ctx, ctx->flags, (size_t)cap * sizeof(unsigned long long), "flag list"))) return s;
+  if ((s = ensure_stage(ctx, nj))) return s;
+  b = MixedBuffers{};
+  b.ctr = static_cast<long long *>(ctx->ctr.p);
+  b.info_a = static_cast<SInfo *>(ctx->info.p);
+  b.info_b = b.info_a;
+  for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
+  for (int d = 0; d < 3; ++d) b.dig_b[d] = b.dig_a[d];
+  b.pitch_a = b.pitch_b = plan.pitch;
+  b.rows_a = b.rows_b = rows;
+  b.jobs = static_cast<Job *>(ctx->jobs.p);
+  b.jobmap = static_cast<int *>(ctx->jobmap.p);
+  b.tiles = static_cast<Tile *>(ctx->tiles.p);
+  b.flags = static_cast<unsigned long long *>(ctx->flags.p);
+  b.flag_cap = cap;
+  b.sc = static_cast<DevScalars *>(ctx->scal.p);
+  return BS_OK;
+}
+
+// Uploads the block map and tile table when they differ from the last call's.
+bs_status upload_tables(bs_ctx *ctx, const Plan &plan, const MixedBuffers &b, const std::vector<int64_t> &key) {
+  if (key == ctx->plan_key) return BS_OK;
+  CK(cudaMemcpyAsync(b.jobmap, plan.jobmap.data(), plan.jobmap.size() * sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream),
+     "upload block map");
+  if (!plan.tiles.empty())
+    CK(cudaMemcpyAsync(b.tiles, plan.tiles.data(), plan.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice,
+                       ctx->stream),
+       "upload tile table");
+  CK(cudaStreamSynchronize(ctx->stream), "upload tables");  // the vectors are pageable and short-lived
+  ctx->plan_key = key;
+  return BS_OK;
+}
+
+std::vector<int64_t> plan_key(bs_ctx *ctx, const Plan &plan, unsigned long long cap) {
+  std::vector<int64_t> k = {(int64_t)ctx->gen, (int64_t)plan.jobs.size(), plan.nblocks, plan.pitch,
+                            (int64_t)plan.tiles.size(), (int64_t)cap};
+  for (const Job &j : plan.jobs) {
+    k.push_back(j.n);
+    k.push_back(j.L);
+  }
+  return k;
+}
+
+// Runs the device sequence of a plan (graph replay when possible) and reads
+// back the counters; the caller synchronises and calls finish_mixed.
+bs_status launch_plan(bs_ctx *ctx, const Plan &plan, const MixedBuffers &b, bool use_graph) {
+  const int nj = (int)plan.jobs.size();
+  memcpy(ctx->job_stage, plan.jobs.data(), (size_t)nj * sizeof(Job));
+  std::string m = get_encoder(&ctx->encode);
+  if (!m.empty()) return set_err(ctx, BS_ERR_CUDA, "%s", m.c_str());
+  CUtensorMap tm[7];
+  m = encode_maps(ctx->encode, b, tm);
+  if (!m.empty()) return set_err(ctx, BS_ERR_CUDA, "%s", m.c_str());
+  const Job *stage = static_cast<const Job *>(ctx->job_stage);
+  ctx->metrics.main_launches = plan.tiles.empty() ? 5 : 9;
+  if (!use_graph) {
+    CK(enqueue_mixed(plan, b, stage, tm, ctx->num_sms, ctx->stream, &ctx->ev[1], false), "mixed-path launch");
+    ctx->metrics.graph = 0;
+  } else {
+    const std::vector<int64_t> key = plan_key(ctx, plan, b.flag_cap);
+    bs_ctx::Graph *hit = nullptr;
+    for (auto &g : ctx->graphs)
+      if (g.key == key) hit = &g;
+    if (hit) {
+      hit->last = ++ctx->tick;
+      CK(cudaGraphLaunch(hit->exec, ctx->stream), "graph launch");
+      ctx->metrics.graph = 2;
+    } else {
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      const cudaError_t e = enqueue_mixed(plan, b, stage, tm, ctx->num_sms, ctx->stream, &ctx->ev[1], true);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return cuda_err(ctx, e != cudaSuccess ? e : e2, "capture of the mixed-path sequence");
+      }
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t e3 = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e3 != cudaSuccess) return cuda_err(ctx, e3, "graph instantiation");
+      if (ctx->graphs.size() >= kMaxGraphs) {
+        auto old = std::min_element(ctx->graphs.begin(), ctx->graphs.end(),
+                                    [](const bs_ctx::Graph &x, const bs_ctx::Graph &y) { return x.last < y.last; });
+        cudaGraphExecDestroy(old->exec);
+        ctx->graphs.erase(old);
+      }
+      ctx->graphs.push_back(bs_ctx::Graph{key, exec, ++ctx->tick});
+      CK(cudaGraphLaunch(exec, ctx->stream), "graph launch");
+      ctx->metrics.graph = 1;
+    }
+  }
+  CK(cudaMemcpyAsync(ctx->job_back, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, ctx->stream),
+     "read job table");
+  CK(cudaMemcpyAsync(ctx->sc_back, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read counters");
+  return BS_OK;
+}
+
+// After synchronisation: errors and metrics of a mixed launch.
+bs_status finish_mixed(bs_ctx *ctx, int nj) {
+  const Job *jobs = static_cast<const Job *>(ctx->job_back);
+  std::string msg;
+  const bs_status s = collect_errors(*ctx->sc_back, jobs, nj, msg);
+  if (s) return set_err(ctx, s, "%s", msg.c_str());
+  float q = 0.f;
+  for (int j = 0; j < nj; ++j) {
+    float f;
+    memcpy(&f, &jobs[j].qres_max_bits, 4);
+    q = std::max(q, f);
+  }
+  ctx->metrics.pairs_refined = (int64_t)ctx->sc_back->flag_count;
+  ctx->metrics.scale_exp = nj > 0 ? jobs[0].scale_exp : 0;
+  ctx->metrics.quant_bound = 2.0 * q;  // worst pair's |dRMSD| from the grid
+  ctx->metrics.jobs = nj;
+  return BS_OK;
+}
+
+// ---------------------------------------------------------- all-vs-all
+struct SetIO {
+  const double *xyz_dev;
+  void *out_dev;
+  size_t in_off, out_off;  // staging offsets (SIZE_MAX: caller's device memory)
+};
+
+bs_status plain_set(bs_ctx *ctx, const double *dxyz, int64_t n, int L, const OutDesc &od) {
   const int lp = lp_for(L);
   bs_status s;
+  if ((s = ensure(ctx, ctx->ctrd, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
+  if ((s = ensure(ctx, ctx->y, (size_t)n * 3 * lp * sizeof(double), "centred coordinates"))) return s;
+  if ((s = ensure(ctx, ctx->g, (size_t)n * sizeof(double), "norms"))) return s;
+  DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
+  CK(launch_prep_plain(dxyz, n, L, lp, static_cast<double *>(ctx->ctrd.p), static_cast<double *>(ctx->y.p),
+                       static_cast<double *>(ctx->g.p), &sc->err, ctx->stream),
+     "prep plain");
+  CK(launch_plain64_all(static_cast<const double *>(ctx->y.p), static_cast<const double *>(ctx->g.p), n, L, lp, od,
+                        ctx->stream),
+     "plain64 all-vs-all");
+  return BS_OK;
+}
+
+bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_opts &o) {
+  ctx->metrics = bs_metrics{};
+  const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
+  // staging of host inputs / outputs
+  std::vector<SetIO> io(nsets);
+  size_t in_bytes = 0, out_bytes = 0;
+  auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
+  int64_t pairs = 0;
+  for (int k = 0; k < nsets; ++k) {
+    const bs_set_desc &d = sets[k];
+    io[k].in_off = io[k].out_off = SIZE_MAX;
+    if (d.n < 2) continue;
+    pairs += d.n * (d.n - 1) / 2;
+    if (!is_device_ptr(d.xyz)) {
+      io[k].in_off = in_bytes;
+      in_bytes = align(in_bytes + (size_t)d.n * d.L * 3 * sizeof(double));
+    }
+    if (!is_device_ptr(d.out)) {
+      io[k].out_off = out_bytes;
+      out_bytes = align(out_bytes + out_elems(d.n, o.layout) * esz);
+    }
+  }
+  bs_status s;
+  if (in_bytes && (s = ensure(ctx, ctx->xyz, in_bytes, "coordinates"))) return s;
+  if (out_bytes && (s = ensure(ctx, ctx->out, out_bytes, "result buffer"))) return s;
   CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
-  const double *dxyz = nullptr;
-  if ((s = stage_coords(ctx, xyz, n, L, &dxyz))) return s;
-  CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-  void *dout = out;
-  if (!out_dev) {
-    if ((s = ensure(ctx, ctx->out, nout * esz, "result buffer"))) return s;
-    dout = ctx->out.p;
+  std::vector<JobSpec> specs;
+  for (int k = 0; k < nsets; ++k) {
+    const bs_set_desc &d = sets[k];
+    if (d.n < 2) continue;
+    io[k].xyz_dev = d.xyz;
+    if (io[k].in_off != SIZE_MAX) {
+      double *dst = reinterpret_cast<double *>(static_cast<char *>(ctx->xyz.p) + io[k].in_off);
+      const size_t bytes = (size_t)d.n * d.L * 3 * sizeof(double);
+      CK(cudaMemcpyAsync(dst, d.xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
+      ctx->metrics.bytes_h2d += (int64_t)bytes;
+      io[k].xyz_dev = dst;
+    }
+    io[k].out_dev = io[k].out_off != SIZE_MAX ? static_cast<char *>(ctx->out.p) + io[k].out_off : d.out;
+    const int layout = o.layout == BS_LAYOUT_TRIANGLE ? kLayoutTriangle : kLayoutSquare;
+    const OutDesc od{io[k].out_dev, d.n, d.n, layout, o.out_type};
+    if (o.layout == BS_LAYOUT_SQUARE)
+      CK(cudaMemset2DAsync(io[k].out_dev, (size_t)(d.n + 1) * esz, 0, esz, (size_t)d.n, ctx->stream), "zero diagonal");
+    specs.push_back(JobSpec{io[k].xyz_dev, d.n, d.L, od});
   }
-  if (o.layout == BS_LAYOUT_SQUARE)
-    CK(cudaMemset2DAsync(dout, (size_t)(n + 1) * esz, 0, esz, (size_t)n, ctx->stream), "zero diagonal");
-  OutDesc od{dout, n, o.layout, o.out_type};
-  DevScalars hs{};
   if (o.precision == BS_PRECISION_PLAIN64) {
-    if ((s = ensure(ctx, ctx->ctr, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
-    if ((s = ensure(ctx, ctx->y, (size_t)n * 3 * lp * sizeof(double), "centred coordinates"))) return s;
-    if ((s = ensure(ctx, ctx->g, (size_t)n * sizeof(double), "norms"))) return s;
-    DevScalars init{};
-    CK(cudaMemcpyAsync(ctx->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream), "init scalars");
-    DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
-    CK(launch_prep_stats(dxyz, n, L, static_cast<double *>(ctx->ctr.p), sc, ctx->stream), "prep stats");
-    CK(launch_prep_plain(dxyz, static_cast<const double *>(ctx->ctr.p), n, L, lp, static_cast<double *>(ctx->y.p),
-                         static_cast<double *>(ctx->g.p), ctx->stream),
-       "prep plain");
+    CK(cudaMemsetAsync(ctx->scal.p, 0, sizeof(DevScalars), ctx->stream), "clear counters");
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
-    CK(launch_plain64_all(static_cast<const double *>(ctx->y.p), static_cast<const double *>(ctx->g.p), n, L, lp, od,
-                          ctx->stream),
-       "plain64 all-vs-all");
+    for (const JobSpec &sp : specs)
+      if ((s = plain_set(ctx, sp.xyz, sp.n, sp.L, sp.out))) return s;
     CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
     CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
-    ctx->metrics.main_launches = 3;
+    CK(cudaMemcpyAsync(ctx->sc_back, ctx->scal.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream),
+       "read counters");
+    ctx->metrics.main_launches = 3 * (int)specs.size();
+    ctx->metrics.jobs = (int)specs.size();
+  } else if (!specs.empty()) {
+    Plan plan;
+    const std::string m = make_symmetric_plan(specs, total_tolerance(o), true, plan);
+    if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
+    const unsigned long long cap = std::min<unsigned long long>(kFlagCap, std::max<int64_t>(pairs, 4096));
+    MixedBuffers b;
+    if ((s = prepare_buffers(ctx, plan, cap, b))) return s;
+    if ((s = upload_tables(ctx, plan, b, plan_key(ctx, plan, cap)))) return s;
+    if ((s = launch_plan(ctx, plan, b, !(o.flags & BS_FLAG_NO_GRAPH)))) return s;
   } else {
-    if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
-    CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
-    const int64_t nb = blocks_for(n);
-    if (ctx->tiles_nb != n) {
-      std::vector<int2> t;
-      build_tiles(n, t);
-      if ((s = ensure(ctx, ctx->tiles, t.size() * sizeof(int2), "tile table"))) return s;
-      CK(cudaMemcpy(ctx->tiles.p, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice), "upload tile table");
-      ctx->tiles_nb = n;
-      ctx->tiles_count = (int64_t)t.size();
-    }
-    if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
-    CUtensorMap tm[7];
-    if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
-    TcArgs a{};
-    a.tiles = static_cast<const int2 *>(ctx->tiles.p);
-    a.ntiles = ctx->tiles_count;
-    a.n = n;
-    a.L = L;
-    a.lp = lp;
-    a.info = static_cast<const SInfo *>(ctx->info.p);
-    a.sc = static_cast<DevScalars *>(ctx->scal.p);
-    a.tol = total_tolerance(o);
-    a.u = ldexpf(1.0f, 2 * hs.scale_exp);
-    a.d34 = (float)ctx->d34;
-    a.out = od;
-    a.flags = static_cast<unsigned long long *>(ctx->flags.p);
-    a.flag_cap = kFlagCap;
-    a.dbg = nullptr;
-    a.num_sms = ctx->num_sms;
-    CK(launch_mixed_tc(tm, a, ctx->stream), "tensor-core all-vs-all");
-    CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
-    __nv_bfloat16 *digs[4];
-    for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
-    CK(launch_refine_list(digs, lp, L, a.info, a.sc, a.flags, kFlagCap, od, ctx->num_sms, ctx->stream),
-       "exact recomputation");
-    if ((s = check_device_errors(ctx, &hs))) return s;
-    if (hs.flag_count > kFlagCap) {
-      CK(launch_refine_scan(digs, lp, L, a.info, a.sc, od, ctx->num_sms, ctx->stream), "exact recomputation (scan)");
-    }
-    CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
-    ctx->metrics.pairs_refined = (int64_t)hs.flag_count;
-    ctx->metrics.scale_exp = hs.scale_exp;
-    ctx->metrics.quant_bound = 2.0 * qres_max(hs);  // worst pair's |dRMSD| from the grid
-    ctx->metrics.main_launches = 5 + (hs.flag_count > kFlagCap ? 1 : 0);
+    for (int k = 1; k <= 4; ++k) CK(cudaEventRecord(ctx->ev[k], ctx->stream), "event");
+    memset(ctx->sc_back, 0, sizeof(DevScalars));
   }
-  if (!out_dev) {
-    CK(cudaMemcpyAsync(out, dout, nout * esz, cudaMemcpyDeviceToHost, ctx->stream), "copy result to host");
-    ctx->metrics.bytes_d2h += (int64_t)(nout * esz);
+  for (int k = 0; k < nsets; ++k) {
+    const bs_set_desc &d = sets[k];
+    if (d.n < 2 || io[k].out_off == SIZE_MAX) continue;
+    const size_t bytes = out_elems(d.n, o.layout) * esz;
+    CK(cudaMemcpyAsync(d.out, io[k].out_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy result to host");
+    ctx->metrics.bytes_d2h += (int64_t)bytes;
   }
   CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
-  if ((s = check_device_errors(ctx, &hs))) return s;
-  ctx->metrics.pairs = n * (n - 1) / 2;
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  if (o.precision == BS_PRECISION_PLAIN64) {
+    if (ctx->sc_back->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
+  } else if (!specs.empty()) {
+    if ((s = finish_mixed(ctx, (int)specs.size()))) return s;
+  }
+  // single structures: their one square entry is the zero diagonal
+  for (int k = 0; k < nsets; ++k) {
+    const bs_set_desc &d = sets[k];
+    if (d.n == 1 && o.layout == BS_LAYOUT_SQUARE) {
+      const double z = 0.0;  // +0.0 has all-zero bits as f64 and as f32
+      CK(cudaMemcpy(d.out, &z, esz, cudaMemcpyDefault), "write result");
+    }
+  }
+  ctx->metrics.pairs = pairs;
   ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
   ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
   ctx->metrics.ms_main = elapsed(ctx, 2, 3);
@@ -367,14 +398,33 @@ bs_status all_vs_all_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, cons
   return BS_OK;
 }
 
+bs_status validate_sets(bs_ctx *ctx, const bs_set_desc *sets, int nsets) {
+  for (int k = 0; k < nsets; ++k) {
+    const bs_set_desc &d = sets[k];
+    if (d.n < 0 || d.L < 1)
+      return set_err(ctx, BS_ERR_INVALID_ARG, "set %d: n must be >= 0 and L >= 1 (n=%lld, L=%d)", k, (long long)d.n,
+                     d.L);
+    if (d.n > 0 && (!d.xyz || !d.out)) return set_err(ctx, BS_ERR_INVALID_ARG, "set %d: null coordinate or result pointer", k);
+    if (d.n > (1LL << 31) - 1) return set_err(ctx, BS_ERR_UNSUPPORTED, "set %d: n above 2^31-1", k);
+  }
+  return BS_OK;
+}
+
+// ------------------------------------------------------------ pair list
 bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int64_t *ii, const int64_t *jj,
                      int64_t np, const bs_opts &o, double *out, float *levels_dbg) {
   ctx->metrics = bs_metrics{};
   const int lp = lp_for(L);
   bs_status s;
   CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
-  const double *dxyz = nullptr;
-  if ((s = stage_coords(ctx, xyz, n, L, &dxyz))) return s;
+  const double *dxyz = xyz;
+  if (!is_device_ptr(xyz)) {
+    const size_t bytes = (size_t)n * (size_t)L * 3 * sizeof(double);
+    if ((s = ensure(ctx, ctx->xyz, bytes, "coordinates"))) return s;
+    CK(cudaMemcpyAsync(ctx->xyz.p, xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
+    ctx->metrics.bytes_h2d += (int64_t)bytes;
+    dxyz = static_cast<const double *>(ctx->xyz.p);
+  }
   const int64_t *dii = ii, *djj = jj;
   if (!is_device_ptr(ii)) {
     if ((s = ensure(ctx, ctx->pairs_i, (size_t)np * 8, "pair list"))) return s;
@@ -393,49 +443,68 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
     dout = static_cast<double *>(ctx->pout.p);
   }
   CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
-  DevScalars hs{};
   if (o.precision == BS_PRECISION_PLAIN64) {
-    if ((s = ensure(ctx, ctx->ctr, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
+    if ((s = ensure(ctx, ctx->ctrd, (size_t)n * 3 * sizeof(double), "centroids"))) return s;
     if ((s = ensure(ctx, ctx->y, (size_t)n * 3 * lp * sizeof(double), "centred coordinates"))) return s;
     if ((s = ensure(ctx, ctx->g, (size_t)n * sizeof(double), "norms"))) return s;
-    DevScalars init{};
-    CK(cudaMemcpyAsync(ctx->scal.p, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream), "init scalars");
     DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
-    CK(launch_prep_stats(dxyz, n, L, static_cast<double *>(ctx->ctr.p), sc, ctx->stream), "prep stats");
-    CK(launch_prep_plain(dxyz, static_cast<const double *>(ctx->ctr.p), n, L, lp, static_cast<double *>(ctx->y.p),
-                         static_cast<double *>(ctx->g.p), ctx->stream),
+    CK(cudaMemsetAsync(sc, 0, sizeof(DevScalars), ctx->stream), "clear counters");
+    CK(launch_prep_plain(dxyz, n, L, lp, static_cast<double *>(ctx->ctrd.p), static_cast<double *>(ctx->y.p),
+                         static_cast<double *>(ctx->g.p), &sc->err, ctx->stream),
        "prep plain");
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
     CK(launch_plain64_pairs(static_cast<const double *>(ctx->y.p), static_cast<const double *>(ctx->g.p), n, L, lp,
                             dii, djj, np, dout, ctx->stream),
        "plain64 pairs");
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
+    CK(cudaMemcpyAsync(ctx->sc_back, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read counters");
   } else {
-    if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
+    std::vector<JobSpec> specs{JobSpec{dxyz, n, L, OutDesc{dout, np, 0, kLayoutRect, 0}}};
+    Plan plan;
+    const std::string m = make_symmetric_plan(specs, total_tolerance(o), false, plan);
+    if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
+    MixedBuffers b;
+    if ((s = prepare_buffers(ctx, plan, 1024, b))) return s;
+    ctx->plan_key.clear();
+    if ((s = upload_tables(ctx, plan, b, plan_key(ctx, plan, 1024)))) return s;
+    memcpy(ctx->job_stage, plan.jobs.data(), sizeof(Job));
+    CUtensorMap tm[7];  // unused without tiles
+    CK(enqueue_mixed(plan, b, static_cast<const Job *>(ctx->job_stage), tm, ctx->num_sms, ctx->stream, nullptr, false),
+       "mixed preparation");
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
-    __nv_bfloat16 *digs[4];
-    for (int d = 0; d < 4; ++d) digs[d] = static_cast<__nv_bfloat16 *>(ctx->dig[d].p);
-    CK(launch_mixed_pairs(digs, lp, L, static_cast<const SInfo *>(ctx->info.p), static_cast<DevScalars *>(ctx->scal.p),
-                          total_tolerance(o), ldexpf(1.0f, 2 * hs.scale_exp), (float)ctx->d34, dii, djj, np, dout,
-                          levels_dbg, ctx->stream),
+    CK(launch_mixed_pairs(DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a}, b.info_a, b.jobs, b.sc, dii, djj,
+                          np, dout, levels_dbg, ctx->stream),
        "mixed pairs");
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
+    CK(cudaMemcpyAsync(ctx->job_back, b.jobs, sizeof(Job), cudaMemcpyDeviceToHost, ctx->stream), "read job table");
+    CK(cudaMemcpyAsync(ctx->sc_back, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read counters");
   }
-  CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
   CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
   if (!out_dev) {
     CK(cudaMemcpyAsync(out, dout, (size_t)np * 8, cudaMemcpyDeviceToHost, ctx->stream), "copy pair results");
     ctx->metrics.bytes_d2h += np * 8;
   }
   CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
-  if ((s = check_device_errors(ctx, &hs))) return s;
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  if (o.precision == BS_PRECISION_PLAIN64) {
+    if (ctx->sc_back->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
+  } else {
+    if ((s = finish_mixed(ctx, 1))) return s;
+  }
   ctx->metrics.pairs = np;
-  ctx->metrics.scale_exp = hs.scale_exp;
-  if (o.precision == BS_PRECISION_MIXED) ctx->metrics.quant_bound = 2.0 * qres_max(hs);
   ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
   ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
   ctx->metrics.ms_main = elapsed(ctx, 2, 3);
   ctx->metrics.ms_d2h = elapsed(ctx, 4, 5);
   ctx->metrics.ms_total = elapsed(ctx, 0, 5);
   return BS_OK;
+}
+
+DevBuf *all_buffers(bs_ctx *ctx, std::vector<DevBuf *> &v) {
+  v = {&ctx->xyz,     &ctx->out,    &ctx->ctr,   &ctx->info,  &ctx->dig[0], &ctx->dig[1], &ctx->dig[2],
+       &ctx->dig[3],  &ctx->jobs,   &ctx->jobmap, &ctx->tiles, &ctx->flags,  &ctx->y,      &ctx->g,
+       &ctx->ctrd,    &ctx->pairs_i, &ctx->pairs_j, &ctx->pout};
+  return nullptr;
 }
 
 }  // namespace
@@ -473,6 +542,7 @@ BS_API void bs_opts_init(bs_opts *o) {
   o->layout = BS_LAYOUT_TRIANGLE;
   o->out_type = BS_OUT_F64;
   o->tolerance = 0.0;
+  o->flags = 0;
 }
 
 BS_API bs_status bs_ctx_create(bs_ctx **out, int32_t device, size_t hbm_budget_bytes) {
@@ -491,7 +561,13 @@ BS_API bs_status bs_ctx_create(bs_ctx **out, int32_t device, size_t hbm_budget_b
   if (!ctx) return BS_ERR_OOM;
   ctx->device = device;
   ctx->num_sms = prop.multiProcessorCount;
-  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return BS_ERR_CUDA;
+  }
+  if (mixed_tc_prepare() != cudaSuccess || prep_prepare() != cudaSuccess) {
+    cudaStreamDestroy(ctx->stream);
     delete ctx;
     return BS_ERR_CUDA;
   }
@@ -499,7 +575,8 @@ BS_API bs_status bs_ctx_create(bs_ctx **out, int32_t device, size_t hbm_budget_b
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   ctx->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)(0.9 * (double)free_b);
-  if (ensure(ctx, ctx->scal, sizeof(DevScalars), "scalars") != BS_OK) {
+  if (ensure(ctx, ctx->scal, sizeof(DevScalars), "scalars") != BS_OK ||
+      cudaHostAlloc((void **)&ctx->sc_back, sizeof(DevScalars), cudaHostAllocDefault) != cudaSuccess) {
     bs_ctx_destroy(ctx);
     return BS_ERR_OOM;
   }
@@ -511,10 +588,14 @@ BS_API void bs_ctx_destroy(bs_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->info, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2], &ctx->dig[3],
-                    &ctx->y, &ctx->g, &ctx->out, &ctx->tiles, &ctx->flags, &ctx->scal, &ctx->pairs_i,
-                    &ctx->pairs_j, &ctx->pout};
+  drop_graphs(ctx);
+  std::vector<DevBuf *> bufs;
+  all_buffers(ctx, bufs);
+  bufs.push_back(&ctx->scal);
   for (DevBuf *b : bufs) release(ctx, *b);
+  if (ctx->job_stage) cudaFreeHost(ctx->job_stage);
+  if (ctx->job_back) cudaFreeHost(ctx->job_back);
+  if (ctx->sc_back) cudaFreeHost(ctx->sc_back);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -525,10 +606,11 @@ BS_API bs_status bs_ctx_trim(bs_ctx *ctx) {
   if (!ctx) return BS_ERR_INVALID_ARG;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf *bufs[] = {&ctx->xyz, &ctx->ctr, &ctx->info, &ctx->dig[0], &ctx->dig[1], &ctx->dig[2], &ctx->dig[3],
-                    &ctx->y, &ctx->g, &ctx->out, &ctx->tiles, &ctx->flags, &ctx->pairs_i, &ctx->pairs_j, &ctx->pout};
+  drop_graphs(ctx);
+  std::vector<DevBuf *> bufs;
+  all_buffers(ctx, bufs);
   for (DevBuf *b : bufs) release(ctx, *b);
-  ctx->tiles_nb = -1;
+  ctx->plan_key.clear();
   return BS_OK;
 }
 
@@ -547,20 +629,23 @@ BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_
   if (opts) o = *opts;
   bs_status s = check_opts(ctx, &o);
   if (s) return s;
-  if (n < 0 || L < 1) return set_err(ctx, BS_ERR_INVALID_ARG, "n must be >= 0 and L >= 1 (n=%lld, L=%d)", (long long)n, L);
-  if (n > 0 && (!xyz || !out)) return set_err(ctx, BS_ERR_INVALID_ARG, "null coordinate or result pointer");
-  if (n > (1LL << 31) - 1) return set_err(ctx, BS_ERR_UNSUPPORTED, "n above 2^31-1");
-  if (n < 2) {
-    ctx->metrics = bs_metrics{};
-    if (n == 1 && o.layout == BS_LAYOUT_SQUARE) {
-      const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
-      double z = 0.0;
-      if (cudaMemcpy(out, &z, esz, cudaMemcpyDefault) != cudaSuccess) return cuda_err(ctx, cudaGetLastError(), "write result");
-    }
-    return BS_OK;
-  }
+  bs_set_desc d{xyz, n, L, 0, out};
+  if ((s = validate_sets(ctx, &d, 1))) return s;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
-  return all_vs_all_impl(ctx, xyz, n, L, o, out);
+  return sets_impl(ctx, &d, 1, o);
+}
+
+BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets, const bs_opts *opts) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (nsets < 0 || (nsets > 0 && !sets)) return set_err(ctx, BS_ERR_INVALID_ARG, "nsets < 0 or null set list");
+  bs_opts o;
+  bs_opts_init(&o);
+  if (opts) o = *opts;
+  bs_status s = check_opts(ctx, &o);
+  if (s) return s;
+  if ((s = validate_sets(ctx, sets, nsets))) return s;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  return sets_impl(ctx, sets, nsets, o);
 }
 
 BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii, const int64_t *jj,
@@ -625,44 +710,42 @@ BS_API bs_status bs_host_free(void *p) {
 BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels) {
   if (!ctx || !xyz || !levels || n < 1 || L < 1) return BS_ERR_INVALID_ARG;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
-  const int lp = lp_for(L);
-  const double *dxyz = nullptr;
+  ctx->metrics = bs_metrics{};
   bs_status s;
-  if ((s = stage_coords(ctx, xyz, n, L, &dxyz))) return s;
-  DevScalars hs{};
-  if ((s = prep_mixed(ctx, dxyz, n, L, lp, &hs))) return s;
-  const int64_t nb = blocks_for(n);
-  const int2 first[2] = {make_int2(0, 0), make_int2(0, 1)};
-  if ((s = ensure(ctx, ctx->tiles, sizeof(first), "tile table"))) return s;
-  CK(cudaMemcpy(ctx->tiles.p, first, sizeof(first), cudaMemcpyHostToDevice), "upload tiles");
-  ctx->tiles_nb = -1;  // the cached table was replaced
+  const size_t bytes = (size_t)n * (size_t)L * 3 * sizeof(double);
+  if ((s = ensure(ctx, ctx->xyz, bytes, "coordinates"))) return s;
+  CK(cudaMemcpyAsync(ctx->xyz.p, xyz, bytes, cudaMemcpyDefault, ctx->stream), "copy coordinates");
   const size_t nout = (size_t)n * (size_t)(n > 1 ? n - 1 : 1) / 2 + 1;
   if ((s = ensure(ctx, ctx->out, nout * 8, "result buffer"))) return s;
-  if ((s = ensure(ctx, ctx->flags, kFlagCap * sizeof(unsigned long long), "flag list"))) return s;
+  std::vector<JobSpec> specs{
+      JobSpec{static_cast<const double *>(ctx->xyz.p), n, L, OutDesc{ctx->out.p, n, n, kLayoutTriangle, 0}}};
+  Plan plan;
+  const std::string m = make_symmetric_plan(specs, (float)kDefaultTol, false, plan);
+  if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
+  plan.tiles.push_back(Tile{0, 0, 0, 0});
+  if (n > 20) plan.tiles.push_back(Tile{0, 1, 0, 0});
+  MixedBuffers b;
+  if ((s = prepare_buffers(ctx, plan, 4096, b))) return s;
+  ctx->plan_key.clear();
+  if ((s = upload_tables(ctx, plan, b, plan_key(ctx, plan, 4096)))) return s;
+  ctx->plan_key.clear();
   if ((s = ensure(ctx, ctx->pout, (size_t)4 * 128 * 128 * sizeof(float), "level dump"))) return s;
   CK(cudaMemsetAsync(ctx->pout.p, 0, (size_t)4 * 128 * 128 * sizeof(float), ctx->stream), "clear level dump");
+  memcpy(ctx->job_stage, plan.jobs.data(), sizeof(Job));
+  std::string em = get_encoder(&ctx->encode);
+  if (!em.empty()) return set_err(ctx, BS_ERR_CUDA, "%s", em.c_str());
   CUtensorMap tm[7];
-  if ((s = encode_maps(ctx, nb * kBlockRows, lp, tm))) return s;
-  TcArgs a{};
-  a.tiles = static_cast<const int2 *>(ctx->tiles.p);
-  a.ntiles = (n > 20) ? 2 : 1;
-  a.n = n;
-  a.L = L;
-  a.lp = lp;
-  a.info = static_cast<const SInfo *>(ctx->info.p);
-  a.sc = static_cast<DevScalars *>(ctx->scal.p);
-  a.tol = (float)kDefaultTol;
-  a.u = ldexpf(1.0f, 2 * hs.scale_exp);
-  a.d34 = (float)ctx->d34;
-  a.out = OutDesc{ctx->out.p, n, BS_LAYOUT_TRIANGLE, BS_OUT_F64};
-  a.flags = static_cast<unsigned long long *>(ctx->flags.p);
-  a.flag_cap = kFlagCap;
-  a.dbg = static_cast<float *>(ctx->pout.p);
-  a.num_sms = ctx->num_sms;
-  CK(launch_mixed_tc(tm, a, ctx->stream), "tensor-core tile");
-  CK(cudaMemcpyAsync(levels, a.dbg, (size_t)4 * 128 * 128 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+  em = encode_maps(ctx->encode, b, tm);
+  if (!em.empty()) return set_err(ctx, BS_ERR_CUDA, "%s", em.c_str());
+  CK(enqueue_mixed(plan, b, static_cast<const Job *>(ctx->job_stage), tm, ctx->num_sms, ctx->stream, nullptr, false,
+                   static_cast<float *>(ctx->pout.p)),
+     "tensor-core tile");
+  CK(cudaMemcpyAsync(levels, ctx->pout.p, (size_t)4 * 128 * 128 * sizeof(float), cudaMemcpyDefault, ctx->stream),
      "copy level dump");
-  return check_device_errors(ctx, &hs);
+  CK(cudaMemcpyAsync(ctx->job_back, b.jobs, sizeof(Job), cudaMemcpyDeviceToHost, ctx->stream), "read job table");
+  CK(cudaMemcpyAsync(ctx->sc_back, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read counters");
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  return finish_mixed(ctx, 1);
 }
 
 BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,

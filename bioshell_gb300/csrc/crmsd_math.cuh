@@ -324,6 +324,25 @@ BS_HD void fast_level(FastState &st, int level, const float s[9]) {
   }
 }
 
+// The same from staged values: levels 0-2 arrive as int32 bit patterns (the
+// exact integer sums, possibly of two atom ranges), level 3 as a float.
+BS_HD void fast_level_staged(FastState &st, int level, const float s[9]) {
+  if (level < 3) {
+    long long u = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      int v;
+      memcpy(&v, &s[i], 4);
+      u += st.T[i] * (long long)v;
+    }
+    if (level == 0) st.U0 += u;
+    else if (level == 1) st.U1 += u;
+    else st.U2 += u;
+  } else {
+    fast_level(st, 3, s);
+  }
+}
+
 // gsum: exact Ga + Gb (units u); gsum_f: the same as float; qsum: the two
 // structures' quantisation residual RMS (Angstrom) -- by Minkowski, the
 // crmsd of the quantised pair is within qsum of the exact one; d34: bound on

@@ -1,0 +1,114 @@
+// engine.h -- internals shared by the C-ABI layer (api.cu), the serving loop
+// (server.cu) and the allocation-free entry point (noalloc.cu): device
+// workspaces, the mixed-path launch plan, the graph cache and the call
+// sequence.  Not part of the public interface.
+#pragma once
+#include <cudaTypedefs.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bioshell_crmsd.h"
+#include "kernels.h"
+
+namespace bs {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+// Device buffers of one mixed-path launch.  The A side holds the jobs' own
+// structures; the B side is the same buffers for symmetric jobs, or a
+// resident library's for rectangular ones.
+struct MixedBuffers {
+  long long *ctr = nullptr;  // [structures][3] fixed-point centroids
+  SInfo *info_a = nullptr;
+  const SInfo *info_b = nullptr;
+  __nv_bfloat16 *dig_a[4] = {};
+  const __nv_bfloat16 *dig_b[3] = {};
+  int64_t pitch_a = 0, pitch_b = 0;  // digit row length (atoms)
+  int64_t rows_a = 0, rows_b = 0;    // digit rows allocated
+  Job *jobs = nullptr;
+  int *jobmap = nullptr;  // job of each 40-structure A block
+  Tile *tiles = nullptr;
+  unsigned long long *flags = nullptr;
+  unsigned long long flag_cap = 0;
+  DevScalars *sc = nullptr;
+};
+
+// A symmetric job as the host describes it (device coordinates and output).
+struct JobSpec {
+  const double *xyz;
+  int64_t n;
+  int L;
+  OutDesc out;
+};
+
+struct Plan {
+  std::vector<Job> jobs;  // host part filled, device part zero
+  std::vector<int> jobmap;
+  std::vector<Tile> tiles;
+  int64_t nblocks = 0;  // 40-structure A blocks
+  int pitch = 0;
+};
+
+// Builds the jobs, block map and tile table of symmetric jobs.  Tiles of the
+// longest chains come first so that the persistent kernel ends with short
+// tiles; within a job they run in super-blocks that keep the working set in
+// L2.  Returns an empty string on success, else the reason.
+std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bool with_tiles, Plan &plan);
+
+// The seven tensor maps (A digits e0 e1 e2 d2/32, B digits e0 e1 e2).
+std::string encode_maps(PFN_cuTensorMapEncodeTiled_v12000 encode, const MixedBuffers &b, CUtensorMap tm[7]);
+std::string get_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out);
+
+// Enqueues the mixed-path sequence of a plan whose tables are on the
+// device: counters reset, job table upload from `job_stage` (pinned or
+// pageable; pinned when captured), preparation, tensor-core tiles, exact
+// recomputation.  `ev` (optional, 4 events) marks prep / main / refine
+// boundaries; `capturing` records them as graph event nodes.
+cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *job_stage, const CUtensorMap tm[7],
+                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg = nullptr);
+
+// Maps the device error bits of a finished launch to a status and message.
+bs_status collect_errors(const DevScalars &sc, const Job *jobs, int njobs, std::string &msg);
+
+}  // namespace bs
+
+struct bs_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  size_t budget = 0;
+  size_t used = 0;
+  uint64_t gen = 0;  // bumped whenever a workspace moves (graphs hold addresses)
+  std::string err;
+  bs_metrics metrics{};
+  // workspaces
+  bs::DevBuf xyz, out, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, y, g, ctrd, pairs_i, pairs_j, pout;
+  void *job_stage = nullptr;  // pinned host copy of the job table
+  size_t job_stage_cap = 0;
+  void *job_back = nullptr;  // pinned read-back of the job table
+  bs::DevScalars *sc_back = nullptr;
+  // cached tables of the last plan
+  std::vector<int64_t> plan_key;
+  // graph cache
+  struct Graph {
+    std::vector<int64_t> key;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t last = 0;
+  };
+  std::vector<Graph> graphs;
+  uint64_t tick = 0;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+};
+
+namespace bs {
+bs_status set_err(bs_ctx *ctx, bs_status s, const char *fmt, ...);
+bs_status cuda_err(bs_ctx *ctx, cudaError_t e, const char *what);
+bs_status ensure(bs_ctx *ctx, DevBuf &b, size_t bytes, const char *what);
+void release(bs_ctx *ctx, DevBuf &b);
+bool is_device_ptr(const void *p);
+}  // namespace bs

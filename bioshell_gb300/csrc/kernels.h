@@ -1,5 +1,6 @@
-// kernels.h -- launch wrappers shared between the kernel translation units
-// and the C-ABI layer.  Internal to the library.
+// kernels.h -- data layout, device-side job descriptors and launch wrappers
+// shared between the kernel translation units and the C-ABI layer.  Internal
+// to the library.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -9,22 +10,31 @@
 namespace bs {
 
 // ---------------------------------------------------------------- layout
-// Digit matrices: one row per (structure, coordinate), `lp` bf16 columns
-// (atoms, zero padded to a multiple of 16).  Structures are packed ten to a
-// 32-row group (rows 30 and 31 of each group are zero), four groups to a
-// 128-row block, so that a tensor-core A tile of 128 rows holds 40 whole
-// structures (B tiles: 64 rows, 20 structures) and each structure's three
-// rows sit in one warp's TMEM lanes.
+// Digit matrices: one row per (structure, coordinate), `pitch` bf16 columns
+// (atoms; a job uses the first lp = L rounded up to 16, zero padded).
+// Structures are packed ten to a 32-row group (rows 30 and 31 of each group
+// are zero), four groups to a 128-row block, so that a tensor-core A tile of
+// 128 rows holds 40 whole structures (B tiles: 64 rows, 20 structures) and
+// each structure's three rows sit in one warp's TMEM lanes.  Structures are
+// numbered globally across the jobs of one launch; every job starts on a
+// 40-structure block boundary.
 constexpr int kGroupRows = 32;
 constexpr int kGroupStructs = 10;
 constexpr int kBlockRows = 128;
 constexpr int kBlockStructs = 40;
+constexpr int kBStructs = 20;
+constexpr int kKChunk = 64;  // atoms per 128-byte swizzled TMA box row
 
 __host__ __device__ inline int64_t digit_row(int64_t s, int c) {
   return (s / kGroupStructs) * kGroupRows + (s % kGroupStructs) * 3 + c;
 }
 inline int64_t blocks_for(int64_t n) { return (n + kBlockStructs - 1) / kBlockStructs; }
 inline int lp_for(int L) { return ((L + 15) / 16) * 16; }
+inline int pitch_for(int L) { return ((L + kKChunk - 1) / kKChunk) * kKChunk; }
+
+// Fixed-point unit of the preparation pass: coordinates are read as
+// integers in units of 2^-32 Angstrom.
+constexpr int kFixBits = 32;
 
 // Per-structure data of the mixed path (one 16-byte load per structure).
 struct __align__(16) SInfo {
@@ -33,78 +43,172 @@ struct __align__(16) SInfo {
   float qres;      // RMS of the quantisation residual y - 2^e n (Angstrom, rounded up)
 };
 
-// Scalars the kernels exchange through device memory.
+// Output description shared by every kernel that writes pair values.
+struct OutDesc {
+  void *ptr;
+  int64_t n;     // rows
+  int64_t ld;    // row stride of the square / rectangular layouts
+  int layout;    // 0 packed triangle, 1 square (both halves), 2 rectangular n x ld
+  int out_type;  // 0 f64, 1 f32
+};
+constexpr int kLayoutTriangle = 0;
+constexpr int kLayoutSquare = 1;
+constexpr int kLayoutRect = 2;
+
+// One block of pairs of a launch: all pairs i < j of one structure set
+// (symmetric), or every pair of a query set against a library range
+// (rectangular).  The host fills the first part; the preparation kernels
+// fill the second on the device, so the whole call sequence needs no host
+// round trip (and can be captured in a CUDA graph).
+struct Job {
+  // ---- host
+  const double *xyz;      // [n][L][3] f64 AoS of the A-side structures (device)
+  long long n;            // A-side structures
+  long long first_a;      // global index of A structure 0 (multiple of 40)
+  long long first_b;      // global index of B structure 0 (multiple of 20)
+  long long n_b;          // B-side structures (symmetric: n)
+  OutDesc out;
+  int L, lp;              // atoms; digit columns used (L rounded up to 16)
+  int mode;               // 0 symmetric, 1 rectangular
+  int fixed_scale;        // 1: grid exponent given (scale_min), no candidate search
+  int scale_min;          // smallest grid exponent allowed
+  float tol;              // certified |dRMSD| budget per pair (Angstrom)
+  // B-side digit norms for rectangular jobs with a fixed grid (the
+  // library's maxima, per digit), used in the exactness bound
+  float norm_b[3];
+  float qres_b;           // largest B-side quantisation residual RMS
+  // ---- device (preparation)
+  unsigned long long maxabs;        // max |centred coordinate|, fixed-point units
+  unsigned long long norm[4][3];    // per candidate grid: max row sum of squared digits (d0, d1, d2)
+  unsigned long long normh[4][3];   // per candidate grid: max over rows and halves of the half-row sums
+  unsigned long long normq[4][3];   // the same over quarters (the parts of a long-layout tile)
+  unsigned int qres_max_bits;       // largest A-side quantisation residual RMS (float bits)
+  int scale_base;                   // grid of candidate 0
+  int scale_exp;                    // chosen grid exponent e
+  int err;                          // kErr* bits of this job
+  float u;                          // Angstrom^2 per unit of quantised products (2^2e)
+  float d34;                        // rounding bound of accumulator levels 2-3, as an error of E (units u)
+  int layout;                       // accumulator layout of the job's tiles (kLayout*)
+  int pad;
+};
+
+// Accumulator layouts of a tile.  Normal: the four levels, one 64-column
+// accumulator each, in one TMEM buffer.  Long (long chains): eight
+// accumulators over both buffers -- level 0 over the whole chain, level 1
+// in two and level 2 in four consecutive parts of the chain (16-atom steps
+// split evenly), level 3 whole -- so that each part's sum stays below 2^24
+// where the whole chain's would not.
+constexpr int kAccNormal = 0;
+constexpr int kAccLong = 1;
+__host__ __device__ inline int acc_part(int k16, int nk16, int parts) { return (k16 * parts) / nk16; }
+// accumulator index (0..7) of level `lv` at 16-atom step k16
+__host__ __device__ inline int acc_index(int layout, int lv, int k16, int nk16) {
+  if (layout == kAccNormal) return lv;
+  if (lv == 0) return 0;
+  if (lv == 1) return 1 + acc_part(k16, nk16, 2);
+  if (lv == 2) return 3 + acc_part(k16, nk16, 4);
+  return 7;
+}
+
+// Counters shared by the kernels of one launch.
 struct DevScalars {
-  unsigned long long maxabs_bits;   // max |centred coordinate| (double bits)
-  unsigned long long norm_max[3];   // max over (structure, coord) of sum d_i^2
-  unsigned long long flag_count;    // pairs queued for exact recomputation
-  unsigned long long qres_max_bits; // max per-structure quantisation residual RMS (float bits)
-  int scale_exp;                    // grid exponent e (coordinates in units 2^e A)
-  int err;                          // error bits (kErr*)
-  int scale_min;                    // lower bound on e requested by the host
+  unsigned long long flag_count;  // pairs queued for exact recomputation
+  int err;                        // kErr* bits not tied to one job
   int pad;
 };
 constexpr int kErrTimeout = 1;
 constexpr int kErrNonFinite = 2;
 constexpr int kErrBounds = 4;
 constexpr int kErrInternal = 8;
+constexpr int kErrUnsupported = 16;  // no grid meets the exactness bound / coordinates out of range
 
-// Output description shared by every kernel that writes pair values.
-struct OutDesc {
-  void *ptr;
-  int64_t n;
-  int layout;    // 0 triangle, 1 square
-  int out_type;  // 0 f64, 1 f32
+// Flag entries: job (16 bits) | global i (24 bits) | global j (24 bits).
+constexpr int64_t kMaxGlobalStructs = 1ll << 24;
+__host__ __device__ inline unsigned long long flag_pack(int job, int64_t i, int64_t j) {
+  return ((unsigned long long)job << 48) | ((unsigned long long)i << 24) | (unsigned long long)j;
+}
+
+// Tensor-core tile: A block (40 structures), B block (20 structures), job,
+// and the job's shape (16-atom steps | accumulator layout << 16), written on
+// the device once the preparation has chosen the layout, so that the TMA and
+// MMA threads read one record per tile.
+struct __align__(16) Tile {
+  int a_blk, b_blk, job, shape;
 };
+__host__ __device__ inline int tile_nk16(const Tile &t) { return t.shape & 0xffff; }
+__host__ __device__ inline int tile_layout(const Tile &t) { return t.shape >> 16; }
 
 // ------------------------------------------------------------- launches
-// prep.cu
-cudaError_t launch_prep_stats(const double *xyz, int64_t n, int L, double *ctr, DevScalars *sc,
-                              cudaStream_t st);
-cudaError_t launch_prep_scale(DevScalars *sc, cudaStream_t st);
-// dig[0..3]: e0, e1, e2 = 16 d2, and d2 / 32 (the level-4 operand)
-cudaError_t launch_prep_digits(const double *xyz, const double *ctr, int64_t n, int L, int lp,
-                               __nv_bfloat16 *const *dig, SInfo *info, DevScalars *sc, cudaStream_t st);
-cudaError_t launch_prep_plain(const double *xyz, const double *ctr, int64_t n, int L, int lp, double *y,
-                              double *g, cudaStream_t st);
+// prep.cu -- mixed path, all jobs of a launch at once
+struct PrepArgs {
+  Job *jobs;
+  int njobs;
+  const int *job_of_struct_block;  // job of each 40-structure block (A side)
+  int64_t nblocks;                 // 40-structure blocks
+  long long *ctr;                  // fixed-point centroid per global structure [3]
+  __nv_bfloat16 *dig[4];           // e0, e1, e2 = 16 d2, d2 / 32
+  int64_t pitch;
+  SInfo *info;
+  DevScalars *sc;
+};
+cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st);
+int prep_max_pitch();
+cudaError_t prep_prepare();
+
+// plain path (single set, FP64 throughout)
+cudaError_t launch_prep_plain(const double *xyz, int64_t n, int L, int lp, double *ctr, double *y, double *g,
+                              int *err, cudaStream_t st);
 
 // plain64.cu
 cudaError_t launch_plain64_all(const double *y, const double *g, int64_t n, int L, int lp, OutDesc out,
                                cudaStream_t st);
 cudaError_t launch_plain64_pairs(const double *y, const double *g, int64_t n, int L, int lp, const int64_t *ii,
                                  const int64_t *jj, int64_t np, double *out, cudaStream_t st);
+cudaError_t launch_plain64_rect(const double *ya, const double *ga, int64_t na, const double *yb, const double *gb,
+                                int64_t nb, int L, int lp, OutDesc out, cudaStream_t st);
 
 // mixed_tc.cu
 struct TcArgs {
-  const int2 *tiles;
+  const Tile *tiles;
   int64_t ntiles;
-  int64_t n;
-  int L, lp;
-  const SInfo *info;
+  const Job *jobs;
+  const SInfo *info_a;
+  const SInfo *info_b;
   DevScalars *sc;
-  float tol;  // certified |dRMSD| budget per pair (Angstrom)
-  float u;    // Angstrom^2 per unit of the quantised products
-  float d34;  // level-3 accumulator rounding bound, as an error of E (units u)
-  OutDesc out;
   unsigned long long *flags;
   unsigned long long flag_cap;
-  float *dbg;  // optional dump of the first tile's raw level sums
+  float *dbg;  // optional dump of the raw level sums of tiles (0,0) and (0,1)
   int num_sms;
 };
 cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [7]: A digits e0 e1 e2 d2/32, B digits e0 e1 e2 */,
                             const TcArgs &a, cudaStream_t st);
+// writes every tile's shape from its job (after the preparation)
+cudaError_t launch_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs, int num_sms, cudaStream_t st);
 size_t mixed_tc_smem_bytes();
+cudaError_t mixed_tc_prepare();
 
 // refine.cu
-cudaError_t launch_refine_list(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               const unsigned long long *flags, unsigned long long cap, OutDesc out, int num_sms,
+struct DigitsView {
+  const __nv_bfloat16 *d0, *d1, *d2;
+  int64_t pitch;
+};
+struct RefineArgs {
+  DigitsView da, db;
+  const SInfo *info_a, *info_b;
+  const Job *jobs;
+  int njobs;
+  DevScalars *sc;
+  const unsigned long long *flags;
+  unsigned long long cap;
+  int num_sms;
+};
+// exact recomputation of the queued pairs; then, only when the queue
+// overflowed (checked on the device), of every sentinel left in the outputs
+cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st);
+// CUDA-core level sums + the same epilogue for an explicit pair list of job 0
+// (used for sparse pair lists and as the tensor-core path's independent check)
+cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Job *job, DevScalars *sc,
+                               const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
                                cudaStream_t st);
-cudaError_t launch_refine_scan(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               OutDesc out, int num_sms, cudaStream_t st);
-// CUDA-core level sums + the same epilogue for an explicit pair list (used
-// for sparse pair lists and as the tensor-core path's independent check).
-cudaError_t launch_mixed_pairs(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               float tol, float u, float d34, const int64_t *ii, const int64_t *jj, int64_t np,
-                               double *out, float *levels_out, cudaStream_t st);
 
 }  // namespace bs

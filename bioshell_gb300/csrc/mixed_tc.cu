@@ -9,9 +9,14 @@
 //     L2 += D0 D2' + D1 D1' + D2 D0'   L3 += D1 D2' + D2 D1' + D2s D2'
 // into four FP32 accumulators of 128 lanes x 64 columns in TMEM.  Levels 0-2
 // are integers below 2^24, so their accumulation is exact; L3 carries the
-// level-4 products at 1/512 scale with a bounded rounding error.  TMEM
-// holds two such accumulator sets, so the epilogue of one tile overlaps the
-// MMAs of the next.
+// level-4 products at 1/512 scale with a bounded rounding error.  TMEM holds
+// two such accumulator sets, so the epilogue of one tile overlaps the MMAs
+// of the next.  Tiles of long chains use both sets at once (the long
+// layout, kernels.h): level 1 accumulated in two and level 2 in four parts
+// of the chain, so each part stays exact where the whole chain's sum would
+// not; the epilogue adds the parts as integers.  (When even that does not
+// bound level 2 below 2^24, it accumulates up to 2^26 with its rounding
+// charged to the job's error budget.)
 //
 // Roles (one persistent CTA per SM, 384 threads):
 //   warp 0  TMA producer: 4 A digit boxes (128 rows x 64 atoms) and 3 B
@@ -24,6 +29,10 @@
 //           coordinate x of structure i finishes pairs (i, j) with
 //           j = x mod 3 through the three phases of crmsd_math.cuh, and
 //           writes the result.
+// Tiles come from a table of (A block, B block, job): one launch serves any
+// number of jobs -- the symmetric all-vs-all of one or many structure sets
+// (pairs i < j), and query-vs-library blocks (every pair) -- each with its
+// own chain length, grid and output.
 // Every mbarrier wait is bounded; a timeout sets an error bit and all roles
 // leave their loops so the block always reaches TMEM deallocation.
 #include "crmsd_math.cuh"
@@ -34,7 +43,6 @@ namespace bs {
 namespace {
 
 constexpr int kStages = 2;
-constexpr int kKChunk = 64;                              // atoms per 128-byte swizzle row
 constexpr int kBRows = 64;                               // B tile rows = 20 structures
 constexpr int kAOpBytes = kBlockRows * kKChunk * 2;      // 16 KB
 constexpr int kBOpBytes = kBRows * kKChunk * 2;          // 8 KB
@@ -46,7 +54,19 @@ constexpr int kTmemCols = 512;                           // 2 buffers x 4 levels
 constexpr int kPitch = 33;                               // staging pitch in floats
 constexpr int kEpiStageBytes = kEpiWarps * 32 * kPitch * 4;
 constexpr int kBarBytes = 256;
-constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kBarBytes;
+
+// What the epilogue needs of one tile, staged in shared memory by warp 3
+// one tile ahead, so that no global load sits on the epilogue's path.
+struct __align__(16) TileMeta {
+  SInfo ia[kBlockStructs];  // A-block structures
+  SInfo ib[kBStructs];      // B-block structures
+  OutDesc out;
+  long long n, n_b, first_a, first_b;
+  int a_blk, b_blk, job, mode, err, layout, L;
+  float tol, u, d34;
+};
+constexpr int kMetaBytes = 2 * (int)sizeof(TileMeta);
+constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes + kBarBytes;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr uint32_t kIdesc = ptx::idesc_bf16_f32(128, kBRows);
 
@@ -55,6 +75,8 @@ struct Shared {
   uint64_t empty[kStages];
   uint64_t tfull[2];
   uint64_t tempty[2];
+  uint64_t mfull[2];   // tile metadata slot written (warp 3)
+  uint64_t mempty[2];  // tile metadata slot released (epilogue)
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -67,18 +89,22 @@ __device__ __forceinline__ int64_t tri_index(int64_t n, int64_t i, int64_t j) {
 // f64 results are written as bit patterns built with integer operations
 // (a float -> double conversion would run on the slow FP64 pipe).
 __device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t j, float v) {
-  if (o.layout == 0) {
+  if (o.layout == kLayoutTriangle) {
     const int64_t idx = tri_index(o.n, i, j);
+    if (o.out_type == 0) static_cast<unsigned long long *>(o.ptr)[idx] = bsm::f32_to_f64_bits(v);
+    else static_cast<float *>(o.ptr)[idx] = v;
+  } else if (o.layout == kLayoutRect) {
+    const int64_t idx = i * o.ld + j;
     if (o.out_type == 0) static_cast<unsigned long long *>(o.ptr)[idx] = bsm::f32_to_f64_bits(v);
     else static_cast<float *>(o.ptr)[idx] = v;
   } else {
     if (o.out_type == 0) {
       const unsigned long long b = bsm::f32_to_f64_bits(v);
-      static_cast<unsigned long long *>(o.ptr)[i * o.n + j] = b;
-      static_cast<unsigned long long *>(o.ptr)[j * o.n + i] = b;
+      static_cast<unsigned long long *>(o.ptr)[i * o.ld + j] = b;
+      static_cast<unsigned long long *>(o.ptr)[j * o.ld + i] = b;
     } else {
-      static_cast<float *>(o.ptr)[i * o.n + j] = v;
-      static_cast<float *>(o.ptr)[j * o.n + i] = v;
+      static_cast<float *>(o.ptr)[i * o.ld + j] = v;
+      static_cast<float *>(o.ptr)[j * o.ld + i] = v;
     }
   }
 }
@@ -96,11 +122,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   float *stage_epi = reinterpret_cast<float *>(smem + (size_t)kStages * kStageBytes);
-  Shared *sh = reinterpret_cast<Shared *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes);
+  TileMeta *meta = reinterpret_cast<TileMeta *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes);
+  Shared *sh = reinterpret_cast<Shared *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk16 = a.lp / 16;
-  const int nchunks = (a.lp + kKChunk - 1) / kKChunk;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -110,6 +135,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&sh->tfull[b], 1);
       ptx::mbar_init(&sh->tempty[b], kEpiWarps * 32);
+      ptx::mbar_init(&sh->mfull[b], 1);
+      ptx::mbar_init(&sh->mempty[b], kEpiWarps * 32);
     }
     ptx::mbar_init(&sh->drain, 1);
     sh->abort = 0;
@@ -136,9 +163,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       // ------------------------------------------------------ TMA producer
       uint32_t it = 0;
+      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
       for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
-        const int2 tile = a.tiles[t];
-        const int rowA = tile.x * kBlockRows, rowB = tile.y * kBRows;
+        const Tile tile = next;
+        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
+        const int rowA = tile.a_blk * kBlockRows, rowB = tile.b_blk * kBRows;
+        const int nchunks = (tile_nk16(tile) * 16 + kKChunk - 1) / kKChunk;
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
@@ -168,16 +198,29 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       // ------------------------------------------------------- MMA issuer
-      uint32_t it = 0, tt = 0;
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
-        const uint32_t buf = tt & 1u, use = tt >> 1;
-        if (!ptx::mbar_wait(&sh->tempty[buf], (use & 1u) ^ 1u, abort, kTimeoutNs)) {
-          fail(sh, a.sc);
-          break;
-        }
-        ptx::tc_fence_after();
-        const uint32_t acc0 = tmem + buf * 256u;
+      // TMEM buffer slots are used in order: slot p is buffer p & 1 for the
+      // (p >> 1)-th time.  A long-layout tile takes two consecutive slots
+      // (eight accumulators: accumulator a lives in slot p + a / 4).
+      uint32_t it = 0, p = 0;
+      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
+      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
+        const Tile tile = next;
+        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
+        const int nk16 = tile_nk16(tile);
+        const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
+        const int lay = tile_layout(tile);
+        const uint32_t need = lay == kAccLong ? 2u : 1u;
         bool ok = true;
+        for (uint32_t u = 0; u < need && ok; ++u) {
+          const uint32_t q = p + u;
+          if (!ptx::mbar_wait(&sh->tempty[q & 1u], ((q >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
+            fail(sh, a.sc);
+            ok = false;
+          }
+        }
+        if (!ok) break;
+        ptx::tc_fence_after();
+        auto acc_col = [&](int ai) -> uint32_t { return tmem + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
@@ -191,6 +234,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t bbase = base + 4 * kAOpBytes;
           const int ksteps = min(4, nk16 - kc * 4);
           for (int kk = 0; kk < ksteps; ++kk) {
+            const int k = kc * 4 + kk;
             const uint32_t off = (uint32_t)kk * 32u;
             const uint64_t da0 = ptx::smem_desc_sw128(base + 0 * kAOpBytes + off);
             const uint64_t da1 = ptx::smem_desc_sw128(base + 1 * kAOpBytes + off);
@@ -199,26 +243,92 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t db0 = ptx::smem_desc_sw128(bbase + 0 * kBOpBytes + off);
             const uint64_t db1 = ptx::smem_desc_sw128(bbase + 1 * kBOpBytes + off);
             const uint64_t db2 = ptx::smem_desc_sw128(bbase + 2 * kBOpBytes + off);
-            const uint32_t acc = (kc | kk) ? 1u : 0u;
-            ptx::tc_mma_f16(acc0 + 0 * 64, da0, db0, kIdesc, acc);
-            ptx::tc_mma_f16(acc0 + 1 * 64, da0, db1, kIdesc, acc);
-            ptx::tc_mma_f16(acc0 + 1 * 64, da1, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(acc0 + 2 * 64, da0, db2, kIdesc, acc);
-            ptx::tc_mma_f16(acc0 + 2 * 64, da1, db1, kIdesc, 1u);
-            ptx::tc_mma_f16(acc0 + 2 * 64, da2, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(acc0 + 3 * 64, da1, db2, kIdesc, acc);
-            ptx::tc_mma_f16(acc0 + 3 * 64, da2, db1, kIdesc, 1u);
-            ptx::tc_mma_f16(acc0 + 3 * 64, da3, db2, kIdesc, 1u);
+            uint32_t col[4], acc[4];  // per level: accumulator column, accumulate (vs overwrite)
+            if (lay == kAccNormal) {
+              // one buffer, level lv at column 64 lv; every level starts at step 0
+              const uint32_t c0 = acc_col(0);
+              const uint32_t first = k > 0 ? 1u : 0u;
+#pragma unroll
+              for (int lv = 0; lv < 4; ++lv) {
+                col[lv] = c0 + lv * 64u;
+                acc[lv] = first;
+              }
+            } else {
+#pragma unroll
+              for (int lv = 0; lv < 4; ++lv) {
+                const int ai = acc_index(lay, lv, k, nk16);
+                col[lv] = acc_col(ai);
+                acc[lv] = (k > 0 && acc_index(lay, lv, k - 1, nk16) == ai) ? 1u : 0u;
+              }
+            }
+            ptx::tc_mma_f16(col[0], da0, db0, kIdesc, acc[0]);
+            ptx::tc_mma_f16(col[1], da0, db1, kIdesc, acc[1]);
+            ptx::tc_mma_f16(col[1], da1, db0, kIdesc, 1u);
+            ptx::tc_mma_f16(col[2], da0, db2, kIdesc, acc[2]);
+            ptx::tc_mma_f16(col[2], da1, db1, kIdesc, 1u);
+            ptx::tc_mma_f16(col[2], da2, db0, kIdesc, 1u);
+            ptx::tc_mma_f16(col[3], da1, db2, kIdesc, acc[3]);
+            ptx::tc_mma_f16(col[3], da2, db1, kIdesc, 1u);
+            ptx::tc_mma_f16(col[3], da3, db2, kIdesc, 1u);
           }
           ptx::tc_commit(&sh->empty[s]);
         }
         if (!ok) break;
-        ptx::tc_commit(&sh->tfull[buf]);
+        for (uint32_t u = 0; u < need; ++u) ptx::tc_commit(&sh->tfull[(p + u) & 1u]);
+        p += need;
       }
       // all MMAs of this thread complete before teardown
       ptx::tc_commit(&sh->drain);
       volatile int no_abort = 0;
       ptx::mbar_wait(&sh->drain, 0, &no_abort, 1000000000ull);
+    }
+    __syncwarp();
+  } else if (warp == 3) {
+    // ------------------------------------------------- tile metadata
+    uint32_t tt = 0;
+    for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
+      const uint32_t slot = tt & 1u;
+      if (!ptx::mbar_wait(&sh->mempty[slot], ((tt >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
+        if (lane == 0) fail(sh, a.sc);
+        break;
+      }
+      TileMeta &mt = meta[slot];
+      const Tile tile = a.tiles[t];
+      const Job &jb = a.jobs[tile.job];
+      if (lane == 0) {
+        mt.out = jb.out;
+        mt.n = jb.n;
+        mt.n_b = jb.n_b;
+        mt.first_a = jb.first_a;
+        mt.first_b = jb.first_b;
+        mt.a_blk = tile.a_blk;
+        mt.b_blk = tile.b_blk;
+        mt.job = tile.job;
+        mt.mode = jb.mode;
+        mt.err = jb.err;
+        mt.layout = jb.layout;
+        mt.L = jb.L;
+        mt.tol = jb.tol;
+        mt.u = jb.u;
+        mt.d34 = jb.d34;
+      }
+      // per-structure data of the tile's A and B blocks (pads and structures
+      // past a job's end read as zero; the epilogue never uses them)
+      const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs, b0 = (int64_t)tile.b_blk * kBStructs;
+      const int64_t aend = jb.first_a + jb.n, bend = jb.first_b + jb.n_b;
+      for (int k = lane; k < kBlockStructs + kBStructs; k += 32) {
+        const int64_t gs = k < kBlockStructs ? a0 + k : b0 + (k - kBlockStructs);
+        SInfo v{};
+        if (k < kBlockStructs) {
+          if (gs < aend) v = a.info_a[gs];
+          mt.ia[k] = v;
+        } else {
+          if (gs < bend) v = a.info_b[gs];
+          mt.ib[k - kBlockStructs] = v;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(&sh->mfull[slot]);
     }
     __syncwarp();
   } else if (warp >= kEpiWarp0) {
@@ -229,39 +339,65 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int il = lane / 3, x = lane - 3 * (lane / 3);
     const int ilr = il < kGroupStructs ? il : kGroupStructs - 1;  // pad lanes read a valid row
     const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * g;
-    uint32_t tt = 0;
+    uint32_t p = 0;   // TMEM buffer slot, as the MMA issuer counts them
+    uint32_t tt = 0;  // tile sequence number (metadata slot)
     for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++tt) {
-      const uint32_t buf = tt & 1u, use = tt >> 1;
-      if (!ptx::mbar_wait(&sh->tfull[buf], use & 1u, abort, kTimeoutNs)) {
+      const uint32_t slot = tt & 1u;
+      if (!ptx::mbar_wait(&sh->mfull[slot], (tt >> 1) & 1u, abort, kTimeoutNs)) {
         fail(sh, a.sc);
         break;
       }
+      const TileMeta &mt = meta[slot];
+      const bool lng = mt.layout == kAccLong;
+      bool ok = true;
+      for (uint32_t u = 0; u < (lng ? 2u : 1u) && ok; ++u) {
+        const uint32_t q = p + u;
+        if (!ptx::mbar_wait(&sh->tfull[q & 1u], (q >> 1) & 1u, abort, kTimeoutNs)) {
+          fail(sh, a.sc);
+          ok = false;
+        }
+      }
+      if (!ok) break;
       ptx::tc_fence_after();
-      const int2 tile = a.tiles[t];
-      const uint32_t col0 = lane_base + buf * 256u;
-      const int64_t i = (int64_t)tile.x * kBlockStructs + qd * kGroupStructs + il;
-      const bool row_ok = (lane < 30) && (i < a.n);
-      SInfo ia{};
-      if (row_ok) ia = a.info[i];
-      const bool dump = (a.dbg != nullptr) && (tile.x == 0) && (tile.y < 2);
+      // the tile's scalars in registers (shared memory would be re-read
+      // after every warp synchronisation)
+      const int64_t jn = mt.n, jnb = mt.n_b, fa = mt.first_a, fb = mt.first_b;
+      const bool sym = mt.mode == 0;
+      const bool job_ok = mt.err == 0;
+      const OutDesc out = mt.out;
+      const float t_d34 = mt.d34, t_u = mt.u, t_tol = mt.tol;
+      const int t_L = mt.L, t_job = mt.job;
+      // accumulators of level lv: normal layout {lv}; long layout L0 {0},
+      // L1 {1, 2}, L2 {3..6}, L3 {7}; accumulator ai sits in slot p + ai / 4
+      auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
+      const int64_t ig = (int64_t)mt.a_blk * kBlockStructs + qd * kGroupStructs + il;
+      const int64_t i = ig - fa;
+      const bool row_ok = job_ok && (lane < 30) && (i < jn);
+      const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
+      const bool dump = (a.dbg != nullptr) && (mt.a_blk == 0) && (mt.b_blk < 2) && !lng;
       // The group's 10 column structures are finished in two halves of five
       // (columns 15h .. 15h+14), so a lane carries at most two pairs at once.
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
-        const int c0 = 15 * h;  // first TMEM column of this half within the group
         // ---- pass A: FP32 covariance rows of this half, staged per lane
         {
           float m[32], v[32];
-          ptx::tmem_ld_32x32b_x32(col0 + 0 * 64, m);
-          ptx::tmem_ld_32x32b_x32(col0 + 1 * 64, v);
+          ptx::tmem_ld_32x32b_x32(acc_col(0), m);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);  // 2^-9
-          ptx::tmem_ld_32x32b_x32(col0 + 2 * 64, v);
+          for (int lv = 1; lv < 4; ++lv) {
+            const float wl = lv == 1 ? 0.001953125f : (lv == 2 ? 3.814697265625e-6f : 7.450580596923828125e-9f);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 3.814697265625e-6f, m[c]);  // 2^-18
-          ptx::tmem_ld_32x32b_x32(col0 + 3 * 64, v);
+            for (int part = 0; part < 4; ++part) {
+              // normal layout: accumulator lv; long: L1 {1, 2}, L2 {3..6}, L3 {7}
+              const int ai = lng ? (lv == 1 ? 1 + part : (lv == 2 ? 3 + part : 7)) : lv;
+              const bool use = part == 0 || (lng && (lv == 2 || (lv == 1 && part < 2)));
+              if (use) {
+                ptx::tmem_ld_32x32b_x32(acc_col(ai), v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 7.450580596923828125e-9f, m[c]);  // 2^-27
+                for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], wl, m[c]);
+              }
+            }
+          }
 #pragma unroll
           for (int c = 0; c < 16; ++c) stg[lane * kPitch + c] = h ? m[15 + c] : m[c];
         }
@@ -274,10 +410,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int sl = 0; sl < 2; ++sl) {
           const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
           const int jc = jh < 5 ? jh : 4;
-          jj[sl] = (int64_t)tile.y * 20 + g * kGroupStructs + 5 * h + jh;
-          valid[sl] = row_ok && (jh < 5) && (jj[sl] < a.n) && (jj[sl] > i);
-          ib[sl] = SInfo{};
-          if (valid[sl]) ib[sl] = a.info[jj[sl]];
+          const int64_t jg = (int64_t)mt.b_blk * kBStructs + g * kGroupStructs + 5 * h + jh;
+          jj[sl] = jg - fb;
+          valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
+          ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
           float m9[9];
 #pragma unroll
           for (int xr = 0; xr < 3; ++xr)
@@ -286,18 +422,36 @@ __global__ void __launch_bounds__(kThreads, 1)
           bsm::fast_begin(m9, valid[sl] ? ia.gf + ib[sl].gf : 0.f, st[sl]);
         }
         __syncwarp();
-        // ---- pass B: exact level sums, one level at a time
+        // ---- pass B: exact level sums, one level at a time (levels 0-2 as
+        // integers: the parts of a long-layout level add exactly)
 #pragma unroll
         for (int lv = 0; lv < 4; ++lv) {
+          const int a0 = lng ? (lv == 0 ? 0 : lv == 1 ? 1 : lv == 2 ? 3 : 7) : lv;
           float v[32];
-          ptx::tmem_ld_32x32b_x32(col0 + lv * 64, v);
+          ptx::tmem_ld_32x32b_x32(acc_col(a0), v);
           if (dump && h == 0) {
-            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * tile.y + 32 * g;
+            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * mt.b_blk + 32 * g;
 #pragma unroll
             for (int c = 0; c < 32; ++c) drow[c] = v[c];
           }
 #pragma unroll
-          for (int c = 0; c < 16; ++c) stg[lane * kPitch + c] = h ? v[15 + c] : v[c];
+          for (int c = 0; c < 16; ++c) {
+            const float w1 = h ? v[15 + c] : v[c];
+            stg[lane * kPitch + c] = lv < 3 ? __int_as_float(__float2int_rn(w1)) : w1;
+          }
+          if (lng && (lv == 1 || lv == 2)) {
+            // further parts of the level: added into the staged row (integers stay exact)
+#pragma unroll
+            for (int part = 1; part < 4; ++part) {
+              if (lv == 1 && part > 1) break;
+              ptx::tmem_ld_32x32b_x32(acc_col(a0 + part), v);
+#pragma unroll
+              for (int c = 0; c < 16; ++c) {
+                float &d = stg[lane * kPitch + c];
+                d = __int_as_float(__float_as_int(d) + __float2int_rn(h ? v[15 + c] : v[c]));
+              }
+            }
+          }
           __syncwarp();
 #pragma unroll
           for (int sl = 0; sl < 2; ++sl) {
@@ -308,14 +462,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
               for (int y = 0; y < 3; ++y) s9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
-            bsm::fast_level(st[sl], lv, s9);
+            bsm::fast_level_staged(st[sl], lv, s9);
           }
           __syncwarp();
         }
         if (h == 1) {
-          // all TMEM reads of this buffer are done: hand it back to the MMA warp
+          // all TMEM reads of this tile are done: hand its buffers back to the MMA warp
           ptx::tc_fence_before();
-          ptx::mbar_arrive(&sh->tempty[buf]);
+          ptx::mbar_arrive(&sh->tempty[p & 1u]);
+          if (lng) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
         }
         // ---- finish and store
 #pragma unroll
@@ -324,16 +479,19 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int64_t j = jj[sl];
           int flag = 0;
           const float r = bsm::fast_finish(st[sl], ia.ghat + ib[sl].ghat, ia.gf + ib[sl].gf, ia.qres + ib[sl].qres,
-                                           a.d34, a.u, a.L, a.tol, flag);
+                                           t_d34, t_u, t_L, t_tol, flag);
           if (flag) {
-            store_pair(a.out, i, j, -1.0f);
-            const unsigned long long slot = atomicAdd(&a.sc->flag_count, 1ull);
-            if (slot < a.flag_cap) a.flags[slot] = ((unsigned long long)i << 32) | (unsigned long long)j;
+            store_pair(out, i, j, -1.0f);
+            const unsigned long long q = atomicAdd(&a.sc->flag_count, 1ull);
+            if (q < a.flag_cap) a.flags[q] = flag_pack(t_job, ig, j + fb);
           } else {
-            store_pair(a.out, i, j, r);
+            store_pair(out, i, j, r);
           }
         }
       }
+      // the tile's metadata is no longer read: release its slot
+      ptx::mbar_arrive(&sh->mempty[slot]);
+      p += lng ? 2u : 1u;
     }
   }
   __syncthreads();
@@ -343,18 +501,30 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+__global__ void k_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
+    const Job &jb = jobs[tiles[t].job];
+    tiles[t].shape = (jb.lp / 16) | (jb.layout << 16);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs, int num_sms, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  k_tile_shapes<<<num_sms * 8, 256, 0, st>>>(tiles, ntiles, jobs);
+  return cudaGetLastError();
+}
 
 size_t mixed_tc_smem_bytes() { return kSmemBytes; }
 
+// Kernel attributes, set once per device before any launch or capture.
+cudaError_t mixed_tc_prepare() {
+  return cudaFuncSetAttribute(k_mixed_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+}
+
 cudaError_t launch_mixed_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t st) {
   if (a.ntiles <= 0) return cudaSuccess;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_mixed_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
   const int64_t grid = a.ntiles < a.num_sms ? a.ntiles : a.num_sms;
   k_mixed_tc<<<(unsigned)grid, kThreads, kSmemBytes, st>>>(tm[0], tm[1], tm[2], tm[3], tm[4], tm[5], tm[6], a);
   return cudaGetLastError();

@@ -34,29 +34,42 @@ __device__ __forceinline__ int64_t tri_index(int64_t n, int64_t i, int64_t j) {
 }
 
 __device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t j, double v) {
-  if (o.layout == 0) {
-    const int64_t idx = tri_index(o.n, i, j);
-    if (o.out_type == 0) static_cast<double *>(o.ptr)[idx] = v;
-    else static_cast<float *>(o.ptr)[idx] = (float)v;
+  int64_t idx, idx2 = -1;
+  if (o.layout == kLayoutTriangle) {
+    idx = tri_index(o.n, i, j);
+  } else if (o.layout == kLayoutRect) {
+    idx = i * o.ld + j;
   } else {
-    if (o.out_type == 0) {
-      static_cast<double *>(o.ptr)[i * o.n + j] = v;
-      static_cast<double *>(o.ptr)[j * o.n + i] = v;
-    } else {
-      static_cast<float *>(o.ptr)[i * o.n + j] = (float)v;
-      static_cast<float *>(o.ptr)[j * o.n + i] = (float)v;
-    }
+    idx = i * o.ld + j;
+    idx2 = j * o.ld + i;
+  }
+  if (o.out_type == 0) {
+    static_cast<double *>(o.ptr)[idx] = v;
+    if (idx2 >= 0) static_cast<double *>(o.ptr)[idx2] = v;
+  } else {
+    static_cast<float *>(o.ptr)[idx] = (float)v;
+    if (idx2 >= 0) static_cast<float *>(o.ptr)[idx2] = (float)v;
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_plain64_all(const double *__restrict__ y, const double *__restrict__ g,
-                                                          int64_t n, int L, int lp, OutDesc out) {
+// SYM: tiles (I <= J) of the upper triangle of one set, pairs i < j;
+// otherwise a grid of na/32 x nb/32 tiles of set A against set B, every pair.
+template <bool SYM>
+__global__ void __launch_bounds__(kThreads)
+    k_plain64_tiles(const double *__restrict__ ya, const double *__restrict__ ga, int64_t na,
+                    const double *__restrict__ yb, const double *__restrict__ gb, int64_t nb, int L, int lp,
+                    OutDesc out) {
   __shared__ double sA[3][kKC][kT];
   __shared__ double sB[3][kKC][kT];
-  const int64_t nb = (n + kT - 1) / kT;
   int64_t I, J;
-  tri_tile(blockIdx.x, nb, I, J);
-  const int ta = threadIdx.x / (kT / kJPer);       // 0..31 row structure
+  if (SYM) {
+    tri_tile(blockIdx.x, (na + kT - 1) / kT, I, J);
+  } else {
+    const int64_t tb_count = (nb + kT - 1) / kT;
+    I = blockIdx.x / tb_count;
+    J = blockIdx.x - I * tb_count;
+  }
+  const int ta = threadIdx.x / (kT / kJPer);            // 0..31 row structure
   const int tb = (threadIdx.x % (kT / kJPer)) * kJPer;  // first column structure
   double acc[kJPer][9];
 #pragma unroll
@@ -73,9 +86,13 @@ __global__ void __launch_bounds__(kThreads) k_plain64_all(const double *__restri
       const int k = r % kKC;
       const int64_t gs = (side == 0 ? I : J) * kT + s;
       double v = 0.0;
-      if (gs < n && k0 + k < lp) v = y[(gs * 3 + c) * (int64_t)lp + k0 + k];
-      if (side == 0) sA[c][k][s] = v;
-      else sB[c][k][s] = v;
+      if (side == 0) {
+        if (gs < na && k0 + k < lp) v = ya[(gs * 3 + c) * (int64_t)lp + k0 + k];
+        sA[c][k][s] = v;
+      } else {
+        if (gs < nb && k0 + k < lp) v = yb[(gs * 3 + c) * (int64_t)lp + k0 + k];
+        sB[c][k][s] = v;
+      }
     }
     __syncthreads();
 #pragma unroll 4
@@ -98,13 +115,13 @@ __global__ void __launch_bounds__(kThreads) k_plain64_all(const double *__restri
     __syncthreads();
   }
   const int64_t i = I * kT + ta;
-  if (i >= n) return;
-  const double gi = g[i];
+  if (i >= na) return;
+  const double gi = ga[i];
 #pragma unroll
   for (int q = 0; q < kJPer; ++q) {
     const int64_t j = J * kT + tb + q;
-    if (j >= n || j <= i) continue;
-    store_pair(out, i, j, bsm::qcp_rmsd_f64(acc[q], gi + g[j], L));
+    if (j >= nb || (SYM && j <= i)) continue;
+    store_pair(out, i, j, bsm::qcp_rmsd_f64(acc[q], gi + gb[j], L));
   }
 }
 
@@ -141,7 +158,16 @@ cudaError_t launch_plain64_all(const double *y, const double *g, int64_t n, int 
   const int64_t nb = (n + kT - 1) / kT;
   const int64_t ntiles = nb * (nb + 1) / 2;
   if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-  k_plain64_all<<<(unsigned)ntiles, kThreads, 0, st>>>(y, g, n, L, lp, out);
+  k_plain64_tiles<true><<<(unsigned)ntiles, kThreads, 0, st>>>(y, g, n, y, g, n, L, lp, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain64_rect(const double *ya, const double *ga, int64_t na, const double *yb, const double *gb,
+                                int64_t nb, int L, int lp, OutDesc out, cudaStream_t st) {
+  if (na < 1 || nb < 1) return cudaSuccess;
+  const int64_t ntiles = ((na + kT - 1) / kT) * ((nb + kT - 1) / kT);
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  k_plain64_tiles<false><<<(unsigned)ntiles, kThreads, 0, st>>>(ya, ga, na, yb, gb, nb, L, lp, out);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,190 @@
+// plan.cu -- the mixed-path launch plan (jobs, block map, tile table), the
+// tensor maps, and the device call sequence shared by every entry point.
+#include <stdio.h>
+
+#include <algorithm>
+#include <numeric>
+
+#include "engine.h"
+
+namespace bs {
+
+std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bool with_tiles, Plan &plan) {
+  plan = Plan{};
+  const int nj = (int)specs.size();
+  if (nj > 65535) return "more than 65535 structure sets in one call";
+  int64_t blk = 0;
+  int pitch = kKChunk;
+  plan.jobs.resize(nj);
+  for (int j = 0; j < nj; ++j) {
+    const JobSpec &s = specs[j];
+    Job &jb = plan.jobs[j];
+    jb = Job{};
+    jb.xyz = s.xyz;
+    jb.n = s.n;
+    jb.first_a = blk * kBlockStructs;
+    jb.first_b = jb.first_a;
+    jb.n_b = s.n;
+    jb.out = s.out;
+    jb.L = s.L;
+    jb.lp = lp_for(s.L);
+    jb.mode = 0;
+    jb.fixed_scale = 0;
+    jb.scale_min = -1000;
+    jb.tol = tol;
+    const int64_t nb = blocks_for(s.n);
+    for (int64_t b = 0; b < nb; ++b) plan.jobmap.push_back(j);
+    blk += nb;
+    pitch = std::max(pitch, pitch_for(s.L));
+  }
+  if (blk * kBlockStructs > kMaxGlobalStructs) return "more than 2^24 structures (padded to blocks of 40) in one call";
+  if (pitch > prep_max_pitch()) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "chain length above the mixed path's limit of %d atoms", prep_max_pitch());
+    return buf;
+  }
+  plan.nblocks = blk;
+  plan.pitch = pitch;
+  if (!with_tiles) return "";
+  std::vector<int> order(nj);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return specs[a].L > specs[b].L; });
+  constexpr int64_t SA = 32, SB = 64;  // super-block: 32 A blocks x 64 B blocks
+  for (int j : order) {
+    const Job &jb = plan.jobs[j];
+    if (jb.n < 2) continue;
+    const int64_t nba = blocks_for(jb.n), nbb = (jb.n + kBStructs - 1) / kBStructs;
+    const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / kBStructs;
+    for (int64_t sa = 0; sa < nba; sa += SA)
+      for (int64_t sb = 2 * sa; sb < nbb; sb += SB)
+        for (int64_t I = sa; I < std::min(sa + SA, nba); ++I)
+          for (int64_t J = std::max(sb, 2 * I); J < std::min(sb + SB, nbb); ++J)
+            plan.tiles.push_back(Tile{(int)(a0 + I), (int)(b0 + J), j, 0});
+  }
+  return "";
+}
+
+std::string get_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out) {
+  if (*out) return "";
+  cudaDriverEntryPointQueryResult q;
+  void *fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return "cuTensorMapEncodeTiled unavailable in the driver";
+  }
+  *out = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return "";
+}
+
+std::string encode_maps(PFN_cuTensorMapEncodeTiled_v12000 encode, const MixedBuffers &b, CUtensorMap tm[7]) {
+  // maps 0-3: A operand boxes (64 atoms x 128 rows) of e0, e1, e2, d2/32;
+  // maps 4-6: B boxes (64 x 64) of e0, e1, e2
+  for (int m = 0; m < 7; ++m) {
+    const bool a = m < 4;
+    const void *base = a ? (const void *)b.dig_a[m] : (const void *)b.dig_b[m - 4];
+    const int64_t pitch = a ? b.pitch_a : b.pitch_b, rows = a ? b.rows_a : b.rows_b;
+    cuuint64_t gdim[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)pitch * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kKChunk, a ? 128u : 64u};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&tm[m], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), gdim, gstride, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      char buf[96];
+      snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d) for map %d", (int)r, m);
+      return buf;
+    }
+  }
+  return "";
+}
+
+cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *job_stage, const CUtensorMap tm[7],
+                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg) {
+  auto rec = [&](int k) -> cudaError_t {
+    if (!ev) return cudaSuccess;
+    return cudaEventRecordWithFlags(ev[k], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+  };
+  const int nj = (int)plan.jobs.size();
+  cudaError_t e;
+  if ((e = rec(0)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(b.jobs, job_stage, (size_t)nj * sizeof(Job), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemsetAsync(b.sc, 0, sizeof(DevScalars), st)) != cudaSuccess) return e;
+  PrepArgs p{};
+  p.jobs = b.jobs;
+  p.njobs = nj;
+  p.job_of_struct_block = b.jobmap;
+  p.nblocks = plan.nblocks;
+  p.ctr = b.ctr;
+  for (int d = 0; d < 4; ++d) p.dig[d] = b.dig_a[d];
+  p.pitch = b.pitch_a;
+  p.info = b.info_a;
+  p.sc = b.sc;
+  if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
+  if ((e = rec(1)) != cudaSuccess) return e;
+  if (!plan.tiles.empty()) {
+    if ((e = launch_tile_shapes(b.tiles, (int64_t)plan.tiles.size(), b.jobs, num_sms, st)) != cudaSuccess) return e;
+    TcArgs a{};
+    a.tiles = b.tiles;
+    a.ntiles = (int64_t)plan.tiles.size();
+    a.jobs = b.jobs;
+    a.info_a = b.info_a;
+    a.info_b = b.info_b;
+    a.sc = b.sc;
+    a.flags = b.flags;
+    a.flag_cap = b.flag_cap;
+    a.dbg = dbg;
+    a.num_sms = num_sms;
+    if ((e = launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
+    if ((e = rec(2)) != cudaSuccess) return e;
+    RefineArgs r{};
+    r.da = DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a};
+    r.db = DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b};
+    r.info_a = b.info_a;
+    r.info_b = b.info_b;
+    r.jobs = b.jobs;
+    r.njobs = nj;
+    r.sc = b.sc;
+    r.flags = b.flags;
+    r.cap = b.flag_cap;
+    r.num_sms = num_sms;
+    if ((e = launch_refine(r, st)) != cudaSuccess) return e;
+  } else {
+    if ((e = rec(2)) != cudaSuccess) return e;
+  }
+  return rec(3);
+}
+
+bs_status collect_errors(const DevScalars &sc, const Job *jobs, int njobs, std::string &msg) {
+  char buf[256];
+  if (sc.err & kErrTimeout) {
+    msg = "a device-side wait timed out";
+    return BS_ERR_TIMEOUT;
+  }
+  if (sc.err & kErrInternal) {
+    msg = "device-side invariant violated";
+    return BS_ERR_INTERNAL;
+  }
+  for (int j = 0; j < njobs; ++j) {
+    if (jobs[j].err & kErrNonFinite) {
+      snprintf(buf, sizeof(buf), "structure set %d: input coordinates contain NaN or Inf", j);
+      msg = buf;
+      return BS_ERR_NONFINITE;
+    }
+  }
+  for (int j = 0; j < njobs; ++j) {
+    if (jobs[j].err & kErrUnsupported) {
+      snprintf(buf, sizeof(buf),
+               "structure set %d: coordinates beyond +-32768 A, or no coordinate grid meets the exactness bound "
+               "(chain of %d atoms)",
+               j, jobs[j].L);
+      msg = buf;
+      return BS_ERR_UNSUPPORTED;
+    }
+  }
+  return BS_OK;
+}
+
+}  // namespace bs

@@ -1,16 +1,26 @@
-// prep.cu -- streaming preparation pass over the input coordinates.
+// prep.cu -- streaming preparation passes over the input coordinates.
 //
-// Per structure: centroid (arithmetic mean, as bioshell-pdb's
-// SubstructureAxis centres, calc/substructures.rs:26-31), largest centred
-// coordinate, then either
-//   - mixed path: quantisation onto the grid 2^e, balanced digits (9, 9 and
-//     5 bits) written as bf16 rows of the digit matrices (plus the low digit
-//     scaled by 1/32, the operand of the level-4 product), exact squared norm
-//     Ghat, the RMS quantisation residual and digit norms for the exactness
-//     bound; or
-//   - plain path: the centred f64 coordinates in K-major [n][3][lp] and G.
-// One block per structure; the [L][3] AoS input of a structure is one
-// contiguous range, read coalesced.
+// Mixed path (all jobs of a launch at once, no host round trip):
+//   center  per structure: coordinates read as fixed-point integers (units
+//           2^-32 A, exact for the 3-decimal coordinates of PDB/mmCIF
+//           files), centroid (arithmetic mean, as bioshell-pdb's
+//           SubstructureAxis centres, calc/substructures.rs:26-31), largest
+//           centred coordinate of the job;
+//   scale   per job: the finest grid 2^e with every centred coordinate below
+//           (2^22 - 1) 2^e;
+//   norms   per structure: for grids e .. e+3, the row norms of the three
+//           balanced digits (9, 9 and 5 bits) of the quantised coordinates;
+//   choose  per job, from Cauchy-Schwarz bounds on the row norms: the
+//           finest grid whose tensor-core level sums 0-2 all stay below 2^24
+//           (exact) while its quantisation fits the error budget; for long
+//           chains, where no such grid exists, the finest grid with levels 0
+//           and 1 exact and level 2 below 2^26, its rounding (and level 3's)
+//           charged to the error budget;
+//   digits  per structure: digit rows (bf16), exact squared norm, RMS
+//           quantisation residual.
+// All of it is integer arithmetic: the FP64 pipe is not used.
+//
+// Plain path: FP64 centring into K-major [n][3][lp] and G.
 #include <math.h>
 
 #include "crmsd_math.cuh"
@@ -19,49 +29,398 @@
 namespace bs {
 namespace {
 
-constexpr int kPrepThreads = 128;
+constexpr int kWarpsPerBlock = 4;
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
+__device__ __forceinline__ long long warp_sum64(long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-
-__device__ __forceinline__ double warp_max(double v) {
+__device__ __forceinline__ unsigned warp_sum32(unsigned v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_max64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
   return v;
 }
 
-// Block-wide sum of N values held per thread; result valid in all threads.
-template <typename T, int N>
-__device__ __forceinline__ void block_sum(T (&v)[N], T *scratch /* [4][N] */) {
+// round(x * 2^32) from the bits of x, with integer operations only.
+// Returns 0, or kErrNonFinite for NaN/Inf, or kErrUnsupported for
+// |x| >= 2^15 A (outside the fixed-point range).
+__device__ __forceinline__ int to_fix(double x, long long &out) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  // |x| = mant 2^(ex - 1075) = mant 2^(sh) fixed-point units, mant in [2^52, 2^53)
+  const int sh = ex - 1043;
+  out = 0;
+  if (ex == 0x7ff) return kErrNonFinite;
+  if (sh > -6) return kErrUnsupported;  // |x| >= 2^15
+  const unsigned long long mant = (b & 0xfffffffffffffull) | 0x10000000000000ull;
+  long long v = 0;
+  if (ex != 0 && sh > -63) v = (long long)((mant + (1ull << (-sh - 1))) >> (-sh));  // round half up
+  out = (b >> 63) ? -v : v;
+  return 0;
+}
+
+struct Where {
+  int job;
+  int64_t local;  // structure index within the job (< n when valid)
+  bool valid;
+};
+
+__device__ __forceinline__ Where locate(const PrepArgs &p, int64_t g) {
+  Where w;
+  w.job = p.job_of_struct_block[g / kBlockStructs];
+  w.local = 0;
+  w.valid = false;
+  if (w.job < 0) return w;
+  const Job &jb = p.jobs[w.job];
+  w.local = g - jb.first_a;
+  w.valid = w.local >= 0 && w.local < jb.n;
+  return w;
+}
+
+// ------------------------------------------------------------------ center
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, int64_t nstructs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t g = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (g >= nstructs) return;
+  const Where w = locate(p, g);
+  if (!w.valid) return;
+  Job &jb = p.jobs[w.job];
+  const int L = jb.L;
+  const double *x = jb.xyz + w.local * 3 * (int64_t)L;
+  long long s[3] = {0, 0, 0};
+  int bad = 0;
+  int c = lane % 3;
+  for (int i = lane; i < 3 * L; i += 32) {
+    long long v;
+    bad |= to_fix(x[i], v);
+    s[0] += c == 0 ? v : 0;
+    s[1] += c == 1 ? v : 0;
+    s[2] += c == 2 ? v : 0;
+    c = (c + 2) % 3;  // (i + 32) mod 3
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  if (bad) {
+    if (lane == 0) atomicOr(&jb.err, bad);
+    return;
+  }
+  long long C[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const long long t = warp_sum64(s[k]);
+    const long long h = L / 2;
+    C[k] = t >= 0 ? (t + h) / L : -((-t + h) / L);
+  }
+  unsigned long long m = 0;
+  c = lane % 3;
+  for (int i = lane; i < 3 * L; i += 32) {
+    long long v;
+    to_fix(x[i], v);
+    const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
+    const unsigned long long a = (unsigned long long)(y < 0 ? -y : y);
+    m = a > m ? a : m;
+    c = (c + 2) % 3;
+  }
+  m = warp_max64(m);
+  if (lane == 0) {
+    p.ctr[3 * g + 0] = C[0];
+    p.ctr[3 * g + 1] = C[1];
+    p.ctr[3 * g + 2] = C[2];
+    atomicMax(&jb.maxabs, m);
+  }
+}
+
+// ------------------------------------------------------------------- scale
+__global__ void k_mx_scale(PrepArgs p) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.njobs) return;
+  Job &jb = p.jobs[j];
+  // smallest e with every centred coordinate <= (2^22 - 1) 2^e (the range of
+  // the three balanced digits); one thread per job, so plain FP64 is fine
+  const double m = (double)jb.maxabs * 2.3283064365386963e-10;  // Angstrom
+  const double lim = 4194303.0;
+  int e = -40;
+  if (m > 0.0) {
+    e = (int)ceil(log2(m / lim));
+    while (ldexp(lim, e) < m) ++e;
+    while (ldexp(lim, e - 1) >= m) --e;
+  }
+  if (jb.fixed_scale) {
+    if (e > jb.scale_min) atomicOr(&jb.err, kErrUnsupported);  // beyond the given grid's range
+    e = jb.scale_min;
+  } else if (e < jb.scale_min) {
+    e = jb.scale_min;
+  }
+  if (e < 1 - kFixBits) e = 1 - kFixBits;  // the grid is never finer than 2 fixed-point units
+  jb.scale_base = e;
+}
+
+// ---------------------------------------------------------------- norms
+// Row norms of the digits per candidate grid, over the whole chain, its two
+// halves and its four quarters (the accumulator parts of a long-layout
+// tile).  The three coordinate rows are done one after another.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, int64_t nstructs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t g = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  if (g >= nstructs) return;
+  const Where w = locate(p, g);
+  if (!w.valid) return;
+  Job &jb = p.jobs[w.job];
+  if (jb.err) return;
+  const int L = jb.L;
+  const int nk16 = jb.lp / 16;
+  const double *x = jb.xyz + w.local * 3 * (int64_t)L;
+  const int ncand = jb.fixed_scale ? 1 : 4;
+  const int t0 = jb.scale_base + kFixBits;
+  unsigned mfull[4][3], mhalf[4][3], mquart[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) mfull[a][d] = mhalf[a][d] = mquart[a][d] = 0;
+  for (int r = 0; r < 3; ++r) {
+    const long long C = p.ctr[3 * g + r];
+    unsigned acc[4][4][3];  // [candidate][quarter][digit]
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int qq = 0; qq < 4; ++qq)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[a][qq][d] = 0;
+    for (int k = lane; k < L; k += 32) {
+      long long v;
+      to_fix(x[3 * k + r], v);
+      const long long y = v - C;
+      const int qt = acc_part(k >> 4, nk16, 4);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        if (a < ncand) {
+          const int t = t0 + a;
+          const int q = (int)((y + (1ll << (t - 1))) >> t);
+          int e0, e1, e2;
+          bsm::split_digits(q, e0, e1, e2);
+          const unsigned s0 = (unsigned)(e0 * e0), s1 = (unsigned)(e1 * e1), s2 = (unsigned)(e2 * e2);
+#pragma unroll
+          for (int qq = 0; qq < 4; ++qq) {
+            if (qt == qq) {
+              acc[a][qq][0] += s0;
+              acc[a][qq][1] += s1;
+              acc[a][qq][2] += s2;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      if (a >= ncand) break;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        unsigned v[4];
+#pragma unroll
+        for (int qq = 0; qq < 4; ++qq) v[qq] = warp_sum32(acc[a][qq][d]);
+        const unsigned h0 = v[0] + v[1], h1 = v[2] + v[3], f = h0 + h1;
+        mfull[a][d] = f > mfull[a][d] ? f : mfull[a][d];
+        mhalf[a][d] = max(mhalf[a][d], max(h0, h1));
+        mquart[a][d] = max(mquart[a][d], max(max(v[0], v[1]), max(v[2], v[3])));
+      }
+    }
+  }
+  if (lane == 0) {
+    for (int a = 0; a < ncand; ++a)
+      for (int d = 0; d < 3; ++d) {
+        atomicMax(&jb.norm[a][d], (unsigned long long)mfull[a][d]);
+        atomicMax(&jb.normh[a][d], (unsigned long long)mhalf[a][d]);
+        atomicMax(&jb.normq[a][d], (unsigned long long)mquart[a][d]);
+      }
+  }
+}
+
+// ---------------------------------------------------------------- choose
+__global__ void k_mx_choose(PrepArgs p) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.njobs) return;
+  Job &jb = p.jobs[j];
+  if (jb.err) return;
+  // Preference, from Cauchy-Schwarz bounds on the row norms: (1) the finest
+  // grid whose level sums 0-2 are all exact (below 2^24) while its
+  // quantisation (about 2^e per pair) leaves a quarter of the budget to the
+  // arithmetic; (2) the same with the long accumulator layout (level 1 in
+  // halves, level 2 in quarters of the chain; long chains); (3) the finest
+  // grid with levels 0-1 exact and level 2 below 2^26, its rounding charged
+  // to the budget.
+  const int ncand = jb.fixed_scale ? 1 : 4;
+  const bool can_long = jb.mode == 0 && jb.lp / 16 >= 4;
+  int pick = -1, relaxed = -1, pick_long = -1;
+  double bb2[4], bb34[4];
+  for (int a = 0; a < ncand; ++a) {
+    double f[3], hh[3], qq[3], nb[3];
+    for (int d = 0; d < 3; ++d) {
+      f[d] = sqrt((double)jb.norm[a][d]);
+      hh[d] = sqrt((double)jb.normh[a][d]);
+      qq[d] = sqrt((double)jb.normq[a][d]);
+      nb[d] = jb.mode == 1 ? (double)jb.norm_b[d] : f[d];
+    }
+    const double b0 = f[0] * nb[0], b1 = f[0] * nb[1] + f[1] * nb[0];
+    const double b2 = f[0] * nb[2] + f[1] * nb[1] + f[2] * nb[0];
+    bb2[a] = b2;
+    bb34[a] = f[1] * nb[2] + f[2] * nb[1] + f[2] * nb[2] / 512.0;
+    const bool grid_ok = jb.fixed_scale || ldexp(1.0, jb.scale_base + a) <= 0.75 * (double)jb.tol;
+    if (grid_ok && b0 < 16777216.0 && b1 < 16777216.0 && b2 < 16777216.0) {
+      pick = a;
+      break;
+    }
+    if (grid_ok && can_long && pick_long < 0 && b0 < 16777216.0 && 2.0 * hh[0] * hh[1] < 16777216.0 &&
+        2.0 * qq[0] * qq[2] + qq[1] * qq[1] < 16777216.0)
+      pick_long = a;
+    if (b0 < 16777216.0 && b1 < 16777216.0 && b2 < 67108864.0 && relaxed < 0) relaxed = a;
+  }
+  jb.layout = kAccNormal;
+  if (pick < 0 && pick_long >= 0) {
+    pick = pick_long;
+    bb2[pick] = 0.0;  // every part of level 2 is exact
+    jb.layout = kAccLong;
+  }
+  if (pick < 0) pick = relaxed;
+  if (pick < 0) {
+    atomicOr(&jb.err, kErrUnsupported);
+    return;
+  }
+  // half-ulp rounding per accumulation step, 3 L steps per entry
+  double err2 = 0.0, err3 = 0.0;
+  if (bb2[pick] >= 16777216.0) err2 = 3.0 * (double)jb.L * ldexp(1.0, (int)floor(log2(bb2[pick])) - 24);
+  if (bb34[pick] >= 8388608.0) err3 = 3.0 * (double)jb.L * ldexp(1.0, (int)floor(log2(bb34[pick])) - 24);
+  // Mhat = 2^28 S0 + 2^19 S1 + 2^10 S2 + 2 S3'; the Rayleigh quotient moves
+  // by at most sqrt(3) ||dMhat||_F per unit |q|^2, and E by twice that
+  jb.d34 = (float)(6.0 * sqrt(3.0) * (1024.0 * err2 + 2.0 * err3) * (1.0 + 1e-6));
+  jb.scale_exp = jb.scale_base + pick;
+  jb.u = ldexpf(1.0f, 2 * jb.scale_exp);
+}
+
+// ---------------------------------------------------------------- digits
+// Warp per structure.  Pass 1 reads the AoS coordinates coalesced and keeps
+// the quantised values in shared memory (three rows of pitch ints); pass 2
+// writes the digit rows 16 bytes at a time.
+__device__ __forceinline__ uint32_t bf16x2(int lo, int hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn((float)lo, (float)hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+__device__ __forceinline__ uint32_t bf16x2s(int lo, int hi) {  // (d2/32) of both, from e2 = 16 d2
+  const __nv_bfloat162 v = __floats2bfloat162_rn((float)lo * (1.0f / 512.0f), (float)hi * (1.0f / 512.0f));
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__global__ void k_mx_digits(PrepArgs p, int64_t nstructs, int wpb) {
+  extern __shared__ int qsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t g = (int64_t)blockIdx.x * wpb + wib;
+  if (g >= nstructs) return;
+  const Where w = locate(p, g);
+  if (!w.valid) return;
+  Job &jb = p.jobs[w.job];
+  if (jb.err) return;
+  const int L = jb.L, lp = jb.lp;
+  int *q = qsm + (size_t)wib * 3 * p.pitch;
+  const double *x = jb.xyz + w.local * 3 * (int64_t)L;
+  const long long C[3] = {p.ctr[3 * g], p.ctr[3 * g + 1], p.ctr[3 * g + 2]};
+  const int t = jb.scale_exp + kFixBits;
+  long long gsum = 0;
+  float rsum = 0.f;  // |r| < 2^31 units; relative rounding charged below
+  int c = lane % 3;
+  for (int i = lane; i < 3 * L; i += 32) {
+    long long v;
+    to_fix(x[i], v);
+    const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
+    const int n = (int)((y + (1ll << (t - 1))) >> t);
+    const long long r = y - ((long long)n << t);
+    gsum += (long long)n * n;
+    const float rf = (float)(int)r;
+    rsum = fmaf(rf, rf, rsum);
+    q[c * p.pitch + i / 3] = n;
+    c = (c + 2) % 3;
+  }
+  for (int i = L + lane; i < lp; i += 32) {
+    q[i] = 0;
+    q[p.pitch + i] = 0;
+    q[2 * p.pitch + i] = 0;
+  }
+  __syncwarp();
+  // pass 2: 8 atoms of one row per lane-step
+  const int chunks = lp / 8;
+  for (int u = lane; u < 3 * chunks; u += 32) {
+    const int r = u / chunks, k0 = (u - r * chunks) * 8;
+    int e0[8], e1[8], e2[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) bsm::split_digits(q[r * p.pitch + k0 + k], e0[k], e1[k], e2[k]);
+    const int64_t off = digit_row(g, r) * p.pitch + k0;
+    uint4 v0, v1, v2, v3;
+    v0.x = bf16x2(e0[0], e0[1]); v0.y = bf16x2(e0[2], e0[3]); v0.z = bf16x2(e0[4], e0[5]); v0.w = bf16x2(e0[6], e0[7]);
+    v1.x = bf16x2(e1[0], e1[1]); v1.y = bf16x2(e1[2], e1[3]); v1.z = bf16x2(e1[4], e1[5]); v1.w = bf16x2(e1[6], e1[7]);
+    v2.x = bf16x2(e2[0], e2[1]); v2.y = bf16x2(e2[2], e2[3]); v2.z = bf16x2(e2[4], e2[5]); v2.w = bf16x2(e2[6], e2[7]);
+    v3.x = bf16x2s(e2[0], e2[1]); v3.y = bf16x2s(e2[2], e2[3]); v3.z = bf16x2s(e2[4], e2[5]); v3.w = bf16x2s(e2[6], e2[7]);
+    *reinterpret_cast<uint4 *>(p.dig[0] + off) = v0;
+    *reinterpret_cast<uint4 *>(p.dig[1] + off) = v1;
+    *reinterpret_cast<uint4 *>(p.dig[2] + off) = v2;
+    *reinterpret_cast<uint4 *>(p.dig[3] + off) = v3;
+  }
+  gsum = warp_sum64(gsum);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rsum += __shfl_xor_sync(0xffffffffu, rsum, o);
+  if (lane == 0) {
+    SInfo in;
+    in.ghat = gsum;
+    in.gf = (float)gsum;
+    // RMS residual in Angstrom, rounded up: a sum of 3L non-negative FP32
+    // terms (each rounded at most twice) is within (3L + 64) 2^-23 of the
+    // exact sum; plus 2^-30 A for the fixed-point reading and the centroid
+    // rounding (each below 2^-32 A per coordinate)
+    const double up = 1.0 + (3.0 * L + 64.0) * 1.1920928955078125e-7;
+    const double rms = sqrt((double)rsum * up / (double)L) * 2.3283064365386963e-10;  // 2^-32
+    in.qres = (float)(rms * (1.0 + 1e-6) + 9.313225746154785e-10);
+    p.info[g] = in;
+    atomicMax(&jb.qres_max_bits, __float_as_uint(in.qres));
+  }
+}
+
+// ------------------------------------------------------------ plain path
+constexpr int kPlainThreads = 128;
+
+template <int N>
+__device__ __forceinline__ void block_sum_d(double (&v)[N], double *scratch /* [4][N] */) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
-  for (int i = 0; i < N; ++i) v[i] = warp_sum(v[i]);
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
   if (lane == 0)
 #pragma unroll
     for (int i = 0; i < N; ++i) scratch[warp * N + i] = v[i];
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    T s = 0;
-    for (int w = 0; w < kPrepThreads / 32; ++w) s += scratch[w * N + i];
+    double s = 0;
+    for (int w = 0; w < kPlainThreads / 32; ++w) s += scratch[w * N + i];
     v[i] = s;
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kPrepThreads) k_prep_stats(const double *__restrict__ xyz, int L,
-                                                             double *__restrict__ ctr, DevScalars *sc) {
+__global__ void __launch_bounds__(kPlainThreads) k_plain_center(const double *__restrict__ xyz, int L, double *ctr,
+                                                                int *err) {
   __shared__ double red[4 * 3];
-  __shared__ double redm[4];
   const int64_t s = blockIdx.x;
   const double *x = xyz + s * 3 * (int64_t)L;
   double acc[3] = {0.0, 0.0, 0.0};
   int bad = 0;
-  for (int i = threadIdx.x; i < 3 * L; i += kPrepThreads) {
+  for (int i = threadIdx.x; i < 3 * L; i += kPlainThreads) {
     const double v = x[i];
     bad |= !isfinite(v);
     const int c = i % 3;
@@ -69,106 +428,18 @@ __global__ void __launch_bounds__(kPrepThreads) k_prep_stats(const double *__res
     acc[1] += (c == 1) ? v : 0.0;
     acc[2] += (c == 2) ? v : 0.0;
   }
-  block_sum<double, 3>(acc, red);
-  const double inv = 1.0 / (double)L;
-  const double c0 = acc[0] * inv, c1 = acc[1] * inv, c2 = acc[2] * inv;
-  double m = 0.0;
-  for (int i = threadIdx.x; i < 3 * L; i += kPrepThreads) {
-    const int c = i % 3;
-    const double v = x[i] - (c == 0 ? c0 : (c == 1 ? c1 : c2));
-    m = fmax(m, fabs(v));
-  }
-  m = warp_max(m);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) redm[warp] = m;
+  block_sum_d<3>(acc, red);
   bad = __syncthreads_or(bad);
   if (threadIdx.x == 0) {
-    double mm = 0.0;
-    for (int w = 0; w < kPrepThreads / 32; ++w) mm = fmax(mm, redm[w]);
-    ctr[3 * s + 0] = c0;
-    ctr[3 * s + 1] = c1;
-    ctr[3 * s + 2] = c2;
-    if (bad || !isfinite(mm)) {
-      atomicOr(&sc->err, kErrNonFinite);
-    } else {
-      atomicMax(&sc->maxabs_bits, (unsigned long long)__double_as_longlong(mm));
-    }
+    const double inv = 1.0 / (double)L;
+    ctr[3 * s + 0] = acc[0] * inv;
+    ctr[3 * s + 1] = acc[1] * inv;
+    ctr[3 * s + 2] = acc[2] * inv;
+    if (bad) atomicOr(err, kErrNonFinite);
   }
 }
 
-// Smallest e >= scale_min with max|y| <= (2^22 - 1) 2^e, so that every
-// quantised coordinate fits the three balanced digits.
-__global__ void k_prep_scale(DevScalars *sc) {
-  const double maxabs = __longlong_as_double((long long)sc->maxabs_bits);
-  const double lim = 4194303.0;  // 2^22 - 1
-  int e = -40;
-  if (maxabs > 0.0) {
-    e = (int)ceil(log2(maxabs / lim));
-    while (ldexp(lim, e) < maxabs) ++e;
-    while (ldexp(lim, e - 1) >= maxabs) --e;
-  }
-  if (e < sc->scale_min) e = sc->scale_min;
-  sc->scale_exp = e;
-}
-
-__global__ void __launch_bounds__(kPrepThreads)
-    k_prep_digits(const double *__restrict__ xyz, const double *__restrict__ ctr, int L, int lp,
-                  __nv_bfloat16 *__restrict__ d0, __nv_bfloat16 *__restrict__ d1, __nv_bfloat16 *__restrict__ d2,
-                  __nv_bfloat16 *__restrict__ d2s, SInfo *__restrict__ info, DevScalars *sc) {
-  __shared__ long long red[4 * 10];
-  __shared__ double redd[4];
-  const int64_t s = blockIdx.x;
-  const int e = sc->scale_exp;
-  const double r = ldexp(1.0, e), inv_r = ldexp(1.0, -e);
-  const double *x = xyz + s * 3 * (int64_t)L;
-  const double cc[3] = {ctr[3 * s], ctr[3 * s + 1], ctr[3 * s + 2]};
-  int64_t row[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) row[c] = digit_row(s, c) * lp;
-  // acc[0] = Ghat, acc[1 + 3*i + c] = sum of e_i^2 for coordinate c
-  long long acc[10];
-#pragma unroll
-  for (int i = 0; i < 10; ++i) acc[i] = 0;
-  double res[1] = {0.0};  // sum of squared quantisation residuals
-  for (int k = threadIdx.x; k < L; k += kPrepThreads) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const double y = x[3 * k + c] - cc[c];
-      const int q = __double2int_rn(y * inv_r);
-      const double dq = y - (double)q * r;
-      res[0] += dq * dq;
-      int a, b, d;
-      bsm::split_digits(q, a, b, d);
-      d0[row[c] + k] = __float2bfloat16_rn((float)a);
-      d1[row[c] + k] = __float2bfloat16_rn((float)b);
-      d2[row[c] + k] = __float2bfloat16_rn((float)d);
-      d2s[row[c] + k] = __float2bfloat16_rn((float)d * (1.0f / 512.0f));  // d2 / 32 = e2 / 512
-      acc[0] += (long long)q * q;
-      acc[1 + c] += (long long)(a * a);
-      acc[4 + c] += (long long)(b * b);
-      acc[7 + c] += (long long)(d * d);
-    }
-  }
-  block_sum<long long, 10>(acc, red);
-  block_sum<double, 1>(res, redd);
-  if (threadIdx.x == 0) {
-    SInfo in;
-    in.ghat = acc[0];
-    in.gf = (float)acc[0];
-    // rounded up so that the Minkowski bound stays a bound
-    in.qres = (float)(sqrt(res[0] / (double)L) * (1.0 + 1e-6)) + 1e-12f;
-    info[s] = in;
-    atomicMax(&sc->qres_max_bits, (unsigned long long)__float_as_uint(in.qres));
-    for (int i = 0; i < 3; ++i) {
-      long long mx = acc[1 + 3 * i];
-      mx = acc[2 + 3 * i] > mx ? acc[2 + 3 * i] : mx;
-      mx = acc[3 + 3 * i] > mx ? acc[3 + 3 * i] : mx;
-      atomicMax(&sc->norm_max[i], (unsigned long long)mx);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(kPrepThreads)
+__global__ void __launch_bounds__(kPlainThreads)
     k_prep_plain(const double *__restrict__ xyz, const double *__restrict__ ctr, int L, int lp,
                  double *__restrict__ y, double *__restrict__ g) {
   __shared__ double red[4];
@@ -177,7 +448,7 @@ __global__ void __launch_bounds__(kPrepThreads)
   const double cc[3] = {ctr[3 * s], ctr[3 * s + 1], ctr[3 * s + 2]};
   double *ys = y + s * 3 * (int64_t)lp;
   double acc[1] = {0.0};
-  for (int k = threadIdx.x; k < lp; k += kPrepThreads) {
+  for (int k = threadIdx.x; k < lp; k += kPlainThreads) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const double v = (k < L) ? x[3 * k + c] - cc[c] : 0.0;
@@ -185,35 +456,40 @@ __global__ void __launch_bounds__(kPrepThreads)
       acc[0] += v * v;
     }
   }
-  block_sum<double, 1>(acc, red);
+  block_sum_d<1>(acc, red);
   if (threadIdx.x == 0) g[s] = acc[0];
 }
 
 }  // namespace
 
-cudaError_t launch_prep_stats(const double *xyz, int64_t n, int L, double *ctr, DevScalars *sc,
-                              cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  k_prep_stats<<<(unsigned)n, kPrepThreads, 0, st>>>(xyz, L, ctr, sc);
+cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st) {
+  const int64_t nstructs = p.nblocks * kBlockStructs;
+  if (nstructs <= 0) return cudaSuccess;
+  const unsigned gw = (unsigned)((nstructs + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
+  k_mx_scale<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
+  k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
+  k_mx_choose<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
+  const size_t per_warp = (size_t)3 * p.pitch * sizeof(int);
+  int wpb = (int)(196608 / per_warp);
+  wpb = wpb > 8 ? 8 : (wpb < 1 ? 1 : wpb);
+  k_mx_digits<<<(unsigned)((nstructs + wpb - 1) / wpb), wpb * 32, wpb * per_warp, st>>>(p, nstructs, wpb);
   return cudaGetLastError();
 }
 
-cudaError_t launch_prep_scale(DevScalars *sc, cudaStream_t st) {
-  k_prep_scale<<<1, 1, 0, st>>>(sc);
-  return cudaGetLastError();
+// Largest digit-row pitch (atoms) the preparation pass supports.
+int prep_max_pitch() { return 196608 / (3 * (int)sizeof(int)); }
+
+// Kernel attributes, set once per device before any launch or capture.
+cudaError_t prep_prepare() {
+  return cudaFuncSetAttribute(k_mx_digits, cudaFuncAttributeMaxDynamicSharedMemorySize, 196608);
 }
 
-cudaError_t launch_prep_digits(const double *xyz, const double *ctr, int64_t n, int L, int lp,
-                               __nv_bfloat16 *const *dig, SInfo *info, DevScalars *sc, cudaStream_t st) {
+cudaError_t launch_prep_plain(const double *xyz, int64_t n, int L, int lp, double *ctr, double *y, double *g,
+                              int *err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  k_prep_digits<<<(unsigned)n, kPrepThreads, 0, st>>>(xyz, ctr, L, lp, dig[0], dig[1], dig[2], dig[3], info, sc);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_prep_plain(const double *xyz, const double *ctr, int64_t n, int L, int lp, double *y,
-                              double *g, cudaStream_t st) {
-  if (n <= 0) return cudaSuccess;
-  k_prep_plain<<<(unsigned)n, kPrepThreads, 0, st>>>(xyz, ctr, L, lp, y, g);
+  k_plain_center<<<(unsigned)n, kPlainThreads, 0, st>>>(xyz, L, ctr, err);
+  k_prep_plain<<<(unsigned)n, kPlainThreads, 0, st>>>(xyz, ctr, L, lp, y, g);
   return cudaGetLastError();
 }
 

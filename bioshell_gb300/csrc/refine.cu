@@ -27,39 +27,39 @@ __device__ __forceinline__ void tri_pair(int64_t n, int64_t t, int64_t &i, int64
 }
 
 __device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t j, double v) {
-  if (o.layout == 0) {
-    const int64_t idx = tri_index(o.n, i, j);
-    if (o.out_type == 0) static_cast<double *>(o.ptr)[idx] = v;
-    else static_cast<float *>(o.ptr)[idx] = (float)v;
+  int64_t idx, idx2 = -1;
+  if (o.layout == kLayoutTriangle) {
+    idx = tri_index(o.n, i, j);
+  } else if (o.layout == kLayoutRect) {
+    idx = i * o.ld + j;
   } else {
-    if (o.out_type == 0) {
-      static_cast<double *>(o.ptr)[i * o.n + j] = v;
-      static_cast<double *>(o.ptr)[j * o.n + i] = v;
-    } else {
-      static_cast<float *>(o.ptr)[i * o.n + j] = (float)v;
-      static_cast<float *>(o.ptr)[j * o.n + i] = (float)v;
-    }
+    idx = i * o.ld + j;
+    idx2 = j * o.ld + i;
+  }
+  if (o.out_type == 0) {
+    static_cast<double *>(o.ptr)[idx] = v;
+    if (idx2 >= 0) static_cast<double *>(o.ptr)[idx2] = v;
+  } else {
+    static_cast<float *>(o.ptr)[idx] = (float)v;
+    if (idx2 >= 0) static_cast<float *>(o.ptr)[idx2] = (float)v;
   }
 }
 
-struct Digits {
-  const __nv_bfloat16 *d0, *d1, *d2;
-  int lp;
-  __device__ __forceinline__ int coord(int64_t s, int c, int k) const {
-    const int64_t off = digit_row(s, c) * lp + k;
-    return bsm::join_digits((int)__bfloat162float(d0[off]), (int)__bfloat162float(d1[off]),
-                            (int)__bfloat162float(d2[off]));
-  }
-};
+__device__ __forceinline__ int coord(const DigitsView &dg, int64_t s, int c, int k) {
+  const int64_t off = digit_row(s, c) * dg.pitch + k;
+  return bsm::join_digits((int)__bfloat162float(dg.d0[off]), (int)__bfloat162float(dg.d1[off]),
+                          (int)__bfloat162float(dg.d2[off]));
+}
 
-// Exact int64 covariance of pair (i, j), partial over atoms k = k0, k0+ks, ...
-__device__ __forceinline__ void exact_cov_partial(const Digits &dg, int64_t i, int64_t j, int L, int k0, int ks,
-                                                  long long mh[9]) {
+// Exact int64 covariance of pair (i on side A, j on side B), partial over
+// atoms k = k0, k0+ks, ...
+__device__ __forceinline__ void exact_cov_partial(const DigitsView &da, const DigitsView &db, int64_t i, int64_t j,
+                                                  int L, int k0, int ks, long long mh[9]) {
 #pragma unroll
   for (int e = 0; e < 9; ++e) mh[e] = 0;
   for (int k = k0; k < L; k += ks) {
-    const int a0 = dg.coord(i, 0, k), a1 = dg.coord(i, 1, k), a2 = dg.coord(i, 2, k);
-    const int b0 = dg.coord(j, 0, k), b1 = dg.coord(j, 1, k), b2 = dg.coord(j, 2, k);
+    const int a0 = coord(da, i, 0, k), a1 = coord(da, i, 1, k), a2 = coord(da, i, 2, k);
+    const int b0 = coord(db, j, 0, k), b1 = coord(db, j, 1, k), b2 = coord(db, j, 2, k);
     mh[0] += (long long)a0 * b0;
     mh[1] += (long long)a0 * b1;
     mh[2] += (long long)a0 * b2;
@@ -72,72 +72,89 @@ __device__ __forceinline__ void exact_cov_partial(const Digits &dg, int64_t i, i
   }
 }
 
-__device__ __forceinline__ double exact_pair_warp(const Digits &dg, int64_t i, int64_t j, int L,
-                                                  const SInfo *info, int scale_exp, int lane) {
+__device__ __forceinline__ double exact_pair_warp(const RefineArgs &r, const Job &jb, int64_t ig, int64_t jg,
+                                                  int lane) {
   long long mh[9];
-  exact_cov_partial(dg, i, j, L, lane, 32, mh);
+  exact_cov_partial(r.da, r.db, ig, jg, jb.L, lane, 32, mh);
 #pragma unroll
   for (int e = 0; e < 9; ++e)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mh[e] += __shfl_xor_sync(0xffffffffu, mh[e], o);
-  return bsm::pair_rmsd_exact(mh, info[i].ghat, info[j].ghat, scale_exp, L);
+  return bsm::pair_rmsd_exact(mh, r.info_a[ig].ghat, r.info_b[jg].ghat, jb.scale_exp, jb.L);
 }
 
-__global__ void k_refine_list(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc,
-                              const unsigned long long *__restrict__ flags, unsigned long long cap, OutDesc out) {
-  const unsigned long long cnt = sc->flag_count < cap ? sc->flag_count : cap;
+__global__ void k_refine_list(RefineArgs r) {
+  const unsigned long long cnt = r.sc->flag_count < r.cap ? r.sc->flag_count : r.cap;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int scale_exp = sc->scale_exp;
   for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)cnt; w += warps) {
-    const unsigned long long f = flags[w];
-    const int64_t i = (int64_t)(f >> 32), j = (int64_t)(f & 0xffffffffull);
-    const double r = exact_pair_warp(dg, i, j, L, info, scale_exp, lane);
-    if (lane == 0) store_pair(out, i, j, r);
+    const unsigned long long f = r.flags[w];
+    const int job = (int)(f >> 48);
+    const int64_t ig = (int64_t)((f >> 24) & 0xffffffull), jg = (int64_t)(f & 0xffffffull);
+    const Job &jb = r.jobs[job];
+    const double v = exact_pair_warp(r, jb, ig, jg, lane);
+    if (lane == 0) store_pair(jb.out, ig - jb.first_a, jg - jb.first_b, v);
   }
 }
 
-// Fallback when the flag list overflowed: every negative (sentinel) entry of
-// the output is recomputed.
-__global__ void k_refine_scan(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc, OutDesc out) {
+// Fallback when the queue overflowed: every negative (sentinel) entry of the
+// jobs' outputs is recomputed.  Returns at once when nothing overflowed.
+__global__ void k_refine_scan(RefineArgs r) {
+  if (r.sc->flag_count <= r.cap) return;
   const int lane = threadIdx.x & 31;
-  const int64_t n = out.n;
-  const int64_t total = n * (n - 1) / 2;
-  const int scale_exp = sc->scale_exp;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t base = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < total;
-       base += warps * 32) {
-    const int64_t t = base + lane;
-    int64_t i = 0, j = 0;
-    bool sent = false;
-    if (t < total) {
-      tri_pair(n, t, i, j);
-      double v;
-      if (out.layout == 0) v = out.out_type == 0 ? static_cast<double *>(out.ptr)[t] : static_cast<float *>(out.ptr)[t];
-      else v = out.out_type == 0 ? static_cast<double *>(out.ptr)[i * n + j] : static_cast<float *>(out.ptr)[i * n + j];
-      sent = v < 0.0;
-    }
-    unsigned m = __ballot_sync(0xffffffffu, sent);
-    while (m) {
-      const int src = __ffs(m) - 1;
-      m &= m - 1;
-      const int64_t si = __shfl_sync(0xffffffffu, i, src);
-      const int64_t sj = __shfl_sync(0xffffffffu, j, src);
-      const double r = exact_pair_warp(dg, si, sj, L, info, scale_exp, lane);
-      if (lane == 0) store_pair(out, si, sj, r);
+  const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int job = 0; job < r.njobs; ++job) {
+    const Job &jb = r.jobs[job];
+    if (jb.err) continue;
+    const OutDesc &out = jb.out;
+    const bool sym = jb.mode == 0;
+    const int64_t n = jb.n, nb = jb.n_b;
+    const int64_t total = sym ? n * (n - 1) / 2 : n * nb;
+    for (int64_t base = w0 * 32; base < total; base += warps * 32) {
+      const int64_t t = base + lane;
+      int64_t i = 0, j = 0;
+      bool sent = false;
+      if (t < total) {
+        int64_t idx;
+        if (sym) {
+          tri_pair(n, t, i, j);
+          idx = out.layout == kLayoutTriangle ? t : i * out.ld + j;
+        } else {
+          i = t / nb;
+          j = t - i * nb;
+          idx = i * out.ld + j;
+        }
+        const double v = out.out_type == 0 ? static_cast<const double *>(out.ptr)[idx]
+                                           : (double)static_cast<const float *>(out.ptr)[idx];
+        sent = v < 0.0;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, sent);
+      while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int64_t si = __shfl_sync(0xffffffffu, i, src);
+        const int64_t sj = __shfl_sync(0xffffffffu, j, src);
+        const double v = exact_pair_warp(r, jb, si + jb.first_a, sj + jb.first_b, lane);
+        if (lane == 0) store_pair(out, si, sj, v);
+      }
     }
   }
 }
 
-// Thread per pair: exact level sums on CUDA cores, the fast epilogue, and
-// the exact path when the pair is flagged.  Level 3 carries S3 + S4/512 as
-// the tensor cores accumulate it (here rounded once from the exact value).
-__global__ void k_mixed_pairs(Digits dg, int L, const SInfo *__restrict__ info, DevScalars *sc, float tol, float u,
-                              float d34, const int64_t *__restrict__ ii, const int64_t *__restrict__ jj, int64_t np,
+// Thread per pair of job 0: exact level sums on CUDA cores, the fast
+// epilogue, and the exact path when the pair is flagged.  Level 3 carries
+// S3 + S4/512 as the tensor cores accumulate it (here rounded once from the
+// exact value).
+__global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, const Job *job, DevScalars *sc,
+                              const int64_t *__restrict__ ii, const int64_t *__restrict__ jj, int64_t np,
                               double *__restrict__ out, float *__restrict__ levels_out) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= np) return;
-  const int64_t i = ii[t], j = jj[t];
+  const Job &jb = *job;
+  if (jb.err) return;
+  const int64_t i = ii[t] + jb.first_a, j = jj[t] + jb.first_a;
+  const int L = jb.L;
   if (i == j) {
     out[t] = 0.0;
     if (levels_out)
@@ -149,12 +166,12 @@ __global__ void k_mixed_pairs(Digits dg, int L, const SInfo *__restrict__ info, 
   for (int l = 0; l < 5; ++l)
 #pragma unroll
     for (int e = 0; e < 9; ++e) S[l][e] = 0;
-  const int lp = dg.lp;
+  const int64_t pitch = dg.pitch;
   for (int k = 0; k < L; ++k) {
     int a[3][3], b[3][3];  // [coord][digit]
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const int64_t oa = digit_row(i, c) * lp + k, ob = digit_row(j, c) * lp + k;
+      const int64_t oa = digit_row(i, c) * pitch + k, ob = digit_row(j, c) * pitch + k;
       a[c][0] = (int)__bfloat162float(dg.d0[oa]);
       a[c][1] = (int)__bfloat162float(dg.d1[oa]);
       a[c][2] = (int)__bfloat162float(dg.d2[oa]);
@@ -199,41 +216,30 @@ __global__ void k_mixed_pairs(Digits dg, int L, const SInfo *__restrict__ info, 
     }
   }
   int flag = 0;
-  const float r = bsm::pair_rmsd_fast(in, u, d34, L, tol, flag);
+  const float r = bsm::pair_rmsd_fast(in, jb.u, jb.d34, L, jb.tol, flag);
   if (!flag) {
     out[t] = (double)r;
     return;
   }
   long long mh[9];
-  exact_cov_partial(dg, i, j, L, 0, 1, mh);
-  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, sc->scale_exp, L);
+  exact_cov_partial(dg, dg, i, j, L, 0, 1, mh);
+  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
 }
 
 }  // namespace
 
-cudaError_t launch_refine_list(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               const unsigned long long *flags, unsigned long long cap, OutDesc out, int num_sms,
+cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st) {
+  k_refine_list<<<r.num_sms * 4, 256, 0, st>>>(r);
+  k_refine_scan<<<r.num_sms * 4, 256, 0, st>>>(r);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Job *job, DevScalars *sc,
+                               const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
                                cudaStream_t st) {
-  Digits dg{dig[0], dig[1], dig[2], lp};
-  k_refine_list<<<num_sms * 4, 256, 0, st>>>(dg, L, info, sc, flags, cap, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_refine_scan(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               OutDesc out, int num_sms, cudaStream_t st) {
-  Digits dg{dig[0], dig[1], dig[2], lp};
-  k_refine_scan<<<num_sms * 4, 256, 0, st>>>(dg, L, info, sc, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_mixed_pairs(__nv_bfloat16 *const *dig, int lp, int L, const SInfo *info, DevScalars *sc,
-                               float tol, float u, float d34, const int64_t *ii, const int64_t *jj, int64_t np,
-                               double *out, float *levels_out, cudaStream_t st) {
   if (np <= 0) return cudaSuccess;
-  Digits dg{dig[0], dig[1], dig[2], lp};
   const int th = 128;
-  k_mixed_pairs<<<(unsigned)((np + th - 1) / th), th, 0, st>>>(dg, L, info, sc, tol, u, d34, ii, jj, np, out,
-                                                               levels_out);
+  k_mixed_pairs<<<(unsigned)((np + th - 1) / th), th, 0, st>>>(dg, info, job, sc, ii, jj, np, out, levels_out);
   return cudaGetLastError();
 }
 

@@ -24,19 +24,26 @@ PRECISION = {"plain64": 0, "mixed": 1}
 LAYOUT = {"triangle": 0, "square": 1}
 OUT_TYPE = {"f64": 0, "f32": 1}
 LINK = {"single": 0, "complete": 1, "average": 2, "median": 3, "centroid": 4, "ward": 5}
+FLAG_NO_GRAPH = 1
 
 
 class bs_opts(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("precision", ctypes.c_int32), ("layout", ctypes.c_int32),
-                ("out_type", ctypes.c_int32), ("tolerance", ctypes.c_double),
-                ("reserved", ctypes.c_int32 * 8)]
+                ("out_type", ctypes.c_int32), ("tolerance", ctypes.c_double), ("flags", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 7)]
+
+
+class bs_set_desc(ctypes.Structure):
+    _fields_ = [("xyz", ctypes.c_void_p), ("n", ctypes.c_int64), ("L", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("out", ctypes.c_void_p)]
 
 
 class bs_metrics(ctypes.Structure):
     _fields_ = [("pairs", ctypes.c_int64), ("pairs_refined", ctypes.c_int64), ("ms_total", ctypes.c_double),
                 ("ms_h2d", ctypes.c_double), ("ms_prep", ctypes.c_double), ("ms_main", ctypes.c_double),
                 ("ms_refine", ctypes.c_double), ("ms_d2h", ctypes.c_double), ("scale_exp", ctypes.c_int32),
-                ("main_launches", ctypes.c_int32), ("quant_bound", ctypes.c_double),
+                ("main_launches", ctypes.c_int32), ("jobs", ctypes.c_int32), ("graph", ctypes.c_int32),
+                ("quant_bound", ctypes.c_double),
                 ("bytes_h2d", ctypes.c_int64), ("bytes_d2h", ctypes.c_int64)]
 
     def as_dict(self):
@@ -62,6 +69,7 @@ SIGNATURES = [
     ("bs_ctx_stream", ctypes.c_void_p, [_vp]),
     ("bs_crmsd", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _dp]),
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
+    ("bs_batched", ctypes.c_int32, [_vp, ctypes.POINTER(bs_set_desc), ctypes.c_int32, ctypes.POINTER(bs_opts)]),
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                   ctypes.POINTER(bs_opts), _vp]),
     ("bs_all_vs_all_static", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),

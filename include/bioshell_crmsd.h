@@ -18,6 +18,9 @@
  *                                   from n(n-1)/2 closure calls
  *                                   (bioshell-clustering/src/hierarchical/
  *                                   clustering_matrix.rs:11-22)
+ *   batched all-vs-all           -> one such matrix per decoy set, for the
+ *                                   per-set clustering loop of a caller
+ *                                   (OPTICS over each set, optics.rs:51-58)
  *
  * Conventions
  *   - Coordinates are f64 AoS xyz triples, `[n][L][3]`, the layout of
@@ -46,7 +49,7 @@ extern "C" {
 
 #define BS_API __attribute__((visibility("default")))
 
-#define BS_ABI_VERSION 1
+#define BS_ABI_VERSION 2
 #define BS_OPTS_VERSION 1
 
 typedef int32_t bs_status;
@@ -96,8 +99,17 @@ typedef struct {
                          arithmetic); pairs whose fast-path bound does not
                          meet it are recomputed exactly.  <= 0 selects the
                          default, 1e-4                                    */
-  int32_t reserved[8];
+  int32_t flags;      /* BS_FLAG_* bits                                    */
+  int32_t reserved[7];
 } bs_opts;
+
+/* bs_opts.flags */
+enum {
+  /* Launch the mixed-path kernels one by one instead of replaying a CUDA
+   * graph captured for the call's shape (a graph is captured the first time
+   * a shape is seen and replayed for every later call of that shape). */
+  BS_FLAG_NO_GRAPH = 1
+};
 
 /* Per-call counters of the last compute call on a context. */
 typedef struct {
@@ -109,8 +121,12 @@ typedef struct {
   double ms_main;          /* covariance + QCP kernel                        */
   double ms_refine;        /* exact recomputation of flagged pairs           */
   double ms_d2h;           /* device -> host copy of the result              */
-  int32_t scale_exp;       /* mixed path: coordinate grid is 2^scale_exp A   */
+  int32_t scale_exp;       /* mixed path: coordinate grid is 2^scale_exp A
+                              (of the first structure set)                   */
   int32_t main_launches;   /* kernels launched by the call                   */
+  int32_t jobs;            /* structure sets (or query blocks) in the call   */
+  int32_t graph;           /* 0 direct launches, 1 graph captured and run,
+                              2 captured graph replayed                      */
   double quant_bound;      /* mixed path: worst RMSD change from the grid    */
   int64_t bytes_h2d;
   int64_t bytes_d2h;
@@ -146,6 +162,23 @@ BS_API bs_status bs_crmsd(bs_ctx *ctx, const double *a, const double *b, int32_t
  * HierarchicalClusteringMatrix::new (clustering_matrix.rs:11-22). */
 BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const bs_opts *opts,
                                void *out);
+
+/* One structure set of a batched call. */
+typedef struct {
+  const double *xyz; /* [n][L][3] f64 AoS, host or device memory            */
+  int64_t n;         /* structures in the set (>= 0)                         */
+  int32_t L;         /* atoms per structure (>= 1)                           */
+  int32_t reserved;
+  void *out;         /* the set's result: layout and element type of opts   */
+} bs_set_desc;
+
+/* All-vs-all crmsd of every set in `sets` (sizes and chain lengths may
+ * differ), each into its own `out`.  On the mixed path all sets run in one
+ * persistent tensor-core launch (one call sequence, replayed as a CUDA
+ * graph for repeated shapes); each set gets its own coordinate grid and
+ * error budget, so a set's result does not depend on the other sets in the
+ * call.  The plain path runs the sets one after another. */
+BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets, const bs_opts *opts);
 
 /* crmsd of an explicit pair list: out[t] = crmsd(xyz[ii[t]], xyz[jj[t]]),
  * f64.  Used for sampled checks and for sparse consumers. */

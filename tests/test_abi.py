@@ -36,7 +36,7 @@ def test_ctypes_signatures_cover_header():
 
 
 def test_abi_version_and_status_strings(enginelib):
-    assert enginelib.bs_abi_version() == 1
+    assert enginelib.bs_abi_version() == 2
     assert enginelib.bs_status_string(0) == b"ok"
     assert enginelib.bs_status_string(8).startswith(b"no usable")
     assert enginelib.bs_status_string(1234) == b"unknown status"
@@ -54,8 +54,10 @@ def test_struct_layout_matches_c():
 #include <stddef.h>
 #include "bioshell_crmsd.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(bs_opts), offsetof(bs_opts, tolerance), sizeof(bs_metrics),
-         offsetof(bs_metrics, scale_exp), offsetof(bs_metrics, quant_bound), offsetof(bs_metrics, bytes_d2h));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(bs_opts), offsetof(bs_opts, tolerance),
+         offsetof(bs_opts, flags), sizeof(bs_metrics), offsetof(bs_metrics, scale_exp),
+         offsetof(bs_metrics, graph), offsetof(bs_metrics, quant_bound), offsetof(bs_metrics, bytes_d2h),
+         sizeof(bs_set_desc), offsetof(bs_set_desc, L), offsetof(bs_set_desc, out));
   return 0;
 }
 """
@@ -65,8 +67,10 @@ int main(void) {
         open(c, "w").write(src)
         subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), c, "-o", exe], check=True)
         got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
-    want = [ctypes.sizeof(L.bs_opts), L.bs_opts.tolerance.offset, ctypes.sizeof(L.bs_metrics),
-            L.bs_metrics.scale_exp.offset, L.bs_metrics.quant_bound.offset, L.bs_metrics.bytes_d2h.offset]
+    want = [ctypes.sizeof(L.bs_opts), L.bs_opts.tolerance.offset, L.bs_opts.flags.offset,
+            ctypes.sizeof(L.bs_metrics), L.bs_metrics.scale_exp.offset, L.bs_metrics.graph.offset,
+            L.bs_metrics.quant_bound.offset, L.bs_metrics.bytes_d2h.offset, ctypes.sizeof(L.bs_set_desc),
+            L.bs_set_desc.L.offset, L.bs_set_desc.out.offset]
     assert got == want
 
 
