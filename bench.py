@@ -14,6 +14,13 @@ One JSON line on stdout (rank 0):
   roofline  the tensor-core kernel: algorithmic 18*L flops/pair over its
             event-timed duration, against the measured bf16 peak;
   plain64   the plain FP64 GPU path on the same workload (the denominator);
+  serving   a device-resident library of 200,000 decoys bucketed by chain
+            length (L 64/128/256/512 at 85/9/4/2%); queries arrive as a
+            Poisson process at 2,000 req/s, each q ~ U{1..512} structures of
+            a bucket drawn by library share, answered with the top-50
+            nearest by crmsd; 500-5,000-decoy clustering jobs are mixed in.
+            p50/p99 latency (submit -> results), pairs/s, and the capacity
+            of the mixed and plain FP64 servers (closed loop);
   batched   256 decoy sets (N log-uniform in [50, 4000], L log-uniform in
             [40, 800], sigma U[0.2, 6]) in one graph-replayed launch per
             step, against the plain FP64 path on the same sets, with per-set
@@ -57,6 +64,9 @@ def args_():
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--skip-accuracy", action="store_true")
     p.add_argument("--skip-batched", action="store_true")
+    p.add_argument("--skip-serving", action="store_true")
+    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     return p.parse_args()
 
@@ -261,6 +271,118 @@ def run_batched(a, eng, stream, torch):
                        "sets_with_distance_within_gap_of_eps": near_eps}}
 
 
+def _closed_loop(srv, pools, shares, seconds, rng, max_inflight=8):
+    """Back-to-back queries for `seconds`: the server's throughput ceiling."""
+    import collections
+    srv.reset_stats()
+    Ls = [L for L, _ in shares]
+    ps = np.array([p for _, p in shares])
+    q = collections.deque()
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        while len(q) < max_inflight:
+            L = int(rng.choice(Ls, p=ps / ps.sum()))
+            n = int(rng.integers(1, 513))
+            o = int(rng.integers(0, pools[L].shape[0] - n + 1))
+            q.append(srv.submit(pools[L][o:o + n]))
+        srv.wait(q.popleft())
+    while q:
+        srv.wait(q.popleft())
+    return srv.stats()
+
+
+def run_serving(a):
+    """Open-loop Poisson load against the resident library, then capacity."""
+    import queue as qmod
+    import threading
+    from bioshell_gb300 import CrmsdServer
+    lib, bases = synth.serving_library()
+    pools = synth.serving_queries(bases)
+    shares = list(synth.SERVING_BUCKETS)
+    rng = np.random.default_rng(6)
+    # clustering jobs mixed in: all-vs-all + OPTICS of 500-5000 decoys
+    cjobs = []
+    for k in range(4):
+        L = 64 if k % 2 == 0 else 128
+        n = int(rng.integers(500, 5001))
+        cjobs.append(synth.decoys(bases[L][k], n, rng, (0.3, 4.0)))
+    t0 = time.perf_counter()
+    srv = CrmsdServer(lib, top_k=50, max_inflight=4)
+    build_s = time.perf_counter() - t0
+    for L in pools:  # warm-up: first batches of every bucket, both extremes of q
+        for n in (1, 512):
+            srv.wait(srv.submit(pools[L][:n]))
+    srv.wait_cluster(srv.submit_cluster(cjobs[0][:500], 3.0, 5))
+    srv.reset_stats()
+    # open loop: Poisson arrivals at the offered rate
+    rate, T = a.serve_rate, a.serve_seconds
+    gaps = rng.exponential(1.0 / rate, size=int(rate * T * 1.5) + 10)
+    times = np.cumsum(gaps)
+    times = times[times < T]
+    Ls = np.array([L for L, _ in shares])
+    ps = np.array([p for _, p in shares])
+    bk = rng.choice(Ls, size=len(times), p=ps / ps.sum())
+    qs = rng.integers(1, 513, size=len(times))
+    offs = [int(rng.integers(0, pools[int(L)].shape[0] - int(n) + 1)) for L, n in zip(bk, qs)]
+    ctimes = np.linspace(0.1, T * 0.9, len(cjobs))
+    tickets = qmod.Queue()
+
+    def collect():
+        while True:
+            item = tickets.get()
+            if item is None:
+                return
+            kind, t = item
+            if kind == 0:
+                srv.wait(t)
+            else:
+                srv.wait_cluster(t)
+
+    th = threading.Thread(target=collect)
+    th.start()
+    lag = []
+    ci = 0
+    start = time.perf_counter()
+    for k, t_arr in enumerate(times):
+        while ci < len(cjobs) and ctimes[ci] <= t_arr:
+            tickets.put((1, srv.submit_cluster(cjobs[ci], 3.0, 5)))
+            ci += 1
+        now = time.perf_counter() - start
+        if t_arr > now:
+            time.sleep(t_arr - now)
+        lag.append((time.perf_counter() - start - t_arr) * 1e3)
+        L, n, o = int(bk[k]), int(qs[k]), offs[k]
+        tickets.put((0, srv.submit(pools[L][o:o + n])))
+    submit_s = time.perf_counter() - start
+    tickets.put(None)
+    th.join()
+    st = srv.stats()
+    offered = float(rate * sum(ps[list(Ls).index(L)] * lib[L].shape[0] for L in Ls) * 256.5)
+    open_loop = {"offered_req_per_s": rate, "seconds": T, "requests": int(len(times)),
+                 "cluster_jobs": len(cjobs), "offered_pairs_per_s": offered,
+                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "mean_ms": st["mean_ms"],
+                 "pairs_per_s": st["pairs_per_s"], "wall_s": st["seconds"], "batches": int(st["batches"]),
+                 "mean_batch_rows": st["mean_batch_rows"], "plain_fallbacks": int(st["plain_fallbacks"]),
+                 "cluster_p50_ms": st["cluster_p50_ms"], "cluster_p99_ms": st["cluster_p99_ms"],
+                 "submit_lag_p99_ms": float(np.percentile(lag, 99)) if lag else None, "submit_s": submit_s}
+    cap = _closed_loop(srv, pools, shares, 2.0, rng)
+    srv.close()
+    # the plain FP64 server on the same library and GPU (closed loop)
+    psrv = CrmsdServer(lib, top_k=50, max_inflight=2, precision="plain64")
+    psrv.wait(psrv.submit(pools[64][:4]))
+    pcap = _closed_loop(psrv, pools, shares, 2.0, rng, max_inflight=2)
+    psrv.close()
+    return {"library": {"structures": int(sum(x.shape[0] for x in lib.values())),
+                        "atoms": int(sum(x.shape[0] * x.shape[1] for x in lib.values())),
+                        "buckets": {str(L): int(lib[L].shape[0]) for L in lib}, "build_s": build_s},
+            "top_k": 50, "open_loop": open_loop,
+            "capacity": {"pairs_per_s": cap["pairs_per_s"], "p50_ms": cap["p50_ms"], "p99_ms": cap["p99_ms"],
+                         "queries": int(cap["queries_done"])},
+            "plain64_capacity": {"pairs_per_s": pcap["pairs_per_s"], "p50_ms": pcap["p50_ms"],
+                                 "p99_ms": pcap["p99_ms"], "queries": int(pcap["queries_done"])},
+            "speedup_vs_plain64": cap["pairs_per_s"] / max(pcap["pairs_per_s"], 1.0)}
+
+
 def run_reference(a, rank):
     if rank != 0:
         return
@@ -394,11 +516,17 @@ def run_ours(a, rank, world, local_rank):
             "issued_tflops": issued_flops(n, L) / (ms_main * 1e-3) / 1e12,
             "kernel_ms": ms_main, "traffic": traffic}
     cb = cpu_baseline(x, a.cpu_seconds) if rank == 0 else None
-    batched = None
-    if not a.skip_batched and rank == 0:
+    batched = serving = None
+    if rank == 0 and not (a.skip_batched and a.skip_serving):
         del outd
         torch.cuda.empty_cache()
+        eng.close()  # frees the 50k workspaces before the next sections
+        eng = Engine(local_rank)
+        stream = torch.cuda.ExternalStream(eng.stream_handle())
+    if not a.skip_batched and rank == 0:
         batched = run_batched(a, eng, stream, torch)
+    if not a.skip_serving and rank == 0:
+        serving = run_serving(a)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16", "data": "synthetic",
@@ -407,7 +535,8 @@ def run_ours(a, rank, world, local_rank):
                        "replicas": world},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
-            "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "batched": batched}
+            "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "batched": batched,
+            "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

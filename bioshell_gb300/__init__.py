@@ -7,6 +7,7 @@ host-side mirror of the Rust API and the synthetic-workload generator.
 from .crmsd import (CrmsdMatrix, CrmsdOptions, Engine, crmsd, crmsd_all_vs_all, crmsd_batched,  # noqa: F401
                     default_engine, tri_index)
 from .lib import CrmsdError  # noqa: F401
+from .serving import CrmsdServer  # noqa: F401
 
 __all__ = ["CrmsdMatrix", "CrmsdOptions", "Engine", "crmsd", "crmsd_all_vs_all", "crmsd_batched", "default_engine", "tri_index",
-           "CrmsdError"]
+           "CrmsdError", "CrmsdServer"]

@@ -88,8 +88,8 @@ struct Job {
   int err;                          // kErr* bits of this job
   float u;                          // Angstrom^2 per unit of quantised products (2^2e)
   float d34;                        // rounding bound of accumulator levels 2-3, as an error of E (units u)
-  int layout;                       // accumulator layout of the job's tiles (kLayout*)
-  int pad;
+  int layout;                       // accumulator layout of the job's tiles (kAcc*)
+  int allow_long;                   // (host) the long layout may be chosen
 };
 
 // Accumulator layouts of a tile.  Normal: the four levels, one 64-column
@@ -210,5 +210,12 @@ cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st);
 cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Job *job, DevScalars *sc,
                                const int64_t *ii, const int64_t *jj, int64_t np, double *out, float *levels_out,
                                cudaStream_t st);
+
+// topk.cu -- per row of a dense [rows][ld] f32 block: the k <= kTopkMax
+// smallest of the first n values, ascending by (value, column); columns
+// that do not exist come back as -1.
+constexpr int kTopkMax = 64;
+cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, int64_t *out_idx,
+                        float *out_val, cudaStream_t st);
 
 }  // namespace bs

@@ -32,6 +32,7 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
     jb.fixed_scale = 0;
     jb.scale_min = -1000;
     jb.tol = tol;
+    jb.allow_long = 1;
     const int64_t nb = blocks_for(s.n);
     for (int64_t b = 0; b < nb; ++b) plan.jobmap.push_back(j);
     blk += nb;

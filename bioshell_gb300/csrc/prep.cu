@@ -258,7 +258,7 @@ __global__ void k_mx_choose(PrepArgs p) {
   // grid with levels 0-1 exact and level 2 below 2^26, its rounding charged
   // to the budget.
   const int ncand = jb.fixed_scale ? 1 : 4;
-  const bool can_long = jb.mode == 0 && jb.lp / 16 >= 4;
+  const bool can_long = jb.mode == 0 && jb.allow_long && jb.lp / 16 >= 4;
   int pick = -1, relaxed = -1, pick_long = -1;
   double bb2[4], bb34[4];
   for (int a = 0; a < ncand; ++a) {

@@ -1,0 +1,969 @@
+// server.cu -- the serving loop (include/bioshell_crmsd.h, bs_server_*).
+//
+// Library: one bucket per chain length, prepared once on the device with the
+// mixed path's preparation (grid, digits, per-structure data) plus the plain
+// path's FP64 centred coordinates; the bucket's grid and digit norms are the
+// B side of every query job against it.
+//
+// Requests: a query is q structures of one bucket's length; its job is the
+// rectangular block q x n_bucket on the tensor cores (query digits on the
+// bucket's grid), written as a dense f32 block and reduced to the top_k
+// nearest per query structure (topk.cu).  A clustering job is an all-vs-all
+// of its own structures (f32 triangle) followed by OPTICS on a host worker.
+//
+// Scheduling (continuous batching): a scheduler thread polls the device
+// slots (one CUDA stream each).  When a slot is free it takes the oldest
+// queued request and, for a query, every other queued query of the same
+// bucket up to max_batch_rows structures, and launches them as one batch
+// (one preparation, one persistent tensor-core launch, one top-k launch).
+// A batch is admitted only when its device memory fits the budget left by
+// the other slots; batches in different slots run concurrently.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+
+namespace bs {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+constexpr unsigned long long kServerFlagCap = 1ull << 20;
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct Bucket {
+  int L = 0, lp = 0, pitch = 0;
+  int64_t n = 0, rows = 0;
+  int scale_exp = 0;
+  float norm_b[3] = {0, 0, 0};
+  float qres = 0.f;
+  DevBuf dig[4], info;  // mixed path
+  DevBuf y, g;          // plain path: centred f64 [n][3][lp], squared norms
+};
+
+struct Request {
+  int64_t id = 0;
+  int kind = 0;  // 0 query, 1 clustering job
+  int bucket = -1;
+  int L = 0;
+  int64_t q = 0;
+  std::vector<double> xyz;
+  double eps = 0.0;
+  int min_points = 0;
+  std::vector<int64_t> idx;
+  std::vector<double> val;
+  std::vector<int64_t> labels;
+  std::vector<float> tri;
+  bs_status status = BS_OK;
+  std::string err;
+  bool done = false;
+  Clock::time_point t_submit, t_done;
+  int64_t pairs = 0;
+};
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool busy = false;
+  int kind = 0, bucket = -1;
+  std::vector<Request *> reqs;
+  std::vector<int64_t> row0;  // first dense row of each query job
+  int64_t rows = 0;           // query structures in the batch
+  int njobs = 0;
+  // device
+  DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
+  // pinned host
+  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri;
+};
+
+}  // namespace
+}  // namespace bs
+
+struct bs_server {
+  int device = 0;
+  int num_sms = 0;
+  int top_k = 50;
+  int max_inflight = 4;
+  int64_t max_rows = 4096;
+  int precision = BS_PRECISION_MIXED;
+  float tol = 1e-4f;
+  size_t budget = 0, used = 0;  // in-flight device memory of the slots
+  std::vector<bs::Bucket> buckets;
+  std::vector<std::unique_ptr<bs::Slot>> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_clus;
+  std::deque<bs::Request *> queue, cluster_post;
+  std::map<int64_t, bs::Request *> reqs;
+  int64_t next_id = 1;
+  bool stop = false;
+  std::thread sched, clus;
+  PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  std::string err;
+  // stats
+  std::vector<double> lat, clat;
+  int64_t qdone = 0, cdone = 0, pairs = 0, batches = 0, fallbacks = 0, rows_batched = 0;
+  bs::Clock::time_point t0;
+};
+
+namespace bs {
+namespace {
+
+// ------------------------------------------------------------ memory
+bool sv_ensure(bs_server *s, DevBuf &b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.cap >= bytes) return true;
+  if (b.p) {
+    cudaFree(b.p);
+    s->used -= b.cap;
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  bytes = bytes + bytes / 4;  // headroom: batches vary in size
+  if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return false;
+  }
+  s->used += bytes;
+  b.cap = bytes;
+  return true;
+}
+
+void sv_release(bs_server *s, DevBuf &b) {
+  if (b.p) {
+    cudaFree(b.p);
+    s->used -= b.cap;
+  }
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+bool host_ensure(HostBuf &h, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (h.cap >= bytes) return true;
+  if (h.p) cudaFreeHost(h.p);
+  h.p = nullptr;
+  h.cap = 0;
+  bytes = bytes + bytes / 4;
+  if (cudaHostAlloc(&h.p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  h.cap = bytes;
+  return true;
+}
+
+void slot_release(bs_server *s, Slot &sl) {
+  DevBuf *list[] = {&sl.xyz,  &sl.ctr,   &sl.info,  &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3], &sl.jobs,
+                    &sl.jobmap, &sl.tiles, &sl.flags, &sl.scal,   &sl.dense,  &sl.topi,   &sl.topv,   &sl.y,
+                    &sl.g,    &sl.ctrd};
+  for (DevBuf *b : list) sv_release(s, *b);
+}
+
+size_t slot_bytes(Slot &sl) {
+  DevBuf *list[] = {&sl.xyz,  &sl.ctr,   &sl.info,  &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3], &sl.jobs,
+                    &sl.jobmap, &sl.tiles, &sl.flags, &sl.scal,   &sl.dense,  &sl.topi,   &sl.topv,   &sl.y,
+                    &sl.g,    &sl.ctrd};
+  size_t t = 0;
+  for (DevBuf *b : list) t += b->cap;
+  return t;
+}
+
+// Device bytes a batch needs (without the headroom of sv_ensure).
+size_t batch_bytes(const bs_server *s, const std::vector<Request *> &b) {
+  if (b.empty()) return 0;
+  const Request *r0 = b[0];
+  const int L = r0->L;
+  const int pitch = pitch_for(L), lp = lp_for(L);
+  int64_t blocks = 0, rows = 0, tiles = 0;
+  size_t xyz = 0;
+  for (const Request *r : b) {
+    blocks += blocks_for(r->q);
+    rows += r->q;
+    xyz += (size_t)r->q * L * 24;
+  }
+  size_t t = xyz + (size_t)blocks * kBlockStructs * (24 + 16) + (size_t)blocks * kBlockRows * pitch * 2 * 4 +
+             b.size() * sizeof(Job) + (size_t)blocks * 4 + sizeof(DevScalars);
+  if (r0->kind == 0) {
+    const int64_t nb = s->buckets[r0->bucket].n;
+    for (const Request *r : b) tiles += blocks_for(r->q) * ((nb + kBStructs - 1) / kBStructs);
+    t += (size_t)tiles * sizeof(Tile) + kServerFlagCap * 8 + (size_t)rows * nb * 4 + (size_t)rows * s->top_k * 12;
+    if (s->precision == BS_PRECISION_PLAIN64) t += (size_t)rows * (3 * lp * 8 + 8 + 24);
+  } else {
+    const int64_t n = r0->q, nba = blocks_for(n), nbb = (n + kBStructs - 1) / kBStructs;
+    for (int64_t i = 0; i < nba; ++i) tiles += std::max<int64_t>(0, nbb - 2 * i);
+    t += (size_t)tiles * sizeof(Tile) + kServerFlagCap * 8 + (size_t)(n * (n - 1) / 2) * 4;
+  }
+  return t;
+}
+
+// ------------------------------------------------------------ library
+bs_status build_bucket(bs_server *s, Bucket &bk, const double *xyz_in) {
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return BS_ERR_CUDA;
+  bs_status status = BS_OK;
+  DevBuf xyz, ctr, jobs, jobmap, scal, ctrd;
+  auto fail = [&](bs_status e, const char *what) {
+    status = e;
+    s->err = what;
+  };
+  const size_t bytes = (size_t)bk.n * bk.L * 3 * sizeof(double);
+  do {
+    const double *dxyz = xyz_in;
+    if (!is_device_ptr(xyz_in)) {
+      if (cudaMalloc(&xyz.p, bytes) != cudaSuccess ||
+          cudaMemcpyAsync(xyz.p, xyz_in, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        fail(BS_ERR_OOM, "library coordinates");
+        break;
+      }
+      dxyz = static_cast<const double *>(xyz.p);
+    }
+    std::vector<JobSpec> specs{JobSpec{dxyz, bk.n, bk.L, OutDesc{nullptr, bk.n, bk.n, kLayoutTriangle, 1}}};
+    Plan plan;
+    const std::string m = make_symmetric_plan(specs, s->tol, false, plan);
+    if (!m.empty()) {
+      fail(BS_ERR_UNSUPPORTED, "library bucket shape unsupported");
+      break;
+    }
+    plan.jobs[0].allow_long = 0;  // query tiles against the library use the normal layout
+    bk.pitch = plan.pitch;
+    bk.lp = lp_for(bk.L);
+    bk.rows = plan.nblocks * kBlockRows;
+    const int64_t ns = plan.nblocks * kBlockStructs;
+    bool ok = cudaMalloc(&ctr.p, (size_t)ns * 24) == cudaSuccess && cudaMalloc(&bk.info.p, (size_t)ns * 16) == cudaSuccess &&
+              cudaMalloc(&jobs.p, sizeof(Job)) == cudaSuccess && cudaMalloc(&jobmap.p, plan.nblocks * 4) == cudaSuccess &&
+              cudaMalloc(&scal.p, sizeof(DevScalars)) == cudaSuccess;
+    for (int d = 0; d < 4 && ok; ++d)
+      ok = cudaMalloc(&bk.dig[d].p, (size_t)bk.rows * bk.pitch * 2) == cudaSuccess;
+    ok = ok && cudaMalloc(&bk.y.p, (size_t)bk.n * 3 * bk.lp * 8) == cudaSuccess &&
+         cudaMalloc(&bk.g.p, (size_t)bk.n * 8) == cudaSuccess && cudaMalloc(&ctrd.p, (size_t)bk.n * 24) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      fail(BS_ERR_OOM, "library device memory");
+      break;
+    }
+    MixedBuffers b{};
+    b.ctr = static_cast<long long *>(ctr.p);
+    b.info_a = static_cast<SInfo *>(bk.info.p);
+    b.info_b = b.info_a;
+    for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(bk.dig[d].p);
+    for (int d = 0; d < 3; ++d) b.dig_b[d] = b.dig_a[d];
+    b.pitch_a = b.pitch_b = bk.pitch;
+    b.rows_a = b.rows_b = bk.rows;
+    b.jobs = static_cast<Job *>(jobs.p);
+    b.jobmap = static_cast<int *>(jobmap.p);
+    b.sc = static_cast<DevScalars *>(scal.p);
+    Job job = plan.jobs[0], back{};
+    DevScalars sc{};
+    CUtensorMap tm[7];  // no tiles: unused
+    if (cudaMemcpyAsync(b.jobmap, plan.jobmap.data(), plan.jobmap.size() * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        enqueue_mixed(plan, b, &job, tm, s->num_sms, st, nullptr, false) != cudaSuccess ||
+        launch_prep_plain(dxyz, bk.n, bk.L, bk.lp, static_cast<double *>(ctrd.p), static_cast<double *>(bk.y.p),
+                          static_cast<double *>(bk.g.p), &b.sc->err, st) != cudaSuccess ||
+        cudaMemcpyAsync(&back, b.jobs, sizeof(Job), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&sc, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      fail(BS_ERR_CUDA, "library preparation");
+      break;
+    }
+    std::string msg;
+    const bs_status e = collect_errors(sc, &back, 1, msg);
+    if (e) {
+      status = e;
+      s->err = "library: " + msg;
+      break;
+    }
+    bk.scale_exp = back.scale_exp;
+    const int pick = back.scale_exp - back.scale_base;
+    for (int d = 0; d < 3; ++d) bk.norm_b[d] = (float)(sqrt((double)back.norm[pick][d]) * (1.0 + 1e-6));
+    memcpy(&bk.qres, &back.qres_max_bits, 4);
+  } while (false);
+  for (DevBuf *d : {&xyz, &ctr, &jobs, &jobmap, &scal, &ctrd})
+    if (d->p) cudaFree(d->p);
+  cudaStreamDestroy(st);
+  return status;
+}
+
+// ------------------------------------------------------------ batches
+bs_status launch_query_batch(bs_server *s, Slot &sl) {
+  const Bucket &bk = s->buckets[sl.bucket];
+  const int L = bk.L, k = s->top_k;
+  const int nj = (int)sl.reqs.size();
+  // host plan: one rectangular job per request
+  Plan plan;
+  plan.pitch = bk.pitch;
+  sl.row0.assign(nj, 0);
+  int64_t blk = 0, rows = 0;
+  size_t xyz_off = 0;
+  std::vector<size_t> xoff(nj);
+  for (int j = 0; j < nj; ++j) {
+    const Request *r = sl.reqs[j];
+    sl.row0[j] = rows;
+    xoff[j] = xyz_off;
+    xyz_off += (size_t)r->q * L * 3;
+    const int64_t nb = blocks_for(r->q);
+    for (int64_t b = 0; b < nb; ++b) plan.jobmap.push_back(j);
+    Job jb{};
+    jb.n = r->q;
+    jb.first_a = blk * kBlockStructs;
+    jb.first_b = 0;
+    jb.n_b = bk.n;
+    jb.L = L;
+    jb.lp = bk.lp;
+    jb.mode = 1;
+    jb.fixed_scale = 1;
+    jb.scale_min = bk.scale_exp;
+    jb.tol = s->tol;
+    for (int d = 0; d < 3; ++d) jb.norm_b[d] = bk.norm_b[d];
+    jb.qres_b = bk.qres;
+    plan.jobs.push_back(jb);
+    const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
+    for (int64_t I = 0; I < nb; ++I)
+      for (int64_t J = 0; J < nbb; ++J) plan.tiles.push_back(Tile{(int)(blk + I), (int)J, j, 0});
+    blk += nb;
+    rows += r->q;
+  }
+  plan.nblocks = blk;
+  sl.rows = rows;
+  sl.njobs = nj;
+  const int64_t ns = blk * kBlockStructs, drows = blk * kBlockRows;
+  const bool plain = s->precision == BS_PRECISION_PLAIN64;
+  bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * bk.n * 4) &&
+            sv_ensure(s, sl.topi, (size_t)rows * k * 8) && sv_ensure(s, sl.topv, (size_t)rows * k * 4) &&
+            sv_ensure(s, sl.scal, sizeof(DevScalars)) && host_ensure(sl.hxyz, xyz_off * 8) &&
+            host_ensure(sl.htopi, (size_t)rows * k * 8) && host_ensure(sl.htopv, (size_t)rows * k * 4) &&
+            host_ensure(sl.hsc, sizeof(DevScalars));
+  if (plain) {
+    ok = ok && sv_ensure(s, sl.y, (size_t)rows * 3 * bk.lp * 8) && sv_ensure(s, sl.g, (size_t)rows * 8) &&
+         sv_ensure(s, sl.ctrd, (size_t)rows * 24);
+  } else {
+    ok = ok && sv_ensure(s, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl.info, (size_t)ns * 16) &&
+         sv_ensure(s, sl.jobs, (size_t)nj * sizeof(Job)) && sv_ensure(s, sl.jobmap, plan.jobmap.size() * 4) &&
+         sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl.flags, kServerFlagCap * 8) &&
+         host_ensure(sl.hjobs, (size_t)nj * sizeof(Job)) && host_ensure(sl.hback, (size_t)nj * sizeof(Job)) &&
+         host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile));
+    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * bk.pitch * 2);
+  }
+  if (!ok) return BS_ERR_OOM;
+  // coordinates in
+  double *hx = static_cast<double *>(sl.hxyz.p);
+  for (int j = 0; j < nj; ++j) memcpy(hx + xoff[j], sl.reqs[j]->xyz.data(), sl.reqs[j]->xyz.size() * 8);
+  double *dx = static_cast<double *>(sl.xyz.p);
+  if (cudaMemcpyAsync(dx, hx, xyz_off * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess) return BS_ERR_CUDA;
+  float *dense = static_cast<float *>(sl.dense.p);
+  if (plain) {
+    if (cudaMemsetAsync(sl.scal.p, 0, sizeof(DevScalars), sl.st) != cudaSuccess) return BS_ERR_CUDA;
+    for (int j = 0; j < nj; ++j) {
+      const Request *r = sl.reqs[j];
+      OutDesc od{dense + sl.row0[j] * bk.n, r->q, bk.n, kLayoutRect, 1};
+      if (launch_prep_plain(dx + xoff[j], r->q, L, bk.lp, static_cast<double *>(sl.ctrd.p),
+                            static_cast<double *>(sl.y.p), static_cast<double *>(sl.g.p),
+                            &static_cast<DevScalars *>(sl.scal.p)->err, sl.st) != cudaSuccess ||
+          launch_plain64_rect(static_cast<const double *>(sl.y.p), static_cast<const double *>(sl.g.p), r->q,
+                              static_cast<const double *>(bk.y.p), static_cast<const double *>(bk.g.p), bk.n, L,
+                              bk.lp, od, sl.st) != cudaSuccess)
+        return BS_ERR_CUDA;
+    }
+  } else {
+    for (int j = 0; j < nj; ++j) plan.jobs[j].xyz = dx + xoff[j];
+    for (int j = 0; j < nj; ++j) plan.jobs[j].out = OutDesc{dense + sl.row0[j] * bk.n, sl.reqs[j]->q, bk.n, kLayoutRect, 1};
+    memcpy(sl.hjobs.p, plan.jobs.data(), (size_t)nj * sizeof(Job));
+    char *ht = static_cast<char *>(sl.htab.p);
+    memcpy(ht, plan.jobmap.data(), plan.jobmap.size() * 4);
+    memcpy(ht + plan.jobmap.size() * 4, plan.tiles.data(), plan.tiles.size() * sizeof(Tile));
+    MixedBuffers b{};
+    b.ctr = static_cast<long long *>(sl.ctr.p);
+    b.info_a = static_cast<SInfo *>(sl.info.p);
+    b.info_b = static_cast<const SInfo *>(bk.info.p);
+    for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(sl.dig[d].p);
+    for (int d = 0; d < 3; ++d) b.dig_b[d] = static_cast<const __nv_bfloat16 *>(bk.dig[d].p);
+    b.pitch_a = bk.pitch;
+    b.pitch_b = bk.pitch;
+    b.rows_a = drows;
+    b.rows_b = bk.rows;
+    b.jobs = static_cast<Job *>(sl.jobs.p);
+    b.jobmap = static_cast<int *>(sl.jobmap.p);
+    b.tiles = static_cast<Tile *>(sl.tiles.p);
+    b.flags = static_cast<unsigned long long *>(sl.flags.p);
+    b.flag_cap = kServerFlagCap;
+    b.sc = static_cast<DevScalars *>(sl.scal.p);
+    CUtensorMap tm[7];
+    if (!encode_maps(s->encode, b, tm).empty()) return BS_ERR_CUDA;
+    if (cudaMemcpyAsync(b.jobmap, ht, plan.jobmap.size() * 4, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+        cudaMemcpyAsync(b.tiles, ht + plan.jobmap.size() * 4, plan.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice,
+                        sl.st) != cudaSuccess ||
+        enqueue_mixed(plan, b, static_cast<const Job *>(sl.hjobs.p), tm, s->num_sms, sl.st, nullptr, false) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(sl.hback.p, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess)
+      return BS_ERR_CUDA;
+  }
+  if (launch_topk(dense, rows, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p), static_cast<float *>(sl.topv.p),
+                  sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.htopi.p, sl.topi.p, (size_t)rows * k * 8, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.htopv.p, sl.topv.p, (size_t)rows * k * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hsc.p, sl.scal.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaEventRecord(sl.ev, sl.st) != cudaSuccess)
+    return BS_ERR_CUDA;
+  return BS_OK;
+}
+
+// A query outside its bucket's grid: the plain FP64 path, synchronously on
+// the slot's stream, into the slot's dense rows of that job.
+bs_status plain_fallback(bs_server *s, Slot &sl, int j) {
+  const Bucket &bk = s->buckets[sl.bucket];
+  const Request *r = sl.reqs[j];
+  const int k = s->top_k;
+  if (!sv_ensure(s, sl.y, (size_t)r->q * 3 * bk.lp * 8) || !sv_ensure(s, sl.g, (size_t)r->q * 8) ||
+      !sv_ensure(s, sl.ctrd, (size_t)r->q * 24) || !sv_ensure(s, sl.xyz, r->xyz.size() * 8))
+    return BS_ERR_OOM;
+  float *dense = static_cast<float *>(sl.dense.p) + sl.row0[j] * bk.n;
+  OutDesc od{dense, r->q, bk.n, kLayoutRect, 1};
+  DevScalars *sc = static_cast<DevScalars *>(sl.scal.p);
+  if (cudaMemsetAsync(sc, 0, sizeof(DevScalars), sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.xyz.p, r->xyz.data(), r->xyz.size() * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+      launch_prep_plain(static_cast<const double *>(sl.xyz.p), r->q, bk.L, bk.lp, static_cast<double *>(sl.ctrd.p),
+                        static_cast<double *>(sl.y.p), static_cast<double *>(sl.g.p), &sc->err, sl.st) != cudaSuccess ||
+      launch_plain64_rect(static_cast<const double *>(sl.y.p), static_cast<const double *>(sl.g.p), r->q,
+                          static_cast<const double *>(bk.y.p), static_cast<const double *>(bk.g.p), bk.n, bk.L, bk.lp,
+                          od, sl.st) != cudaSuccess ||
+      launch_topk(dense, r->q, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p) + sl.row0[j] * k,
+                  static_cast<float *>(sl.topv.p) + sl.row0[j] * k, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(static_cast<int64_t *>(sl.htopi.p) + sl.row0[j] * k,
+                      static_cast<int64_t *>(sl.topi.p) + sl.row0[j] * k, (size_t)r->q * k * 8, cudaMemcpyDeviceToHost,
+                      sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(static_cast<float *>(sl.htopv.p) + sl.row0[j] * k,
+                      static_cast<float *>(sl.topv.p) + sl.row0[j] * k, (size_t)r->q * k * 4, cudaMemcpyDeviceToHost,
+                      sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hsc.p, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaStreamSynchronize(sl.st) != cudaSuccess)
+    return BS_ERR_CUDA;
+  if (static_cast<DevScalars *>(sl.hsc.p)->err & kErrNonFinite) return BS_ERR_NONFINITE;
+  return BS_OK;
+}
+
+bs_status launch_cluster_batch(bs_server *s, Slot &sl) {
+  Request *r = sl.reqs[0];
+  const int64_t n = r->q;
+  const size_t tri = (size_t)(n * (n - 1) / 2);
+  if (!sv_ensure(s, sl.xyz, r->xyz.size() * 8) || !sv_ensure(s, sl.dense, tri * 4) ||
+      !host_ensure(sl.htri, tri * 4) || !host_ensure(sl.hxyz, r->xyz.size() * 8) ||
+      !sv_ensure(s, sl.scal, sizeof(DevScalars)) || !host_ensure(sl.hsc, sizeof(DevScalars)))
+    return BS_ERR_OOM;
+  memcpy(sl.hxyz.p, r->xyz.data(), r->xyz.size() * 8);
+  if (cudaMemcpyAsync(sl.xyz.p, sl.hxyz.p, r->xyz.size() * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess)
+    return BS_ERR_CUDA;
+  std::vector<JobSpec> specs{JobSpec{static_cast<const double *>(sl.xyz.p), n, r->L,
+                                     OutDesc{sl.dense.p, n, n, kLayoutTriangle, 1}}};
+  if (s->precision == BS_PRECISION_PLAIN64) {
+    const int lp = lp_for(r->L);
+    if (!sv_ensure(s, sl.y, (size_t)n * 3 * lp * 8) || !sv_ensure(s, sl.g, (size_t)n * 8) ||
+        !sv_ensure(s, sl.ctrd, (size_t)n * 24))
+      return BS_ERR_OOM;
+    DevScalars *sc = static_cast<DevScalars *>(sl.scal.p);
+    if (cudaMemsetAsync(sc, 0, sizeof(DevScalars), sl.st) != cudaSuccess ||
+        launch_prep_plain(specs[0].xyz, n, r->L, lp, static_cast<double *>(sl.ctrd.p), static_cast<double *>(sl.y.p),
+                          static_cast<double *>(sl.g.p), &sc->err, sl.st) != cudaSuccess ||
+        launch_plain64_all(static_cast<const double *>(sl.y.p), static_cast<const double *>(sl.g.p), n, r->L, lp,
+                           specs[0].out, sl.st) != cudaSuccess)
+      return BS_ERR_CUDA;
+    sl.njobs = 0;
+  } else {
+    Plan plan;
+    if (!make_symmetric_plan(specs, s->tol, true, plan).empty()) return BS_ERR_UNSUPPORTED;
+    const int64_t ns = plan.nblocks * kBlockStructs, drows = plan.nblocks * kBlockRows;
+    bool ok = sv_ensure(s, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl.info, (size_t)ns * 16) &&
+              sv_ensure(s, sl.jobs, sizeof(Job)) && sv_ensure(s, sl.jobmap, plan.jobmap.size() * 4) &&
+              sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl.flags, kServerFlagCap * 8) &&
+              host_ensure(sl.hjobs, sizeof(Job)) && host_ensure(sl.hback, sizeof(Job)) &&
+              host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile));
+    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * plan.pitch * 2);
+    if (!ok) return BS_ERR_OOM;
+    MixedBuffers b{};
+    b.ctr = static_cast<long long *>(sl.ctr.p);
+    b.info_a = static_cast<SInfo *>(sl.info.p);
+    b.info_b = b.info_a;
+    for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(sl.dig[d].p);
+    for (int d = 0; d < 3; ++d) b.dig_b[d] = b.dig_a[d];
+    b.pitch_a = b.pitch_b = plan.pitch;
+    b.rows_a = b.rows_b = drows;
+    b.jobs = static_cast<Job *>(sl.jobs.p);
+    b.jobmap = static_cast<int *>(sl.jobmap.p);
+    b.tiles = static_cast<Tile *>(sl.tiles.p);
+    b.flags = static_cast<unsigned long long *>(sl.flags.p);
+    b.flag_cap = kServerFlagCap;
+    b.sc = static_cast<DevScalars *>(sl.scal.p);
+    memcpy(sl.hjobs.p, plan.jobs.data(), sizeof(Job));
+    char *ht = static_cast<char *>(sl.htab.p);
+    memcpy(ht, plan.jobmap.data(), plan.jobmap.size() * 4);
+    memcpy(ht + plan.jobmap.size() * 4, plan.tiles.data(), plan.tiles.size() * sizeof(Tile));
+    CUtensorMap tm[7];
+    if (!encode_maps(s->encode, b, tm).empty()) return BS_ERR_CUDA;
+    if (cudaMemcpyAsync(b.jobmap, ht, plan.jobmap.size() * 4, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+        cudaMemcpyAsync(b.tiles, ht + plan.jobmap.size() * 4, plan.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice,
+                        sl.st) != cudaSuccess ||
+        enqueue_mixed(plan, b, static_cast<const Job *>(sl.hjobs.p), tm, s->num_sms, sl.st, nullptr, false) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(sl.hback.p, b.jobs, sizeof(Job), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess)
+      return BS_ERR_CUDA;
+    sl.njobs = 1;
+  }
+  if (cudaMemcpyAsync(sl.htri.p, sl.dense.p, tri * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hsc.p, sl.scal.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaEventRecord(sl.ev, sl.st) != cudaSuccess)
+    return BS_ERR_CUDA;
+  return BS_OK;
+}
+
+void complete(bs_server *s, Request *r, bs_status st, const std::string &msg) {
+  r->status = st;
+  r->err = msg;
+  r->t_done = Clock::now();
+  r->done = true;
+  const double ms = ms_between(r->t_submit, r->t_done);
+  if (st == BS_OK) {
+    if (r->kind == 0) {
+      s->lat.push_back(ms);
+      ++s->qdone;
+    } else {
+      s->clat.push_back(ms);
+      ++s->cdone;
+    }
+    s->pairs += r->pairs;
+  }
+  s->cv_done.notify_all();
+}
+
+// After the slot's event: results to the requests (lock held; released
+// while a clustering job's triangle is copied out of the slot).
+void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
+  const DevScalars &sc = *static_cast<const DevScalars *>(sl.hsc.p);
+  if (sl.kind == 1) {
+    Request *r = sl.reqs[0];
+    std::string msg;
+    bs_status st = BS_OK;
+    if (sl.njobs == 1) st = collect_errors(sc, static_cast<const Job *>(sl.hback.p), 1, msg);
+    else if (sc.err & kErrNonFinite) st = BS_ERR_NONFINITE, msg = "input coordinates contain NaN or Inf";
+    if (st) {
+      complete(s, r, st, msg);
+    } else {
+      const size_t tri = (size_t)(r->q * (r->q - 1) / 2);
+      lk.unlock();  // the slot stays busy until the copy is done
+      r->tri.assign(static_cast<const float *>(sl.htri.p), static_cast<const float *>(sl.htri.p) + tri);
+      lk.lock();
+      s->cluster_post.push_back(r);
+      s->cv_clus.notify_one();
+    }
+  } else {
+    const Bucket &bk = s->buckets[sl.bucket];
+    const int k = s->top_k;
+    const Job *back = static_cast<const Job *>(sl.hback.p);
+    for (int j = 0; j < (int)sl.reqs.size(); ++j) {
+      Request *r = sl.reqs[j];
+      bs_status st = BS_OK;
+      std::string msg;
+      if (s->precision == BS_PRECISION_MIXED) {
+        st = collect_errors(sc, back + j, 1, msg);
+        if (st == BS_ERR_UNSUPPORTED) {  // outside the bucket's grid: plain FP64 path
+          st = plain_fallback(s, sl, j);
+          if (st == BS_OK) ++s->fallbacks;
+          else msg = "plain fallback failed";
+        }
+      } else if (sc.err & kErrNonFinite) {
+        st = BS_ERR_NONFINITE;
+        msg = "input coordinates contain NaN or Inf";
+      }
+      if (st == BS_OK) {
+        const int64_t *hi = static_cast<const int64_t *>(sl.htopi.p) + sl.row0[j] * k;
+        const float *hv = static_cast<const float *>(sl.htopv.p) + sl.row0[j] * k;
+        r->idx.assign(hi, hi + r->q * k);
+        r->val.resize(r->q * k);
+        for (int64_t t = 0; t < r->q * k; ++t) r->val[t] = (double)hv[t];
+        r->pairs = r->q * bk.n;
+      }
+      complete(s, r, st, msg);
+    }
+  }
+  sl.reqs.clear();
+  sl.busy = false;
+}
+
+void cluster_loop(bs_server *s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (true) {
+    s->cv_clus.wait(lk, [&] { return s->stop || !s->cluster_post.empty(); });
+    if (s->cluster_post.empty()) {
+      if (s->stop) break;
+      continue;
+    }
+    Request *r = s->cluster_post.front();
+    s->cluster_post.pop_front();
+    lk.unlock();
+    std::vector<int64_t> order(r->q), cl(r->q);
+    std::vector<double> reach(r->q);
+    const bs_status st = bs_optics(r->tri.data(), r->q, BS_OUT_F32, r->eps, r->min_points, order.data(), reach.data(),
+                                   cl.data());
+    r->tri.clear();
+    r->tri.shrink_to_fit();
+    lk.lock();
+    r->labels = std::move(cl);
+    r->pairs = r->q * (r->q - 1) / 2;
+    complete(s, r, st, st ? "OPTICS failed" : "");
+  }
+}
+
+void fail_batch(bs_server *s, Slot &sl, bs_status st, const std::string &msg) {
+  for (Request *r : sl.reqs) complete(s, r, st, msg);
+  sl.reqs.clear();
+  sl.busy = false;
+}
+
+void sched_loop(bs_server *s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (true) {
+    bool progress = false, inflight = false;
+    for (auto &up : s->slots) {
+      Slot &sl = *up;
+      if (!sl.busy) continue;
+      const cudaError_t q = cudaEventQuery(sl.ev);
+      if (q == cudaSuccess) {
+        finish_slot(s, sl, lk);
+        progress = true;
+      } else if (q == cudaErrorNotReady) {
+        inflight = true;
+      } else {
+        cudaGetLastError();
+        fail_batch(s, sl, BS_ERR_CUDA, cudaGetErrorString(q));
+        progress = true;
+      }
+    }
+    for (auto &up : s->slots) {
+      Slot &sl = *up;
+      if (sl.busy || s->queue.empty()) continue;
+      // form a batch: the oldest request, plus same-bucket queries behind it
+      std::vector<Request *> batch{s->queue.front()};
+      const Request *r0 = batch[0];
+      int64_t rows = r0->q;
+      if (r0->kind == 0) {
+        for (size_t i = 1; i < s->queue.size(); ++i) {
+          Request *r = s->queue[i];
+          if (r->kind != 0 || r->bucket != r0->bucket || rows + r->q > s->max_rows) continue;
+          batch.push_back(r);
+          rows += r->q;
+        }
+      }
+      // admission by device memory: shrink the batch until it fits the
+      // budget left by the other slots (idle slots give theirs back first)
+      size_t need = batch_bytes(s, batch);
+      if (s->used - slot_bytes(sl) + need * 5 / 4 > s->budget) {
+        for (auto &o : s->slots)
+          if (!o->busy && o.get() != &sl) slot_release(s, *o);
+      }
+      while (batch.size() > 1 && s->used - slot_bytes(sl) + need * 5 / 4 > s->budget) {
+        batch.pop_back();
+        need = batch_bytes(s, batch);
+      }
+      if (s->used - slot_bytes(sl) + need * 5 / 4 > s->budget) {
+        bool others = false;
+        for (auto &o : s->slots) others |= o->busy;
+        if (others) break;  // wait for memory to free up
+        Request *r = s->queue.front();
+        s->queue.pop_front();
+        complete(s, r, BS_ERR_BUDGET, "request larger than the server's device memory budget");
+        progress = true;
+        continue;
+      }
+      for (Request *r : batch) s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
+      sl.busy = true;
+      sl.reqs = batch;
+      sl.kind = r0->kind;
+      sl.bucket = r0->bucket;
+      ++s->batches;
+      if (r0->kind == 0) s->rows_batched += rows;
+      // release the unused part of this slot's buffers before growing others
+      const bs_status st = r0->kind == 0 ? launch_query_batch(s, sl) : launch_cluster_batch(s, sl);
+      if (st) {
+        cudaGetLastError();
+        cudaStreamSynchronize(sl.st);
+        fail_batch(s, sl, st, st == BS_ERR_OOM ? "device memory" : "batch launch failed");
+      }
+      progress = true;
+      inflight = true;
+    }
+    if (s->stop && s->queue.empty()) {
+      bool busy = false;
+      for (auto &up : s->slots) busy |= up->busy;
+      if (!busy) break;
+    }
+    if (!progress) {
+      if (inflight) {
+        lk.unlock();
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+        lk.lock();
+      } else {
+        s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+      }
+    }
+  }
+}
+
+double percentile(std::vector<double> v, double p) {
+  if (v.empty()) return 0.0;
+  const size_t k = std::min(v.size() - 1, (size_t)std::floor(p * (double)(v.size() - 1) + 0.5));
+  std::nth_element(v.begin(), v.begin() + k, v.end());
+  return v[k];
+}
+
+}  // namespace
+}  // namespace bs
+
+using namespace bs;
+
+extern "C" {
+
+BS_API const char *bs_server_last_error(const bs_server *s) { return s ? s->err.c_str() : "null server"; }
+
+BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_server_config *cfg) {
+  if (!out || !cfg) return BS_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (cfg->nbuckets < 1 || !cfg->bucket_L || !cfg->bucket_n || !cfg->bucket_xyz) return BS_ERR_INVALID_ARG;
+  if (cfg->top_k < 1 || cfg->top_k > kTopkMax) return BS_ERR_INVALID_ARG;
+  if (cfg->precision != BS_PRECISION_MIXED && cfg->precision != BS_PRECISION_PLAIN64) return BS_ERR_INVALID_ARG;
+  for (int b = 0; b < cfg->nbuckets; ++b) {
+    if (cfg->bucket_L[b] < 1 || cfg->bucket_n[b] < 1 || !cfg->bucket_xyz[b]) return BS_ERR_INVALID_ARG;
+    for (int c = 0; c < b; ++c)
+      if (cfg->bucket_L[c] == cfg->bucket_L[b]) return BS_ERR_INVALID_ARG;  // one bucket per length
+    if (cfg->bucket_n[b] >= kMaxGlobalStructs) return BS_ERR_UNSUPPORTED;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    return BS_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return BS_ERR_INVALID_ARG;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || !(prop.major == 10 && prop.minor == 3))
+    return BS_ERR_NO_DEVICE;
+  bs_server *s = new (std::nothrow) bs_server();
+  if (!s) return BS_ERR_OOM;
+  s->device = device;
+  s->num_sms = prop.multiProcessorCount;
+  s->top_k = cfg->top_k;
+  s->max_inflight = cfg->max_inflight > 0 ? cfg->max_inflight : 4;
+  s->max_rows = cfg->max_batch_rows > 0 ? cfg->max_batch_rows : 4096;
+  s->precision = cfg->precision;
+  s->tol = (float)(cfg->tolerance > 0 ? cfg->tolerance : 1e-4);
+  cudaSetDevice(device);
+  if (mixed_tc_prepare() != cudaSuccess || prep_prepare() != cudaSuccess || !get_encoder(&s->encode).empty()) {
+    delete s;
+    return BS_ERR_CUDA;
+  }
+  s->buckets.resize(cfg->nbuckets);
+  for (int b = 0; b < cfg->nbuckets; ++b) {
+    s->buckets[b].L = cfg->bucket_L[b];
+    s->buckets[b].n = cfg->bucket_n[b];
+    const bs_status st = build_bucket(s, s->buckets[b], cfg->bucket_xyz[b]);
+    if (st) {
+      const std::string e = s->err;
+      bs_server_destroy(s);
+      return st;
+    }
+  }
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  s->budget = cfg->hbm_budget ? cfg->hbm_budget : free_b / 2;
+  for (int i = 0; i < s->max_inflight; ++i) {
+    auto sl = std::make_unique<Slot>();
+    if (cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming) != cudaSuccess) {
+      bs_server_destroy(s);
+      return BS_ERR_CUDA;
+    }
+    s->slots.push_back(std::move(sl));
+  }
+  s->t0 = Clock::now();
+  s->sched = std::thread(sched_loop, s);
+  s->clus = std::thread(cluster_loop, s);
+  *out = s;
+  return BS_OK;
+}
+
+BS_API void bs_server_destroy(bs_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  s->cv_clus.notify_all();
+  if (s->sched.joinable()) s->sched.join();
+  if (s->clus.joinable()) s->clus.join();
+  cudaSetDevice(s->device);
+  for (auto &up : s->slots) {
+    Slot &sl = *up;
+    if (sl.st) cudaStreamSynchronize(sl.st);
+    slot_release(s, sl);
+    for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri})
+      if (h->p) cudaFreeHost(h->p);
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.st) cudaStreamDestroy(sl.st);
+  }
+  for (Bucket &bk : s->buckets)
+    for (DevBuf *d : {&bk.dig[0], &bk.dig[1], &bk.dig[2], &bk.dig[3], &bk.info, &bk.y, &bk.g})
+      if (d->p) cudaFree(d->p);
+  for (auto &kv : s->reqs) delete kv.second;
+  delete s;
+}
+
+static bs_status submit_common(bs_server *s, Request *r, int64_t *ticket) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) {
+    delete r;
+    return BS_ERR_INVALID_ARG;
+  }
+  r->id = s->next_id++;
+  r->t_submit = Clock::now();
+  s->reqs[r->id] = r;
+  s->queue.push_back(r);
+  *ticket = r->id;
+  s->cv_work.notify_one();
+  return BS_OK;
+}
+
+BS_API bs_status bs_server_submit(bs_server *s, const double *xyz, int32_t q, int32_t L, int64_t *ticket) {
+  if (!s || !xyz || !ticket || q < 1) return BS_ERR_INVALID_ARG;
+  int bucket = -1;
+  for (int b = 0; b < (int)s->buckets.size(); ++b)
+    if (s->buckets[b].L == L) bucket = b;
+  if (bucket < 0) return BS_ERR_INVALID_ARG;
+  Request *r = new (std::nothrow) Request();
+  if (!r) return BS_ERR_OOM;
+  r->kind = 0;
+  r->bucket = bucket;
+  r->L = L;
+  r->q = q;
+  r->xyz.assign(xyz, xyz + (size_t)q * L * 3);
+  return submit_common(s, r, ticket);
+}
+
+BS_API bs_status bs_server_submit_cluster(bs_server *s, const double *xyz, int64_t n, int32_t L, double eps,
+                                          int32_t min_points, int64_t *ticket) {
+  if (!s || !xyz || !ticket || n < 2 || L < 1 || !(eps > 0) || min_points < 1) return BS_ERR_INVALID_ARG;
+  Request *r = new (std::nothrow) Request();
+  if (!r) return BS_ERR_OOM;
+  r->kind = 1;
+  r->L = L;
+  r->q = n;
+  r->eps = eps;
+  r->min_points = min_points;
+  r->xyz.assign(xyz, xyz + (size_t)n * L * 3);
+  return submit_common(s, r, ticket);
+}
+
+BS_API bs_status bs_server_poll(bs_server *s, int64_t ticket, int32_t *done) {
+  if (!s || !done) return BS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return BS_ERR_INVALID_ARG;
+  *done = it->second->done ? 1 : 0;
+  return BS_OK;
+}
+
+static bs_status wait_common(bs_server *s, int64_t ticket, double timeout_s, int kind, Request **out) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end() || it->second->kind != kind) return BS_ERR_INVALID_ARG;
+  Request *r = it->second;
+  auto pred = [&] { return r->done; };
+  if (timeout_s > 0) {
+    if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return BS_ERR_TIMEOUT;
+  } else {
+    s->cv_done.wait(lk, pred);
+  }
+  s->reqs.erase(it);
+  *out = r;
+  if (r->status) s->err = r->err;
+  return r->status;
+}
+
+BS_API bs_status bs_server_wait(bs_server *s, int64_t ticket, int64_t *hit_index, double *hit_rmsd, double timeout_s) {
+  if (!s || !hit_index || !hit_rmsd) return BS_ERR_INVALID_ARG;
+  Request *r = nullptr;
+  const bs_status st = wait_common(s, ticket, timeout_s, 0, &r);
+  if (r) {
+    if (st == BS_OK) {
+      memcpy(hit_index, r->idx.data(), r->idx.size() * 8);
+      memcpy(hit_rmsd, r->val.data(), r->val.size() * 8);
+    }
+    delete r;
+  }
+  return st;
+}
+
+BS_API bs_status bs_server_wait_cluster(bs_server *s, int64_t ticket, int64_t *cluster_of, double timeout_s) {
+  if (!s || !cluster_of) return BS_ERR_INVALID_ARG;
+  Request *r = nullptr;
+  const bs_status st = wait_common(s, ticket, timeout_s, 1, &r);
+  if (r) {
+    if (st == BS_OK) memcpy(cluster_of, r->labels.data(), r->labels.size() * 8);
+    delete r;
+  }
+  return st;
+}
+
+BS_API bs_status bs_server_get_stats(bs_server *s, bs_server_stats *out) {
+  if (!s || !out) return BS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *out = bs_server_stats{};
+  out->queries_done = s->qdone;
+  out->clusters_done = s->cdone;
+  out->pairs = s->pairs;
+  out->batches = s->batches;
+  out->plain_fallbacks = s->fallbacks;
+  int64_t pending = 0;
+  for (auto &kv : s->reqs) pending += kv.second->done ? 0 : 1;
+  out->pending = pending;
+  out->p50_ms = percentile(s->lat, 0.50);
+  out->p99_ms = percentile(s->lat, 0.99);
+  out->max_ms = s->lat.empty() ? 0.0 : *std::max_element(s->lat.begin(), s->lat.end());
+  double sum = 0.0;
+  for (double v : s->lat) sum += v;
+  out->mean_ms = s->lat.empty() ? 0.0 : sum / (double)s->lat.size();
+  out->cluster_p50_ms = percentile(s->clat, 0.50);
+  out->cluster_p99_ms = percentile(s->clat, 0.99);
+  out->seconds = ms_between(s->t0, Clock::now()) * 1e-3;
+  out->pairs_per_s = out->seconds > 0 ? (double)s->pairs / out->seconds : 0.0;
+  out->mean_batch_rows = s->batches ? (double)s->rows_batched / (double)s->batches : 0.0;
+  return BS_OK;
+}
+
+BS_API bs_status bs_server_reset_stats(bs_server *s) {
+  if (!s) return BS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->lat.clear();
+  s->clat.clear();
+  s->qdone = s->cdone = s->pairs = s->batches = s->fallbacks = s->rows_batched = 0;
+  s->t0 = Clock::now();
+  return BS_OK;
+}
+
+}  // extern "C"

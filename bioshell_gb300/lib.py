@@ -50,6 +50,26 @@ class bs_metrics(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class bs_server_config(ctypes.Structure):
+    _fields_ = [("nbuckets", ctypes.c_int32), ("bucket_L", ctypes.POINTER(ctypes.c_int32)),
+                ("bucket_n", ctypes.POINTER(ctypes.c_int64)), ("bucket_xyz", ctypes.POINTER(ctypes.c_void_p)),
+                ("top_k", ctypes.c_int32), ("max_inflight", ctypes.c_int32), ("hbm_budget", ctypes.c_size_t),
+                ("precision", ctypes.c_int32), ("max_batch_rows", ctypes.c_int32), ("tolerance", ctypes.c_double),
+                ("reserved", ctypes.c_int32 * 6)]
+
+
+class bs_server_stats(ctypes.Structure):
+    _fields_ = [("queries_done", ctypes.c_int64), ("clusters_done", ctypes.c_int64), ("pairs", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("plain_fallbacks", ctypes.c_int64), ("pending", ctypes.c_int64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("cluster_p50_ms", ctypes.c_double),
+                ("cluster_p99_ms", ctypes.c_double), ("pairs_per_s", ctypes.c_double),
+                ("mean_batch_rows", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -73,6 +93,17 @@ SIGNATURES = [
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                   ctypes.POINTER(bs_opts), _vp]),
     ("bs_all_vs_all_static", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp]),
+    ("bs_server_create", ctypes.c_int32, [ctypes.POINTER(_vp), ctypes.c_int32, ctypes.POINTER(bs_server_config)]),
+    ("bs_server_destroy", None, [_vp]),
+    ("bs_server_last_error", ctypes.c_char_p, [_vp]),
+    ("bs_server_submit", ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.c_int32, _i64p]),
+    ("bs_server_submit_cluster", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                                                  ctypes.c_int32, _i64p]),
+    ("bs_server_poll", ctypes.c_int32, [_vp, ctypes.c_int64, _i32p]),
+    ("bs_server_wait", ctypes.c_int32, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_double]),
+    ("bs_server_wait_cluster", ctypes.c_int32, [_vp, ctypes.c_int64, _vp, ctypes.c_double]),
+    ("bs_server_get_stats", ctypes.c_int32, [_vp, ctypes.POINTER(bs_server_stats)]),
+    ("bs_server_reset_stats", ctypes.c_int32, [_vp]),
     ("bs_hierarchical", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _i64p, _fp]),
     ("bs_cut_tree", ctypes.c_int32, [_i64p, _fp, ctypes.c_int64, ctypes.c_float, _i64p]),
     ("bs_optics", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _i64p,

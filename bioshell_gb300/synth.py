@@ -146,3 +146,33 @@ def batched_sets(nsets: int = 256, seed: int = 3, n_range=(50, 4000), l_range=(4
         base = base_chain(L, rng)
         sets.append(decoys(base, n, rng, sigma))
     return sets
+
+
+# The serving workload: a library bucketed by chain length with shares that
+# total ~1.7e7 atoms for 200,000 structures (85/9/4/2% at L = 64/128/256/512),
+# each bucket made of decoy families around independent base chains.
+SERVING_BUCKETS = ((64, 0.85), (128, 0.09), (256, 0.04), (512, 0.02))
+
+
+def serving_library(n_total: int = 200_000, families: int = 32, seed: int = 4, sigma=(0.5, 4.0)):
+    """{L: [n_L][L][3] decoys} and {L: [families] base chains (centred)}."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lib, bases = {}, {}
+    for L, share in SERVING_BUCKETS:
+        n = int(round(n_total * share))
+        fb = [base_chain(L, rng) for _ in range(families)]
+        fb = [b - b.mean(axis=0) for b in fb]
+        per = [n // families + (1 if f < n % families else 0) for f in range(families)]
+        lib[L] = np.concatenate([decoys(fb[f], per[f], rng, sigma) for f in range(families)])
+        bases[L] = fb
+    return lib, bases
+
+
+def serving_queries(bases, pool: int = 1024, seed: int = 5, sigma=(0.5, 4.0)):
+    """A pool of query decoys per bucket (contiguous slices are the requests)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = {}
+    for L, fb in bases.items():
+        fam = rng.integers(len(fb), size=pool)
+        out[L] = np.concatenate([decoys(fb[f], 1, rng, sigma) for f in fam])
+    return out

@@ -205,6 +205,83 @@ BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, 
  *     race and must not be issued. */
 BS_API bs_status bs_all_vs_all_static(const double *xyz, int64_t n, int32_t L, double *out, void *stream);
 
+/* ---- serving ------------------------------------------------------------
+ * A request loop over a device-resident structure library (the
+ * CrmsdServer::{new, submit, wait} handle a maintainer would add beside the
+ * all-vs-all call; no counterpart exists in the reference).  The library is
+ * bucketed by chain length; a query is a batch of structures of one
+ * bucket's length and gets, for every query structure, the top_k library
+ * structures of that bucket nearest by crmsd.  Mixed-in clustering jobs run
+ * an all-vs-all plus OPTICS (optics.rs:51-148) on their own structures.
+ *
+ * Batching is continuous: a scheduler thread launches whatever is queued for
+ * a bucket as one batch as soon as one of max_inflight device slots is free
+ * and the batch's device memory fits the server's budget, so requests that
+ * arrive while others are on the GPU are admitted as slots and memory free
+ * up, and their work overlaps on the device.  Every query's result depends
+ * only on the query and the library: the same alone or in any mix.
+ * submit, poll, wait and stats may be called from any thread. */
+typedef struct bs_server bs_server;
+
+typedef struct {
+  int32_t nbuckets;
+  const int32_t *bucket_L;           /* atoms per structure of each bucket    */
+  const int64_t *bucket_n;           /* structures in each bucket             */
+  const double *const *bucket_xyz;   /* [n][L][3] f64 per bucket (host/device) */
+  int32_t top_k;                     /* hits per query structure, 1..64      */
+  int32_t max_inflight;              /* batches on the device at once (0 = 4) */
+  size_t hbm_budget;                 /* device bytes for in-flight work
+                                        (0 = half the free memory after the
+                                        library is resident)                 */
+  int32_t precision;                 /* BS_PRECISION_MIXED or _PLAIN64       */
+  int32_t max_batch_rows;            /* query structures per batch (0 = 4096) */
+  double tolerance;                  /* as bs_opts.tolerance (<= 0: 1e-4)    */
+  int32_t reserved[6];
+} bs_server_config;
+
+typedef struct {
+  int64_t queries_done;     /* query requests completed                      */
+  int64_t clusters_done;    /* clustering jobs completed                     */
+  int64_t pairs;            /* crmsd values computed by completed requests   */
+  int64_t batches;          /* device batches launched                       */
+  int64_t plain_fallbacks;  /* queries outside their bucket's grid, served
+                               by the plain FP64 path                        */
+  int64_t pending;          /* requests submitted and not yet completed      */
+  double p50_ms;            /* query latency, submit -> results ready        */
+  double p99_ms;
+  double max_ms;
+  double mean_ms;
+  double cluster_p50_ms;    /* clustering-job latency                        */
+  double cluster_p99_ms;
+  double pairs_per_s;       /* pairs / wall time since the last reset        */
+  double mean_batch_rows;   /* query structures per batch                    */
+  double seconds;           /* wall time since the last reset                */
+} bs_server_stats;
+
+BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_server_config *cfg);
+/* Stops the scheduler after the requests in flight and frees everything. */
+BS_API void bs_server_destroy(bs_server *s);
+BS_API const char *bs_server_last_error(const bs_server *s);
+/* Queues q structures xyz[q][L][3] (copied before the call returns); L must
+ * be one of the bucket lengths. */
+BS_API bs_status bs_server_submit(bs_server *s, const double *xyz, int32_t q, int32_t L, int64_t *ticket);
+/* Queues an all-vs-all + OPTICS clustering job over n structures. */
+BS_API bs_status bs_server_submit_cluster(bs_server *s, const double *xyz, int64_t n, int32_t L, double eps,
+                                          int32_t min_points, int64_t *ticket);
+/* done = 1 once the request's results are ready. */
+BS_API bs_status bs_server_poll(bs_server *s, int64_t ticket, int32_t *done);
+/* Waits (at most timeout_s seconds; <= 0: no limit) and returns a query's
+ * results: hit_index[q][top_k] (library index within the bucket, -1 where
+ * the bucket has fewer structures) and hit_rmsd[q][top_k], ascending.  The
+ * ticket is released.  BS_ERR_TIMEOUT if not ready in time. */
+BS_API bs_status bs_server_wait(bs_server *s, int64_t ticket, int64_t *hit_index, double *hit_rmsd,
+                                double timeout_s);
+/* The same for a clustering job: OPTICS cluster index of every structure. */
+BS_API bs_status bs_server_wait_cluster(bs_server *s, int64_t ticket, int64_t *cluster_of, double timeout_s);
+BS_API bs_status bs_server_get_stats(bs_server *s, bs_server_stats *out);
+/* Clears the latency record and restarts the wall clock of the stats. */
+BS_API bs_status bs_server_reset_stats(bs_server *s);
+
 /* ---- clustering of a crmsd matrix --------------------------------------- */
 /* Merge rules of bioshell-clustering/src/hierarchical/strategies/mod.rs. */
 enum {

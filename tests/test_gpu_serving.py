@@ -1,0 +1,159 @@
+"""Serving (bs_server_*) on the GPU: a device-resident library bucketed by
+chain length, continuous batching, top-k queries and mixed-in clustering
+jobs.
+
+* Top-k: every returned value is within 1e-4 A of the FP64 oracle, and the
+  returned indices are the oracle's k nearest except where two library
+  structures lie within 2e-4 A of each other at the cut.
+* Alone vs mix: a query's result is identical (indices and values, bit for
+  bit) when it runs alone and when it is batched with other queries and
+  clustering jobs.
+* Clustering jobs: OPTICS labels equal those of OPTICS run on the engine's
+  own all-vs-all of the same structures.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from bioshell_gb300 import clustering as K
+from bioshell_gb300 import synth
+from bioshell_gb300.crmsd import CrmsdOptions
+from bioshell_gb300.lib import CrmsdError
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+TOPK = 20
+
+
+def _family_library(rng, L, n, families=4):
+    parts = []
+    for _ in range(families):
+        parts.append(synth.decoys(synth.base_chain(L, rng), n // families, rng, sigma=(0.3, 3.0)))
+    return np.concatenate(parts), parts
+
+
+@pytest.fixture(scope="module")
+def library():
+    rng = np.random.default_rng(77)
+    lib64, fam64 = _family_library(rng, 64, 600)
+    lib128, fam128 = _family_library(rng, 128, 160)
+    return {64: lib64, 128: lib128}, {64: fam64, 128: fam128}, rng
+
+
+@pytest.fixture(scope="module")
+def server(library, enginelib):
+    from bioshell_gb300 import CrmsdServer
+    lib, _, _ = library
+    s = CrmsdServer(lib, top_k=TOPK, max_inflight=3)
+    yield s
+    s.close()
+
+
+def _queries(library, L, q, seed):
+    _, fams, _ = library
+    rng = np.random.default_rng(seed)
+    base = fams[L][rng.integers(len(fams[L]))][0]
+    return synth.decoys(base - base.mean(axis=0), q, rng, sigma=(0.3, 2.0))
+
+
+def _check_against_oracle(lib, x, idx, val, oracle_mod):
+    n = lib.shape[0]
+    for r in range(x.shape[0]):
+        pair = np.concatenate([x[r:r + 1], lib])
+        ref = oracle_mod.crmsd_pairs(pair, np.zeros(n, dtype=np.int64), np.arange(1, n + 1))
+        assert np.all(idx[r] >= 0)
+        np.testing.assert_allclose(val[r], ref[idx[r]], rtol=0, atol=TOL)
+        order = np.lexsort((np.arange(n), ref))
+        kth = ref[order[TOPK - 1]]
+        want = set(order[:TOPK][ref[order[:TOPK]] < kth - 2 * TOL].tolist())
+        got = set(idx[r].tolist())
+        assert want <= got
+        assert np.all(np.diff(val[r]) >= 0)
+
+
+def test_topk_against_oracle(server, library, oracle_mod):
+    lib, _, _ = library
+    for L, q, seed in ((64, 7, 1), (128, 3, 2), (64, 45, 3)):
+        x = _queries(library, L, q, seed)
+        idx, val = server.wait(server.submit(x))
+        assert idx.shape == (q, TOPK)
+        _check_against_oracle(lib[L], x[: min(q, 6)], idx[: min(q, 6)], val[: min(q, 6)], oracle_mod)
+
+
+def test_same_result_alone_and_in_the_mix(server, library):
+    lib, _, rng = library
+    probes = [_queries(library, 64, 33, 10), _queries(library, 128, 5, 11), _queries(library, 64, 1, 12)]
+    alone = [server.wait(server.submit(x)) for x in probes]
+    # now the same queries among concurrent traffic from several threads
+    tickets = {}
+    others = []
+
+    def noise(seed):
+        r = np.random.default_rng(seed)
+        for _ in range(6):
+            L = 64 if r.random() < 0.7 else 128
+            others.append(server.submit(_queries(library, L, int(r.integers(1, 60)), int(r.integers(1 << 30)))))
+
+    threads = [threading.Thread(target=noise, args=(s,)) for s in range(3)]
+    for t in threads:
+        t.start()
+    cl = server.submit_cluster(lib[64][:150], 2.5, 4)
+    for k, x in enumerate(probes):
+        tickets[k] = server.submit(x)
+    for t in threads:
+        t.join()
+    mixed = [server.wait(tickets[k]) for k in range(len(probes))]
+    for t in others:
+        server.wait(t)
+    server.wait_cluster(cl)
+    for (ia, va), (ib, vb) in zip(alone, mixed):
+        np.testing.assert_array_equal(ia, ib)
+        np.testing.assert_array_equal(va, vb)
+    st = server.stats()
+    assert st["batches"] >= 1 and st["queries_done"] >= 3 and st["p99_ms"] >= st["p50_ms"] > 0
+
+
+def test_cluster_job_matches_engine_optics(server, library, engine):
+    lib, _, _ = library
+    x = lib[128][:90]
+    labels = server.wait_cluster(server.submit_cluster(x, 3.0, 5))
+    m = engine.all_vs_all(x, CrmsdOptions(out_type="f32"))
+    _, _, want = K.optics(m, 3.0, 5)
+    np.testing.assert_array_equal(labels, want)
+
+
+def test_plain_precision_server(library, oracle_mod, enginelib):
+    from bioshell_gb300 import CrmsdServer
+    lib, _, _ = library
+    s = CrmsdServer({64: lib[64]}, top_k=TOPK, precision="plain64")
+    try:
+        x = _queries(library, 64, 4, 21)
+        idx, val = s.wait(s.submit(x))
+        _check_against_oracle(lib[64], x, idx, val, oracle_mod)
+    finally:
+        s.close()
+
+
+def test_out_of_range_query_uses_the_fp64_path(server, library, oracle_mod):
+    lib, _, _ = library
+    x = _queries(library, 64, 2, 31) * 40.0  # far beyond the bucket's grid range
+    before = server.stats()["plain_fallbacks"]
+    idx, val = server.wait(server.submit(x))
+    assert server.stats()["plain_fallbacks"] == before + 1
+    _check_against_oracle(lib[64], x, idx, val, oracle_mod)
+
+
+def test_server_errors(server, library):
+    with pytest.raises(CrmsdError) as e:
+        server.submit(np.zeros((2, 77, 3)))  # no bucket of that length
+    assert e.value.status == 1
+    x = _queries(library, 64, 3, 41)
+    x[1, 5, 2] = np.nan
+    t = server.submit(x)
+    with pytest.raises(CrmsdError) as e:
+        server.wait(t)
+    assert e.value.status == 6
+    idx, _ = server.wait(server.submit(_queries(library, 64, 2, 42)))  # still serving
+    assert np.all(idx >= 0)
