@@ -171,6 +171,53 @@ BS_HD float qcp_top_eig(const float s[9], float &xout, float q[4]) {
   return best;
 }
 
+// Largest root x of the normalised QCP quartic of sn = S / lambda0 (x <= 1):
+// the Halley iterations of qcp_top_eig, without the eigenvector.
+BS_HD float qcp_top_root(const float s[9]) {
+  const Key k = key_from_s(s);
+  float fro2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fro2 = fmaf(s[i], s[i], fro2);
+  const float c2 = -2.f * fro2;
+  const float c1 = -8.f * det3f(s);
+  const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
+  float x = 1.0f;
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
+    const float x2 = x * x;
+    const float p = fmaf(fmaf(x2 + c2, x, c1), x, c0);
+    const float dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
+    const float ddp = fmaf(12.f, x2, 2.f * c2);
+    const float den = fmaf(2.f * dp, dp, -p * ddp);
+    const float step = BS_FDIV(2.f * p * dp, den);
+    x = (den > 0.f) ? x - step : x;
+  }
+  return x;
+}
+
+// Screen of one pair from the leading levels only (m = S0 + 2^-9 S1, units
+// 2^28 u): E = (Ga+Gb)(1 - x) in FP32, and crmsd bounds lo <= crmsd <= hi
+// from dtrunc (bound on what the omitted levels move E, units u) plus
+// 2^-16 (Ga+Gb) for the FP32 arithmetic -- a margin far above the FP32
+// eigenvalue error of the well-conditioned top root (~2^-22 (Ga+Gb)).
+BS_HD void screen_bounds(const float m[9], float gsum_f, float dtrunc, float u, int L, float &lo, float &hi) {
+  if (!(gsum_f > 0.f)) {
+    lo = hi = 0.f;
+    return;
+  }
+  const float lam0 = gsum_f * 1.862645149230957e-09f;  // 2^-29: (Ga+Gb)/2 in units of m
+  const float inv = BS_FDIV(1.0f, lam0);
+  float sn[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
+  const float x = qcp_top_root(sn);
+  const float e = gsum_f * (1.0f - x);
+  const float de = dtrunc + gsum_f * 1.52587890625e-05f;  // 2^-16
+  const float scale = BS_FDIV(u, (float)L);
+  lo = sqrtf(fmaxf(e - de, 0.f) * scale);
+  hi = sqrtf(fmaxf(e + de, 0.f) * scale);
+}
+
 // ------------------------------------------------- quaternion -> T = R^T
 // T(q) with q = (w, x, y, z); quadratic, homogeneous.
 template <typename V>

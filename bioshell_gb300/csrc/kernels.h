@@ -77,6 +77,8 @@ struct Job {
   // library's maxima, per digit), used in the exactness bound
   float norm_b[3];
   float qres_b;           // largest B-side quantisation residual RMS
+  int screen;             // 1: rectangular screen job (bounds from the leading levels)
+  void *out_lo;           // screen jobs: lower bounds, same layout as `out` (upper bounds)
   // ---- device (preparation)
   unsigned long long maxabs;        // max |centred coordinate|, fixed-point units
   unsigned long long norm[4][3];    // per candidate grid: max row sum of squared digits (d0, d1, d2)
@@ -90,6 +92,8 @@ struct Job {
   float d34;                        // rounding bound of accumulator levels 2-3, as an error of E (units u)
   int layout;                       // accumulator layout of the job's tiles (kAcc*)
   int allow_long;                   // (host) the long layout may be chosen
+  float dtrunc;                     // screen jobs: bound on E of the omitted levels (units u)
+  int pad2;
 };
 
 // Accumulator layouts of a tile.  Normal: the four levels, one 64-column
@@ -100,6 +104,10 @@ struct Job {
 // where the whole chain's would not.
 constexpr int kAccNormal = 0;
 constexpr int kAccLong = 1;
+// Screen tiles: only the leading digit products (levels 0 and 1, three per
+// 16-atom step, digits 0 and 1 of each side) and an FP32 epilogue writing
+// crmsd bounds -- the first stage of top-k queries.
+constexpr int kAccScreen = 2;
 __host__ __device__ inline int acc_part(int k16, int nk16, int parts) { return (k16 * parts) / nk16; }
 // accumulator index (0..7) of level `lv` at 16-atom step k16
 __host__ __device__ inline int acc_index(int layout, int lv, int k16, int nk16) {
@@ -205,6 +213,14 @@ struct RefineArgs {
 // exact recomputation of the queued pairs; then, only when the queue
 // overflowed (checked on the device), of every sentinel left in the outputs
 cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st);
+// Certified crmsd of the screen candidates of rectangular jobs: row r is
+// global A structure row_ig[r] of job row_job[r]; candidate c of the row is
+// B structure cand_j[r * cap + c] (c < min(cand_n[r], cap)); values go to
+// cand_v[r * cap + c].
+cudaError_t launch_exact_candidates(const DigitsView &da, const DigitsView &db, const SInfo *info_a,
+                                    const SInfo *info_b, const Job *jobs, const int *row_job, const int64_t *row_ig,
+                                    int64_t rows, const int *cand_j, const int *cand_n, int cap, float *cand_v,
+                                    cudaStream_t st);
 // CUDA-core level sums + the same epilogue for an explicit pair list of job 0
 // (used for sparse pair lists and as the tensor-core path's independent check)
 cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Job *job, DevScalars *sc,
@@ -217,5 +233,14 @@ cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Jo
 constexpr int kTopkMax = 64;
 cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, int64_t *out_idx,
                         float *out_val, cudaStream_t st);
+// The same with a per-row count of valid values (row_n[r] <= n) and a map
+// from column to reported index (col_map[r * ld + c]; may be null).
+cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, int64_t ld, int k,
+                             const int *col_map, int64_t *out_idx, float *out_val, cudaStream_t st);
+// Screen candidates: per row r, every column c with lo[r][c] not above the
+// k-th smallest hi[r][.] (the row's k-th smallest upper bound), up to cap
+// per row (cand_n[r] counts all, so cand_n[r] > cap marks an overflowing row).
+cudaError_t launch_screen_select(const float *hi, const float *lo, int64_t rows, int64_t n, int64_t ld, int k,
+                                 int cap, int *cand_j, int *cand_n, cudaStream_t st);
 
 }  // namespace bs

@@ -47,6 +47,7 @@ constexpr int kBRows = 64;                               // B tile rows = 20 str
 constexpr int kAOpBytes = kBlockRows * kKChunk * 2;      // 16 KB
 constexpr int kBOpBytes = kBRows * kKChunk * 2;          // 8 KB
 constexpr int kStageBytes = 4 * kAOpBytes + 3 * kBOpBytes;
+constexpr int kScreenStageBytes = 2 * kAOpBytes + 2 * kBOpBytes;  // digits 0 and 1 only
 constexpr int kThreads = 384;
 constexpr int kEpiWarp0 = 4;
 constexpr int kEpiWarps = 8;
@@ -61,9 +62,10 @@ struct __align__(16) TileMeta {
   SInfo ia[kBlockStructs];  // A-block structures
   SInfo ib[kBStructs];      // B-block structures
   OutDesc out;
+  void *out_lo;
   long long n, n_b, first_a, first_b;
   int a_blk, b_blk, job, mode, err, layout, L;
-  float tol, u, d34;
+  float tol, u, d34, dtrunc;
 };
 constexpr int kMetaBytes = 2 * (int)sizeof(TileMeta);
 constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes + kBarBytes;
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
         const int rowA = tile.a_blk * kBlockRows, rowB = tile.b_blk * kBRows;
         const int nchunks = (tile_nk16(tile) * 16 + kKChunk - 1) / kKChunk;
+        const bool scr = tile_layout(tile) == kAccScreen;
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
@@ -176,16 +179,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             fail(sh, a.sc);
             break;
           }
-          ptx::mbar_arrive_expect_tx(&sh->full[s], kStageBytes);
+          ptx::mbar_arrive_expect_tx(&sh->full[s], scr ? kScreenStageBytes : kStageBytes);
           uint8_t *st = smem + (size_t)s * kStageBytes;
           const int k0 = kc * kKChunk;
           ptx::tma_load_2d(st + 0 * kAOpBytes, &ta0, k0, rowA, &sh->full[s]);
           ptx::tma_load_2d(st + 1 * kAOpBytes, &ta1, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 2 * kAOpBytes, &ta2, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 3 * kAOpBytes, &ta3, k0, rowA, &sh->full[s]);
+          if (!scr) {
+            ptx::tma_load_2d(st + 2 * kAOpBytes, &ta2, k0, rowA, &sh->full[s]);
+            ptx::tma_load_2d(st + 3 * kAOpBytes, &ta3, k0, rowA, &sh->full[s]);
+          }
           ptx::tma_load_2d(st + 4 * kAOpBytes + 0 * kBOpBytes, &tb0, k0, rowB, &sh->full[s]);
           ptx::tma_load_2d(st + 4 * kAOpBytes + 1 * kBOpBytes, &tb1, k0, rowB, &sh->full[s]);
-          ptx::tma_load_2d(st + 4 * kAOpBytes + 2 * kBOpBytes, &tb2, k0, rowB, &sh->full[s]);
+          if (!scr) ptx::tma_load_2d(st + 4 * kAOpBytes + 2 * kBOpBytes, &tb2, k0, rowB, &sh->full[s]);
         }
       }
       // let the stages still in flight land before the block can retire
@@ -243,6 +248,15 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t db0 = ptx::smem_desc_sw128(bbase + 0 * kBOpBytes + off);
             const uint64_t db1 = ptx::smem_desc_sw128(bbase + 1 * kBOpBytes + off);
             const uint64_t db2 = ptx::smem_desc_sw128(bbase + 2 * kBOpBytes + off);
+            if (lay == kAccScreen) {
+              // levels 0 and 1 only
+              const uint32_t c0 = acc_col(0);
+              const uint32_t first = k > 0 ? 1u : 0u;
+              ptx::tc_mma_f16(c0, da0, db0, kIdesc, first);
+              ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc, first);
+              ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc, 1u);
+              continue;
+            }
             uint32_t col[4], acc[4];  // per level: accumulator column, accumulate (vs overwrite)
             if (lay == kAccNormal) {
               // one buffer, level lv at column 64 lv; every level starts at step 0
@@ -311,6 +325,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         mt.tol = jb.tol;
         mt.u = jb.u;
         mt.d34 = jb.d34;
+        mt.dtrunc = jb.dtrunc;
+        mt.out_lo = jb.out_lo;
       }
       // per-structure data of the tile's A and B blocks (pads and structures
       // past a job's end read as zero; the epilogue never uses them)
@@ -367,6 +383,55 @@ __global__ void __launch_bounds__(kThreads, 1)
       const OutDesc out = mt.out;
       const float t_d34 = mt.d34, t_u = mt.u, t_tol = mt.tol;
       const int t_L = mt.L, t_job = mt.job;
+      if (mt.layout == kAccScreen) {
+        // ---- screen tile: crmsd bounds from levels 0 and 1 (FP32)
+        const float t_dtrunc = mt.dtrunc;
+        float *hi_out = static_cast<float *>(out.ptr), *lo_out = static_cast<float *>(mt.out_lo);
+        const uint32_t c0 = lane_base + (p & 1u) * 256u;
+        const int64_t ig = (int64_t)mt.a_blk * kBlockStructs + qd * kGroupStructs + il;
+        const int64_t i = ig - fa;
+        const bool row_ok = job_ok && (lane < 30) && (i < jn);
+        const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          {
+            float m[32], v[32];
+            ptx::tmem_ld_32x32b_x32(c0, m);
+            ptx::tmem_ld_32x32b_x32(c0 + 64, v);
+#pragma unroll
+            for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+#pragma unroll
+            for (int c = 0; c < 16; ++c) stg[lane * kPitch + c] = h ? m[15 + c] : m[c];
+          }
+          if (h == 1) {
+            ptx::tc_fence_before();
+            ptx::mbar_arrive(&sh->tempty[p & 1u]);
+          }
+          __syncwarp();
+#pragma unroll
+          for (int sl = 0; sl < 2; ++sl) {
+            const int jh = 3 * sl + x;
+            const int jc = jh < 5 ? jh : 4;
+            const int64_t jg = (int64_t)mt.b_blk * kBStructs + g * kGroupStructs + 5 * h + jh;
+            const int64_t j = jg - fb;
+            if (!(row_ok && (jh < 5) && (j < jnb))) continue;
+            float m9[9];
+#pragma unroll
+            for (int xr = 0; xr < 3; ++xr)
+#pragma unroll
+              for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+            const SInfo ib = mt.ib[g * kGroupStructs + 5 * h + jc];
+            float lo, hi;
+            bsm::screen_bounds(m9, ia.gf + ib.gf, t_dtrunc, t_u, t_L, lo, hi);
+            hi_out[i * out.ld + j] = hi;
+            lo_out[i * out.ld + j] = lo;
+          }
+          __syncwarp();
+        }
+        ptx::mbar_arrive(&sh->mempty[slot]);
+        p += 1u;
+        continue;
+      }
       // accumulators of level lv: normal layout {lv}; long layout L0 {0},
       // L1 {1, 2}, L2 {3..6}, L3 {7}; accumulator ai sits in slot p + ai / 4
       auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };

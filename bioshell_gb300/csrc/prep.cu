@@ -303,6 +303,14 @@ __global__ void k_mx_choose(PrepArgs p) {
   jb.d34 = (float)(6.0 * sqrt(3.0) * (1024.0 * err2 + 2.0 * err3) * (1.0 + 1e-6));
   jb.scale_exp = jb.scale_base + pick;
   jb.u = ldexpf(1.0f, 2 * jb.scale_exp);
+  if (jb.screen) {
+    // The screen keeps levels 0 and 1: the rest of Mhat, 2^10 S2 + 2 S3',
+    // is at most 2^10 b2 + 2 b34 per entry, so the top eigenvalue moves by
+    // at most 2 ||dM||_F <= 6 (2^10 b2 + 2 b34) and E by twice that.
+    const double b2 = bb2[pick] > 0.0 ? bb2[pick] : 0.0;
+    jb.dtrunc = (float)(12.0 * (1024.0 * b2 + 2.0 * bb34[pick]) * (1.0 + 1e-6));
+    jb.layout = kAccScreen;
+  }
 }
 
 // ---------------------------------------------------------------- digits

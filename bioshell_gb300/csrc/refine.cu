@@ -142,42 +142,30 @@ __global__ void k_refine_scan(RefineArgs r) {
   }
 }
 
-// Thread per pair of job 0: exact level sums on CUDA cores, the fast
-// epilogue, and the exact path when the pair is flagged.  Level 3 carries
-// S3 + S4/512 as the tensor cores accumulate it (here rounded once from the
-// exact value).
-__global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, const Job *job, DevScalars *sc,
-                              const int64_t *__restrict__ ii, const int64_t *__restrict__ jj, int64_t np,
-                              double *__restrict__ out, float *__restrict__ levels_out) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= np) return;
-  const Job &jb = *job;
-  if (jb.err) return;
-  const int64_t i = ii[t] + jb.first_a, j = jj[t] + jb.first_a;
+// One pair (A structure ig, B structure jg) with exact level sums on CUDA
+// cores, the fast epilogue, and the exact path when the pair is flagged.
+// Level 3 carries S3 + S4/512 as the tensor cores accumulate it (here
+// rounded once from the exact value).  levels_out (optional) receives the
+// 36 level sums.
+__device__ double certified_pair(const DigitsView &da, const DigitsView &db, int64_t ig, int64_t jg, const SInfo &ia,
+                                 const SInfo &ib, const Job &jb, float *levels_out) {
   const int L = jb.L;
-  if (i == j) {
-    out[t] = 0.0;
-    if (levels_out)
-      for (int e = 0; e < 36; ++e) levels_out[t * 36 + e] = 0.f;
-    return;
-  }
   int S[5][9];
 #pragma unroll
   for (int l = 0; l < 5; ++l)
 #pragma unroll
     for (int e = 0; e < 9; ++e) S[l][e] = 0;
-  const int64_t pitch = dg.pitch;
   for (int k = 0; k < L; ++k) {
     int a[3][3], b[3][3];  // [coord][digit]
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const int64_t oa = digit_row(i, c) * pitch + k, ob = digit_row(j, c) * pitch + k;
-      a[c][0] = (int)__bfloat162float(dg.d0[oa]);
-      a[c][1] = (int)__bfloat162float(dg.d1[oa]);
-      a[c][2] = (int)__bfloat162float(dg.d2[oa]);
-      b[c][0] = (int)__bfloat162float(dg.d0[ob]);
-      b[c][1] = (int)__bfloat162float(dg.d1[ob]);
-      b[c][2] = (int)__bfloat162float(dg.d2[ob]);
+      const int64_t oa = digit_row(ig, c) * da.pitch + k, ob = digit_row(jg, c) * db.pitch + k;
+      a[c][0] = (int)__bfloat162float(da.d0[oa]);
+      a[c][1] = (int)__bfloat162float(da.d1[oa]);
+      a[c][2] = (int)__bfloat162float(da.d2[oa]);
+      b[c][0] = (int)__bfloat162float(db.d0[ob]);
+      b[c][1] = (int)__bfloat162float(db.d1[ob]);
+      b[c][2] = (int)__bfloat162float(db.d2[ob]);
     }
 #pragma unroll
     for (int x = 0; x < 3; ++x)
@@ -191,7 +179,6 @@ __global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, con
         S[4][e] += (a[x][2] >> 4) * (b[y][2] >> 4);  // sum d2a d2b; S4/512 = (sum d2a d2b) / 2
       }
   }
-  const SInfo ia = info[i], ib = info[j];
   bsm::EpilogueIn in;
 #pragma unroll
   for (int e = 0; e < 9; ++e) {
@@ -209,21 +196,55 @@ __global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, con
   if (levels_out) {
 #pragma unroll
     for (int e = 0; e < 9; ++e) {
-      levels_out[t * 36 + e] = in.s0[e];
-      levels_out[t * 36 + 9 + e] = in.s1[e];
-      levels_out[t * 36 + 18 + e] = in.s2[e];
-      levels_out[t * 36 + 27 + e] = in.s3[e];
+      levels_out[e] = in.s0[e];
+      levels_out[9 + e] = in.s1[e];
+      levels_out[18 + e] = in.s2[e];
+      levels_out[27 + e] = in.s3[e];
     }
   }
   int flag = 0;
   const float r = bsm::pair_rmsd_fast(in, jb.u, jb.d34, L, jb.tol, flag);
-  if (!flag) {
-    out[t] = (double)r;
+  if (!flag) return (double)r;
+  long long mh[9];
+  exact_cov_partial(da, db, ig, jg, L, 0, 1, mh);
+  return bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
+}
+
+// Thread per pair of job 0 (explicit pair lists, and the tensor-core path's
+// independent check).
+__global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, const Job *job, DevScalars *sc,
+                              const int64_t *__restrict__ ii, const int64_t *__restrict__ jj, int64_t np,
+                              double *__restrict__ out, float *__restrict__ levels_out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const Job &jb = *job;
+  if (jb.err) return;
+  const int64_t i = ii[t] + jb.first_a, j = jj[t] + jb.first_a;
+  if (i == j) {
+    out[t] = 0.0;
+    if (levels_out)
+      for (int e = 0; e < 36; ++e) levels_out[t * 36 + e] = 0.f;
     return;
   }
-  long long mh[9];
-  exact_cov_partial(dg, dg, i, j, L, 0, 1, mh);
-  out[t] = bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
+  out[t] = certified_pair(dg, dg, i, j, info[i], info[j], jb, levels_out ? levels_out + t * 36 : nullptr);
+}
+
+// Block per query row: the certified crmsd of each of its screen candidates.
+__global__ void k_exact_candidates(DigitsView da, DigitsView db, const SInfo *__restrict__ info_a,
+                                   const SInfo *__restrict__ info_b, const Job *__restrict__ jobs,
+                                   const int *__restrict__ row_job, const int64_t *__restrict__ row_ig,
+                                   const int *__restrict__ cand_j, const int *__restrict__ cand_n, int cap,
+                                   float *__restrict__ cand_v) {
+  const int64_t r = blockIdx.x;
+  const Job &jb = jobs[row_job[r]];
+  if (jb.err) return;
+  const int64_t ig = row_ig[r];
+  const int n = min(cand_n[r], cap);
+  const SInfo ia = info_a[ig];
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    const int64_t jg = (int64_t)cand_j[r * cap + c] + jb.first_b;
+    cand_v[r * cap + c] = (float)certified_pair(da, db, ig, jg, ia, info_b[jg], jb, nullptr);
+  }
 }
 
 }  // namespace
@@ -231,6 +252,16 @@ __global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, con
 cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st) {
   k_refine_list<<<r.num_sms * 4, 256, 0, st>>>(r);
   k_refine_scan<<<r.num_sms * 4, 256, 0, st>>>(r);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_exact_candidates(const DigitsView &da, const DigitsView &db, const SInfo *info_a,
+                                    const SInfo *info_b, const Job *jobs, const int *row_job, const int64_t *row_ig,
+                                    int64_t rows, const int *cand_j, const int *cand_n, int cap, float *cand_v,
+                                    cudaStream_t st) {
+  if (rows <= 0) return cudaSuccess;
+  k_exact_candidates<<<(unsigned)rows, 64, 0, st>>>(da, db, info_a, info_b, jobs, row_job, row_ig, cand_j, cand_n,
+                                                   cap, cand_v);
   return cudaGetLastError();
 }
 

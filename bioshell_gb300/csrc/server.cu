@@ -40,6 +40,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr unsigned long long kServerFlagCap = 1ull << 20;
+constexpr int kCandCap = 2048;  // screen candidates kept per query structure
 
 double ms_between(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
@@ -89,10 +90,12 @@ struct Slot {
   std::vector<int64_t> row0;  // first dense row of each query job
   int64_t rows = 0;           // query structures in the batch
   int njobs = 0;
+  bool screen = false;        // the batch ran the two-stage (screen + exact) top-k
   // device
   DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
+  DevBuf dense_lo, cand_j, cand_n, cand_v, rowtab;
   // pinned host
-  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri;
+  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n;
 };
 
 }  // namespace
@@ -173,16 +176,18 @@ bool host_ensure(HostBuf &h, size_t bytes) {
 }
 
 void slot_release(bs_server *s, Slot &sl) {
-  DevBuf *list[] = {&sl.xyz,  &sl.ctr,   &sl.info,  &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3], &sl.jobs,
-                    &sl.jobmap, &sl.tiles, &sl.flags, &sl.scal,   &sl.dense,  &sl.topi,   &sl.topv,   &sl.y,
-                    &sl.g,    &sl.ctrd};
+  DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
+                    &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
+                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.dense_lo,
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
   for (DevBuf *b : list) sv_release(s, *b);
 }
 
 size_t slot_bytes(Slot &sl) {
-  DevBuf *list[] = {&sl.xyz,  &sl.ctr,   &sl.info,  &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3], &sl.jobs,
-                    &sl.jobmap, &sl.tiles, &sl.flags, &sl.scal,   &sl.dense,  &sl.topi,   &sl.topv,   &sl.y,
-                    &sl.g,    &sl.ctrd};
+  DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
+                    &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
+                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.dense_lo,
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
   size_t t = 0;
   for (DevBuf *b : list) t += b->cap;
   return t;
@@ -208,6 +213,7 @@ size_t batch_bytes(const bs_server *s, const std::vector<Request *> &b) {
     for (const Request *r : b) tiles += blocks_for(r->q) * ((nb + kBStructs - 1) / kBStructs);
     t += (size_t)tiles * sizeof(Tile) + kServerFlagCap * 8 + (size_t)rows * nb * 4 + (size_t)rows * s->top_k * 12;
     if (s->precision == BS_PRECISION_PLAIN64) t += (size_t)rows * (3 * lp * 8 + 8 + 24);
+    else t += (size_t)rows * nb * 4 + (size_t)rows * (s->top_k * 12 + (size_t)kCandCap * 8 + 16);
   } else {
     const int64_t n = r0->q, nba = blocks_for(n), nbb = (n + kBStructs - 1) / kBStructs;
     for (int64_t i = 0; i < nba; ++i) tiles += std::max<int64_t>(0, nbb - 2 * i);
@@ -304,7 +310,10 @@ bs_status build_bucket(bs_server *s, Bucket &bk, const double *xyz_in) {
 }
 
 // ------------------------------------------------------------ batches
-bs_status launch_query_batch(bs_server *s, Slot &sl) {
+// Enqueues a query batch on the slot.  screen: the two-stage top-k (bounds
+// from the leading levels on the tensor cores, then the certified crmsd of
+// each row's candidates); otherwise every pair is certified densely.
+bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   const Bucket &bk = s->buckets[sl.bucket];
   const int L = bk.L, k = s->top_k;
   const int nj = (int)sl.reqs.size();
@@ -335,6 +344,7 @@ bs_status launch_query_batch(bs_server *s, Slot &sl) {
     jb.tol = s->tol;
     for (int d = 0; d < 3; ++d) jb.norm_b[d] = bk.norm_b[d];
     jb.qres_b = bk.qres;
+    jb.screen = screen ? 1 : 0;
     plan.jobs.push_back(jb);
     const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
     for (int64_t I = 0; I < nb; ++I)
@@ -345,6 +355,7 @@ bs_status launch_query_batch(bs_server *s, Slot &sl) {
   plan.nblocks = blk;
   sl.rows = rows;
   sl.njobs = nj;
+  sl.screen = screen && s->precision == BS_PRECISION_MIXED;
   const int64_t ns = blk * kBlockStructs, drows = blk * kBlockRows;
   const bool plain = s->precision == BS_PRECISION_PLAIN64;
   bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * bk.n * 4) &&
@@ -360,8 +371,12 @@ bs_status launch_query_batch(bs_server *s, Slot &sl) {
          sv_ensure(s, sl.jobs, (size_t)nj * sizeof(Job)) && sv_ensure(s, sl.jobmap, plan.jobmap.size() * 4) &&
          sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl.flags, kServerFlagCap * 8) &&
          host_ensure(sl.hjobs, (size_t)nj * sizeof(Job)) && host_ensure(sl.hback, (size_t)nj * sizeof(Job)) &&
-         host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile));
+         host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16);
     for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * bk.pitch * 2);
+    if (sl.screen)
+      ok = ok && sv_ensure(s, sl.dense_lo, (size_t)rows * bk.n * 4) && sv_ensure(s, sl.cand_j, (size_t)rows * kCandCap * 4) &&
+           sv_ensure(s, sl.cand_n, (size_t)rows * 4) && sv_ensure(s, sl.cand_v, (size_t)rows * kCandCap * 4) &&
+           sv_ensure(s, sl.rowtab, (size_t)rows * 12 + 8) && host_ensure(sl.hcand_n, (size_t)rows * 4);
   }
   if (!ok) return BS_ERR_OOM;
   // coordinates in
@@ -384,8 +399,12 @@ bs_status launch_query_batch(bs_server *s, Slot &sl) {
         return BS_ERR_CUDA;
     }
   } else {
+    float *dense_lo = sl.screen ? static_cast<float *>(sl.dense_lo.p) : nullptr;
     for (int j = 0; j < nj; ++j) plan.jobs[j].xyz = dx + xoff[j];
-    for (int j = 0; j < nj; ++j) plan.jobs[j].out = OutDesc{dense + sl.row0[j] * bk.n, sl.reqs[j]->q, bk.n, kLayoutRect, 1};
+    for (int j = 0; j < nj; ++j) {
+      plan.jobs[j].out = OutDesc{dense + sl.row0[j] * bk.n, sl.reqs[j]->q, bk.n, kLayoutRect, 1};
+      plan.jobs[j].out_lo = dense_lo ? dense_lo + sl.row0[j] * bk.n : nullptr;
+    }
     memcpy(sl.hjobs.p, plan.jobs.data(), (size_t)nj * sizeof(Job));
     char *ht = static_cast<char *>(sl.htab.p);
     memcpy(ht, plan.jobmap.data(), plan.jobmap.size() * 4);
@@ -415,9 +434,39 @@ bs_status launch_query_batch(bs_server *s, Slot &sl) {
             cudaSuccess ||
         cudaMemcpyAsync(sl.hback.p, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess)
       return BS_ERR_CUDA;
+    if (sl.screen) {
+      // per row: job and global A structure, for the certified candidates
+      // (int job[rows] padded to 8 bytes, then int64 structure[rows])
+      const size_t jbytes = ((size_t)rows * 4 + 7) & ~size_t(7);
+      char *rt = ht + plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile);
+      rt = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(rt) + 7) & ~uintptr_t(7));
+      int *rjob = reinterpret_cast<int *>(rt);
+      int64_t *rig = reinterpret_cast<int64_t *>(rt + jbytes);
+      for (int j = 0; j < nj; ++j)
+        for (int64_t t = 0; t < sl.reqs[j]->q; ++t) {
+          rjob[sl.row0[j] + t] = j;
+          rig[sl.row0[j] + t] = plan.jobs[j].first_a + t;
+        }
+      int *drjob = static_cast<int *>(sl.rowtab.p);
+      const int64_t *drig = reinterpret_cast<const int64_t *>(static_cast<char *>(sl.rowtab.p) + jbytes);
+      const int *cj = static_cast<const int *>(sl.cand_j.p);
+      const int *cn = static_cast<const int *>(sl.cand_n.p);
+      if (cudaMemcpyAsync(drjob, rt, jbytes + (size_t)rows * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+          launch_screen_select(dense, static_cast<const float *>(sl.dense_lo.p), rows, bk.n, bk.n, k, kCandCap,
+                               static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) !=
+              cudaSuccess ||
+          launch_exact_candidates(DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a},
+                                  DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b}, b.info_a, b.info_b, b.jobs,
+                                  drjob, drig, rows, cj, cn, kCandCap, static_cast<float *>(sl.cand_v.p),
+                                  sl.st) != cudaSuccess ||
+          launch_topk_rows(static_cast<const float *>(sl.cand_v.p), rows, cn, kCandCap, k, cj,
+                           static_cast<int64_t *>(sl.topi.p), static_cast<float *>(sl.topv.p), sl.st) != cudaSuccess ||
+          cudaMemcpyAsync(sl.hcand_n.p, cn, (size_t)rows * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess)
+        return BS_ERR_CUDA;
+    }
   }
-  if (launch_topk(dense, rows, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p), static_cast<float *>(sl.topv.p),
-                  sl.st) != cudaSuccess ||
+  if ((!sl.screen && launch_topk(dense, rows, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p),
+                                 static_cast<float *>(sl.topv.p), sl.st) != cudaSuccess) ||
       cudaMemcpyAsync(sl.htopi.p, sl.topi.p, (size_t)rows * k * 8, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
       cudaMemcpyAsync(sl.htopv.p, sl.topv.p, (size_t)rows * k * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
       cudaMemcpyAsync(sl.hsc.p, sl.scal.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
@@ -576,6 +625,16 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
     const Bucket &bk = s->buckets[sl.bucket];
     const int k = s->top_k;
     const Job *back = static_cast<const Job *>(sl.hback.p);
+    const int *hcn = sl.screen ? static_cast<const int *>(sl.hcand_n.p) : nullptr;
+    std::vector<int> redo;
+    auto take = [&](Request *r, int64_t row0) {
+      const int64_t *hi = static_cast<const int64_t *>(sl.htopi.p) + row0 * k;
+      const float *hv = static_cast<const float *>(sl.htopv.p) + row0 * k;
+      r->idx.assign(hi, hi + r->q * k);
+      r->val.resize(r->q * k);
+      for (int64_t t = 0; t < r->q * k; ++t) r->val[t] = (double)hv[t];
+      r->pairs = r->q * bk.n;
+    };
     for (int j = 0; j < (int)sl.reqs.size(); ++j) {
       Request *r = sl.reqs[j];
       bs_status st = BS_OK;
@@ -586,19 +645,33 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
           st = plain_fallback(s, sl, j);
           if (st == BS_OK) ++s->fallbacks;
           else msg = "plain fallback failed";
+        } else if (st == BS_OK && hcn) {
+          bool overflow = false;
+          for (int64_t t = 0; t < r->q; ++t) overflow |= hcn[sl.row0[j] + t] > kCandCap;
+          if (overflow) {  // more screen candidates than kept: certify the whole row
+            redo.push_back(j);
+            continue;
+          }
         }
       } else if (sc.err & kErrNonFinite) {
         st = BS_ERR_NONFINITE;
         msg = "input coordinates contain NaN or Inf";
       }
-      if (st == BS_OK) {
-        const int64_t *hi = static_cast<const int64_t *>(sl.htopi.p) + sl.row0[j] * k;
-        const float *hv = static_cast<const float *>(sl.htopv.p) + sl.row0[j] * k;
-        r->idx.assign(hi, hi + r->q * k);
-        r->val.resize(r->q * k);
-        for (int64_t t = 0; t < r->q * k; ++t) r->val[t] = (double)hv[t];
-        r->pairs = r->q * bk.n;
-      }
+      if (st == BS_OK) take(r, sl.row0[j]);
+      complete(s, r, st, msg);
+    }
+    // rows whose screen band held more candidates than kept: every pair of
+    // the request certified densely, synchronously on this slot
+    std::vector<Request *> all = sl.reqs;
+    for (int j : redo) {
+      Request *r = all[j];
+      sl.reqs.assign(1, r);
+      bs_status st = launch_query_batch(s, sl, false);
+      if (st == BS_OK && cudaStreamSynchronize(sl.st) != cudaSuccess) st = BS_ERR_CUDA;
+      std::string msg;
+      if (st == BS_OK)
+        st = collect_errors(*static_cast<const DevScalars *>(sl.hsc.p), static_cast<const Job *>(sl.hback.p), 1, msg);
+      if (st == BS_OK) take(r, 0);
       complete(s, r, st, msg);
     }
   }
@@ -700,7 +773,7 @@ void sched_loop(bs_server *s) {
       ++s->batches;
       if (r0->kind == 0) s->rows_batched += rows;
       // release the unused part of this slot's buffers before growing others
-      const bs_status st = r0->kind == 0 ? launch_query_batch(s, sl) : launch_cluster_batch(s, sl);
+      const bs_status st = r0->kind == 0 ? launch_query_batch(s, sl, true) : launch_cluster_batch(s, sl);
       if (st) {
         cudaGetLastError();
         cudaStreamSynchronize(sl.st);
