@@ -39,6 +39,7 @@ class CrmsdOptions:
     out_type: str = "f64"
     tolerance: Optional[float] = None
     graph: bool = True  # replay a captured CUDA graph for repeated shapes
+    autotune: bool = False  # time the tile shapes per set class (mixed path)
 
     def to_c(self) -> _l.bs_opts:
         o = _l.bs_opts()
@@ -47,7 +48,7 @@ class CrmsdOptions:
         o.layout = _l.LAYOUT[self.layout]
         o.out_type = _l.OUT_TYPE[self.out_type]
         o.tolerance = float(self.tolerance or 0.0)
-        o.flags = 0 if self.graph else _l.FLAG_NO_GRAPH
+        o.flags = (0 if self.graph else _l.FLAG_NO_GRAPH) | (_l.FLAG_AUTOTUNE if self.autotune else 0)
         return o
 
 
@@ -201,6 +202,16 @@ class Engine:
         o = opts.to_c()
         self._check(self._lib.bs_batched(self._h, descs, len(sets), ctypes.byref(o)))
         return mats
+
+    def tile_shape(self, L: int, n: int):
+        """The autotuner's choice for sets of L atoms and n structures:
+        "narrow" (40 x 10 tiles), "wide" (40 x 20), or None if not timed."""
+        v = ctypes.c_int32()
+        self._check(self._lib.bs_tune_get(self._h, int(L), int(n), ctypes.byref(v)))
+        return None if v.value < 0 else ("narrow" if v.value else "wide")
+
+    def set_tile_shape(self, L: int, n: int, shape: str):
+        self._check(self._lib.bs_tune_set(self._h, int(L), int(n), 1 if shape == "narrow" else 0))
 
     def pairs(self, xyz, ii, jj, opts: Optional[CrmsdOptions] = None, out=None):
         opts = opts or CrmsdOptions()

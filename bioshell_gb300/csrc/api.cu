@@ -101,7 +101,8 @@ bs_status check_opts(bs_ctx *ctx, const bs_opts *o) {
     return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.layout %d unknown", o->layout);
   if (o->out_type != BS_OUT_F64 && o->out_type != BS_OUT_F32)
     return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.out_type %d unknown", o->out_type);
-  if (o->flags & ~BS_FLAG_NO_GRAPH) return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.flags %d unknown", o->flags);
+  if (o->flags & ~(BS_FLAG_NO_GRAPH | BS_FLAG_AUTOTUNE))
+    return set_err(ctx, BS_ERR_INVALID_ARG, "bs_opts.flags %d unknown", o->flags);
   return BS_OK;
 }
 
@@ -195,6 +196,7 @@ std::vector<int64_t> plan_key(bs_ctx *ctx, const Plan &plan, unsigned long long 
   for (const Job &j : plan.jobs) {
     k.push_back(j.n);
     k.push_back(j.L);
+    k.push_back(j.narrow);
   }
   return k;
 }
@@ -273,6 +275,74 @@ bs_status finish_mixed(bs_ctx *ctx, int nj) {
   return BS_OK;
 }
 
+// ---------------------------------------------------------- autotuner
+// Shape class of a structure set: 64-atom chain bucket and log2 of its size.
+int64_t tune_key(int L, int64_t n) {
+  int nb = 1;
+  while ((1ll << nb) < n) ++nb;
+  return (int64_t)(pitch_for(L) / kKChunk) * 64 + nb;
+}
+
+// Times 40 x 20 against 40 x 10 tiles on a synthetic set of the class (the
+// class's upper size, at most 2048 structures, random 3.8 A chains of the
+// set's length) and caches the faster; ties go to the wide tiles, which
+// issue half the tensor-core instructions per pair.
+bs_status tune_class(bs_ctx *ctx, int L, int64_t n_real, float tol, int &narrow, bool &tuned) {
+  const int64_t key = tune_key(L, n_real);
+  auto it = ctx->tune.find(key);
+  tuned = false;
+  if (it != ctx->tune.end()) {
+    narrow = it->second;
+    return BS_OK;
+  }
+  const int64_t n = std::max<int64_t>(2, std::min<int64_t>(1ll << (key % 64), 2048));
+  std::vector<double> xyz((size_t)n * L * 3);
+  uint64_t st = 0x9e3779b97f4a7c15ull ^ (uint64_t)key;
+  auto rnd = [&]() {  // uniform in [-1, 1)
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return (double)(st >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  };
+  for (int64_t s = 0; s < n; ++s) {
+    double p[3] = {0, 0, 0};
+    for (int k = 0; k < L; ++k) {
+      double d[3] = {rnd(), rnd(), rnd()};
+      const double nd = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) + 1e-9;
+      for (int c = 0; c < 3; ++c) {
+        p[c] += 3.8 * d[c] / nd;
+        xyz[((size_t)s * L + k) * 3 + c] = p[c];
+      }
+    }
+  }
+  bs_status stt;
+  if ((stt = ensure(ctx, ctx->pout, xyz.size() * 8, "autotuner coordinates"))) return stt;
+  if ((stt = ensure(ctx, ctx->out, (size_t)(n * (n - 1) / 2) * 4, "autotuner result"))) return stt;
+  CK(cudaMemcpy(ctx->pout.p, xyz.data(), xyz.size() * 8, cudaMemcpyHostToDevice), "autotuner coordinates");
+  float best[2] = {1e30f, 1e30f};
+  for (int v = 0; v < 2; ++v) {
+    std::vector<JobSpec> specs{JobSpec{static_cast<const double *>(ctx->pout.p), n, L,
+                                       OutDesc{ctx->out.p, n, n, kLayoutTriangle, 1}, v}};
+    Plan plan;
+    if (!make_symmetric_plan(specs, tol, true, plan).empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "autotuner plan");
+    MixedBuffers b;
+    if ((stt = prepare_buffers(ctx, plan, 4096, b))) return stt;
+    ctx->plan_key.clear();
+    if ((stt = upload_tables(ctx, plan, b, plan_key(ctx, plan, 4096)))) return stt;
+    for (int rep = 0; rep < 3; ++rep) {
+      if ((stt = launch_plan(ctx, plan, b, false))) return stt;
+      CK(cudaStreamSynchronize(ctx->stream), "autotuner run");
+      if ((stt = finish_mixed(ctx, 1))) return stt;
+      if (rep > 0) best[v] = std::min(best[v], elapsed(ctx, 2, 3));
+    }
+  }
+  ctx->plan_key.clear();
+  narrow = best[1] < 0.97f * best[0] ? 1 : 0;
+  ctx->tune[key] = narrow;
+  tuned = true;
+  return BS_OK;
+}
+
 // ---------------------------------------------------------- all-vs-all
 struct SetIO {
   const double *xyz_dev;
@@ -299,6 +369,19 @@ bs_status plain_set(bs_ctx *ctx, const double *dxyz, int64_t n, int L, const Out
 bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_opts &o) {
   ctx->metrics = bs_metrics{};
   const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
+  // tile shape per set (autotuner, mixed path), before anything is staged
+  std::vector<int> narrow(nsets, 0);
+  int tuned_classes = 0;
+  if ((o.flags & BS_FLAG_AUTOTUNE) && o.precision == BS_PRECISION_MIXED) {
+    for (int k = 0; k < nsets; ++k) {
+      if (sets[k].n < 2) continue;
+      bool tuned = false;
+      const bs_status ts = tune_class(ctx, sets[k].L, sets[k].n, total_tolerance(o), narrow[k], tuned);
+      if (ts) return ts;
+      tuned_classes += tuned ? 1 : 0;
+    }
+    ctx->metrics = bs_metrics{};
+  }
   // staging of host inputs / outputs
   std::vector<SetIO> io(nsets);
   size_t in_bytes = 0, out_bytes = 0;
@@ -339,7 +422,8 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     const OutDesc od{io[k].out_dev, d.n, d.n, layout, o.out_type};
     if (o.layout == BS_LAYOUT_SQUARE)
       CK(cudaMemset2DAsync(io[k].out_dev, (size_t)(d.n + 1) * esz, 0, esz, (size_t)d.n, ctx->stream), "zero diagonal");
-    specs.push_back(JobSpec{io[k].xyz_dev, d.n, d.L, od});
+    specs.push_back(JobSpec{io[k].xyz_dev, d.n, d.L, od, narrow[k]});
+    ctx->metrics.narrow_jobs += narrow[k];
   }
   if (o.precision == BS_PRECISION_PLAIN64) {
     CK(cudaMemsetAsync(ctx->scal.p, 0, sizeof(DevScalars), ctx->stream), "clear counters");
@@ -389,6 +473,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     }
   }
   ctx->metrics.pairs = pairs;
+  ctx->metrics.tuned_classes = tuned_classes;
   ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
   ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
   ctx->metrics.ms_main = elapsed(ctx, 2, 3);
@@ -646,6 +731,19 @@ BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets,
   if ((s = validate_sets(ctx, sets, nsets))) return s;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
   return sets_impl(ctx, sets, nsets, o);
+}
+
+BS_API bs_status bs_tune_get(bs_ctx *ctx, int32_t L, int64_t n, int32_t *narrow) {
+  if (!ctx || !narrow || L < 1 || n < 1) return BS_ERR_INVALID_ARG;
+  auto it = ctx->tune.find(tune_key(L, n));
+  *narrow = it == ctx->tune.end() ? -1 : it->second;
+  return BS_OK;
+}
+
+BS_API bs_status bs_tune_set(bs_ctx *ctx, int32_t L, int64_t n, int32_t narrow) {
+  if (!ctx || L < 1 || n < 1 || (narrow != 0 && narrow != 1)) return BS_ERR_INVALID_ARG;
+  ctx->tune[tune_key(L, n)] = narrow;
+  return BS_OK;
 }
 
 BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii, const int64_t *jj,

@@ -5,6 +5,7 @@
 #pragma once
 #include <cudaTypedefs.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -37,12 +38,14 @@ struct MixedBuffers {
   DevScalars *sc = nullptr;
 };
 
-// A symmetric job as the host describes it (device coordinates and output).
+// A symmetric job as the host describes it (device coordinates and output;
+// narrow: 40 x 10 tiles, chosen by the autotuner for small sets).
 struct JobSpec {
   const double *xyz;
   int64_t n;
   int L;
   OutDesc out;
+  int narrow = 0;
 };
 
 struct Plan {
@@ -103,6 +106,8 @@ struct bs_ctx {
   std::vector<Graph> graphs;
   uint64_t tick = 0;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  // autotuner: shape class (64-atom chain bucket, log2 size) -> narrow tiles
+  std::map<int64_t, int> tune;
 };
 
 namespace bs {

@@ -78,6 +78,7 @@ struct Job {
   float norm_b[3];
   float qres_b;           // largest B-side quantisation residual RMS
   int screen;             // 1: rectangular screen job (bounds from the leading levels)
+  int narrow;             // 1: tiles of 40 x 10 structures (MMA N = 32) instead of 40 x 20
   void *out_lo;           // screen jobs: lower bounds, same layout as `out` (upper bounds)
   // ---- device (preparation)
   unsigned long long maxabs;        // max |centred coordinate|, fixed-point units
@@ -136,15 +137,17 @@ __host__ __device__ inline unsigned long long flag_pack(int job, int64_t i, int6
   return ((unsigned long long)job << 48) | ((unsigned long long)i << 24) | (unsigned long long)j;
 }
 
-// Tensor-core tile: A block (40 structures), B block (20 structures), job,
-// and the job's shape (16-atom steps | accumulator layout << 16), written on
-// the device once the preparation has chosen the layout, so that the TMA and
-// MMA threads read one record per tile.
+// Tensor-core tile: A block (40 structures), B block (20 structures; 10 for
+// a narrow job's tiles), job, and the job's shape (16-atom steps | layout <<
+// 16 | narrow << 24), written on the device once the preparation has chosen
+// the layout, so that the TMA and MMA threads read one record per tile.
 struct __align__(16) Tile {
   int a_blk, b_blk, job, shape;
 };
 __host__ __device__ inline int tile_nk16(const Tile &t) { return t.shape & 0xffff; }
-__host__ __device__ inline int tile_layout(const Tile &t) { return t.shape >> 16; }
+__host__ __device__ inline int tile_layout(const Tile &t) { return (t.shape >> 16) & 0xff; }
+__host__ __device__ inline bool tile_narrow(const Tile &t) { return (t.shape >> 24) & 1; }
+constexpr int kNarrowStructs = 10;  // B structures of a narrow tile (one 32-row group)
 
 // ------------------------------------------------------------- launches
 // prep.cu -- mixed path, all jobs of a launch at once

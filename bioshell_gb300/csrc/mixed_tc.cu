@@ -64,13 +64,14 @@ struct __align__(16) TileMeta {
   OutDesc out;
   void *out_lo;
   long long n, n_b, first_a, first_b;
-  int a_blk, b_blk, job, mode, err, layout, L;
+  int a_blk, b_blk, job, mode, err, layout, L, narrow;
   float tol, u, d34, dtrunc;
 };
 constexpr int kMetaBytes = 2 * (int)sizeof(TileMeta);
 constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes + kBarBytes;
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr uint32_t kIdesc = ptx::idesc_bf16_f32(128, kBRows);
+constexpr uint32_t kIdescNarrow = ptx::idesc_bf16_f32(128, 32);  // narrow tiles: first 32 B rows
 
 struct Shared {
   uint64_t full[kStages];
@@ -169,7 +170,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
         const Tile tile = next;
         if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
-        const int rowA = tile.a_blk * kBlockRows, rowB = tile.b_blk * kBRows;
+        const int rowA = tile.a_blk * kBlockRows;
+        const int rowB = tile_narrow(tile) ? tile.b_blk * kGroupRows : tile.b_blk * kBRows;
         const int nchunks = (tile_nk16(tile) * 16 + kKChunk - 1) / kKChunk;
         const bool scr = tile_layout(tile) == kAccScreen;
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
@@ -214,6 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int nk16 = tile_nk16(tile);
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
         const int lay = tile_layout(tile);
+        const uint32_t idesc = tile_narrow(tile) ? kIdescNarrow : kIdesc;
         const uint32_t need = lay == kAccLong ? 2u : 1u;
         bool ok = true;
         for (uint32_t u = 0; u < need && ok; ++u) {
@@ -275,15 +278,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                 acc[lv] = (k > 0 && acc_index(lay, lv, k - 1, nk16) == ai) ? 1u : 0u;
               }
             }
-            ptx::tc_mma_f16(col[0], da0, db0, kIdesc, acc[0]);
-            ptx::tc_mma_f16(col[1], da0, db1, kIdesc, acc[1]);
-            ptx::tc_mma_f16(col[1], da1, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(col[2], da0, db2, kIdesc, acc[2]);
-            ptx::tc_mma_f16(col[2], da1, db1, kIdesc, 1u);
-            ptx::tc_mma_f16(col[2], da2, db0, kIdesc, 1u);
-            ptx::tc_mma_f16(col[3], da1, db2, kIdesc, acc[3]);
-            ptx::tc_mma_f16(col[3], da2, db1, kIdesc, 1u);
-            ptx::tc_mma_f16(col[3], da3, db2, kIdesc, 1u);
+            ptx::tc_mma_f16(col[0], da0, db0, idesc, acc[0]);
+            ptx::tc_mma_f16(col[1], da0, db1, idesc, acc[1]);
+            ptx::tc_mma_f16(col[1], da1, db0, idesc, 1u);
+            ptx::tc_mma_f16(col[2], da0, db2, idesc, acc[2]);
+            ptx::tc_mma_f16(col[2], da1, db1, idesc, 1u);
+            ptx::tc_mma_f16(col[2], da2, db0, idesc, 1u);
+            ptx::tc_mma_f16(col[3], da1, db2, idesc, acc[3]);
+            ptx::tc_mma_f16(col[3], da2, db1, idesc, 1u);
+            ptx::tc_mma_f16(col[3], da3, db2, idesc, 1u);
           }
           ptx::tc_commit(&sh->empty[s]);
         }
@@ -321,6 +324,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         mt.mode = jb.mode;
         mt.err = jb.err;
         mt.layout = jb.layout;
+        mt.narrow = jb.narrow;
         mt.L = jb.L;
         mt.tol = jb.tol;
         mt.u = jb.u;
@@ -330,7 +334,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       // per-structure data of the tile's A and B blocks (pads and structures
       // past a job's end read as zero; the epilogue never uses them)
-      const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs, b0 = (int64_t)tile.b_blk * kBStructs;
+      const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs;
+      const int64_t b0 = (int64_t)tile.b_blk * (jb.narrow ? kNarrowStructs : kBStructs);
       const int64_t aend = jb.first_a + jb.n, bend = jb.first_b + jb.n_b;
       for (int k = lane; k < kBlockStructs + kBStructs; k += 32) {
         const int64_t gs = k < kBlockStructs ? a0 + k : b0 + (k - kBlockStructs);
@@ -383,6 +388,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       const OutDesc out = mt.out;
       const float t_d34 = mt.d34, t_u = mt.u, t_tol = mt.tol;
       const int t_L = mt.L, t_job = mt.job;
+      // first B structure of this warp's column group (narrow tiles: group 1 has none)
+      const int64_t jg0 = (int64_t)mt.b_blk * (mt.narrow ? kNarrowStructs : kBStructs) + g * kGroupStructs;
+      const bool cols_ok = !(mt.narrow && g == 1);
       if (mt.layout == kAccScreen) {
         // ---- screen tile: crmsd bounds from levels 0 and 1 (FP32)
         const float t_dtrunc = mt.dtrunc;
@@ -437,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
       const int64_t ig = (int64_t)mt.a_blk * kBlockStructs + qd * kGroupStructs + il;
       const int64_t i = ig - fa;
-      const bool row_ok = job_ok && (lane < 30) && (i < jn);
+      const bool row_ok = job_ok && cols_ok && (lane < 30) && (i < jn);
       const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
       const bool dump = (a.dbg != nullptr) && (mt.a_blk == 0) && (mt.b_blk < 2) && !lng;
       // The group's 10 column structures are finished in two halves of five
@@ -475,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int sl = 0; sl < 2; ++sl) {
           const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
           const int jc = jh < 5 ? jh : 4;
-          const int64_t jg = (int64_t)mt.b_blk * kBStructs + g * kGroupStructs + 5 * h + jh;
+          const int64_t jg = jg0 + 5 * h + jh;
           jj[sl] = jg - fb;
           valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
           ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
@@ -569,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 __global__ void k_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
     const Job &jb = jobs[tiles[t].job];
-    tiles[t].shape = (jb.lp / 16) | (jb.layout << 16);
+    tiles[t].shape = (jb.lp / 16) | (jb.layout << 16) | (jb.narrow << 24);
   }
 }
 

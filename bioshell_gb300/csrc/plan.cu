@@ -33,6 +33,7 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
     jb.scale_min = -1000;
     jb.tol = tol;
     jb.allow_long = 1;
+    jb.narrow = s.narrow ? 1 : 0;
     const int64_t nb = blocks_for(s.n);
     for (int64_t b = 0; b < nb; ++b) plan.jobmap.push_back(j);
     blk += nb;
@@ -54,12 +55,15 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
   for (int j : order) {
     const Job &jb = plan.jobs[j];
     if (jb.n < 2) continue;
-    const int64_t nba = blocks_for(jb.n), nbb = (jb.n + kBStructs - 1) / kBStructs;
-    const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / kBStructs;
+    // B blocks of bs structures; tile (I, J) holds a pair i < j iff
+    // bs J + bs - 1 > 40 I, i.e. J >= r I with r = 40 / bs
+    const int64_t bs = jb.narrow ? kNarrowStructs : kBStructs, r = kBlockStructs / bs;
+    const int64_t nba = blocks_for(jb.n), nbb = (jb.n + bs - 1) / bs;
+    const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / bs;
     for (int64_t sa = 0; sa < nba; sa += SA)
-      for (int64_t sb = 2 * sa; sb < nbb; sb += SB)
+      for (int64_t sb = r * sa; sb < nbb; sb += SB * r / 2)
         for (int64_t I = sa; I < std::min(sa + SA, nba); ++I)
-          for (int64_t J = std::max(sb, 2 * I); J < std::min(sb + SB, nbb); ++J)
+          for (int64_t J = std::max(sb, r * I); J < std::min(sb + SB * r / 2, nbb); ++J)
             plan.tiles.push_back(Tile{(int)(a0 + I), (int)(b0 + J), j, 0});
   }
   return "";

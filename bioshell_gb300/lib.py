@@ -25,6 +25,7 @@ LAYOUT = {"triangle": 0, "square": 1}
 OUT_TYPE = {"f64": 0, "f32": 1}
 LINK = {"single": 0, "complete": 1, "average": 2, "median": 3, "centroid": 4, "ward": 5}
 FLAG_NO_GRAPH = 1
+FLAG_AUTOTUNE = 2
 
 
 class bs_opts(ctypes.Structure):
@@ -44,7 +45,8 @@ class bs_metrics(ctypes.Structure):
                 ("ms_refine", ctypes.c_double), ("ms_d2h", ctypes.c_double), ("scale_exp", ctypes.c_int32),
                 ("main_launches", ctypes.c_int32), ("jobs", ctypes.c_int32), ("graph", ctypes.c_int32),
                 ("quant_bound", ctypes.c_double),
-                ("bytes_h2d", ctypes.c_int64), ("bytes_d2h", ctypes.c_int64)]
+                ("bytes_h2d", ctypes.c_int64), ("bytes_d2h", ctypes.c_int64), ("narrow_jobs", ctypes.c_int32),
+                ("tuned_classes", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -89,6 +91,8 @@ SIGNATURES = [
     ("bs_ctx_stream", ctypes.c_void_p, [_vp]),
     ("bs_crmsd", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _dp]),
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
+    ("bs_tune_get", ctypes.c_int32, [_vp, ctypes.c_int32, ctypes.c_int64, _i32p]),
+    ("bs_tune_set", ctypes.c_int32, [_vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32]),
     ("bs_batched", ctypes.c_int32, [_vp, ctypes.POINTER(bs_set_desc), ctypes.c_int32, ctypes.POINTER(bs_opts)]),
     ("bs_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                   ctypes.POINTER(bs_opts), _vp]),

@@ -108,7 +108,13 @@ enum {
   /* Launch the mixed-path kernels one by one instead of replaying a CUDA
    * graph captured for the call's shape (a graph is captured the first time
    * a shape is seen and replayed for every later call of that shape). */
-  BS_FLAG_NO_GRAPH = 1
+  BS_FLAG_NO_GRAPH = 1,
+  /* Mixed path: pick each structure set's tile shape (40 x 20 structures,
+   * or 40 x 10, which wastes fewer pair slots on small sets but costs twice
+   * the tensor-core instructions per pair) by timing both on a synthetic set
+   * of the same chain-length and size class the first time the class is
+   * seen on the context; the choice is cached for later calls. */
+  BS_FLAG_AUTOTUNE = 2
 };
 
 /* Per-call counters of the last compute call on a context. */
@@ -130,6 +136,8 @@ typedef struct {
   double quant_bound;      /* mixed path: worst RMSD change from the grid    */
   int64_t bytes_h2d;
   int64_t bytes_d2h;
+  int32_t narrow_jobs;     /* structure sets run with 40 x 10 tiles          */
+  int32_t tuned_classes;   /* shape classes the autotuner timed in this call */
 } bs_metrics;
 
 /* ---- version / errors -------------------------------------------------- */
@@ -179,6 +187,13 @@ typedef struct {
  * error budget, so a set's result does not depend on the other sets in the
  * call.  The plain path runs the sets one after another. */
 BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets, const bs_opts *opts);
+
+/* The autotuner's cache of a context: the tile shape of the class of sets
+ * with chain length L and size n (narrow = 1: 40 x 10 tiles, 0: 40 x 20).
+ * bs_tune_get returns -1 for a class not timed yet; bs_tune_set fixes a
+ * class's choice (it is then not timed). */
+BS_API bs_status bs_tune_get(bs_ctx *ctx, int32_t L, int64_t n, int32_t *narrow);
+BS_API bs_status bs_tune_set(bs_ctx *ctx, int32_t L, int64_t n, int32_t narrow);
 
 /* crmsd of an explicit pair list: out[t] = crmsd(xyz[ii[t]], xyz[jj[t]]),
  * f64.  Used for sampled checks and for sparse consumers. */

@@ -150,3 +150,27 @@ def test_batched_rejects_bad_sets(engine):
     # the context stays usable
     ok = engine.batched(_sets(11, [(10, 20)]))
     assert np.all(ok[0].values >= 0)
+
+
+def test_narrow_tiles_match_wide_bit_for_bit(engine):
+    # the same exact integer level sums on 40 x 10 tiles (MMA N = 32)
+    sets = _sets(12, [(57, 70), (130, 200), (23, 500), (3, 40)])
+    wide = [m.values for m in engine.batched(sets, CrmsdOptions(graph=False))]
+    for x in sets:
+        engine.set_tile_shape(x.shape[1], x.shape[0], "narrow")
+    narrow = engine.batched(sets, CrmsdOptions(graph=False, autotune=True))
+    assert engine.metrics()["narrow_jobs"] == len(sets)
+    for u, v in zip(wide, narrow):
+        np.testing.assert_array_equal(u, v.values)
+
+
+def test_autotuner_times_each_class_once(engine):
+    sets = _sets(13, [(61, 90), (62, 90), (900, 300)])
+    engine.batched(sets, CrmsdOptions(autotune=True))
+    m = engine.metrics()
+    assert 1 <= m["tuned_classes"] <= 2  # the first two sets share a class
+    assert engine.tile_shape(90, 61) in ("wide", "narrow")
+    again = engine.batched(sets, CrmsdOptions(autotune=True))
+    assert engine.metrics()["tuned_classes"] == 0
+    for x, mtx in zip(sets, again):
+        np.testing.assert_array_equal(mtx.values, engine.all_vs_all(x).values)
