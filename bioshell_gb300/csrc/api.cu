@@ -919,6 +919,13 @@ BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t g
   return BS_OK;
 }
 
+BS_API bs_status bs_selftest_screen(const float *m9, double gsum, double de, double dr, int32_t scale_exp, int32_t L,
+                                    float *lo, float *hi) {
+  if (!m9 || !lo || !hi || L < 1) return BS_ERR_INVALID_ARG;
+  bsm::screen_bracket(m9, (float)gsum, (float)de, (float)dr, ldexpf(1.0f, 2 * scale_exp), L, *lo, *hi);
+  return BS_OK;
+}
+
 BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t L, int32_t scale_exp, double *rmsd) {
   if (!na || !nb || !rmsd || L < 1) return BS_ERR_INVALID_ARG;
   long long mh[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};

@@ -97,6 +97,62 @@ inline ColMin column_min(const std::vector<float> &m, int64_t n, int64_t j) {
 
 }  // namespace
 
+namespace {
+
+// OPTICS (optics.rs:51-148) with the neighbour lists supplied by a callback
+// that fills `nb` with {j, d} for d <= eps, the point itself included,
+// stably sorted by distance from a list in ascending j.
+template <typename Neighbors>
+void optics_run(int64_t n, double eps, int32_t min_points, Neighbors &&neighbors_of,
+                std::vector<std::pair<int64_t, double>> &nb, int64_t *order_out, double *reach_out,
+                int64_t *cluster_of) {
+  const double undefined = eps * 10.0;
+  std::vector<double> reach((size_t)n, undefined);
+  std::vector<char> processed((size_t)n, 0);
+  std::vector<int64_t> order, seeds;
+  order.reserve((size_t)n);
+  auto by_reach = [&](int64_t a, int64_t b) { return reach[a] < reach[b]; };
+  auto update = [&]() {
+    const double core = nb[(size_t)min_points - 1].second;
+    for (const auto &p : nb) {
+      if (processed[p.first]) continue;
+      const double nr = std::max(p.second, core);
+      if (reach[p.first] == undefined) seeds.push_back(p.first);
+      if (reach[p.first] > nr) reach[p.first] = nr;
+    }
+    std::stable_sort(seeds.begin(), seeds.end(), by_reach);
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    if (processed[i]) continue;
+    order.push_back(i);
+    neighbors_of(i);
+    processed[i] = 1;
+    if ((int64_t)nb.size() < min_points) continue;
+    seeds.clear();
+    update();
+    while (!seeds.empty()) {
+      const int64_t pi = seeds[0];
+      seeds[0] = seeds.back();
+      seeds.pop_back();
+      std::stable_sort(seeds.begin(), seeds.end(), by_reach);
+      order.push_back(pi);
+      neighbors_of(pi);
+      processed[pi] = 1;
+      if ((int64_t)nb.size() < min_points) continue;
+      update();
+    }
+  }
+  int64_t label = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    if (k > 0 && reach[order[k]] == undefined) ++label;
+    cluster_of[order[k]] = label;
+    order_out[k] = order[k];
+    reach_out[k] = reach[order[k]];
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 BS_API bs_status bs_hierarchical(const void *tri, int64_t n, int32_t out_type, int32_t rule, int64_t *merges,
@@ -251,12 +307,7 @@ BS_API bs_status bs_optics(const void *tri, int64_t n, int32_t out_type, double 
   if (out_type != BS_OUT_F64 && out_type != BS_OUT_F32) return BS_ERR_INVALID_ARG;
   if (n == 0) return BS_OK;
   const Tri t{tri, n, out_type};
-  const double undefined = eps * 10.0;
-  std::vector<double> reach((size_t)n, undefined);
-  std::vector<char> processed((size_t)n, 0);
-  std::vector<int64_t> order, seeds;
   std::vector<std::pair<int64_t, double>> nb;
-  order.reserve((size_t)n);
   auto neighbors_of = [&](int64_t i) {
     nb.clear();
     for (int64_t j = 0; j < n; ++j) {
@@ -265,45 +316,44 @@ BS_API bs_status bs_optics(const void *tri, int64_t n, int32_t out_type, double 
     }
     std::stable_sort(nb.begin(), nb.end(), [](const auto &a, const auto &b) { return a.second < b.second; });
   };
-  auto by_reach = [&](int64_t a, int64_t b) { return reach[a] < reach[b]; };
-  auto update = [&]() {
-    const double core = nb[(size_t)min_points - 1].second;
-    for (const auto &p : nb) {
-      if (processed[p.first]) continue;
-      const double nr = std::max(p.second, core);
-      if (reach[p.first] == undefined) seeds.push_back(p.first);
-      if (reach[p.first] > nr) reach[p.first] = nr;
-    }
-    std::stable_sort(seeds.begin(), seeds.end(), by_reach);
-  };
-  for (int64_t i = 0; i < n; ++i) {
-    if (processed[i]) continue;
-    order.push_back(i);
-    neighbors_of(i);
-    processed[i] = 1;
-    if ((int64_t)nb.size() < min_points) continue;
-    seeds.clear();
-    update();
-    while (!seeds.empty()) {
-      const int64_t pi = seeds[0];
-      seeds[0] = seeds.back();
-      seeds.pop_back();
-      std::stable_sort(seeds.begin(), seeds.end(), by_reach);
-      order.push_back(pi);
-      neighbors_of(pi);
-      processed[pi] = 1;
-      if ((int64_t)nb.size() < min_points) continue;
-      update();
-    }
-  }
-  int64_t label = 0;
-  for (int64_t k = 0; k < n; ++k) {
-    if (k > 0 && reach[order[k]] == undefined) ++label;
-    cluster_of[order[k]] = label;
-    order_out[k] = order[k];
-    reach_out[k] = reach[order[k]];
-  }
+  optics_run(n, eps, min_points, neighbors_of, nb, order_out, reach_out, cluster_of);
   return BS_OK;
+}
+
+BS_API bs_status bs_optics_neighbors(const int64_t *row_ptr, const int32_t *col, const float *dist, int64_t n,
+                                     double eps, int32_t min_points, int64_t *order_out, double *reach_out,
+                                     int64_t *cluster_of) {
+  if (n < 0 || min_points < 1 || !(eps > 0.0)) return BS_ERR_INVALID_ARG;
+  if (n > 0 && (!row_ptr || !order_out || !reach_out || !cluster_of)) return BS_ERR_INVALID_ARG;
+  if (n == 0) return BS_OK;
+  if (row_ptr[0] != 0 || (row_ptr[n] > 0 && (!col || !dist))) return BS_ERR_INVALID_ARG;
+  for (int64_t i = 0; i < n; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return BS_ERR_INVALID_ARG;
+  std::vector<std::pair<int64_t, double>> nb;
+  bool bad = false;
+  auto neighbors_of = [&](int64_t i) {
+    // the row's list, ordered by (d, j), with the point itself (d = 0) put
+    // where a stable sort of the ascending-j scan would put it
+    nb.clear();
+    bool self = false;
+    for (int64_t e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+      const int64_t j = col[e];
+      const double d = (double)dist[e];
+      if (j < 0 || j >= n || j == i) {
+        bad = true;
+        continue;
+      }
+      if (!(d <= eps)) continue;
+      if (!self && (0.0 < d || (d == 0.0 && i < j))) {
+        nb.emplace_back(i, 0.0);
+        self = true;
+      }
+      nb.emplace_back(j, d);
+    }
+    if (!self) nb.emplace_back(i, 0.0);
+  };
+  optics_run(n, eps, min_points, neighbors_of, nb, order_out, reach_out, cluster_of);
+  return bad ? BS_ERR_INVALID_ARG : BS_OK;
 }
 
 }  // extern "C"

@@ -171,51 +171,66 @@ BS_HD float qcp_top_eig(const float s[9], float &xout, float q[4]) {
   return best;
 }
 
-// Largest root x of the normalised QCP quartic of sn = S / lambda0 (x <= 1):
-// the Halley iterations of qcp_top_eig, without the eigenvector.
-BS_HD float qcp_top_root(const float s[9]) {
-  const Key k = key_from_s(s);
-  float fro2 = 0.f;
-#pragma unroll
-  for (int i = 0; i < 9; ++i) fro2 = fmaf(s[i], s[i], fro2);
-  const float c2 = -2.f * fro2;
-  const float c1 = -8.f * det3f(s);
-  const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
-  float x = 1.0f;
-#pragma unroll
-  for (int it = 0; it < 5; ++it) {
-    const float x2 = x * x;
-    const float p = fmaf(fmaf(x2 + c2, x, c1), x, c0);
-    const float dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
-    const float ddp = fmaf(12.f, x2, 2.f * c2);
-    const float den = fmaf(2.f * dp, dp, -p * ddp);
-    const float step = BS_FDIV(2.f * p * dp, den);
-    x = (den > 0.f) ? x - step : x;
-  }
-  return x;
-}
-
-// Screen of one pair from the leading levels only (m = S0 + 2^-9 S1, units
-// 2^28 u): E = (Ga+Gb)(1 - x) in FP32, and crmsd bounds lo <= crmsd <= hi
-// from dtrunc (bound on what the omitted levels move E, units u) plus
-// 2^-16 (Ga+Gb) for the FP32 arithmetic -- a margin far above the FP32
-// eigenvalue error of the well-conditioned top root (~2^-22 (Ga+Gb)).
-BS_HD void screen_bounds(const float m[9], float gsum_f, float dtrunc, float u, int L, float &lo, float &hi) {
+// Screen of one pair from digits 0 and 1 only: m = S0 + 2^-9 S1 + 2^-18 S11
+// (S11 = sum e1 e1; units 2^28 u) is the covariance of the truncated
+// structures t = n - d2 (digit 2 dropped), gsum_f their G_a + G_b (units
+// u), de a bound on the FP32 rounding of the accumulated S11 as an error of
+// E (units u; 0 when it is exact).  Returns a bracket
+// lo <= crmsd(n_a, n_b) <= hi without the eigenvector.
+//
+// P(x), the QCP quartic of t normalised by lambda0 = gsum/2, has four real
+// roots (the eigenvalues of the symmetric key matrix over lambda0) and the
+// top one is x* <= sqrt(G_a G_b) / lambda0 <= 1.  Above its largest root a
+// real-rooted polynomial is increasing and convex, so Newton's method from
+// x = 1 decreases monotonically towards x*: every iterate x satisfies
+// x - P(x)/P'(x) >= x*.  And since P'/P = sum 1 / (x - x_i) over the four
+// roots, the root nearest to x -- here x* -- lies within 4 P(x)/P'(x) of x.
+// In FP32 the quartic is known only to within eP = 2^-18 (the rounding of
+// the normalised covariance, of the coefficients -- c0 = det K is a sum of
+// O(1) products -- and of the evaluation; |x| <= 1 and ||K / lambda0|| <= 1
+// keep every term O(1)): eight times the largest |P(x*)| measured in FP32
+// over 11,000 decoy pairs of 64-300 atoms (2^-21.3).  P' is known to within
+// eD = 2^-18 likewise.  With these, for x >= x*:
+//     x - max(P - eP, 0) / (P' + eD)  >=  x*  >=  x - 4 (P + eP) / (P' - eD),
+// widened by 2^-20 for the rounding of the final steps.  The bracket holds whether or not the iteration
+// has converged: near pairs converge in two or three steps, far pairs only
+// need a loose bracket, and where the top root is nearly double (P' small)
+// the bracket widens instead of failing.  Finally crmsd(t) is within dr =
+// rms(d2_a) + rms(d2_b) (Angstrom) of crmsd(n) (Minkowski: each structure
+// moves by the RMS of its dropped digit).
+BS_HD void screen_bracket(const float m[9], float gsum_f, float de, float dr, float u, int L, float &lo,
+                          float &hi) {
   if (!(gsum_f > 0.f)) {
-    lo = hi = 0.f;
+    lo = 0.f;
+    hi = dr;
     return;
   }
-  const float lam0 = gsum_f * 1.862645149230957e-09f;  // 2^-29: (Ga+Gb)/2 in units of m
+  const float lam0 = gsum_f * 1.862645149230957e-09f;  // 2^-29: gsum/2 in units of m
   const float inv = BS_FDIV(1.0f, lam0);
   float sn[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
-  const float x = qcp_top_root(sn);
-  const float e = gsum_f * (1.0f - x);
-  const float de = dtrunc + gsum_f * 1.52587890625e-05f;  // 2^-16
+  const Key k = key_from_s(sn);
+  float fro2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fro2 = fmaf(sn[i], sn[i], fro2);
+  const float c2 = -2.f * fro2;
+  const float c1 = -8.f * det3f(sn);
+  const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
+  constexpr float eP = 3.814697265625e-06f, eD = 3.814697265625e-06f;  // 2^-18
+  float x = 1.0f, p = 0.f, dp = 0.f;
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const float x2 = x * x;
+    p = fmaf(fmaf(x2 + c2, x, c1), x, c0);
+    dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
+    if (it < 3) x -= BS_FDIV(fmaxf(p - eP, 0.f), fmaxf(dp + eD, eD));  // P' >= 0 for x >= x*
+  }
+  const float xhi = fminf(x - BS_FDIV(fmaxf(p - eP, 0.f), fmaxf(dp + eD, eD)) + 9.5367431640625e-07f, 1.0f);  // >= x*
+  const float xlo = dp > eD ? fmaxf(x - BS_FDIV(4.f * (p + eP), dp - eD) - 9.5367431640625e-07f, 0.f) : 0.f;
   const float scale = BS_FDIV(u, (float)L);
-  lo = sqrtf(fmaxf(e - de, 0.f) * scale);
-  hi = sqrtf(fmaxf(e + de, 0.f) * scale);
+  lo = fmaxf(sqrtf(fmaxf(fmaf(gsum_f, 1.0f - xhi, -de), 0.f) * scale) - dr, 0.f);
+  hi = sqrtf(fmaf(gsum_f, 1.0f - xlo, de) * scale) + dr;
 }
 
 // ------------------------------------------------- quaternion -> T = R^T

@@ -26,6 +26,8 @@ struct MixedBuffers {
   long long *ctr = nullptr;  // [structures][3] fixed-point centroids
   SInfo *info_a = nullptr;
   const SInfo *info_b = nullptr;
+  float2 *tinfo_a = nullptr;  // screen jobs only
+  const float2 *tinfo_b = nullptr;
   __nv_bfloat16 *dig_a[4] = {};
   const __nv_bfloat16 *dig_b[3] = {};
   int64_t pitch_a = 0, pitch_b = 0;  // digit row length (atoms)

@@ -60,7 +60,7 @@ constexpr int kLayoutRect = 2;
 // (rectangular).  The host fills the first part; the preparation kernels
 // fill the second on the device, so the whole call sequence needs no host
 // round trip (and can be captured in a CUDA graph).
-struct Job {
+struct __align__(16) Job {  // 16-byte multiple: the tensor-core kernel bulk-copies it
   // ---- host
   const double *xyz;      // [n][L][3] f64 AoS of the A-side structures (device)
   long long n;            // A-side structures
@@ -79,7 +79,6 @@ struct Job {
   float qres_b;           // largest B-side quantisation residual RMS
   int screen;             // 1: rectangular screen job (bounds from the leading levels)
   int narrow;             // 1: tiles of 40 x 10 structures (MMA N = 32) instead of 40 x 20
-  void *out_lo;           // screen jobs: lower bounds, same layout as `out` (upper bounds)
   // ---- device (preparation)
   unsigned long long maxabs;        // max |centred coordinate|, fixed-point units
   unsigned long long norm[4][3];    // per candidate grid: max row sum of squared digits (d0, d1, d2)
@@ -93,7 +92,6 @@ struct Job {
   float d34;                        // rounding bound of accumulator levels 2-3, as an error of E (units u)
   int layout;                       // accumulator layout of the job's tiles (kAcc*)
   int allow_long;                   // (host) the long layout may be chosen
-  float dtrunc;                     // screen jobs: bound on E of the omitted levels (units u)
   int pad2;
 };
 
@@ -160,6 +158,10 @@ struct PrepArgs {
   __nv_bfloat16 *dig[4];           // e0, e1, e2 = 16 d2, d2 / 32
   int64_t pitch;
   SInfo *info;
+  // optional (screen jobs): per structure {G of the coordinates without
+  // digit 2, RMS of digit 2 in Angstrom} -- the truncated structure the
+  // screen's levels 0 and 1 describe, and its distance from the full one
+  float2 *tinfo;
   DevScalars *sc;
 };
 cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st);
@@ -185,6 +187,8 @@ struct TcArgs {
   const Job *jobs;
   const SInfo *info_a;
   const SInfo *info_b;
+  const float2 *tinfo_a;  // screen jobs: truncated-structure data (PrepArgs::tinfo)
+  const float2 *tinfo_b;
   DevScalars *sc;
   unsigned long long *flags;
   unsigned long long flag_cap;
@@ -240,10 +244,16 @@ cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, 
 // from column to reported index (col_map[r * ld + c]; may be null).
 cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, int64_t ld, int k,
                              const int *col_map, int64_t *out_idx, float *out_val, cudaStream_t st);
-// Screen candidates: per row r, every column c with lo[r][c] not above the
-// k-th smallest hi[r][.] (the row's k-th smallest upper bound), up to cap
-// per row (cand_n[r] counts all, so cand_n[r] > cap marks an overflowing row).
-cudaError_t launch_screen_select(const float *hi, const float *lo, int64_t rows, int64_t n, int64_t ld, int k,
-                                 int cap, int *cand_j, int *cand_n, cudaStream_t st);
+// Screen candidates from the packed brackets of a screen job (one word per
+// pair: hi rounded up to half precision in the top 16 bits, lo rounded down
+// in the bottom 16).  Per row r: T[r] = an upper bound of the row's k-th
+// smallest hi -- the top edge of the bin of the 4096-bin histogram of hi
+// (bins of 1/64 of an octave) that holds it -- then every column c with
+// lo[r][c] <= T[r], up to cap per row (cand_n[r] counts all, so
+// cand_n[r] > cap marks an overflowing row).  hist ([rows][4096] u32),
+// thresholds ([rows] u32) and cand_n are scratch the call clears itself.
+constexpr int kScreenBins = 4096;
+cudaError_t launch_screen_select(const uint32_t *packed, int64_t rows, int64_t n, int64_t ld, int k, int cap,
+                                 uint32_t *hist, uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st);
 
 }  // namespace bs

@@ -21,8 +21,14 @@
 // Roles (one persistent CTA per SM, 384 threads):
 //   warp 0  TMA producer: 4 A digit boxes (128 rows x 64 atoms) and 3 B
 //           digit boxes (64 rows x 64 atoms), 128-byte swizzle, 2 stages;
-//   warp 1  MMA issuer (one thread), tcgen05.mma kind::f16, M = 128, N = 64;
+//           and per tile a bulk copy of its job and per-structure data
+//           (kMetaSlots tiles ahead);
+//   warp 1  MMA issuer (one thread), tcgen05.mma kind::f16, M = 128,
+//           N = 64 to 192: one instruction per A digit covers the adjacent
+//           level accumulators its products go to (4 instructions per
+//           16-atom step instead of 9);
 //   warp 2  TMEM allocation (512 columns);
+//   warp 3  idle (keeps the epilogue warps on TMEM lane quarters w % 4);
 //   warps 4-11  epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 (10 row
 //           structures) and column group (w - 4) / 4 (10 column structures);
 //           it stages one level at a time in shared memory, the thread of
@@ -35,6 +41,8 @@
 // own chain length, grid and output.
 // Every mbarrier wait is bounded; a timeout sets an error bit and all roles
 // leave their loops so the block always reaches TMEM deallocation.
+#include <cuda_fp16.h>
+
 #include "crmsd_math.cuh"
 #include "kernels.h"
 #include "ptx.cuh"
@@ -56,30 +64,40 @@ constexpr int kPitch = 33;                               // staging pitch in flo
 constexpr int kEpiStageBytes = kEpiWarps * 32 * kPitch * 4;
 constexpr int kBarBytes = 256;
 
-// What the epilogue needs of one tile, staged in shared memory by warp 3
-// one tile ahead, so that no global load sits on the epilogue's path.
+// What the epilogue needs of one tile: its record, its job and the
+// per-structure data of its A and B blocks, bulk-copied into shared memory by
+// the TMA thread together with the tile's operands, kMetaSlots tiles deep.
+constexpr int kMetaSlots = 4;
 struct __align__(16) TileMeta {
-  SInfo ia[kBlockStructs];  // A-block structures
-  SInfo ib[kBStructs];      // B-block structures
-  OutDesc out;
-  void *out_lo;
-  long long n, n_b, first_a, first_b;
-  int a_blk, b_blk, job, mode, err, layout, L, narrow;
-  float tol, u, d34, dtrunc;
+  SInfo ia[kBlockStructs];   // A-block structures (normal and long tiles)
+  SInfo ib[kBStructs];       // B-block structures
+  float2 ta[kBlockStructs];  // screen tiles: {G, RMS of digit 2} of the truncated structures
+  float2 tb[kBStructs];
+  Job job;
+  Tile tile;
 };
-constexpr int kMetaBytes = 2 * (int)sizeof(TileMeta);
+constexpr int kMetaBytes = kMetaSlots * (int)sizeof(TileMeta);
 constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes + kBarBytes;
+static_assert(kSmemBytes <= 232448, "dynamic shared memory above the 227 KB a block may use");
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr uint32_t kIdesc = ptx::idesc_bf16_f32(128, kBRows);
 constexpr uint32_t kIdescNarrow = ptx::idesc_bf16_f32(128, 32);  // narrow tiles: first 32 B rows
+// One instruction per A digit against several B digits at once: the B digit
+// boxes of a stage lie back to back (64 rows each), so an N = 128 or 192
+// operand starting at digit d spans digits d, d+1 (, d+2), and the product
+// lands in as many adjacent 64-column accumulators -- which is where the
+// levels sit (level l at column 64 l).  An M = 128 instruction costs about
+// the same up to N = 128, so this halves the instruction count.
+constexpr uint32_t kIdesc128 = ptx::idesc_bf16_f32(128, 128);
+constexpr uint32_t kIdesc192 = ptx::idesc_bf16_f32(128, 192);
 
 struct Shared {
   uint64_t full[kStages];
   uint64_t empty[kStages];
   uint64_t tfull[2];
   uint64_t tempty[2];
-  uint64_t mfull[2];   // tile metadata slot written (warp 3)
-  uint64_t mempty[2];  // tile metadata slot released (epilogue)
+  uint64_t mfull[kMetaSlots];   // tile metadata slot landed (bulk copies)
+  uint64_t mempty[kMetaSlots];  // tile metadata slot released (epilogue)
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -138,6 +156,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&sh->tfull[b], 1);
       ptx::mbar_init(&sh->tempty[b], kEpiWarps * 32);
+    }
+    for (int b = 0; b < kMetaSlots; ++b) {
       ptx::mbar_init(&sh->mfull[b], 1);
       ptx::mbar_init(&sh->mempty[b], kEpiWarps * 32);
     }
@@ -165,11 +185,34 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------------ TMA producer
-      uint32_t it = 0;
+      uint32_t it = 0, tt = 0;
       Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
+      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
         const Tile tile = next;
         if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
+        {
+          // the tile's metadata: record, job, per-structure data
+          const uint32_t ms = tt % kMetaSlots;
+          if (!ptx::mbar_wait(&sh->mempty[ms], ((tt / kMetaSlots) & 1u) ^ 1u, abort, kTimeoutNs)) {
+            fail(sh, a.sc);
+            break;
+          }
+          TileMeta &mt = meta[ms];
+          mt.tile = tile;
+          const bool nar = tile_narrow(tile), scr = tile_layout(tile) == kAccScreen;
+          const int nbs = nar ? kNarrowStructs : kBStructs;
+          const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs, b0 = (int64_t)tile.b_blk * nbs;
+          const uint32_t per = scr ? 8u : 16u;
+          ptx::mbar_arrive_expect_tx(&sh->mfull[ms], (uint32_t)sizeof(Job) + per * (kBlockStructs + nbs));
+          ptx::bulk_load(&mt.job, a.jobs + tile.job, (uint32_t)sizeof(Job), &sh->mfull[ms]);
+          if (scr) {
+            ptx::bulk_load(mt.ta, a.tinfo_a + a0, 8u * kBlockStructs, &sh->mfull[ms]);
+            ptx::bulk_load(mt.tb, a.tinfo_b + b0, 8u * nbs, &sh->mfull[ms]);
+          } else {
+            ptx::bulk_load(mt.ia, a.info_a + a0, 16u * kBlockStructs, &sh->mfull[ms]);
+            ptx::bulk_load(mt.ib, a.info_b + b0, 16u * nbs, &sh->mfull[ms]);
+          }
+        }
         const int rowA = tile.a_blk * kBlockRows;
         const int rowB = tile_narrow(tile) ? tile.b_blk * kGroupRows : tile.b_blk * kBRows;
         const int nchunks = (tile_nk16(tile) * 16 + kKChunk - 1) / kKChunk;
@@ -195,10 +238,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!scr) ptx::tma_load_2d(st + 4 * kAOpBytes + 2 * kBOpBytes, &tb2, k0, rowB, &sh->full[s]);
         }
       }
-      // let the stages still in flight land before the block can retire
+      // let the copies still in flight land before the block can retire
       for (uint32_t d = (it > kStages ? it - kStages : 0); d < it; ++d) {
         volatile int no_abort = 0;
         ptx::mbar_wait(&sh->full[d % kStages], (d / kStages) & 1u, &no_abort, 100000000ull);
+      }
+      for (uint32_t d = (tt > kMetaSlots ? tt - kMetaSlots : 0); d < tt; ++d) {
+        volatile int no_abort = 0;
+        ptx::mbar_wait(&sh->mfull[d % kMetaSlots], (d / kMetaSlots) & 1u, &no_abort, 100000000ull);
       }
     }
     __syncwarp();
@@ -252,12 +299,32 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t db1 = ptx::smem_desc_sw128(bbase + 1 * kBOpBytes + off);
             const uint64_t db2 = ptx::smem_desc_sw128(bbase + 2 * kBOpBytes + off);
             if (lay == kAccScreen) {
-              // levels 0 and 1 only
+              // digits 0 and 1 only: [L0 | L1 | L11] = [e0e0 | e0e1 + e1e0 |
+              // e1e1], the exact covariance of the structures without digit 2
               const uint32_t c0 = acc_col(0);
-              const uint32_t first = k > 0 ? 1u : 0u;
-              ptx::tc_mma_f16(c0, da0, db0, kIdesc, first);
-              ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc, first);
-              ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc, 1u);
+              if (k == 0) {  // each accumulator's first write overwrites
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);   // L1 = e1e0, L11 = e1e1
+                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc, 1u);      // L1 += e0e1
+              } else {
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);        // L0 += e0e0, L1 += e0e1
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);   // L1 += e1e0, L11 += e1e1
+              }
+              continue;
+            }
+            if (lay == kAccNormal && !tile_narrow(tile)) {
+              // [L0 | L1 | L2 | L3] in columns c0 .. c0 + 255
+              const uint32_t c0 = acc_col(0);
+              if (k == 0) {
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
+                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
+              } else {
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc192, 1u);        // L0 += e0e0, L1 += e0e1, L2 += e0e2
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 1u);   // L1 += e1e0, L2 += e1e1, L3 += e1e2
+              }
+              ptx::tc_mma_f16(c0 + 128, da2, db0, kIdesc128, 1u);    // L2 += e2e0, L3 += e2e1
+              ptx::tc_mma_f16(c0 + 192, da3, db2, kIdesc, 1u);       // L3 += (e2/512) e2
               continue;
             }
             uint32_t col[4], acc[4];  // per level: accumulator column, accumulate (vs overwrite)
@@ -300,58 +367,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       ptx::mbar_wait(&sh->drain, 0, &no_abort, 1000000000ull);
     }
     __syncwarp();
-  } else if (warp == 3) {
-    // ------------------------------------------------- tile metadata
-    uint32_t tt = 0;
-    for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
-      const uint32_t slot = tt & 1u;
-      if (!ptx::mbar_wait(&sh->mempty[slot], ((tt >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
-        if (lane == 0) fail(sh, a.sc);
-        break;
-      }
-      TileMeta &mt = meta[slot];
-      const Tile tile = a.tiles[t];
-      const Job &jb = a.jobs[tile.job];
-      if (lane == 0) {
-        mt.out = jb.out;
-        mt.n = jb.n;
-        mt.n_b = jb.n_b;
-        mt.first_a = jb.first_a;
-        mt.first_b = jb.first_b;
-        mt.a_blk = tile.a_blk;
-        mt.b_blk = tile.b_blk;
-        mt.job = tile.job;
-        mt.mode = jb.mode;
-        mt.err = jb.err;
-        mt.layout = jb.layout;
-        mt.narrow = jb.narrow;
-        mt.L = jb.L;
-        mt.tol = jb.tol;
-        mt.u = jb.u;
-        mt.d34 = jb.d34;
-        mt.dtrunc = jb.dtrunc;
-        mt.out_lo = jb.out_lo;
-      }
-      // per-structure data of the tile's A and B blocks (pads and structures
-      // past a job's end read as zero; the epilogue never uses them)
-      const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs;
-      const int64_t b0 = (int64_t)tile.b_blk * (jb.narrow ? kNarrowStructs : kBStructs);
-      const int64_t aend = jb.first_a + jb.n, bend = jb.first_b + jb.n_b;
-      for (int k = lane; k < kBlockStructs + kBStructs; k += 32) {
-        const int64_t gs = k < kBlockStructs ? a0 + k : b0 + (k - kBlockStructs);
-        SInfo v{};
-        if (k < kBlockStructs) {
-          if (gs < aend) v = a.info_a[gs];
-          mt.ia[k] = v;
-        } else {
-          if (gs < bend) v = a.info_b[gs];
-          mt.ib[k - kBlockStructs] = v;
-        }
-      }
-      __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(&sh->mfull[slot]);
-    }
-    __syncwarp();
   } else if (warp >= kEpiWarp0) {
     // ---------------------------------------------------------- epilogue
     const int qd = warp & 3;                // TMEM lane quarter of this warp
@@ -363,13 +378,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t p = 0;   // TMEM buffer slot, as the MMA issuer counts them
     uint32_t tt = 0;  // tile sequence number (metadata slot)
     for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++tt) {
-      const uint32_t slot = tt & 1u;
-      if (!ptx::mbar_wait(&sh->mfull[slot], (tt >> 1) & 1u, abort, kTimeoutNs)) {
+      const uint32_t slot = tt % kMetaSlots;
+      if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) {
         fail(sh, a.sc);
         break;
       }
       const TileMeta &mt = meta[slot];
-      const bool lng = mt.layout == kAccLong;
+      const Job &mj = mt.job;
+      const bool lng = mj.layout == kAccLong;
       bool ok = true;
       for (uint32_t u = 0; u < (lng ? 2u : 1u) && ok; ++u) {
         const uint32_t q = p + u;
@@ -382,60 +398,58 @@ __global__ void __launch_bounds__(kThreads, 1)
       ptx::tc_fence_after();
       // the tile's scalars in registers (shared memory would be re-read
       // after every warp synchronisation)
-      const int64_t jn = mt.n, jnb = mt.n_b, fa = mt.first_a, fb = mt.first_b;
-      const bool sym = mt.mode == 0;
-      const bool job_ok = mt.err == 0;
-      const OutDesc out = mt.out;
-      const float t_d34 = mt.d34, t_u = mt.u, t_tol = mt.tol;
-      const int t_L = mt.L, t_job = mt.job;
+      const int64_t jn = mj.n, jnb = mj.n_b, fa = mj.first_a, fb = mj.first_b;
+      const bool sym = mj.mode == 0;
+      const bool job_ok = mj.err == 0;
+      const OutDesc out = mj.out;
+      const float t_d34 = mj.d34, t_u = mj.u, t_tol = mj.tol;
+      const int t_L = mj.L, t_job = mt.tile.job;
+      const int t_ablk = mt.tile.a_blk, t_bblk = mt.tile.b_blk;
       // first B structure of this warp's column group (narrow tiles: group 1 has none)
-      const int64_t jg0 = (int64_t)mt.b_blk * (mt.narrow ? kNarrowStructs : kBStructs) + g * kGroupStructs;
-      const bool cols_ok = !(mt.narrow && g == 1);
-      if (mt.layout == kAccScreen) {
-        // ---- screen tile: crmsd bounds from levels 0 and 1 (FP32)
-        const float t_dtrunc = mt.dtrunc;
-        float *hi_out = static_cast<float *>(out.ptr), *lo_out = static_cast<float *>(mt.out_lo);
-        const uint32_t c0 = lane_base + (p & 1u) * 256u;
-        const int64_t ig = (int64_t)mt.a_blk * kBlockStructs + qd * kGroupStructs + il;
-        const int64_t i = ig - fa;
-        const bool row_ok = job_ok && (lane < 30) && (i < jn);
-        const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-          {
-            float m[32], v[32];
-            ptx::tmem_ld_32x32b_x32(c0, m);
-            ptx::tmem_ld_32x32b_x32(c0 + 64, v);
+      const int64_t jg0 = (int64_t)t_bblk * (mj.narrow ? kNarrowStructs : kBStructs) + g * kGroupStructs;
+      const bool cols_ok = !(mj.narrow && g == 1);
+      if (mj.layout == kAccScreen) {
+        // ---- screen tile: a crmsd bracket per pair from levels 0 and 1 (the
+        // truncated structures), stored as one word: hi (rounded up) and lo
+        // (rounded down) halves
+        uint32_t *sout = static_cast<uint32_t *>(out.ptr);
+        {
+          // m = L0 + 2^-9 L1 + 2^-18 L11: the covariance of the truncated
+          // structures in units of 2^28 grid products
+          const uint32_t c0 = lane_base + (p & 1u) * 256u;
+          float m[32], v[32];
+          ptx::tmem_ld2_32x32b_x32(c0 + 64, c0 + 128, m, v);
 #pragma unroll
-            for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+          ptx::tmem_ld_32x32b_x32(c0, v);
+          ptx::tc_fence_before();
+          ptx::mbar_arrive(&sh->tempty[p & 1u]);
 #pragma unroll
-            for (int c = 0; c < 16; ++c) stg[lane * kPitch + c] = h ? m[15 + c] : m[c];
-          }
-          if (h == 1) {
-            ptx::tc_fence_before();
-            ptx::mbar_arrive(&sh->tempty[p & 1u]);
-          }
-          __syncwarp();
-#pragma unroll
-          for (int sl = 0; sl < 2; ++sl) {
-            const int jh = 3 * sl + x;
-            const int jc = jh < 5 ? jh : 4;
-            const int64_t jg = (int64_t)mt.b_blk * kBStructs + g * kGroupStructs + 5 * h + jh;
-            const int64_t j = jg - fb;
-            if (!(row_ok && (jh < 5) && (j < jnb))) continue;
-            float m9[9];
-#pragma unroll
-            for (int xr = 0; xr < 3; ++xr)
-#pragma unroll
-              for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
-            const SInfo ib = mt.ib[g * kGroupStructs + 5 * h + jc];
-            float lo, hi;
-            bsm::screen_bounds(m9, ia.gf + ib.gf, t_dtrunc, t_u, t_L, lo, hi);
-            hi_out[i * out.ld + j] = hi;
-            lo_out[i * out.ld + j] = lo;
-          }
-          __syncwarp();
+          for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
         }
+        __syncwarp();
+        // the warp's 10 x 10 pairs over its 32 lanes, four rounds
+        const int64_t i0 = (int64_t)t_ablk * kBlockStructs + qd * kGroupStructs - fa;
+        const int64_t j0 = jg0 - fb;
+#pragma unroll 1
+        for (int rd = 0; rd < 4; ++rd) {
+          const int pp = rd * 32 + lane;
+          const int ir = pp / kGroupStructs, jc = pp - kGroupStructs * (pp / kGroupStructs);
+          const int64_t i = i0 + ir, j = j0 + jc;
+          if (!(job_ok && cols_ok && pp < kGroupStructs * kGroupStructs && i < jn && j < jnb)) continue;
+          float m9[9];
+#pragma unroll
+          for (int xr = 0; xr < 3; ++xr)
+#pragma unroll
+            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+          const float2 ta = mt.ta[qd * kGroupStructs + ir], tb = mt.tb[g * kGroupStructs + jc];
+          float lo, hi;
+          bsm::screen_bracket(m9, ta.x + tb.x, t_d34, ta.y + tb.y, t_u, t_L, lo, hi);
+          const uint32_t wlo = __half_as_ushort(__float2half_rd(lo));
+          const uint32_t whi = __half_as_ushort(__float2half_ru(hi));
+          sout[i * out.ld + j] = (whi << 16) | wlo;
+        }
+        __syncwarp();
         ptx::mbar_arrive(&sh->mempty[slot]);
         p += 1u;
         continue;
@@ -443,11 +457,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       // accumulators of level lv: normal layout {lv}; long layout L0 {0},
       // L1 {1, 2}, L2 {3..6}, L3 {7}; accumulator ai sits in slot p + ai / 4
       auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
-      const int64_t ig = (int64_t)mt.a_blk * kBlockStructs + qd * kGroupStructs + il;
+      const int64_t ig = (int64_t)t_ablk * kBlockStructs + qd * kGroupStructs + il;
       const int64_t i = ig - fa;
       const bool row_ok = job_ok && cols_ok && (lane < 30) && (i < jn);
       const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
-      const bool dump = (a.dbg != nullptr) && (mt.a_blk == 0) && (mt.b_blk < 2) && !lng;
+      const bool dump = (a.dbg != nullptr) && (t_ablk == 0) && (t_bblk < 2) && !lng;
       // The group's 10 column structures are finished in two halves of five
       // (columns 15h .. 15h+14), so a lane carries at most two pairs at once.
 #pragma unroll 1
@@ -503,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           float v[32];
           ptx::tmem_ld_32x32b_x32(acc_col(a0), v);
           if (dump && h == 0) {
-            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * mt.b_blk + 32 * g;
+            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * t_bblk + 32 * g;
 #pragma unroll
             for (int c = 0; c < 32; ++c) drow[c] = v[c];
           }

@@ -126,6 +126,7 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
   for (int d = 0; d < 4; ++d) p.dig[d] = b.dig_a[d];
   p.pitch = b.pitch_a;
   p.info = b.info_a;
+  p.tinfo = b.tinfo_a;
   p.sc = b.sc;
   if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
   if ((e = rec(1)) != cudaSuccess) return e;
@@ -137,6 +138,8 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     a.jobs = b.jobs;
     a.info_a = b.info_a;
     a.info_b = b.info_b;
+    a.tinfo_a = b.tinfo_a;
+    a.tinfo_b = b.tinfo_b;
     a.sc = b.sc;
     a.flags = b.flags;
     a.flag_cap = b.flag_cap;

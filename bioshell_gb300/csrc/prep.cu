@@ -304,11 +304,13 @@ __global__ void k_mx_choose(PrepArgs p) {
   jb.scale_exp = jb.scale_base + pick;
   jb.u = ldexpf(1.0f, 2 * jb.scale_exp);
   if (jb.screen) {
-    // The screen keeps levels 0 and 1: the rest of Mhat, 2^10 S2 + 2 S3',
-    // is at most 2^10 b2 + 2 b34 per entry, so the top eigenvalue moves by
-    // at most 2 ||dM||_F <= 6 (2^10 b2 + 2 b34) and E by twice that.
-    const double b2 = bb2[pick] > 0.0 ? bb2[pick] : 0.0;
-    jb.dtrunc = (float)(12.0 * (1024.0 * b2 + 2.0 * bb34[pick]) * (1.0 + 1e-6));
+    // The screen accumulates digits 0 and 1 only (levels 0 and 1, and e1 e1):
+    // levels 0-1 are exact here; e1 e1 is exact below 2^24, otherwise its
+    // half-ulp roundings (L steps per entry) are charged as an error of E.
+    const double b11 = sqrt((double)jb.norm[pick][1]) * (jb.mode == 1 ? (double)jb.norm_b[1] : sqrt((double)jb.norm[pick][1]));
+    double e11 = 0.0;
+    if (b11 >= 16777216.0) e11 = (double)jb.L * ldexp(1.0, (int)floor(log2(b11)) - 24);
+    jb.d34 = (float)(6.0 * sqrt(3.0) * 1024.0 * e11 * (1.0 + 1e-6));
     jb.layout = kAccScreen;
   }
 }
@@ -361,13 +363,22 @@ __global__ void k_mx_digits(PrepArgs p, int64_t nstructs, int wpb) {
     q[2 * p.pitch + i] = 0;
   }
   __syncwarp();
-  // pass 2: 8 atoms of one row per lane-step
+  // pass 2: 8 atoms of one row per lane-step; also the truncated structure
+  // t = n - d2 that levels 0 and 1 describe (sum of t^2, sum of d2^2)
   const int chunks = lp / 8;
+  long long gt = 0;
+  int d2s = 0;
   for (int u = lane; u < 3 * chunks; u += 32) {
     const int r = u / chunks, k0 = (u - r * chunks) * 8;
     int e0[8], e1[8], e2[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) bsm::split_digits(q[r * p.pitch + k0 + k], e0[k], e1[k], e2[k]);
+    for (int k = 0; k < 8; ++k) {
+      const int nv = q[r * p.pitch + k0 + k];
+      bsm::split_digits(nv, e0[k], e1[k], e2[k]);
+      const int d2 = e2[k] >> 4, tv = nv - d2;
+      gt += (long long)tv * tv;
+      d2s += d2 * d2;
+    }
     const int64_t off = digit_row(g, r) * p.pitch + k0;
     uint4 v0, v1, v2, v3;
     v0.x = bf16x2(e0[0], e0[1]); v0.y = bf16x2(e0[2], e0[3]); v0.z = bf16x2(e0[4], e0[5]); v0.w = bf16x2(e0[6], e0[7]);
@@ -395,6 +406,15 @@ __global__ void k_mx_digits(PrepArgs p, int64_t nstructs, int wpb) {
     in.qres = (float)(rms * (1.0 + 1e-6) + 9.313225746154785e-10);
     p.info[g] = in;
     atomicMax(&jb.qres_max_bits, __float_as_uint(in.qres));
+  }
+  if (p.tinfo) {
+    gt = warp_sum64(gt);
+    d2s = (int)warp_sum32((unsigned)d2s);
+    if (lane == 0) {
+      // RMS of the omitted digit in Angstrom (2^scale_exp per unit), rounded up
+      const double rt = sqrt((double)d2s / (double)L) * ldexp(1.0, jb.scale_exp);
+      p.tinfo[g] = make_float2((float)gt, (float)(rt * (1.0 + 1e-6)));
+    }
   }
 }
 

@@ -58,6 +58,7 @@ struct Bucket {
   float norm_b[3] = {0, 0, 0};
   float qres = 0.f;
   DevBuf dig[4], info;  // mixed path
+  DevBuf tinfo;         // screen: truncated-structure data per structure
   DevBuf y, g;          // plain path: centred f64 [n][3][lp], squared norms
 };
 
@@ -93,7 +94,7 @@ struct Slot {
   bool screen = false;        // the batch ran the two-stage (screen + exact) top-k
   // device
   DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
-  DevBuf dense_lo, cand_j, cand_n, cand_v, rowtab;
+  DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab;
   // pinned host
   HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n;
 };
@@ -178,7 +179,7 @@ bool host_ensure(HostBuf &h, size_t bytes) {
 void slot_release(bs_server *s, Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
-                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.dense_lo,
+                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
                     &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
   for (DevBuf *b : list) sv_release(s, *b);
 }
@@ -186,7 +187,7 @@ void slot_release(bs_server *s, Slot &sl) {
 size_t slot_bytes(Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
-                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.dense_lo,
+                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
                     &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
   size_t t = 0;
   for (DevBuf *b : list) t += b->cap;
@@ -206,14 +207,15 @@ size_t batch_bytes(const bs_server *s, const std::vector<Request *> &b) {
     rows += r->q;
     xyz += (size_t)r->q * L * 24;
   }
-  size_t t = xyz + (size_t)blocks * kBlockStructs * (24 + 16) + (size_t)blocks * kBlockRows * pitch * 2 * 4 +
+  size_t t = xyz + (size_t)blocks * kBlockStructs * (24 + 16 + 8) + (size_t)blocks * kBlockRows * pitch * 2 * 4 +
              b.size() * sizeof(Job) + (size_t)blocks * 4 + sizeof(DevScalars);
   if (r0->kind == 0) {
     const int64_t nb = s->buckets[r0->bucket].n;
     for (const Request *r : b) tiles += blocks_for(r->q) * ((nb + kBStructs - 1) / kBStructs);
-    t += (size_t)tiles * sizeof(Tile) + kServerFlagCap * 8 + (size_t)rows * nb * 4 + (size_t)rows * s->top_k * 12;
+    t += (size_t)tiles * sizeof(Tile) + kServerFlagCap * 8 + (size_t)rows * ((nb + 3) & ~int64_t(3)) * 4 +
+         (size_t)rows * s->top_k * 12;
     if (s->precision == BS_PRECISION_PLAIN64) t += (size_t)rows * (3 * lp * 8 + 8 + 24);
-    else t += (size_t)rows * nb * 4 + (size_t)rows * (s->top_k * 12 + (size_t)kCandCap * 8 + 16);
+    else t += (size_t)rows * (4 * kScreenBins + s->top_k * 12 + (size_t)kCandCap * 8 + 24);
   } else {
     const int64_t n = r0->q, nba = blocks_for(n), nbb = (n + kBStructs - 1) / kBStructs;
     for (int64_t i = 0; i < nba; ++i) tiles += std::max<int64_t>(0, nbb - 2 * i);
@@ -256,6 +258,7 @@ bs_status build_bucket(bs_server *s, Bucket &bk, const double *xyz_in) {
     bk.rows = plan.nblocks * kBlockRows;
     const int64_t ns = plan.nblocks * kBlockStructs;
     bool ok = cudaMalloc(&ctr.p, (size_t)ns * 24) == cudaSuccess && cudaMalloc(&bk.info.p, (size_t)ns * 16) == cudaSuccess &&
+              cudaMalloc(&bk.tinfo.p, (size_t)ns * 8) == cudaSuccess &&
               cudaMalloc(&jobs.p, sizeof(Job)) == cudaSuccess && cudaMalloc(&jobmap.p, plan.nblocks * 4) == cudaSuccess &&
               cudaMalloc(&scal.p, sizeof(DevScalars)) == cudaSuccess;
     for (int d = 0; d < 4 && ok; ++d)
@@ -271,6 +274,7 @@ bs_status build_bucket(bs_server *s, Bucket &bk, const double *xyz_in) {
     b.ctr = static_cast<long long *>(ctr.p);
     b.info_a = static_cast<SInfo *>(bk.info.p);
     b.info_b = b.info_a;
+    b.tinfo_a = static_cast<float2 *>(bk.tinfo.p);
     for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(bk.dig[d].p);
     for (int d = 0; d < 3; ++d) b.dig_b[d] = b.dig_a[d];
     b.pitch_a = b.pitch_b = bk.pitch;
@@ -358,7 +362,9 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   sl.screen = screen && s->precision == BS_PRECISION_MIXED;
   const int64_t ns = blk * kBlockStructs, drows = blk * kBlockRows;
   const bool plain = s->precision == BS_PRECISION_PLAIN64;
-  bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * bk.n * 4) &&
+  // screen batches: one packed bracket word per pair, rows padded to 4 words
+  const int64_t ld = sl.screen ? ((bk.n + 3) & ~int64_t(3)) : bk.n;
+  bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * ld * 4) &&
             sv_ensure(s, sl.topi, (size_t)rows * k * 8) && sv_ensure(s, sl.topv, (size_t)rows * k * 4) &&
             sv_ensure(s, sl.scal, sizeof(DevScalars)) && host_ensure(sl.hxyz, xyz_off * 8) &&
             host_ensure(sl.htopi, (size_t)rows * k * 8) && host_ensure(sl.htopv, (size_t)rows * k * 4) &&
@@ -374,7 +380,9 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
          host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16);
     for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * bk.pitch * 2);
     if (sl.screen)
-      ok = ok && sv_ensure(s, sl.dense_lo, (size_t)rows * bk.n * 4) && sv_ensure(s, sl.cand_j, (size_t)rows * kCandCap * 4) &&
+      ok = ok && sv_ensure(s, sl.tinfo, (size_t)ns * 8) && sv_ensure(s, sl.hist, (size_t)rows * kScreenBins * 4) &&
+           sv_ensure(s, sl.thr, (size_t)rows * 4) &&
+           sv_ensure(s, sl.cand_j, (size_t)rows * kCandCap * 4) &&
            sv_ensure(s, sl.cand_n, (size_t)rows * 4) && sv_ensure(s, sl.cand_v, (size_t)rows * kCandCap * 4) &&
            sv_ensure(s, sl.rowtab, (size_t)rows * 12 + 8) && host_ensure(sl.hcand_n, (size_t)rows * 4);
   }
@@ -399,12 +407,8 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
         return BS_ERR_CUDA;
     }
   } else {
-    float *dense_lo = sl.screen ? static_cast<float *>(sl.dense_lo.p) : nullptr;
     for (int j = 0; j < nj; ++j) plan.jobs[j].xyz = dx + xoff[j];
-    for (int j = 0; j < nj; ++j) {
-      plan.jobs[j].out = OutDesc{dense + sl.row0[j] * bk.n, sl.reqs[j]->q, bk.n, kLayoutRect, 1};
-      plan.jobs[j].out_lo = dense_lo ? dense_lo + sl.row0[j] * bk.n : nullptr;
-    }
+    for (int j = 0; j < nj; ++j) plan.jobs[j].out = OutDesc{dense + sl.row0[j] * ld, sl.reqs[j]->q, ld, kLayoutRect, 1};
     memcpy(sl.hjobs.p, plan.jobs.data(), (size_t)nj * sizeof(Job));
     char *ht = static_cast<char *>(sl.htab.p);
     memcpy(ht, plan.jobmap.data(), plan.jobmap.size() * 4);
@@ -413,6 +417,10 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
     b.ctr = static_cast<long long *>(sl.ctr.p);
     b.info_a = static_cast<SInfo *>(sl.info.p);
     b.info_b = static_cast<const SInfo *>(bk.info.p);
+    if (sl.screen) {
+      b.tinfo_a = static_cast<float2 *>(sl.tinfo.p);
+      b.tinfo_b = static_cast<const float2 *>(bk.tinfo.p);
+    }
     for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(sl.dig[d].p);
     for (int d = 0; d < 3; ++d) b.dig_b[d] = static_cast<const __nv_bfloat16 *>(bk.dig[d].p);
     b.pitch_a = bk.pitch;
@@ -452,9 +460,9 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
       const int *cj = static_cast<const int *>(sl.cand_j.p);
       const int *cn = static_cast<const int *>(sl.cand_n.p);
       if (cudaMemcpyAsync(drjob, rt, jbytes + (size_t)rows * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
-          launch_screen_select(dense, static_cast<const float *>(sl.dense_lo.p), rows, bk.n, bk.n, k, kCandCap,
-                               static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) !=
-              cudaSuccess ||
+          launch_screen_select(reinterpret_cast<const uint32_t *>(dense), rows, bk.n, ld, k, kCandCap,
+                               static_cast<uint32_t *>(sl.hist.p), static_cast<uint32_t *>(sl.thr.p),
+                               static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) != cudaSuccess ||
           launch_exact_candidates(DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a},
                                   DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b}, b.info_a, b.info_b, b.jobs,
                                   drjob, drig, rows, cj, cn, kCandCap, static_cast<float *>(sl.cand_v.p),
@@ -901,7 +909,7 @@ BS_API void bs_server_destroy(bs_server *s) {
     if (sl.st) cudaStreamDestroy(sl.st);
   }
   for (Bucket &bk : s->buckets)
-    for (DevBuf *d : {&bk.dig[0], &bk.dig[1], &bk.dig[2], &bk.dig[3], &bk.info, &bk.y, &bk.g})
+    for (DevBuf *d : {&bk.dig[0], &bk.dig[1], &bk.dig[2], &bk.dig[3], &bk.info, &bk.tinfo, &bk.y, &bk.g})
       if (d->p) cudaFree(d->p);
   for (auto &kv : s->reqs) delete kv.second;
   delete s;

@@ -141,49 +141,123 @@ __global__ void __launch_bounds__(kTopkWarps * 32) k_topk(const float *__restric
   }
 }
 
-// Screen candidates of one row (block per row): the k-th smallest upper
-// bound of the row (the scan of k_topk), then every column whose lower
-// bound does not exceed it.
-__global__ void __launch_bounds__(kTopkWarps * 32) k_screen_select(const float *__restrict__ hi,
-                                                                   const float *__restrict__ lo, int64_t n,
-                                                                   int64_t ld, int k, int cap,
-                                                                   int *__restrict__ cand_j,
-                                                                   int *__restrict__ cand_n) {
-  __shared__ float sv[kTopkWarps][kTopkMax];
-  __shared__ int si[kTopkWarps][kTopkMax];
-  __shared__ float thr;
-  __shared__ int count;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r = blockIdx.x;
-  const float inf = __int_as_float(0x7f800000);
-  float lv[2] = {inf, inf};
-  int li[2] = {0x7fffffff, 0x7fffffff};
-  float tv = inf;
-  int ti = 0x7fffffff;
-  warp_scan(hi + r * ld, n, warp, lane, k, lv, li, tv, ti);
-  sv[warp][2 * lane] = lv[0];
-  sv[warp][2 * lane + 1] = lv[1];
-  si[warp][2 * lane] = li[0];
-  si[warp][2 * lane + 1] = li[1];
-  if (threadIdx.x == 0) count = 0;
+// ------------------------------------------------- screen candidates
+// A row of packed brackets (ld a multiple of 4 words, rows 16-byte aligned)
+// is read in chunks of kSelChunk words by blocks of 256 threads (grid:
+// chunks x rows); each thread issues all eight of its 16-byte loads before
+// using any.  Positive half-precision bit patterns order like the values,
+// so a bin of hi is its top 12 bits (sign, exponent, six mantissa bits) and
+// comparisons of lo run on the raw bits.
+constexpr int kSelThreads = 256;
+constexpr int kSelChunk = 8192;
+constexpr int kSelPer = kSelChunk / 4 / kSelThreads;  // 16-byte loads per thread
+
+__device__ __forceinline__ void load_chunk(const uint32_t *__restrict__ row, int64_t c0, uint4 (&w)[kSelPer],
+                                           int64_t c1) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(row + c0);
+#pragma unroll
+  for (int u = 0; u < kSelPer; ++u) {
+    const int64_t t = (int64_t)u * kSelThreads + threadIdx.x;
+    w[u] = c0 + 4 * t < c1 ? q[t] : make_uint4(0, 0, 0, 0);
+  }
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_screen_hist(const uint32_t *__restrict__ packed, int64_t n,
+                                                             int64_t ld, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t h[kScreenBins];
+  for (int b = threadIdx.x; b < kScreenBins; b += kSelThreads) h[b] = 0;
+  const int64_t r = blockIdx.y;
+  const int64_t c0 = (int64_t)blockIdx.x * kSelChunk, c1 = min(n, c0 + kSelChunk);
+  uint4 w[kSelPer];
+  load_chunk(packed + r * ld, c0, w, c1);
   __syncthreads();
-  if (warp == 0) {
-    merge_lists(sv, si, lane, k, lv, li, tv, ti);
-    // fewer than k columns: every column is a candidate
-    if (lane == 0) thr = ti == 0x7fffffff ? inf : tv;
+#pragma unroll
+  for (int u = 0; u < kSelPer; ++u) {
+    const int64_t c = c0 + 4 * ((int64_t)u * kSelThreads + threadIdx.x);
+    if (c < c1) atomicAdd(&h[w[u].x >> 20], 1u);
+    if (c + 1 < c1) atomicAdd(&h[w[u].y >> 20], 1u);
+    if (c + 2 < c1) atomicAdd(&h[w[u].z >> 20], 1u);
+    if (c + 3 < c1) atomicAdd(&h[w[u].w >> 20], 1u);
   }
   __syncthreads();
-  const float t = thr;
-  const float *v = lo + r * ld;
-  int *cj = cand_j + r * (int64_t)cap;
-  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-    if (v[j] <= t) {
-      const int slot = atomicAdd(&count, 1);
-      if (slot < cap) cj[slot] = (int)j;
+  uint32_t *gh = hist + r * kScreenBins;
+  for (int b = threadIdx.x; b < kScreenBins; b += kSelThreads)
+    if (h[b]) atomicAdd(&gh[b], h[b]);
+}
+
+// Block per row: the first bin at which the cumulative count reaches k; the
+// threshold is that bin's top edge (all bins when the row has fewer than k).
+__global__ void __launch_bounds__(kSelThreads) k_screen_thresh(const uint32_t *__restrict__ hist, int k,
+                                                               uint32_t *__restrict__ thr) {
+  constexpr int kPer = kScreenBins / kSelThreads;  // 16 consecutive bins per thread
+  __shared__ uint32_t wsum[kSelThreads / 32];
+  __shared__ uint32_t found;
+  const int64_t r = blockIdx.x;
+  const uint32_t *gh = hist + r * kScreenBins + threadIdx.x * kPer;
+  uint32_t v[kPer], tot = 0;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    v[i] = gh[i];
+    tot += v[i];
+  }
+  if (threadIdx.x == 0) found = 0xffffffffu;
+  // exclusive prefix of the per-thread totals across the block
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t base = 0;
+  for (int w = 0; w < warp; ++w) base += wsum[w];
+  uint32_t cum = base + inc - tot;
+  if (cum < (uint32_t)k && cum + tot >= (uint32_t)k) {
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      cum += v[i];
+      if (cum >= (uint32_t)k) {
+        found = (uint32_t)(threadIdx.x * kPer + i);
+        break;
+      }
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) cand_n[r] = count;
+  if (threadIdx.x == 0) thr[r] = found == 0xffffffffu ? 0xffffu : ((found << 4) | 0xfu);
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_screen_extract(const uint32_t *__restrict__ packed, int64_t n,
+                                                                int64_t ld, const uint32_t *__restrict__ thr,
+                                                                int cap, int *__restrict__ cand_j,
+                                                                int *__restrict__ cand_n) {
+  const int64_t r = blockIdx.y;
+  const int64_t c0 = (int64_t)blockIdx.x * kSelChunk, c1 = min(n, c0 + kSelChunk);
+  uint4 w[kSelPer];
+  load_chunk(packed + r * ld, c0, w, c1);
+  const uint32_t t = thr[r];
+  const int lane = threadIdx.x & 31;
+  int *cj = cand_j + r * (int64_t)cap;
+  // one atomic per warp and word position; every lane runs the same rounds
+#pragma unroll
+  for (int u = 0; u < kSelPer; ++u) {
+    const int64_t c = c0 + 4 * ((int64_t)u * kSelThreads + threadIdx.x);
+    const uint32_t v[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const bool hit = c + e < c1 && (v[e] & 0xffffu) <= t;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (!m) continue;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&cand_n[r], __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (hit) {
+        const int slot = base + __popc(m & ((1u << lane) - 1u));
+        if (slot < cap) cj[slot] = (int)(c + e);
+      }
+    }
+  }
 }
 
 }  // namespace
@@ -204,11 +278,20 @@ cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_screen_select(const float *hi, const float *lo, int64_t rows, int64_t n, int64_t ld, int k,
-                                 int cap, int *cand_j, int *cand_n, cudaStream_t st) {
+cudaError_t launch_screen_select(const uint32_t *packed, int64_t rows, int64_t n, int64_t ld, int k, int cap,
+                                 uint32_t *hist, uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st) {
   if (rows <= 0) return cudaSuccess;
-  if (n > 0x7ffffffe || cap < 1 || k < 1 || k > kTopkMax) return cudaErrorInvalidValue;
-  k_screen_select<<<(unsigned)rows, kTopkWarps * 32, 0, st>>>(hi, lo, n, ld, k, cap, cand_j, cand_n);
+  if (n > 0x7ffffffe || n > ld || cap < 1 || k < 1 || rows > 65535 || (ld & 3) || ((uintptr_t)packed & 15))
+    return cudaErrorInvalidValue;
+  const unsigned chunks = (unsigned)((n + kSelChunk - 1) / kSelChunk);
+  cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)rows * kScreenBins * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cand_n, 0, (size_t)rows * 4, st);
+  if (e != cudaSuccess) return e;
+  if (chunks > 0) k_screen_hist<<<dim3(chunks, (unsigned)rows), kSelThreads, 0, st>>>(packed, n, ld, hist);
+  k_screen_thresh<<<(unsigned)rows, kSelThreads, 0, st>>>(hist, k, thresholds);
+  if (chunks > 0)
+    k_screen_extract<<<dim3(chunks, (unsigned)rows), kSelThreads, 0, st>>>(packed, n, ld, thresholds, cap, cand_j,
+                                                                         cand_n);
   return cudaGetLastError();
 }
 

@@ -119,6 +119,8 @@ SIGNATURES = [
                                               ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp,
                                               _i32p]),
     ("bs_selftest_exact", ctypes.c_int32, [_i32p, _i32p, ctypes.c_int32, ctypes.c_int32, _dp]),
+    ("bs_selftest_screen", ctypes.c_int32, [_fp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                            ctypes.c_int32, _fp, _fp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                               _fp, _dp]),

@@ -328,6 +328,15 @@ BS_API bs_status bs_cut_tree(const int64_t *merges, const float *merge_dist, int
  * every item (clusters split where reachability is undefined = 10 eps). */
 BS_API bs_status bs_optics(const void *tri, int64_t n, int32_t out_type, double eps, int32_t min_points,
                            int64_t *order, double *reach, int64_t *cluster_of);
+/* The same over sparse neighbour lists (CSR: the neighbours of item i are
+ * col[row_ptr[i] .. row_ptr[i+1]) at distances dist[...], as bs_neighbors
+ * returns them: every j != i with d(i, j) <= eps, ordered by (d, j)).  The
+ * point itself is added at distance 0 as CartesianPoints::neighbors_of
+ * includes it (points_set.rs:150-169); results equal bs_optics on the dense
+ * f32 matrix holding the same values. */
+BS_API bs_status bs_optics_neighbors(const int64_t *row_ptr, const int32_t *col, const float *dist, int64_t n,
+                                     double eps, int32_t min_points, int64_t *order, double *reach,
+                                     int64_t *cluster_of);
 
 /* ---- pinned host memory ------------------------------------------------- */
 /* Page-locked host buffers for fast host<->device staging (cudaHostAlloc);
@@ -354,6 +363,16 @@ BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_
 BS_API bs_status bs_selftest_epilogue(const float *levels, int64_t ga, int64_t gb, double qa, double qb,
                                       double d34, int32_t scale_exp, int32_t L, double tolerance, double *rmsd,
                                       int32_t *flag);
+/* The serving screen's bracket for one pair: m9 = S0 + S1/512 + S11/2^18
+ * (S11 = sum e1 e1: the covariance of the structures with digit 2 dropped,
+ * t = n - e2/16, in units of 2^28 grid products), gsum = the sum of the two
+ * truncated structures' squared norms (grid units), de = a bound on the
+ * rounding of S11 as an error of E (grid units; 0 when exact), dr = the sum
+ * of their RMS distances from the full structures (Angstrom); returns
+ * lo <= crmsd(n_a, n_b) <= hi (Angstrom) before their rounding to half
+ * precision. */
+BS_API bs_status bs_selftest_screen(const float *m9, double gsum, double de, double dr, int32_t scale_exp, int32_t L,
+                                    float *lo, float *hi);
 /* The exact recomputation from integer coordinates n_a[3][L], n_b[3][L]. */
 BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t L, int32_t scale_exp,
                                    double *rmsd);

@@ -138,3 +138,59 @@ def test_identical_structures_exact_zero(hooks):
     assert hooks.exact(d, d, e) == pytest.approx(0.0, abs=1e-9)
     r, f = hooks.fast(hooks.levels(d, d), g, g, q, q, e, 64)
     assert f == 1 or r <= 1e-4
+
+
+def _truncated(d, e):
+    """The structure the screen's levels 0 and 1 describe (digit 2 dropped):
+    its squared norm (grid units) and RMS distance from the full one (A)."""
+    n = join(d)
+    d2 = d[2] // 16
+    t = n - d2
+    return float((t.astype(np.float64) ** 2).sum()), float(np.sqrt((d2.astype(np.float64) ** 2).sum() / d.shape[2])
+                                                          * 2.0 ** e)
+
+
+@pytest.mark.parametrize("L", [8, 64, 300])
+def test_screen_bracket_contains_crmsd(hooks, oracle_mod, L):
+    """The serving screen's Newton bracket (levels 0 and 1 only) contains the
+    exact crmsd of the quantised pair, for near, far, identical, mirrored and
+    planar pairs; and it is tight for near pairs."""
+    rng = np.random.default_rng(100 + L)
+    base = synth.base_chain(L, rng)
+    xs = list(synth.decoys(base, 10, rng, near_dup_frac=0.3))
+    xs.append(xs[0].copy())                                 # identical
+    xs.append(xs[1] * np.array([1.0, 1.0, -1.0]))           # mirror image
+    flat = rng.normal(size=(L, 3)) * 10.0
+    flat[:, 2] = 0.0
+    xs.append(flat)                                          # planar
+    xs.append(synth.base_chain(L, rng))                      # unrelated chain
+    xs = np.stack(xs)
+    e = _grid_exp(xs)
+    dig = [hooks.digits(x, e) for x in xs]
+    tr = [_truncated(d[0], e) for d in dig]
+    fp = ctypes.POINTER(ctypes.c_float)
+    widths = []
+    for i in range(len(xs)):
+        for j in range(i + 1, len(xs)):
+            da, ga, qa = dig[i]
+            db, gb, qb = dig[j]
+            s = hooks.levels(da, db)
+            s11 = np.array([[(da[1, x] * db[1, y]).sum() for y in range(3)] for x in range(3)], dtype=np.float64)
+            m9 = np.ascontiguousarray((s[0] + s[1] / 512.0 + s11 / 2.0 ** 18).reshape(9), dtype=np.float32)
+            lo, hi = ctypes.c_float(), ctypes.c_float()
+            st = hooks.lib.bs_selftest_screen(m9.ctypes.data_as(fp), tr[i][0] + tr[j][0], 0.0, tr[i][1] + tr[j][1], e,
+                                              L, ctypes.byref(lo), ctypes.byref(hi))
+            assert st == 0
+            rx = hooks.exact(da, db, e)
+            assert lo.value <= rx * (1 + 1e-6) + 1e-9 and rx <= hi.value * (1 + 1e-6) + 1e-9, (i, j, lo.value, rx,
+                                                                                                 hi.value)
+            ref = oracle_mod.crmsd(xs[i], xs[j])
+            assert lo.value - (qa + qb) - 1e-6 <= ref <= hi.value + qa + qb + 1e-6
+            if 0.5 < rx < 5.0:
+                # the bracket's width in E / L = 2 r dr, relative to (Ga + Gb) / L
+                widths.append(2 * (hi.value - lo.value) * rx / ((tr[i][0] + tr[j][0]) * 2.0 ** (2 * e) / L))
+    # near pairs of protein-sized chains: the FP32 quartic fixes the top root
+    # to ~2^-15 (0.02 A at 1 A for 64 atoms); short chains are elongated, their
+    # top root nearly double: wider
+    if L >= 64:
+        assert max(widths) < 1e-4, max(widths)
