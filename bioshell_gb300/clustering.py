@@ -91,3 +91,43 @@ def optics(matrix: CrmsdMatrix, eps: float, min_points: int):
                              cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
     _check(st, "bs_optics")
     return order, reach, cl
+
+
+def optics_neighbors(row_ptr, col, dist, eps: float, min_points: int):
+    """OPTICS over sparse neighbour lists (CSR, as ``Engine.neighbors`` returns
+    them): (clustering order, reachability in that order, cluster index per
+    item) -- the same as ``optics`` on a dense f32 matrix holding the values."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    dist = np.ascontiguousarray(dist, dtype=np.float32)
+    n = row_ptr.shape[0] - 1
+    order = np.zeros(n, dtype=np.int64)
+    reach = np.zeros(n, dtype=np.float64)
+    cl = np.zeros(n, dtype=np.int64)
+    st = _l.load().bs_optics_neighbors(row_ptr.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                       col.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                       dist.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), n, float(eps),
+                                       int(min_points), order.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                       reach.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       cl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    _check(st, "bs_optics_neighbors")
+    return order, reach, cl
+
+
+def neighbors_from_dense(m, eps: float):
+    """CSR neighbour lists of a dense symmetric matrix: for every row i the
+    columns j != i with m[i, j] <= eps, ordered by (distance, j)."""
+    m = np.asarray(m, dtype=np.float32)
+    n = m.shape[0]
+    rows, cols, vals = [], [], []
+    row_ptr = np.zeros(n + 1, dtype=np.int64)
+    for i in range(n):
+        j = np.flatnonzero(m[i] <= eps)
+        j = j[j != i]
+        o = np.lexsort((j, m[i, j]))
+        cols.append(j[o].astype(np.int32))
+        vals.append(m[i, j[o]])
+        row_ptr[i + 1] = row_ptr[i] + len(j)
+    col = np.concatenate(cols) if cols else np.zeros(0, np.int32)
+    val = np.concatenate(vals) if vals else np.zeros(0, np.float32)
+    return row_ptr, col, val

@@ -105,6 +105,29 @@ def test_optics_matches_oracle(enginelib, seed):
         np.testing.assert_array_equal(cl, want)
 
 
+@pytest.mark.parametrize("seed", [0, 3])
+def test_optics_on_neighbor_lists_equals_dense(enginelib, seed):
+    """OPTICS over sparse (CSR) neighbour lists gives the dense f32 matrix's
+    order, reachability and labels -- including exact ties and zero distances
+    (identical items), where the point itself must sit in its stable-sort
+    place."""
+    rng = np.random.default_rng(seed)
+    pts = np.concatenate([rng.normal(size=(30, 2)) * 0.4, rng.normal(size=(30, 2)) * 0.4 + 3.0,
+                          rng.uniform(-3, 6, size=(10, 2))])
+    pts = np.round(pts, 1)          # ties
+    pts[5] = pts[4]                 # identical items: distance 0
+    pts[40] = pts[41] = pts[45]
+    sq = np.linalg.norm(pts[:, None] - pts[None], axis=2).astype(np.float32)
+    m = _matrix(sq, np.float32)
+    for eps, mp in ((0.8, 4), (1.2, 6), (0.3, 2), (0.5, 1)):
+        rp, col, val = K.neighbors_from_dense(sq, eps)
+        o1, r1, c1 = K.optics(m, eps, mp)
+        o2, r2, c2 = K.optics_neighbors(rp, col, val, eps, mp)
+        np.testing.assert_array_equal(o1, o2)
+        np.testing.assert_array_equal(r1, r2)
+        np.testing.assert_array_equal(c1, c2)
+
+
 def test_degenerate_sizes(enginelib):
     for n in (0, 1, 2):
         m = CrmsdMatrix(n, np.ones(n * (n - 1) // 2), "triangle")
