@@ -204,6 +204,34 @@ def profiled_traffic(name):
         return None
 
 
+def run_neighbors(eng, xd, outd, n, torch, eps=1.0, steps=3):
+    """eps-neighbour lists of the headline set without the dense matrix: device
+    time of the sparse form, and a check of sampled rows against the dense
+    result of the same set."""
+    rp, col, dist = eng.neighbors(xd, eps)
+    ms = []
+    for _ in range(steps):
+        rp, col, dist = eng.neighbors(xd, eps)
+        ms.append(eng.metrics()["ms_total"])
+    ok = True
+    rows = (0, 1, n // 2, n - 1)
+    for i in rows:
+        j = np.arange(n)
+        j = j[j != i]
+        lo, hi = np.minimum(i, j), np.maximum(i, j)
+        t = lo * n - lo * (lo + 1) // 2 + (hi - lo - 1)
+        d = outd[torch.from_numpy(t).cuda()].cpu().numpy().astype(np.float32)
+        keep = d <= eps
+        o = np.lexsort((j[keep], d[keep]))
+        ok &= bool(np.array_equal(col[rp[i]:rp[i + 1]], j[keep][o]) and
+                   np.array_equal(dist[rp[i]:rp[i + 1]], d[keep][o]))
+    nnz = int(rp[-1])
+    msd = statistics.median(ms)
+    return {"eps": eps, "nnz": nnz, "mean_neighbors": nnz / n, "ms_device": msd,
+            "pairs_per_s": n * (n - 1) / 2 / (msd * 1e-3), "csr_bytes": int(8 * (n + 1) + 8 * nnz),
+            "dense_f32_bytes": int(4 * n * (n - 1) // 2), "rows_checked_against_dense": len(rows), "match": ok}
+
+
 def run_batched(a, eng, stream, torch):
     """The batched form: all sets in one call per step (graph replay)."""
     from bioshell_gb300 import clustering as K
@@ -514,6 +542,8 @@ def run_ours(a, rank, world, local_rank):
                "near_dup_p99_abs": float(np.percentile(d2, 99)) if len(d2) else None,
                "tolerance": 1e-4, "pass": bool(d.max() <= 1e-4 and (len(d2) == 0 or d2.max() <= 1e-4))}
 
+    neighbors = run_neighbors(eng, xd, outd, n, torch) if rank == 0 else None
+
     pk, pk_kind = peaks()
     achieved = 18.0 * L * npairs / (ms_main * 1e-3) / 1e12
     peak = pk["bf16_tflops_sustained"]
@@ -542,7 +572,8 @@ def run_ours(a, rank, world, local_rank):
                        "replicas": world},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
-            "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "batched": batched,
+            "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
+            "batched": batched,
             "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)

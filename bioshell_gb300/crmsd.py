@@ -175,6 +175,26 @@ class Engine:
         self._check(self._lib.bs_all_vs_all(self._h, xp, n, L, ctypes.byref(o), op))
         return CrmsdMatrix(n, out, opts.layout)
 
+    def neighbors(self, xyz, eps: float, opts: Optional[CrmsdOptions] = None):
+        """eps-neighbour lists without the dense matrix: CSR (row_ptr int64
+        [n+1], col int32, dist f32); row i holds every j != i with crmsd <= eps,
+        ordered by (crmsd, j).  Feed them to ``clustering.optics_neighbors``."""
+        opts = opts or CrmsdOptions()
+        if isinstance(xyz, np.ndarray):
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        if len(xyz.shape) != 3 or xyz.shape[2] != 3:
+            raise ValueError("coordinates must be [n][L][3]")
+        n, L = int(xyz.shape[0]), int(xyz.shape[1])
+        xp, _k1 = _ptr(xyz)
+        o = opts.to_c()
+        nnz = ctypes.c_int64()
+        self._check(self._lib.bs_neighbors(self._h, xp, n, L, float(eps), ctypes.byref(o), ctypes.byref(nnz)))
+        row_ptr = np.zeros(n + 1, dtype=np.int64)
+        col = np.zeros(nnz.value, dtype=np.int32)
+        dist = np.zeros(nnz.value, dtype=np.float32)
+        self._check(self._lib.bs_neighbors_get(self._h, row_ptr.ctypes.data, col.ctypes.data, dist.ctypes.data))
+        return row_ptr, col, dist
+
     def batched(self, sets, opts: Optional[CrmsdOptions] = None, outs=None):
         """All-vs-all of every set in ``sets`` (each [n][L][3], numpy or CUDA
         tensor; n and L may differ) in one call; returns one CrmsdMatrix per set."""

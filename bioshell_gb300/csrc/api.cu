@@ -588,8 +588,101 @@ bs_status pairs_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int
 DevBuf *all_buffers(bs_ctx *ctx, std::vector<DevBuf *> &v) {
   v = {&ctx->xyz,     &ctx->out,    &ctx->ctr,   &ctx->info,  &ctx->dig[0], &ctx->dig[1], &ctx->dig[2],
        &ctx->dig[3],  &ctx->jobs,   &ctx->jobmap, &ctx->tiles, &ctx->flags,  &ctx->y,      &ctx->g,
-       &ctx->ctrd,    &ctx->pairs_i, &ctx->pairs_j, &ctx->pout};
+       &ctx->ctrd,    &ctx->pairs_i, &ctx->pairs_j, &ctx->pout,
+       &ctx->nbr_sink, &ctx->nbr_count, &ctx->nbr_ij, &ctx->nbr_d, &ctx->nbr_rows, &ctx->nbr_key, &ctx->nbr_tmp,
+       &ctx->nbr_rowptr, &ctx->nbr_col, &ctx->nbr_dist};
   return nullptr;
+}
+
+// ------------------------------------------------------ neighbour lists
+// The all-vs-all of one set in the neighbour layout: every pair with crmsd
+// <= eps appended (both directions), then sorted into CSR rows on the
+// device.  The append buffer starts at the previous call's size (or 2^22
+// entries) and grows to the exact count once if it overflowed.
+bs_status neighbors_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, float eps, const bs_opts &o,
+                         int64_t *nnz_out) {
+  ctx->metrics = bs_metrics{};
+  ctx->nbr_n = -1;
+  bs_status s;
+  if ((s = ensure(ctx, ctx->nbr_rowptr, (size_t)(n + 1) * 8, "neighbour rows"))) return s;
+  if (n < 2) {
+    CK(cudaMemsetAsync(ctx->nbr_rowptr.p, 0, (size_t)(n + 1) * 8, ctx->stream), "clear rows");
+    CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+    ctx->nbr_n = n;
+    ctx->nbr_nnz = 0;
+    *nnz_out = 0;
+    return BS_OK;
+  }
+  CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+  const double *dxyz = xyz;
+  if (!is_device_ptr(xyz)) {
+    const size_t bytes = (size_t)n * (size_t)L * 3 * sizeof(double);
+    if ((s = ensure(ctx, ctx->xyz, bytes, "coordinates"))) return s;
+    CK(cudaMemcpyAsync(ctx->xyz.p, xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
+    ctx->metrics.bytes_h2d += (int64_t)bytes;
+    dxyz = static_cast<const double *>(ctx->xyz.p);
+  }
+  const unsigned long long all = (unsigned long long)n * (unsigned long long)(n - 1);
+  unsigned long long cap = std::min(all, std::max(ctx->nbr_cap_hint, 1ull << 22));
+  if ((s = ensure(ctx, ctx->nbr_sink, sizeof(NbrSink), "neighbour sink")) ||
+      (s = ensure(ctx, ctx->nbr_count, 8, "neighbour count")))
+    return s;
+  unsigned long long count = 0;
+  const int64_t pairs = n * (n - 1) / 2;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if ((s = ensure(ctx, ctx->nbr_ij, (size_t)cap * 8, "neighbour pairs")) ||
+        (s = ensure(ctx, ctx->nbr_d, (size_t)cap * 4, "neighbour distances")))
+      return s;
+    const NbrSink sink{static_cast<unsigned long long *>(ctx->nbr_count.p), cap, static_cast<int2 *>(ctx->nbr_ij.p),
+                       static_cast<float *>(ctx->nbr_d.p)};
+    CK(cudaMemcpyAsync(ctx->nbr_sink.p, &sink, sizeof(sink), cudaMemcpyHostToDevice, ctx->stream), "sink");
+    CK(cudaMemsetAsync(ctx->nbr_count.p, 0, 8, ctx->stream), "clear count");
+    OutDesc od{ctx->nbr_sink.p, n, n, kLayoutNeighbors, 1};
+    od.eps = eps;
+    std::vector<JobSpec> specs{JobSpec{dxyz, n, L, od, 0}};
+    Plan plan;
+    const std::string m = make_symmetric_plan(specs, total_tolerance(o), true, plan);
+    if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
+    const unsigned long long fcap = std::min<unsigned long long>(kFlagCap, std::max<int64_t>(pairs, 4096));
+    MixedBuffers b;
+    if ((s = prepare_buffers(ctx, plan, fcap, b))) return s;
+    if ((s = upload_tables(ctx, plan, b, plan_key(ctx, plan, fcap)))) return s;
+    if ((s = launch_plan(ctx, plan, b, false))) return s;
+    CK(cudaMemcpyAsync(&count, ctx->nbr_count.p, 8, cudaMemcpyDeviceToHost, ctx->stream), "read count");
+    CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+    if ((s = finish_mixed(ctx, 1))) return s;
+    if (ctx->sc_back->flag_count > fcap)
+      return set_err(ctx, BS_ERR_UNSUPPORTED, "more than %llu pairs needed exact recomputation (neighbour lists)",
+                     fcap);
+    if (count <= cap) break;
+    cap = count;
+  }
+  if (count > cap) return set_err(ctx, BS_ERR_INTERNAL, "neighbour count changed between attempts");
+  ctx->nbr_cap_hint = count;
+  if ((s = ensure(ctx, ctx->nbr_rows, (size_t)n * 16, "row counters")) ||
+      (s = ensure(ctx, ctx->nbr_key, (size_t)count * 8, "neighbour keys")) ||
+      (s = ensure(ctx, ctx->nbr_tmp, (size_t)count * 8, "neighbour keys")) ||
+      (s = ensure(ctx, ctx->nbr_col, (size_t)count * 4, "neighbour columns")) ||
+      (s = ensure(ctx, ctx->nbr_dist, (size_t)count * 4, "neighbour distances")))
+    return s;
+  CK(launch_neighbors_csr(static_cast<const int2 *>(ctx->nbr_ij.p), static_cast<const float *>(ctx->nbr_d.p),
+                          (int64_t)count, n, ctx->num_sms, static_cast<int64_t *>(ctx->nbr_rowptr.p),
+                          static_cast<int32_t *>(ctx->nbr_col.p), static_cast<float *>(ctx->nbr_dist.p),
+                          static_cast<unsigned long long *>(ctx->nbr_rows.p),
+                          static_cast<unsigned long long *>(ctx->nbr_key.p),
+                          static_cast<unsigned long long *>(ctx->nbr_tmp.p), ctx->stream),
+     "neighbour rows");
+  CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  ctx->nbr_n = n;
+  ctx->nbr_nnz = (int64_t)count;
+  ctx->metrics.pairs = pairs;
+  ctx->metrics.ms_prep = elapsed(ctx, 1, 2);
+  ctx->metrics.ms_main = elapsed(ctx, 2, 3);
+  ctx->metrics.ms_refine = elapsed(ctx, 3, 4);
+  ctx->metrics.ms_total = elapsed(ctx, 0, 5);
+  *nnz_out = (int64_t)count;
+  return BS_OK;
 }
 
 }  // namespace
@@ -731,6 +824,41 @@ BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets,
   if ((s = validate_sets(ctx, sets, nsets))) return s;
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
   return sets_impl(ctx, sets, nsets, o);
+}
+
+BS_API bs_status bs_neighbors(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, double eps, const bs_opts *opts,
+                              int64_t *nnz) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (!nnz) return set_err(ctx, BS_ERR_INVALID_ARG, "null nnz");
+  if (!(eps >= 0.0) || !(eps < 3.0e38)) return set_err(ctx, BS_ERR_INVALID_ARG, "eps must be finite and >= 0");
+  bs_opts o;
+  bs_opts_init(&o);
+  if (opts) o = *opts;
+  bs_status s = check_opts(ctx, &o);
+  if (s) return s;
+  if (o.precision != BS_PRECISION_MIXED)
+    return set_err(ctx, BS_ERR_UNSUPPORTED, "neighbour lists are built by the mixed-precision path only");
+  if (n < 0 || L < 1) return set_err(ctx, BS_ERR_INVALID_ARG, "n must be >= 0 and L >= 1");
+  if (n > 0 && !xyz) return set_err(ctx, BS_ERR_INVALID_ARG, "null coordinates");
+  if (n > (1LL << 31) - 1) return set_err(ctx, BS_ERR_UNSUPPORTED, "n above 2^31-1");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  return neighbors_impl(ctx, xyz, n, L, (float)eps, o, nnz);
+}
+
+BS_API bs_status bs_neighbors_get(bs_ctx *ctx, int64_t *row_ptr, int32_t *col, float *dist) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (ctx->nbr_n < 0) return set_err(ctx, BS_ERR_INVALID_ARG, "no neighbour lists: call bs_neighbors first");
+  if (!row_ptr || (ctx->nbr_nnz > 0 && (!col || !dist))) return set_err(ctx, BS_ERR_INVALID_ARG, "null output");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  CK(cudaMemcpyAsync(row_ptr, ctx->nbr_rowptr.p, (size_t)(ctx->nbr_n + 1) * 8, cudaMemcpyDefault, ctx->stream),
+     "copy rows");
+  if (ctx->nbr_nnz > 0) {
+    CK(cudaMemcpyAsync(col, ctx->nbr_col.p, (size_t)ctx->nbr_nnz * 4, cudaMemcpyDefault, ctx->stream), "copy columns");
+    CK(cudaMemcpyAsync(dist, ctx->nbr_dist.p, (size_t)ctx->nbr_nnz * 4, cudaMemcpyDefault, ctx->stream),
+       "copy distances");
+  }
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  return BS_OK;
 }
 
 BS_API bs_status bs_tune_get(bs_ctx *ctx, int32_t L, int64_t n, int32_t *narrow) {

@@ -93,6 +93,10 @@ struct bs_ctx {
   bs_metrics metrics{};
   // workspaces
   bs::DevBuf xyz, out, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, y, g, ctrd, pairs_i, pairs_j, pout;
+  // eps-neighbour lists: appended pairs, then the CSR of the last bs_neighbors
+  bs::DevBuf nbr_sink, nbr_count, nbr_ij, nbr_d, nbr_rows, nbr_key, nbr_tmp, nbr_rowptr, nbr_col, nbr_dist;
+  int64_t nbr_n = -1, nbr_nnz = 0;
+  unsigned long long nbr_cap_hint = 0;
   void *job_stage = nullptr;  // pinned host copy of the job table
   size_t job_stage_cap = 0;
   void *job_back = nullptr;  // pinned read-back of the job table

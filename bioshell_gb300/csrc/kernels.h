@@ -45,15 +45,28 @@ struct __align__(16) SInfo {
 
 // Output description shared by every kernel that writes pair values.
 struct OutDesc {
-  void *ptr;
+  void *ptr;     // neighbour layout: a NbrSink in device memory
   int64_t n;     // rows
   int64_t ld;    // row stride of the square / rectangular layouts
-  int layout;    // 0 packed triangle, 1 square (both halves), 2 rectangular n x ld
+  int layout;    // 0 packed triangle, 1 square (both halves), 2 rectangular n x ld, 3 neighbour pairs
   int out_type;  // 0 f64, 1 f32
+  float eps;     // neighbour layout: pairs with crmsd <= eps are kept
+  int pad;
 };
 constexpr int kLayoutTriangle = 0;
 constexpr int kLayoutSquare = 1;
 constexpr int kLayoutRect = 2;
+constexpr int kLayoutNeighbors = 3;
+
+// Where the neighbour layout appends: every kept pair i < j of a job as the
+// two entries (i, j, d) and (j, i, d), job-local indices; `count` may end
+// above `cap` (the entries past cap are dropped and the caller retries).
+struct NbrSink {
+  unsigned long long *count;
+  unsigned long long cap;
+  int2 *ij;
+  float *d;
+};
 
 // One block of pairs of a launch: all pairs i < j of one structure set
 // (symmetric), or every pair of a query set against a library range
@@ -201,6 +214,10 @@ cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [7]: A digits e0 e1 e2 d2/3
 cudaError_t launch_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs, int num_sms, cudaStream_t st);
 size_t mixed_tc_smem_bytes();
 cudaError_t mixed_tc_prepare();
+// screen_tc.cu -- the same for launches whose tiles are all screen tiles
+// (tensor maps 0, 1, 4, 5 of the seven)
+cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t st);
+cudaError_t screen_tc_prepare();
 
 // refine.cu
 struct DigitsView {
@@ -253,6 +270,13 @@ cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, 
 // cand_n[r] > cap marks an overflowing row).  hist ([rows][4096] u32),
 // thresholds ([rows] u32) and cand_n are scratch the call clears itself.
 constexpr int kScreenBins = 4096;
+
+// neighbors.cu -- CSR rows (ordered by (d, j), without i itself) from the
+// cnt entries a neighbour-layout launch appended.  scratch_rows: 2n words;
+// key, tmp: cnt words each.
+cudaError_t launch_neighbors_csr(const int2 *ij, const float *d, int64_t cnt, int64_t n, int num_sms,
+                                 int64_t *row_ptr, int32_t *col, float *dist, unsigned long long *scratch_rows,
+                                 unsigned long long *key, unsigned long long *tmp, cudaStream_t st);
 cudaError_t launch_screen_select(const uint32_t *packed, int64_t rows, int64_t n, int64_t ld, int k, int cap,
                                  uint32_t *hist, uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st);
 

@@ -130,6 +130,27 @@ __device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t 
   }
 }
 
+// Neighbour layout: the warp's kept pairs appended with one atomic per warp
+// (every lane of the warp calls this).
+__device__ __forceinline__ void nbr_append(const OutDesc &o, bool hit, int64_t i, int64_t j, float v, int lane) {
+  const unsigned m = __ballot_sync(0xffffffffu, hit);
+  if (!m) return;
+  const NbrSink *sk = static_cast<const NbrSink *>(o.ptr);
+  const int lead = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == lead) base = atomicAdd(sk->count, 2ull * (unsigned long long)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, lead);
+  if (hit) {
+    const unsigned long long s = base + 2ull * (unsigned long long)__popc(m & ((1u << lane) - 1u));
+    if (s + 1 < sk->cap) {
+      sk->ij[s] = make_int2((int)i, (int)j);
+      sk->d[s] = v;
+      sk->ij[s + 1] = make_int2((int)j, (int)i);
+      sk->d[s + 1] = v;
+    }
+  }
+}
+
 __device__ __forceinline__ void fail(Shared *sh, DevScalars *sc) {
   sh->abort = 1;
   atomicOr(&sc->err, kErrTimeout);
@@ -428,26 +449,38 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
         }
         __syncwarp();
-        // the warp's 10 x 10 pairs over its 32 lanes, four rounds
+        // the warp's 10 x 10 pairs over its 32 lanes in four rounds, two
+        // rounds at a time (two independent dependency chains per lane)
         const int64_t i0 = (int64_t)t_ablk * kBlockStructs + qd * kGroupStructs - fa;
         const int64_t j0 = jg0 - fb;
 #pragma unroll 1
-        for (int rd = 0; rd < 4; ++rd) {
-          const int pp = rd * 32 + lane;
-          const int ir = pp / kGroupStructs, jc = pp - kGroupStructs * (pp / kGroupStructs);
-          const int64_t i = i0 + ir, j = j0 + jc;
-          if (!(job_ok && cols_ok && pp < kGroupStructs * kGroupStructs && i < jn && j < jnb)) continue;
-          float m9[9];
+        for (int rd = 0; rd < 4; rd += 2) {
+          float lo[2], hi[2];
+          bool ok[2];
+          int64_t oi[2];
 #pragma unroll
-          for (int xr = 0; xr < 3; ++xr)
+          for (int u = 0; u < 2; ++u) {
+            const int pp = (rd + u) * 32 + lane;
+            const int pc = pp < kGroupStructs * kGroupStructs ? pp : 0;  // pad slots read a valid pair
+            const int ir = pc / kGroupStructs, jc = pc - kGroupStructs * (pc / kGroupStructs);
+            const int64_t i = i0 + ir, j = j0 + jc;
+            ok[u] = job_ok && cols_ok && pp < kGroupStructs * kGroupStructs && i < jn && j < jnb;
+            oi[u] = i * out.ld + j;
+            float m9[9];
 #pragma unroll
-            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
-          const float2 ta = mt.ta[qd * kGroupStructs + ir], tb = mt.tb[g * kGroupStructs + jc];
-          float lo, hi;
-          bsm::screen_bracket(m9, ta.x + tb.x, t_d34, ta.y + tb.y, t_u, t_L, lo, hi);
-          const uint32_t wlo = __half_as_ushort(__float2half_rd(lo));
-          const uint32_t whi = __half_as_ushort(__float2half_ru(hi));
-          sout[i * out.ld + j] = (whi << 16) | wlo;
+            for (int xr = 0; xr < 3; ++xr)
+#pragma unroll
+              for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+            const float2 ta = mt.ta[qd * kGroupStructs + ir], tb = mt.tb[g * kGroupStructs + jc];
+            bsm::screen_bracket(m9, ta.x + tb.x, t_d34, ta.y + tb.y, t_u, t_L, lo[u], hi[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            if (!ok[u]) continue;
+            const uint32_t wlo = __half_as_ushort(__float2half_rd(lo[u]));
+            const uint32_t whi = __half_as_ushort(__float2half_ru(hi[u]));
+            sout[oi[u]] = (whi << 16) | wlo;
+          }
         }
         __syncwarp();
         ptx::mbar_arrive(&sh->mempty[slot]);
@@ -559,21 +592,26 @@ __global__ void __launch_bounds__(kThreads, 1)
           ptx::mbar_arrive(&sh->tempty[p & 1u]);
           if (lng) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
         }
-        // ---- finish and store
+        // ---- finish and store (neighbour layout: flagged pairs are kept or
+        // dropped by the exact recomputation)
+        const bool nbr = out.layout == kLayoutNeighbors;  // the same for the whole warp
 #pragma unroll
         for (int sl = 0; sl < 2; ++sl) {
-          if (!valid[sl]) continue;
           const int64_t j = jj[sl];
           int flag = 0;
-          const float r = bsm::fast_finish(st[sl], ia.ghat + ib[sl].ghat, ia.gf + ib[sl].gf, ia.qres + ib[sl].qres,
-                                           t_d34, t_u, t_L, t_tol, flag);
-          if (flag) {
-            store_pair(out, i, j, -1.0f);
-            const unsigned long long q = atomicAdd(&a.sc->flag_count, 1ull);
-            if (q < a.flag_cap) a.flags[q] = flag_pack(t_job, ig, j + fb);
-          } else {
-            store_pair(out, i, j, r);
+          float r = 0.f;
+          if (valid[sl]) {
+            r = bsm::fast_finish(st[sl], ia.ghat + ib[sl].ghat, ia.gf + ib[sl].gf, ia.qres + ib[sl].qres, t_d34,
+                                 t_u, t_L, t_tol, flag);
+            if (flag) {
+              if (!nbr) store_pair(out, i, j, -1.0f);
+              const unsigned long long q = atomicAdd(&a.sc->flag_count, 1ull);
+              if (q < a.flag_cap) a.flags[q] = flag_pack(t_job, ig, j + fb);
+            } else if (!nbr) {
+              store_pair(out, i, j, r);
+            }
           }
+          if (nbr) nbr_append(out, valid[sl] && !flag && r <= out.eps, i, j, r, lane);
         }
       }
       // the tile's metadata is no longer read: release its slot

@@ -145,7 +145,10 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     a.flag_cap = b.flag_cap;
     a.dbg = dbg;
     a.num_sms = num_sms;
-    if ((e = launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
+    // launches of screen jobs only run the screen-shaped kernel
+    bool all_screen = nj > 0;
+    for (const Job &jb : plan.jobs) all_screen = all_screen && jb.screen;
+    if ((e = all_screen ? launch_screen_tc(tm, a, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
     if ((e = rec(2)) != cudaSuccess) return e;
     RefineArgs r{};
     r.da = DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a};

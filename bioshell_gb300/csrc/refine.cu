@@ -27,6 +27,19 @@ __device__ __forceinline__ void tri_pair(int64_t n, int64_t t, int64_t &i, int64
 }
 
 __device__ __forceinline__ void store_pair(const OutDesc &o, int64_t i, int64_t j, double v) {
+  if (o.layout == kLayoutNeighbors) {  // the pair's crmsd as the tensor-core path keeps it: f32
+    const float f = (float)v;
+    if (!(f <= o.eps)) return;
+    const NbrSink *sk = static_cast<const NbrSink *>(o.ptr);
+    const unsigned long long s = atomicAdd(sk->count, 2ull);
+    if (s + 1 < sk->cap) {
+      sk->ij[s] = make_int2((int)i, (int)j);
+      sk->d[s] = f;
+      sk->ij[s + 1] = make_int2((int)j, (int)i);
+      sk->d[s + 1] = f;
+    }
+    return;
+  }
   int64_t idx, idx2 = -1;
   if (o.layout == kLayoutTriangle) {
     idx = tri_index(o.n, i, j);
@@ -106,7 +119,7 @@ __global__ void k_refine_scan(RefineArgs r) {
   const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   for (int job = 0; job < r.njobs; ++job) {
     const Job &jb = r.jobs[job];
-    if (jb.err) continue;
+    if (jb.err || jb.out.layout == kLayoutNeighbors) continue;  // no sentinels to find: the host reports it
     const OutDesc &out = jb.out;
     const bool sym = jb.mode == 0;
     const int64_t n = jb.n, nb = jb.n_b;

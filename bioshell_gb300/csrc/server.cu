@@ -350,11 +350,17 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
     jb.qres_b = bk.qres;
     jb.screen = screen ? 1 : 0;
     plan.jobs.push_back(jb);
-    const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
-    for (int64_t I = 0; I < nb; ++I)
-      for (int64_t J = 0; J < nbb; ++J) plan.tiles.push_back(Tile{(int)(blk + I), (int)J, j, 0});
     blk += nb;
     rows += r->q;
+  }
+  // tiles column block by column block: the persistent blocks sweep the
+  // library once, each library block read from HBM once and reused from L2
+  // by every query block of the batch
+  {
+    const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
+    plan.tiles.reserve((size_t)(blk * nbb));
+    for (int64_t J = 0; J < nbb; ++J)
+      for (int64_t I = 0; I < blk; ++I) plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], 0});
   }
   plan.nblocks = blk;
   sl.rows = rows;
@@ -854,7 +860,8 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
   s->precision = cfg->precision;
   s->tol = (float)(cfg->tolerance > 0 ? cfg->tolerance : 1e-4);
   cudaSetDevice(device);
-  if (mixed_tc_prepare() != cudaSuccess || prep_prepare() != cudaSuccess || !get_encoder(&s->encode).empty()) {
+  if (mixed_tc_prepare() != cudaSuccess || screen_tc_prepare() != cudaSuccess || prep_prepare() != cudaSuccess ||
+      !get_encoder(&s->encode).empty()) {
     delete s;
     return BS_ERR_CUDA;
   }

@@ -112,6 +112,9 @@ SIGNATURES = [
     ("bs_cut_tree", ctypes.c_int32, [_i64p, _fp, ctypes.c_int64, ctypes.c_float, _i64p]),
     ("bs_optics", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, _i64p,
                                    _dp, _i64p]),
+    ("bs_neighbors", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.POINTER(bs_opts), _i64p]),
+    ("bs_neighbors_get", ctypes.c_int32, [_vp, _vp, _vp, _vp]),
     ("bs_optics_neighbors", ctypes.c_int32, [_i64p, _i32p, _fp, ctypes.c_int64, ctypes.c_double, ctypes.c_int32,
                                              _i64p, _dp, _i64p]),
     ("bs_host_alloc", ctypes.c_int32, [ctypes.c_size_t, ctypes.POINTER(_vp)]),

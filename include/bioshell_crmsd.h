@@ -188,6 +188,17 @@ typedef struct {
  * call.  The plain path runs the sets one after another. */
 BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets, const bs_opts *opts);
 
+/* eps-neighbour lists of n structures (the input of OPTICS,
+ * optics.rs:51-148, through NeighborsOf, points_set.rs:29-39) without the
+ * dense matrix: the all-vs-all runs on the mixed path and keeps, for every
+ * structure i, the structures j != i with crmsd(i, j) <= eps, ordered by
+ * (crmsd, j) -- the f32 values the dense f32 matrix would hold.  The lists
+ * stay on the context; *nnz receives their total length, and
+ * bs_neighbors_get copies them out (CSR: row_ptr[n + 1] int64, col[nnz]
+ * int32, dist[nnz] f32; host or device memory).  Mixed precision only. */
+BS_API bs_status bs_neighbors(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, double eps, const bs_opts *opts,
+                              int64_t *nnz);
+BS_API bs_status bs_neighbors_get(bs_ctx *ctx, int64_t *row_ptr, int32_t *col, float *dist);
 /* The autotuner's cache of a context: the tile shape of the class of sets
  * with chain length L and size n (narrow = 1: 40 x 10 tiles, 0: 40 x 20).
  * bs_tune_get returns -1 for a class not timed yet; bs_tune_set fixes a
