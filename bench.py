@@ -232,6 +232,53 @@ def run_neighbors(eng, xd, outd, n, torch, eps=1.0, steps=3):
             "dense_f32_bytes": int(4 * n * (n - 1) // 2), "rows_checked_against_dense": len(rows), "match": ok}
 
 
+def run_formats(eng, torch, n_models=1000, L=300, n_tsv=4000):
+    """Throughput of the formats either side of the path: multi-model PDB
+    ingestion (a synthetic ensemble of n_models x L residues, 4 atoms each,
+    CA selected) and TSV export of a device-resident f64 triangle."""
+    import tempfile
+    import time
+    from bioshell_gb300 import formats as F
+    rng = np.random.default_rng(12)
+    base = synth.base_chain(L, rng)
+    ens = synth.decoys(base, n_models, rng)
+    names = (" N  ", " CA ", " C  ", " O  ")
+    with tempfile.TemporaryDirectory() as d:
+        pdb = os.path.join(d, "ens.pdb")
+        with open(pdb, "w") as fh:
+            for m in range(n_models):
+                fh.write(f"MODEL     {m + 1:4d}\n")
+                rows = []
+                for r in range(L):
+                    for k, nm in enumerate(names):
+                        x, y, z = ens[m, r] + 0.5 * k
+                        rows.append(f"ATOM  {4 * r + k + 1:5d} {nm} ALA A{r + 1:4d}    {x:8.3f}{y:8.3f}{z:8.3f}"
+                                    f"  1.00  0.00           {nm.strip()[0]}\n")
+                fh.write("".join(rows))
+                fh.write("ENDMDL\n")
+        size = os.path.getsize(pdb)
+        t0 = time.perf_counter()
+        ca = F.read_models(pdb, ca_only=True)
+        t_read = time.perf_counter() - t0
+        ok = bool(np.array_equal(ca, np.round(ens, 3)))
+        x = synth.decoys(synth.base_chain(150, rng), n_tsv, rng)
+        npair = n_tsv * (n_tsv - 1) // 2
+        dev = torch.empty(npair, dtype=torch.float64, device="cuda")
+        eng.all_vs_all(torch.from_numpy(x).cuda(), out=dev)
+        tsv = os.path.join(d, "m.tsv")
+        labels = [f"model_{i}" for i in range(n_tsv)]
+        t0 = time.perf_counter()
+        F.write_tsv(tsv, dev, labels, n=n_tsv)
+        t_tsv = time.perf_counter() - t0
+        tsv_bytes = os.path.getsize(tsv)
+    return {"models": {"file": f"PDB, {n_models} models x {L} residues x 4 atoms, CA selected",
+                       "bytes": size, "seconds": t_read, "MB_per_s": size / t_read / 1e6,
+                       "models_per_s": n_models / t_read, "exact": ok},
+            "tsv_export": {"pairs": npair, "source": "device f64 triangle", "bytes": tsv_bytes, "seconds": t_tsv,
+                           "lines_per_s": npair / t_tsv, "MB_per_s": tsv_bytes / t_tsv / 1e6,
+                           "threads": host_threads()}}
+
+
 def run_batched(a, eng, stream, torch):
     """The batched form: all sets in one call per step (graph replay)."""
     from bioshell_gb300 import clustering as K
@@ -560,6 +607,7 @@ def run_ours(a, rank, world, local_rank):
         eng.close()  # frees the 50k workspaces before the next sections
         eng = Engine(local_rank)
         stream = torch.cuda.ExternalStream(eng.stream_handle())
+    formats = run_formats(eng, torch) if rank == 0 and not a.skip_batched else None
     if not a.skip_batched and rank == 0:
         batched = run_batched(a, eng, stream, torch)
     if not a.skip_serving and rank == 0:
@@ -573,6 +621,7 @@ def run_ours(a, rank, world, local_rank):
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
             "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
+            "formats": formats,
             "batched": batched,
             "serving": serving}
     if rank == 0:

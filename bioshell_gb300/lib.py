@@ -117,6 +117,16 @@ SIGNATURES = [
     ("bs_neighbors_get", ctypes.c_int32, [_vp, _vp, _vp, _vp]),
     ("bs_optics_neighbors", ctypes.c_int32, [_i64p, _i32p, _fp, ctypes.c_int64, ctypes.c_double, ctypes.c_int32,
                                              _i64p, _dp, _i64p]),
+    ("bs_io_last_error", ctypes.c_char_p, []),
+    ("bs_models_read", ctypes.c_int32, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_vp), _i64p,
+                                        _i32p]),
+    ("bs_models_copy", ctypes.c_int32, [_vp, _vp]),
+    ("bs_models_free", None, [_vp]),
+    ("bs_tsv_write", ctypes.c_int32, [ctypes.c_char_p, _vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32]),
+    ("bs_tsv_read", ctypes.c_int32, [ctypes.c_char_p, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(_vp), _i64p]),
+    ("bs_tsv_matrix", ctypes.c_int32, [_vp, _fp]),
+    ("bs_tsv_label", ctypes.c_char_p, [_vp, ctypes.c_int64]),
+    ("bs_tsv_free", None, [_vp]),
     ("bs_host_alloc", ctypes.c_int32, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
     ("bs_host_free", ctypes.c_int32, [_vp]),
     ("bs_selftest_digits", ctypes.c_int32, [_dp, ctypes.c_int32, ctypes.c_int32, _i32p, _i64p, _dp]),

@@ -349,6 +349,43 @@ BS_API bs_status bs_optics_neighbors(const int64_t *row_ptr, const int32_t *col,
                                      double eps, int32_t min_points, int64_t *order, double *reach,
                                      int64_t *cluster_of);
 
+/* ---- data formats on either side of the path (host) --------------------- */
+/* Message of the last failed call below on this thread (never NULL). */
+BS_API const char *bs_io_last_error(void);
+/* Multi-model ingestion: the coordinates of every model of a PDB or mmCIF
+ * file (format 0 = detect from the first line, 1 = PDB, 2 = mmCIF) as
+ * bioshell-pdb keeps them in Structure::model_coordinates (structure.rs:100),
+ * read in one pass instead of a set_model per model: PDB ATOM/HETATM records
+ * with models split at ENDMDL (load_pdb.rs:52-115, Vec3::from_pdb_line,
+ * vec3.rs:241-246); mmCIF _atom_site rows with models in order of first
+ * appearance of pdbx_PDB_model_num (pdb_atom.rs:130-170).  selection 0 keeps
+ * every atom, 1 the atoms named " CA " (IsCA, pdb_atom_filters.rs:388-413;
+ * mmCIF names formatted as format_atom_name does, pdb_atom.rs:306-331).
+ * Every model must hold the same atoms.  *n_models x *n_atoms coordinates
+ * are then copied by bs_models_copy into xyz[n][L][3] (host or device
+ * memory, e.g. a bs_host_alloc buffer that feeds bs_all_vs_all). */
+typedef struct bs_models bs_models;
+BS_API bs_status bs_models_read(const char *path, int32_t format, int32_t selection, bs_models **out, int64_t *n_models,
+                                int32_t *n_atoms);
+BS_API bs_status bs_models_copy(const bs_models *m, double *xyz);
+BS_API void bs_models_free(bs_models *m);
+/* Distance-matrix TSV, the input of the clust tool (clust.rs:102-105,
+ * tests/test_files/d5.tsv): "label<TAB>label<TAB>value" lines.
+ * bs_tsv_write writes the n(n-1)/2 pairs of a packed triangle (host or
+ * device memory, element type out_type) in row order, labels[i] (NULL: the
+ * index) and `decimals` digits after the point (<= 0: 6), rounded as
+ * printf("%.*f") rounds; device triangles are streamed through pinned
+ * buffers while all host threads format.  bs_tsv_read numbers the labels in
+ * order of first appearance (row, then column label); pair {i, j} takes the
+ * value of line (i, j), else of line (j, i) when `symmetric`, else
+ * default_value; bs_tsv_matrix copies the f32 packed triangle out. */
+typedef struct bs_tsv bs_tsv;
+BS_API bs_status bs_tsv_write(const char *path, const void *tri, int64_t n, int32_t out_type, const char *const *labels,
+                              int32_t decimals);
+BS_API bs_status bs_tsv_read(const char *path, double default_value, int32_t symmetric, bs_tsv **out, int64_t *n);
+BS_API bs_status bs_tsv_matrix(const bs_tsv *t, float *tri);
+BS_API const char *bs_tsv_label(const bs_tsv *t, int64_t i);
+BS_API void bs_tsv_free(bs_tsv *t);
 /* ---- pinned host memory ------------------------------------------------- */
 /* Page-locked host buffers for fast host<->device staging (cudaHostAlloc);
  * free with bs_host_free.  Pageable memory is accepted everywhere too. */
