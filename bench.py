@@ -68,6 +68,9 @@ def args_():
     p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--probe-serving", type=int, default=0, metavar="K",
+                   help="only run K query batches of 256 structures of the 64-atom bucket through a one-slot "
+                        "server over the 200,000-structure library (a profiling target), print one JSON line")
     return p.parse_args()
 
 
@@ -260,7 +263,9 @@ def run_formats(eng, torch, n_models=1000, L=300, n_tsv=4000):
         t0 = time.perf_counter()
         ca = F.read_models(pdb, ca_only=True)
         t_read = time.perf_counter() - t0
-        ok = bool(np.array_equal(ca, np.round(ens, 3)))
+        # the CA record of residue r is written at ens + 0.5 (atom index 1)
+        want = np.array([float(f"{v:.3f}") for v in (ens[:4] + 0.5).ravel()]).reshape(4, L, 3)
+        ok = bool(np.array_equal(ca[:4], want) and ca.shape == (n_models, L, 3))
         x = synth.decoys(synth.base_chain(150, rng), n_tsv, rng)
         npair = n_tsv * (n_tsv - 1) // 2
         dev = torch.empty(npair, dtype=torch.float64, device="cuda")
@@ -277,6 +282,27 @@ def run_formats(eng, torch, n_models=1000, L=300, n_tsv=4000):
             "tsv_export": {"pairs": npair, "source": "device f64 triangle", "bytes": tsv_bytes, "seconds": t_tsv,
                            "lines_per_s": npair / t_tsv, "MB_per_s": tsv_bytes / t_tsv / 1e6,
                            "threads": host_threads()}}
+
+
+def run_hierarchical(eng, n=3000, L=150, rule="average"):
+    """Agglomerative clustering of an n-structure crmsd matrix: the host
+    version against the GPU one (same merges required)."""
+    import time
+    from bioshell_gb300 import clustering as K
+    from bioshell_gb300.crmsd import CrmsdOptions
+    rng = np.random.default_rng(13)
+    x = synth.decoys(synth.base_chain(L, rng), n, rng)
+    m = eng.all_vs_all(x, CrmsdOptions(out_type="f32"))
+    t0 = time.perf_counter()
+    dev = K.hierarchical_clustering(m, rule, engine=eng)
+    t_gpu = time.perf_counter() - t0
+    kernel_ms = eng.metrics()["ms_main"]
+    t0 = time.perf_counter()
+    host = K.hierarchical_clustering(m, rule)
+    t_host = time.perf_counter() - t0
+    same = bool(np.array_equal(dev.merges, host.merges) and np.array_equal(dev.dist, host.dist))
+    return {"n": n, "rule": rule, "gpu_s": t_gpu, "gpu_kernel_ms": kernel_ms,
+            "host_s": t_host, "speedup": t_host / t_gpu, "identical_merges": same}
 
 
 def run_batched(a, eng, stream, torch):
@@ -608,6 +634,7 @@ def run_ours(a, rank, world, local_rank):
         eng = Engine(local_rank)
         stream = torch.cuda.ExternalStream(eng.stream_handle())
     formats = run_formats(eng, torch) if rank == 0 and not a.skip_batched else None
+    hier = run_hierarchical(eng) if rank == 0 and not a.skip_batched else None
     if not a.skip_batched and rank == 0:
         batched = run_batched(a, eng, stream, torch)
     if not a.skip_serving and rank == 0:
@@ -621,13 +648,31 @@ def run_ours(a, rank, world, local_rank):
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
             "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
-            "formats": formats,
+            "formats": formats, "hierarchical": hier,
             "batched": batched,
             "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def probe_serving(k):
+    import time
+    from bioshell_gb300 import CrmsdServer
+    lib, bases = synth.serving_library()
+    pools = synth.serving_queries(bases)
+    srv = CrmsdServer(lib, top_k=50, max_inflight=1)
+    srv.wait(srv.submit(pools[64][:256]))
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    for q in range(k):
+        srv.wait(srv.submit(pools[64][(q * 64) % 768:(q * 64) % 768 + 256]))
+    dt = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    print(json.dumps({"probe": "serving", "batches": k, "rows": 256, "library": int(lib[64].shape[0]),
+                      "seconds": dt, "pairs_per_s": k * 256 * lib[64].shape[0] / dt, "p50_ms": st["p50_ms"]}))
 
 
 def main():
@@ -637,6 +682,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if a.impl == "reference":
         run_reference(a, rank)
+        return
+    if a.probe_serving > 0:
+        probe_serving(a.probe_serving)
         return
     run_ours(a, rank, world, local_rank)
 

@@ -57,15 +57,19 @@ def _check(st, what):
         raise _l.CrmsdError(st, what)
 
 
-def hierarchical_clustering(matrix: CrmsdMatrix, rule: str = "single") -> ClusteringTree:
+def hierarchical_clustering(matrix: CrmsdMatrix, rule: str = "single", engine=None) -> ClusteringTree:
+    """Agglomerative clustering of the matrix; on the GPU of ``engine`` when
+    one is given (same merges, bit for bit), else on the host."""
     v, ot = _tri(matrix)
     n = matrix.n
     merges = np.zeros((max(n - 1, 0), 4), dtype=np.int64)
     dist = np.zeros(max(n - 1, 0), dtype=np.float32)
-    st = _l.load().bs_hierarchical(v.ctypes.data, n, ot, _l.LINK[rule],
-                                   merges.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-                                   dist.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
-    _check(st, "bs_hierarchical")
+    mp = merges.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    dp = dist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    if engine is not None:
+        engine._check(_l.load().bs_hierarchical_gpu(engine._h, v.ctypes.data, n, ot, _l.LINK[rule], mp, dp))
+    else:
+        _check(_l.load().bs_hierarchical(v.ctypes.data, n, ot, _l.LINK[rule], mp, dp), "bs_hierarchical")
     return ClusteringTree(n, merges, dist)
 
 

@@ -590,7 +590,7 @@ DevBuf *all_buffers(bs_ctx *ctx, std::vector<DevBuf *> &v) {
        &ctx->dig[3],  &ctx->jobs,   &ctx->jobmap, &ctx->tiles, &ctx->flags,  &ctx->y,      &ctx->g,
        &ctx->ctrd,    &ctx->pairs_i, &ctx->pairs_j, &ctx->pout,
        &ctx->nbr_sink, &ctx->nbr_count, &ctx->nbr_ij, &ctx->nbr_d, &ctx->nbr_rows, &ctx->nbr_key, &ctx->nbr_tmp,
-       &ctx->nbr_rowptr, &ctx->nbr_col, &ctx->nbr_dist};
+       &ctx->nbr_rowptr, &ctx->nbr_col, &ctx->nbr_dist, &ctx->hier_ws, &ctx->hier_tri, &ctx->hier_out};
   return nullptr;
 }
 
@@ -843,6 +843,51 @@ BS_API bs_status bs_neighbors(bs_ctx *ctx, const double *xyz, int64_t n, int32_t
   if (n > (1LL << 31) - 1) return set_err(ctx, BS_ERR_UNSUPPORTED, "n above 2^31-1");
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
   return neighbors_impl(ctx, xyz, n, L, (float)eps, o, nnz);
+}
+
+BS_API bs_status bs_hierarchical_gpu(bs_ctx *ctx, const void *tri, int64_t n, int32_t out_type, int32_t rule,
+                                     int64_t *merges, float *merge_dist) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (n < 0 || (n > 1 && (!tri || !merges || !merge_dist))) return set_err(ctx, BS_ERR_INVALID_ARG, "bad argument");
+  if (out_type != BS_OUT_F64 && out_type != BS_OUT_F32) return set_err(ctx, BS_ERR_INVALID_ARG, "out_type");
+  if (rule < BS_LINK_SINGLE || rule > BS_LINK_WARD) return set_err(ctx, BS_ERR_INVALID_ARG, "unknown merge rule");
+  if (n < 2) return BS_OK;
+  if (n > (1LL << 20)) return set_err(ctx, BS_ERR_UNSUPPORTED, "n above 2^20");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  ctx->metrics = bs_metrics{};
+  const int grid = hier_grid(ctx->num_sms);
+  const size_t esz = out_type == BS_OUT_F64 ? 8 : 4;
+  const size_t tri_bytes = (size_t)(n * (n - 1) / 2) * esz;
+  bs_status s;
+  if ((s = ensure(ctx, ctx->hier_ws, hier_workspace_bytes(n, grid), "clustering matrix")) ||
+      (s = ensure(ctx, ctx->hier_out, (size_t)(n - 1) * 36, "clustering merges")))
+    return s;
+  CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+  const void *dtri = tri;
+  if (!is_device_ptr(tri)) {
+    if ((s = ensure(ctx, ctx->hier_tri, tri_bytes, "matrix staging"))) return s;
+    CK(cudaMemcpyAsync(ctx->hier_tri.p, tri, tri_bytes, cudaMemcpyHostToDevice, ctx->stream), "copy matrix");
+    dtri = ctx->hier_tri.p;
+  }
+  int64_t *dm = static_cast<int64_t *>(ctx->hier_out.p);
+  float *dd = reinterpret_cast<float *>(dm + 4 * (n - 1));
+  CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+  int *derr = nullptr;
+  CK(launch_hierarchical(dtri, out_type == BS_OUT_F64 ? 0 : 1, n, rule, ctx->hier_ws.p, grid, dm, dd, &derr,
+                         ctx->stream),
+     "clustering launch");
+  CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "read status");
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  if (herr == 100) return set_err(ctx, BS_ERR_INTERNAL, "clustering: inconsistent merge pair");
+  if (herr) return set_err(ctx, BS_ERR_TIMEOUT, "clustering: grid barrier of phase %d timed out", herr - 1);
+  CK(cudaMemcpyAsync(merges, dm, (size_t)(n - 1) * 32, cudaMemcpyDefault, ctx->stream), "copy merges");
+  CK(cudaMemcpyAsync(merge_dist, dd, (size_t)(n - 1) * 4, cudaMemcpyDefault, ctx->stream), "copy distances");
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  ctx->metrics.ms_main = elapsed(ctx, 1, 2);
+  ctx->metrics.ms_total = elapsed(ctx, 0, 2);
+  return BS_OK;
 }
 
 BS_API bs_status bs_neighbors_get(bs_ctx *ctx, int64_t *row_ptr, int32_t *col, float *dist) {

@@ -81,12 +81,14 @@ struct ColMin {
   int64_t i;
 };
 
-// min over rows r < j of column j, first (smallest r) on ties
+// min over rows r < j of column j, first (smallest r) on ties.  The working
+// matrix stays exactly symmetric through every update below, so the column
+// is read along row j (contiguous).
 inline ColMin column_min(const std::vector<float> &m, int64_t n, int64_t j) {
   ColMin c{FLT_MAX, 0};
-  const float *col = m.data();
+  const float *row = m.data() + j * n;
   for (int64_t r = 0; r < j; ++r) {
-    const float v = col[r * n + j];
+    const float v = row[r];
     if (v < c.v) {
       c.v = v;
       c.i = r;

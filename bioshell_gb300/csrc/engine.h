@@ -56,6 +56,7 @@ struct Plan {
   std::vector<Tile> tiles;
   int64_t nblocks = 0;  // 40-structure A blocks
   int pitch = 0;
+  bool strips = false;  // screen plan whose `tiles` are strip records (launch_screen_tc)
 };
 
 // Builds the jobs, block map and tile table of symmetric jobs.  Tiles of the
@@ -96,6 +97,8 @@ struct bs_ctx {
   // eps-neighbour lists: appended pairs, then the CSR of the last bs_neighbors
   bs::DevBuf nbr_sink, nbr_count, nbr_ij, nbr_d, nbr_rows, nbr_key, nbr_tmp, nbr_rowptr, nbr_col, nbr_dist;
   int64_t nbr_n = -1, nbr_nnz = 0;
+  // hierarchical clustering on the device: workspace, staged triangle, results
+  bs::DevBuf hier_ws, hier_tri, hier_out;
   unsigned long long nbr_cap_hint = 0;
   void *job_stage = nullptr;  // pinned host copy of the job table
   size_t job_stage_cap = 0;

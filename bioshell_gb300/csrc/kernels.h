@@ -215,9 +215,12 @@ cudaError_t launch_tile_shapes(Tile *tiles, int64_t ntiles, const Job *jobs, int
 size_t mixed_tc_smem_bytes();
 cudaError_t mixed_tc_prepare();
 // screen_tc.cu -- the same for launches whose tiles are all screen tiles
-// (tensor maps 0, 1, 4, 5 of the seven)
-cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t st);
+// (tensor maps 0, 1, 4, 5 of the seven).  strips: a.tiles holds strip
+// records {query block, first library block, job, nk16 | count << 16} (chains
+// of at most screen_strip_max_nk16() 16-atom steps); else screen tiles.
+cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, bool strips, cudaStream_t st);
 cudaError_t screen_tc_prepare();
+int screen_strip_max_nk16();
 
 // refine.cu
 struct DigitsView {
@@ -270,6 +273,15 @@ cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, 
 // cand_n[r] > cap marks an overflowing row).  hist ([rows][4096] u32),
 // thresholds ([rows] u32) and cand_n are scratch the call clears itself.
 constexpr int kScreenBins = 4096;
+
+// hier.cu -- hierarchical clustering of a packed triangle on the device (one
+// cooperative launch; merges[n-1][4] and merge_dist[n-1] device buffers)
+size_t hier_workspace_bytes(int64_t n, int grid);
+int hier_grid(int num_sms);
+// *err_out: a device int, 0 after a complete run, else 1 + the phase whose
+// grid barrier timed out (100: an inconsistent merge pair)
+cudaError_t launch_hierarchical(const void *tri, int out_type, int64_t n, int rule, void *ws, int grid,
+                                int64_t *merges, float *merge_dist, int **err_out, cudaStream_t st);
 
 // neighbors.cu -- CSR rows (ordered by (d, j), without i itself) from the
 // cnt entries a neighbour-layout launch appended.  scratch_rows: 2n words;

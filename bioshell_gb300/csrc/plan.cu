@@ -131,7 +131,10 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
   if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
   if ((e = rec(1)) != cudaSuccess) return e;
   if (!plan.tiles.empty()) {
-    if ((e = launch_tile_shapes(b.tiles, (int64_t)plan.tiles.size(), b.jobs, num_sms, st)) != cudaSuccess) return e;
+    // strip records carry their shape; tiles get theirs from the prepared jobs
+    if (!plan.strips &&
+        (e = launch_tile_shapes(b.tiles, (int64_t)plan.tiles.size(), b.jobs, num_sms, st)) != cudaSuccess)
+      return e;
     TcArgs a{};
     a.tiles = b.tiles;
     a.ntiles = (int64_t)plan.tiles.size();
@@ -148,7 +151,8 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     // launches of screen jobs only run the screen-shaped kernel
     bool all_screen = nj > 0;
     for (const Job &jb : plan.jobs) all_screen = all_screen && jb.screen;
-    if ((e = all_screen ? launch_screen_tc(tm, a, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
+    if ((e = all_screen ? launch_screen_tc(tm, a, plan.strips, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess)
+      return e;
     if ((e = rec(2)) != cudaSuccess) return e;
     RefineArgs r{};
     r.da = DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a};

@@ -8,15 +8,19 @@
 // library chain of 64 atoms is four 16-atom steps of two or three MMAs, so a
 // tile's tensor work is ~1 us and the pipeline around it decides the rate.
 // This kernel is shaped for that:
-//   * three operand stages of 48 KB (A digits 0-1, B digits 0-1), so loads
-//     run two tiles ahead;
 //   * per 16-atom step two instructions: A digit d against the B digits
 //     [0 | 1] (N = 128), into the adjacent accumulators [L0 | L1 | L11]
 //     (e0e0 | e0e1 + e1e0 | e1e1) -- three at the first step, where each
 //     accumulator's first write must overwrite;
 //   * sixteen epilogue warps (four per TMEM lane quarter, each finishing 10 x
 //     5 pairs), so that the dependent FP32 chains of the bracket have enough
-//     warps to hide their latency.
+//     warps to hide their latency;
+//   * two ways of feeding the operands.  Tile list: three stages of 48 KB
+//     (A digits 0-1, B digits 0-1 of one tile).  Strips (chains of up to 128
+//     atoms): a record is a query block and a run of library column blocks;
+//     the query block's digits stay resident in shared memory for the whole
+//     run (64 KB) and four 16 KB stages stream only the library blocks --
+//     a third of the bytes per tile, which is what bounds short tiles.
 // Roles (one persistent CTA per SM, 640 threads): warp 0 TMA (operands, and a
 // bulk copy of each tile's job and per-structure data), warp 1 MMA issuer,
 // warp 2 TMEM allocation, warp 3 idle, warps 4-19 epilogue.  Every mbarrier
@@ -31,11 +35,24 @@
 namespace bs {
 namespace {
 
-constexpr int kStages = 3;
 constexpr int kBRows = 64;
 constexpr int kAOpBytes = kBlockRows * kKChunk * 2;  // 16 KB
 constexpr int kBOpBytes = kBRows * kKChunk * 2;      // 8 KB
-constexpr int kStageBytes = 2 * kAOpBytes + 2 * kBOpBytes;
+// tile list: [A0 A1 B0 B1] per stage; strips: [B0 B1] per stage + resident A
+template <bool S> struct Feed;
+template <> struct Feed<false> {
+  static constexpr int kStages = 3;
+  static constexpr int kStageBytes = 2 * kAOpBytes + 2 * kBOpBytes;
+  static constexpr int kABytes = 0;
+  static constexpr int kBOff = 2 * kAOpBytes;  // B digits within a stage
+};
+template <> struct Feed<true> {
+  static constexpr int kStages = 4;
+  static constexpr int kStageBytes = 2 * kBOpBytes;
+  static constexpr int kStripChunks = 2;  // chains up to 128 atoms
+  static constexpr int kABytes = kStripChunks * 2 * kAOpBytes;
+  static constexpr int kBOff = 0;
+};
 constexpr int kEpiWarp0 = 4;
 constexpr int kEpiWarps = 16;
 constexpr int kThreads = (kEpiWarp0 + kEpiWarps) * 32;
@@ -53,19 +70,25 @@ struct __align__(16) ScreenMeta {
   Tile tile;
 };
 constexpr int kMetaBytes = kMetaSlots * (int)sizeof(ScreenMeta);
-constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes + kBarBytes;
-static_assert(kSmemBytes <= 232448, "dynamic shared memory above the 227 KB a block may use");
+template <bool S>
+constexpr size_t smem_bytes() {
+  return 1024 + (size_t)Feed<S>::kStages * Feed<S>::kStageBytes + Feed<S>::kABytes + kEpiStageBytes + kMetaBytes +
+         kBarBytes;
+}
+static_assert(smem_bytes<false>() <= 232448 && smem_bytes<true>() <= 232448,
+              "dynamic shared memory above the 227 KB a block may use");
 constexpr uint64_t kTimeoutNs = 4000000000ull;
 constexpr uint32_t kIdesc64 = ptx::idesc_bf16_f32(128, 64);
 constexpr uint32_t kIdesc128 = ptx::idesc_bf16_f32(128, 128);
 
 struct Shared {
-  uint64_t full[kStages];
-  uint64_t empty[kStages];
+  uint64_t full[4];
+  uint64_t empty[4];
   uint64_t tfull[2];
   uint64_t tempty[2];
   uint64_t mfull[kMetaSlots];
   uint64_t mempty[kMetaSlots];
+  uint64_t afull, aempty;  // strips: the resident query block loaded / released
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -77,20 +100,39 @@ __device__ __forceinline__ void fail(Shared *sh, DevScalars *sc) {
   atomicOr(&sc->err, kErrTimeout);
 }
 
+// A record of the launch's list: a tile (tile list), or a strip (query
+// block a_blk, library column blocks b_blk .. b_blk + count - 1, shape =
+// nk16 | count << 16).
+template <bool S>
+__device__ __forceinline__ void record_shape(const Tile &r, int &nk16, int &count) {
+  if (S) {
+    nk16 = r.shape & 0xffff;
+    count = r.shape >> 16;
+  } else {
+    nk16 = tile_nk16(r);
+    count = 1;
+  }
+}
+
+template <bool S>
 __global__ void __launch_bounds__(kThreads, 1)
     k_screen_tc(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                 const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1, TcArgs a) {
+  using F = Feed<S>;
+  constexpr int kStages = F::kStages;
+  constexpr int kStageBytes = F::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float *stage_epi = reinterpret_cast<float *>(smem + (size_t)kStages * kStageBytes);
-  ScreenMeta *meta = reinterpret_cast<ScreenMeta *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes);
-  Shared *sh = reinterpret_cast<Shared *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes);
+  uint8_t *abuf = smem + (size_t)kStages * kStageBytes;  // strips: resident query block
+  float *stage_epi = reinterpret_cast<float *>(abuf + F::kABytes);
+  ScreenMeta *meta = reinterpret_cast<ScreenMeta *>(reinterpret_cast<uint8_t *>(stage_epi) + kEpiStageBytes);
+  Shared *sh = reinterpret_cast<Shared *>(reinterpret_cast<uint8_t *>(meta) + kMetaBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      ptx::mbar_init(&sh->full[s], 1);
-      ptx::mbar_init(&sh->empty[s], 1);
+    for (int st = 0; st < kStages; ++st) {
+      ptx::mbar_init(&sh->full[st], 1);
+      ptx::mbar_init(&sh->empty[st], 1);
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&sh->tfull[b], 1);
@@ -100,6 +142,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       ptx::mbar_init(&sh->mfull[b], 1);
       ptx::mbar_init(&sh->mempty[b], kEpiWarps * 32);
     }
+    ptx::mbar_init(&sh->afull, 1);
+    ptx::mbar_init(&sh->aempty, 1);
     ptx::mbar_init(&sh->drain, 1);
     sh->abort = 0;
     ptx::fence_mbar_init();
@@ -121,15 +165,33 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       // ------------------------------------------------------ TMA producer
-      uint32_t it = 0, tt = 0;
-      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
-        const Tile tile = next;
-        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];
-        {
+      uint32_t it = 0, tt = 0, ns = 0;
+      bool ok = true;
+      for (int64_t r = blockIdx.x; r < a.ntiles && ok && !*abort; r += gridDim.x, ++ns) {
+        const Tile rec = a.tiles[r];
+        int nk16, count;
+        record_shape<S>(rec, nk16, count);
+        const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
+        const int rowA = rec.a_blk * kBlockRows;
+        if (S) {
+          // the query block, resident for the strip (after the previous
+          // strip's MMAs have read their copy)
+          if (!ptx::mbar_wait(&sh->aempty, (ns & 1u) ^ 1u, abort, kTimeoutNs)) {
+            fail(sh, a.sc);
+            break;
+          }
+          ptx::mbar_arrive_expect_tx(&sh->afull, (uint32_t)(nchunks * 2 * kAOpBytes));
+          for (int kc = 0; kc < nchunks; ++kc) {
+            ptx::tma_load_2d(abuf + kc * 2 * kAOpBytes, &ta0, kc * kKChunk, rowA, &sh->afull);
+            ptx::tma_load_2d(abuf + kc * 2 * kAOpBytes + kAOpBytes, &ta1, kc * kKChunk, rowA, &sh->afull);
+          }
+        }
+        for (int u = 0; u < count && ok; ++u, ++tt) {
+          const Tile tile{rec.a_blk, rec.b_blk + u, rec.job, rec.shape};
           const uint32_t ms = tt % kMetaSlots;
           if (!ptx::mbar_wait(&sh->mempty[ms], ((tt / kMetaSlots) & 1u) ^ 1u, abort, kTimeoutNs)) {
             fail(sh, a.sc);
+            ok = false;
             break;
           }
           ScreenMeta &mt = meta[ms];
@@ -139,24 +201,27 @@ __global__ void __launch_bounds__(kThreads, 1)
           ptx::bulk_load(&mt.job, a.jobs + tile.job, (uint32_t)sizeof(Job), &sh->mfull[ms]);
           ptx::bulk_load(mt.ta, a.tinfo_a + a0, 8u * kBlockStructs, &sh->mfull[ms]);
           ptx::bulk_load(mt.tb, a.tinfo_b + b0, 8u * kBStructs, &sh->mfull[ms]);
-        }
-        const int rowA = tile.a_blk * kBlockRows, rowB = tile.b_blk * kBRows;
-        const int nchunks = (tile_nk16(tile) * 16 + kKChunk - 1) / kKChunk;
-        for (int kc = 0; kc < nchunks; ++kc, ++it) {
-          const int s = it % kStages;
-          if (!ptx::mbar_wait(&sh->empty[s], ((it / kStages) & 1u) ^ 1u, abort, kTimeoutNs)) {
-            fail(sh, a.sc);
-            break;
+          const int rowB = tile.b_blk * kBRows;
+          for (int kc = 0; kc < nchunks; ++kc, ++it) {
+            const int st = it % kStages;
+            if (!ptx::mbar_wait(&sh->empty[st], ((it / kStages) & 1u) ^ 1u, abort, kTimeoutNs)) {
+              fail(sh, a.sc);
+              ok = false;
+              break;
+            }
+            ptx::mbar_arrive_expect_tx(&sh->full[st], kStageBytes);
+            uint8_t *sp = smem + (size_t)st * kStageBytes;
+            const int k0 = kc * kKChunk;
+            if (!S) {
+              ptx::tma_load_2d(sp, &ta0, k0, rowA, &sh->full[st]);
+              ptx::tma_load_2d(sp + kAOpBytes, &ta1, k0, rowA, &sh->full[st]);
+            }
+            ptx::tma_load_2d(sp + F::kBOff, &tb0, k0, rowB, &sh->full[st]);
+            ptx::tma_load_2d(sp + F::kBOff + kBOpBytes, &tb1, k0, rowB, &sh->full[st]);
           }
-          ptx::mbar_arrive_expect_tx(&sh->full[s], kStageBytes);
-          uint8_t *st = smem + (size_t)s * kStageBytes;
-          const int k0 = kc * kKChunk;
-          ptx::tma_load_2d(st, &ta0, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + kAOpBytes, &ta1, k0, rowA, &sh->full[s]);
-          ptx::tma_load_2d(st + 2 * kAOpBytes, &tb0, k0, rowB, &sh->full[s]);
-          ptx::tma_load_2d(st + 2 * kAOpBytes + kBOpBytes, &tb1, k0, rowB, &sh->full[s]);
         }
       }
+      // let the copies still in flight land before the block can retire
       for (uint32_t d = (it > kStages ? it - kStages : 0); d < it; ++d) {
         volatile int no_abort = 0;
         ptx::mbar_wait(&sh->full[d % kStages], (d / kStages) & 1u, &no_abort, 100000000ull);
@@ -165,54 +230,66 @@ __global__ void __launch_bounds__(kThreads, 1)
         volatile int no_abort = 0;
         ptx::mbar_wait(&sh->mfull[d % kMetaSlots], (d / kMetaSlots) & 1u, &no_abort, 100000000ull);
       }
+      if (S && ns > 0) {
+        volatile int no_abort = 0;
+        ptx::mbar_wait(&sh->afull, (ns - 1) & 1u, &no_abort, 100000000ull);
+      }
     }
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {
       // ------------------------------------------------------- MMA issuer
-      uint32_t it = 0, p = 0;
-      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++p) {
-        const Tile tile = next;
-        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];
-        const int nk16 = tile_nk16(tile);
+      uint32_t it = 0, p = 0, ns = 0;
+      bool ok = true;
+      for (int64_t r = blockIdx.x; r < a.ntiles && ok && !*abort; r += gridDim.x, ++ns) {
+        const Tile rec = a.tiles[r];
+        int nk16, count;
+        record_shape<S>(rec, nk16, count);
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
-        if (!ptx::mbar_wait(&sh->tempty[p & 1u], ((p >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
+        if (S && !ptx::mbar_wait(&sh->afull, ns & 1u, abort, kTimeoutNs)) {
           fail(sh, a.sc);
           break;
         }
-        ptx::tc_fence_after();
-        const uint32_t c0 = tmem + (p & 1u) * 256u;
-        bool ok = true;
-        for (int kc = 0; kc < nchunks; ++kc, ++it) {
-          const int s = it % kStages;
-          if (!ptx::mbar_wait(&sh->full[s], (it / kStages) & 1u, abort, kTimeoutNs)) {
+        for (int u = 0; u < count && ok; ++u, ++p) {
+          if (!ptx::mbar_wait(&sh->tempty[p & 1u], ((p >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
             fail(sh, a.sc);
             ok = false;
             break;
           }
           ptx::tc_fence_after();
-          const uint32_t base = ptx::smem_u32(smem + (size_t)s * kStageBytes);
-          const int ksteps = min(4, nk16 - kc * 4);
-          for (int kk = 0; kk < ksteps; ++kk) {
-            const uint32_t off = (uint32_t)kk * 32u;
-            const uint64_t da0 = ptx::smem_desc_sw128(base + off);
-            const uint64_t da1 = ptx::smem_desc_sw128(base + kAOpBytes + off);
-            const uint64_t db0 = ptx::smem_desc_sw128(base + 2 * kAOpBytes + off);
-            const uint64_t db1 = ptx::smem_desc_sw128(base + 2 * kAOpBytes + kBOpBytes + off);
-            if (kc == 0 && kk == 0) {  // each accumulator's first write overwrites
-              ptx::tc_mma_f16(c0, da0, db0, kIdesc64, 0u);          // L0 = e0e0
-              ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);    // L1 = e1e0, L11 = e1e1
-              ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc64, 1u);     // L1 += e0e1
-            } else {
-              ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);         // L0 += e0e0, L1 += e0e1
-              ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);    // L1 += e1e0, L11 += e1e1
+          const uint32_t c0 = tmem + (p & 1u) * 256u;
+          for (int kc = 0; kc < nchunks; ++kc, ++it) {
+            const int st = it % kStages;
+            if (!ptx::mbar_wait(&sh->full[st], (it / kStages) & 1u, abort, kTimeoutNs)) {
+              fail(sh, a.sc);
+              ok = false;
+              break;
             }
+            ptx::tc_fence_after();
+            const uint32_t base = ptx::smem_u32(smem + (size_t)st * kStageBytes);
+            const uint32_t abase = S ? ptx::smem_u32(abuf + kc * 2 * kAOpBytes) : base;
+            const int ksteps = min(4, nk16 - kc * 4);
+            for (int kk = 0; kk < ksteps; ++kk) {
+              const uint32_t off = (uint32_t)kk * 32u;
+              const uint64_t da0 = ptx::smem_desc_sw128(abase + off);
+              const uint64_t da1 = ptx::smem_desc_sw128(abase + kAOpBytes + off);
+              const uint64_t db0 = ptx::smem_desc_sw128(base + F::kBOff + off);
+              const uint64_t db1 = ptx::smem_desc_sw128(base + F::kBOff + kBOpBytes + off);
+              if (kc == 0 && kk == 0) {  // each accumulator's first write overwrites
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc64, 0u);          // L0 = e0e0
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);    // L1 = e1e0, L11 = e1e1
+                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc64, 1u);     // L1 += e0e1
+              } else {
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);         // L0 += e0e0, L1 += e0e1
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);    // L1 += e1e0, L11 += e1e1
+              }
+            }
+            ptx::tc_commit(&sh->empty[st]);
           }
-          ptx::tc_commit(&sh->empty[s]);
+          if (!ok) break;
+          ptx::tc_commit(&sh->tfull[p & 1u]);
         }
-        if (!ok) break;
-        ptx::tc_commit(&sh->tfull[p & 1u]);
+        if (S) ptx::tc_commit(&sh->aempty);  // the resident block is free once these MMAs complete
       }
       ptx::tc_commit(&sh->drain);
       volatile int no_abort = 0;
@@ -229,67 +306,73 @@ __global__ void __launch_bounds__(kThreads, 1)
     float *stg = stage_epi + (warp - kEpiWarp0) * 32 * kPitch;
     const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * grp;
     uint32_t tt = 0;
-    for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++tt) {
-      const uint32_t slot = tt % kMetaSlots;
-      if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs) ||
-          !ptx::mbar_wait(&sh->tfull[tt & 1u], (tt >> 1) & 1u, abort, kTimeoutNs)) {
-        fail(sh, a.sc);
-        break;
-      }
-      ptx::tc_fence_after();
-      const ScreenMeta &mt = meta[slot];
-      const Job &mj = mt.job;
-      {
-        // m = L0 + 2^-9 L1 + 2^-18 L11: the covariance of the truncated
-        // structures in units of 2^28 grid products
-        const uint32_t c0 = lane_base + (tt & 1u) * 256u;
-        float m[32], v[32];
-        ptx::tmem_ld2_32x32b_x32(c0 + 64, c0 + 128, m, v);
-#pragma unroll
-        for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
-        ptx::tmem_ld_32x32b_x32(c0, v);
-        ptx::tc_fence_before();
-        ptx::mbar_arrive(&sh->tempty[tt & 1u]);
-        if (off) {
-#pragma unroll
-          for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[kCols + c], 0.001953125f, v[kCols + c]);
-        } else {
-#pragma unroll
-          for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
+    bool ok = true;
+    for (int64_t r = blockIdx.x; r < a.ntiles && ok; r += gridDim.x) {
+      int nk16, count;
+      record_shape<S>(a.tiles[r], nk16, count);
+      for (int u = 0; u < count; ++u, ++tt) {
+        const uint32_t slot = tt % kMetaSlots;
+        if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs) ||
+            !ptx::mbar_wait(&sh->tfull[tt & 1u], (tt >> 1) & 1u, abort, kTimeoutNs)) {
+          fail(sh, a.sc);
+          ok = false;
+          break;
         }
-      }
-      __syncwarp();
-      const bool job_ok = mj.err == 0;
-      const int64_t jn = mj.n, jnb = mj.n_b;
-      const int64_t i0 = (int64_t)mt.tile.a_blk * kBlockStructs + qd * kGroupStructs - mj.first_a;
-      const int64_t j0 = (int64_t)mt.tile.b_blk * kBStructs + 5 * cq - mj.first_b;
-      const float t_u = mj.u, t_de = mj.d34;
-      const int t_L = mj.L;
-      uint32_t *sout = static_cast<uint32_t *>(mj.out.ptr);
-      const int64_t ld = mj.out.ld;
-      // 10 x 5 pairs over the 32 lanes, two rounds
+        ptx::tc_fence_after();
+        const ScreenMeta &mt = meta[slot];
+        const Job &mj = mt.job;
+        {
+          // m = L0 + 2^-9 L1 + 2^-18 L11: the covariance of the truncated
+          // structures in units of 2^28 grid products
+          const uint32_t c0 = lane_base + (tt & 1u) * 256u;
+          float m[32], v[32];
+          ptx::tmem_ld2_32x32b_x32(c0 + 64, c0 + 128, m, v);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+          ptx::tmem_ld_32x32b_x32(c0, v);
+          ptx::tc_fence_before();
+          ptx::mbar_arrive(&sh->tempty[tt & 1u]);
+          if (off) {
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[kCols + c], 0.001953125f, v[kCols + c]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
+          }
+        }
+        __syncwarp();
+        const bool job_ok = mj.err == 0;
+        const int64_t jn = mj.n, jnb = mj.n_b;
+        const int64_t i0 = (int64_t)mt.tile.a_blk * kBlockStructs + qd * kGroupStructs - mj.first_a;
+        const int64_t j0 = (int64_t)mt.tile.b_blk * kBStructs + 5 * cq - mj.first_b;
+        const float t_u = mj.u, t_de = mj.d34;
+        const int t_L = mj.L;
+        uint32_t *sout = static_cast<uint32_t *>(mj.out.ptr);
+        const int64_t ld = mj.out.ld;
+        // 10 x 5 pairs over the 32 lanes, two rounds
 #pragma unroll 1
-      for (int rd = 0; rd < 2; ++rd) {
-        const int pp = rd * 32 + lane;
-        const int pc = pp < 50 ? pp : 0;  // pad slots read a valid pair
-        const int ir = pc / 5, jc = pc - 5 * (pc / 5);
-        const int64_t i = i0 + ir, j = j0 + jc;
-        float m9[9];
+        for (int rd = 0; rd < 2; ++rd) {
+          const int pp = rd * 32 + lane;
+          const int pc = pp < 50 ? pp : 0;  // pad slots read a valid pair
+          const int ir = pc / 5, jc = pc - 5 * (pc / 5);
+          const int64_t i = i0 + ir, j = j0 + jc;
+          float m9[9];
 #pragma unroll
-        for (int xr = 0; xr < 3; ++xr)
+          for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-          for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
-        const float2 fa = mt.ta[qd * kGroupStructs + ir], fb = mt.tb[5 * cq + jc];
-        float lo, hi;
-        bsm::screen_bracket(m9, fa.x + fb.x, t_de, fa.y + fb.y, t_u, t_L, lo, hi);
-        if (job_ok && pp < 50 && i < jn && j < jnb) {
-          const uint32_t wlo = __half_as_ushort(__float2half_rd(lo));
-          const uint32_t whi = __half_as_ushort(__float2half_ru(hi));
-          sout[i * ld + j] = (whi << 16) | wlo;
+            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+          const float2 fa = mt.ta[qd * kGroupStructs + ir], fb = mt.tb[5 * cq + jc];
+          float lo, hi;
+          bsm::screen_bracket(m9, fa.x + fb.x, t_de, fa.y + fb.y, t_u, t_L, lo, hi);
+          if (job_ok && pp < 50 && i < jn && j < jnb) {
+            const uint32_t wlo = __half_as_ushort(__float2half_rd(lo));
+            const uint32_t whi = __half_as_ushort(__float2half_ru(hi));
+            sout[i * ld + j] = (whi << 16) | wlo;
+          }
         }
+        __syncwarp();
+        ptx::mbar_arrive(&sh->mempty[slot]);
       }
-      __syncwarp();
-      ptx::mbar_arrive(&sh->mempty[slot]);
     }
   }
   __syncthreads();
@@ -302,13 +385,22 @@ __global__ void __launch_bounds__(kThreads, 1)
 }  // namespace
 
 cudaError_t screen_tc_prepare() {
-  return cudaFuncSetAttribute(k_screen_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+  cudaError_t e = cudaFuncSetAttribute(k_screen_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_bytes<false>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_screen_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<true>());
+  return e;
 }
 
-cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, cudaStream_t st) {
+int screen_strip_max_nk16() { return Feed<true>::kStripChunks * kKChunk / 16; }
+
+cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, bool strips, cudaStream_t st) {
   if (a.ntiles <= 0) return cudaSuccess;
   const int64_t grid = a.ntiles < a.num_sms ? a.ntiles : a.num_sms;
-  k_screen_tc<<<(unsigned)grid, kThreads, kSmemBytes, st>>>(tm[0], tm[1], tm[4], tm[5], a);
+  if (strips)
+    k_screen_tc<true><<<(unsigned)grid, kThreads, smem_bytes<true>(), st>>>(tm[0], tm[1], tm[4], tm[5], a);
+  else
+    k_screen_tc<false><<<(unsigned)grid, kThreads, smem_bytes<false>(), st>>>(tm[0], tm[1], tm[4], tm[5], a);
   return cudaGetLastError();
 }
 

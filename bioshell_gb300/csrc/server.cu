@@ -355,12 +355,27 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   }
   // tiles column block by column block: the persistent blocks sweep the
   // library once, each library block read from HBM once and reused from L2
-  // by every query block of the batch
+  // by every query block of the batch.  Screens of chains the strip kernel
+  // takes run as strips: a query block against a run of library blocks,
+  // the query block's digits resident in shared memory for the run; runs
+  // sized for about a dozen per block of the grid.
   {
     const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
-    plan.tiles.reserve((size_t)(blk * nbb));
-    for (int64_t J = 0; J < nbb; ++J)
-      for (int64_t I = 0; I < blk; ++I) plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], 0});
+    const int nk16 = bk.lp / 16;
+    plan.strips = screen && s->precision == BS_PRECISION_MIXED && nk16 <= screen_strip_max_nk16();
+    if (plan.strips) {
+      const int64_t total = blk * nbb;
+      const int64_t run = std::max<int64_t>(8, std::min<int64_t>(4096, (total + 12 * s->num_sms - 1) / (12 * s->num_sms)));
+      for (int64_t J = 0; J < nbb; J += run)
+        for (int64_t I = 0; I < blk; ++I) {
+          const int64_t cnt = std::min(run, nbb - J);
+          plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], nk16 | (int)(cnt << 16)});
+        }
+    } else {
+      plan.tiles.reserve((size_t)(blk * nbb));
+      for (int64_t J = 0; J < nbb; ++J)
+        for (int64_t I = 0; I < blk; ++I) plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], 0});
+    }
   }
   plan.nblocks = blk;
   sl.rows = rows;

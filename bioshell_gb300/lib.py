@@ -115,6 +115,7 @@ SIGNATURES = [
     ("bs_neighbors", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                       ctypes.POINTER(bs_opts), _i64p]),
     ("bs_neighbors_get", ctypes.c_int32, [_vp, _vp, _vp, _vp]),
+    ("bs_hierarchical_gpu", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _i64p, _fp]),
     ("bs_optics_neighbors", ctypes.c_int32, [_i64p, _i32p, _fp, ctypes.c_int64, ctypes.c_double, ctypes.c_int32,
                                              _i64p, _dp, _i64p]),
     ("bs_io_last_error", ctypes.c_char_p, []),

@@ -329,6 +329,13 @@ enum {
  * clusters n, n+1, ... (the root is 2n-2).  Runs on the host. */
 BS_API bs_status bs_hierarchical(const void *tri, int64_t n, int32_t out_type, int32_t rule, int64_t *merges,
                                  float *merge_dist);
+/* The same on the GPU of `ctx`: the whole merge loop in one cooperative
+ * launch over a device-resident n x n f32 matrix (n^2 x 4 bytes of the
+ * context's budget), with the same merges and merge distances as
+ * bs_hierarchical bit for bit.  tri may be host or device memory; merges
+ * and merge_dist receive the results (host or device memory). */
+BS_API bs_status bs_hierarchical_gpu(bs_ctx *ctx, const void *tri, int64_t n, int32_t out_type, int32_t rule,
+                                     int64_t *merges, float *merge_dist);
 /* Cluster label of every item at a distance cutoff, as retrieve_clusters
  * (hierarchical.rs:136-169) splits the tree; labels number the clusters in
  * the order that function returns them. */

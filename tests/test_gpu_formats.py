@@ -25,4 +25,5 @@ def test_tsv_from_device_equals_host(engine, tmp_path):
     assert open(pd, "rb").read() == open(ph, "rb").read()
     labs, m = F.read_tsv(pd)
     assert labs == labels
-    np.testing.assert_allclose(m.values, host, rtol=0, atol=5e-7)
+    # 6 decimals, then f32: within half a unit of the 6th decimal plus an f32 rounding
+    np.testing.assert_allclose(m.values, host, rtol=1.2e-7, atol=5.0001e-7)
