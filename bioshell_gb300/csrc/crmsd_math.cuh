@@ -233,6 +233,81 @@ BS_HD void screen_bracket(const float m[9], float gsum_f, float de, float dr, fl
   hi = sqrtf(fmaf(gsum_f, 1.0f - xlo, de) * scale) + dr;
 }
 
+#if defined(__CUDACC__)
+// Two pairs at once on the packed FP32x2 pipe (sm_100 and later): each
+// operation below is one instruction for both lanes of the pair, rounded as
+// the scalar operation (a - b is fma(b, -1, a): one rounding).  Division,
+// maxima and square roots stay per component.
+struct F2 {
+  float2 v;
+};
+__device__ __forceinline__ F2 f2(float a) { return F2{make_float2(a, a)}; }
+__device__ __forceinline__ F2 f2(float a, float b) { return F2{make_float2(a, b)}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2{__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2{__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2{__ffma2_rn(b.v, make_float2(-1.f, -1.f), a.v)}; }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return F2{__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 max2(F2 a, F2 b) { return F2{make_float2(fmaxf(a.v.x, b.v.x), fmaxf(a.v.y, b.v.y))}; }
+__device__ __forceinline__ F2 div2(F2 a, F2 b) {
+  return F2{make_float2(__fdividef(a.v.x, b.v.x), __fdividef(a.v.y, b.v.y))};
+}
+
+// screen_bracket for two pairs (the same bracket, the same margins).
+__device__ __forceinline__ void screen_bracket2(const F2 m[9], F2 gsum, float de, F2 dr, float u, int L, F2 &lo,
+                                                F2 &hi) {
+  const F2 lam0 = gsum * f2(1.862645149230957e-09f);  // 2^-29: gsum/2 in units of m
+  const F2 inv = div2(f2(1.0f), lam0);
+  F2 sn[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
+  const F2 sxx = sn[0], sxy = sn[1], sxz = sn[2], syx = sn[3], syy = sn[4], syz = sn[5], szx = sn[6], szy = sn[7],
+           szz = sn[8];
+  const F2 k00 = sxx + syy + szz, k01 = syz - szy, k02 = szx - sxz, k03 = sxy - syx;
+  const F2 k11 = sxx - syy - szz, k12 = sxy + syx, k13 = szx + sxz;
+  const F2 k22 = syy - sxx - szz, k23 = syz + szy, k33 = szz - sxx - syy;
+  F2 fro2 = f2(0.f);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fro2 = fma2(sn[i], sn[i], fro2);
+  const F2 c2 = f2(-2.f) * fro2;
+  const F2 det3 = sxx * (syy * szz - syz * szy) - sxy * (syx * szz - syz * szx) + sxz * (syx * szy - syy * szx);
+  const F2 c1 = f2(-8.f) * det3;
+  const F2 s01 = k00 * k11 - k01 * k01, s02 = k00 * k12 - k02 * k01, s03 = k00 * k13 - k03 * k01;
+  const F2 s12 = k01 * k12 - k02 * k11, s13 = k01 * k13 - k03 * k11, s23 = k02 * k13 - k03 * k12;
+  const F2 t23 = k22 * k33 - k23 * k23, t13 = k12 * k33 - k23 * k13, t12 = k12 * k23 - k22 * k13;
+  const F2 t03 = k02 * k33 - k23 * k03, t02 = k02 * k23 - k22 * k03, t01 = k02 * k13 - k12 * k03;
+  const F2 c0 = s01 * t23 - s02 * t13 + s03 * t12 + s12 * t03 - s13 * t02 + s23 * t01;
+  const F2 eP = f2(3.814697265625e-06f), eD = eP;  // 2^-18
+  F2 x = f2(1.0f), p = f2(0.f), dp = f2(0.f);
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const F2 x2 = x * x;
+    p = fma2(fma2(x2 + c2, x, c1), x, c0);
+    dp = fma2(fma2(f2(4.f), x2, f2(2.f) * c2), x, c1);
+    if (it < 3) x = x - div2(max2(p - eP, f2(0.f)), max2(dp + eD, eD));  // P' >= 0 for x >= x*
+  }
+  const F2 d1 = div2(max2(p - eP, f2(0.f)), max2(dp + eD, eD));
+  const F2 d4 = div2(f2(4.f) * (p + eP), dp - eD);
+  const float scale = __fdividef(u, (float)L);
+  float lx[2], hx[2];
+  const float xs[2] = {x.v.x, x.v.y}, d1s[2] = {d1.v.x, d1.v.y}, d4s[2] = {d4.v.x, d4.v.y};
+  const float dps[2] = {dp.v.x, dp.v.y}, gs[2] = {gsum.v.x, gsum.v.y}, drs[2] = {dr.v.x, dr.v.y};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    if (!(gs[c] > 0.f)) {
+      lx[c] = 0.f;
+      hx[c] = drs[c];
+      continue;
+    }
+    const float xhi = fminf(xs[c] - d1s[c] + 9.5367431640625e-07f, 1.0f);                      // >= x*
+    const float xlo = dps[c] > 3.814697265625e-06f ? fmaxf(xs[c] - d4s[c] - 9.5367431640625e-07f, 0.f) : 0.f;
+    lx[c] = fmaxf(sqrtf(fmaxf(fmaf(gs[c], 1.0f - xhi, -de), 0.f) * scale) - drs[c], 0.f);
+    hx[c] = sqrtf(fmaf(gs[c], 1.0f - xlo, de) * scale) + drs[c];
+  }
+  lo = f2(lx[0], lx[1]);
+  hi = f2(hx[0], hx[1]);
+}
+#endif
+
 // ------------------------------------------------- quaternion -> T = R^T
 // T(q) with q = (w, x, y, z); quadratic, homogeneous.
 template <typename V>
@@ -366,6 +441,183 @@ BS_HD void fast_begin(const float m[9], float gsum_f, FastState &st) {
   for (int i = 0; i < 4; ++i) qq = fmaf(qn[i], qn[i], qq);
   st.qq = qq;
 }
+
+#if defined(__CUDACC__)
+// fast_begin for two pairs at once: the FP32 parts (QCP, eigenvector, the
+// small bilinear terms) on the packed FP32x2 pipe, the integer parts per
+// pair.  The same steps and margins as fast_begin.
+__device__ __forceinline__ void fast_begin2(const F2 m[9], F2 gsum, FastState &s0, FastState &s1) {
+  FastState *st[2] = {&s0, &s1};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    FastState &t = *st[c];
+    t.U0 = t.U1 = t.U2 = 0;
+    t.U3 = 0.f;
+    t.flag = 0;
+    t.rest = 0.f;
+    t.qq = 1.f;
+    t.q2 = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) t.T[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t.qh[i] = 0.f;
+  }
+  const F2 lam0 = gsum * f2(1.862645149230957e-9f);
+  const F2 inv = div2(f2(1.0f), lam0);
+  F2 sn[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) sn[i] = m[i] * inv;
+  const F2 sxx = sn[0], sxy = sn[1], sxz = sn[2], syx = sn[3], syy = sn[4], syz = sn[5], szx = sn[6], szy = sn[7],
+           szz = sn[8];
+  const F2 k00 = sxx + syy + szz, k01 = syz - szy, k02 = szx - sxz, k03 = sxy - syx;
+  const F2 k11 = sxx - syy - szz, k12 = sxy + syx, k13 = szx + sxz;
+  const F2 k22 = syy - sxx - szz, k23 = syz + szy, k33 = szz - sxx - syy;
+  F2 fro2 = f2(0.f);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) fro2 = fma2(sn[i], sn[i], fro2);
+  const F2 c2 = f2(-2.f) * fro2;
+  const F2 c1 = f2(-8.f) * (sxx * (syy * szz - syz * szy) - sxy * (syx * szz - syz * szx) + sxz * (syx * szy - syy * szx));
+  const F2 s01 = k00 * k11 - k01 * k01, s02 = k00 * k12 - k02 * k01, s03 = k00 * k13 - k03 * k01;
+  const F2 s12 = k01 * k12 - k02 * k11, s13 = k01 * k13 - k03 * k11, s23 = k02 * k13 - k03 * k12;
+  const F2 t23 = k22 * k33 - k23 * k23, t13 = k12 * k33 - k23 * k13, t12 = k12 * k23 - k22 * k13;
+  const F2 t03 = k02 * k33 - k23 * k03, t02 = k02 * k23 - k22 * k03, t01 = k02 * k13 - k12 * k03;
+  const F2 c0 = s01 * t23 - s02 * t13 + s03 * t12 + s12 * t03 - s13 * t02 + s23 * t01;
+  // Halley from x = 1, five steps (qcp_top_eig)
+  F2 x = f2(1.0f);
+#pragma unroll
+  for (int it = 0; it < 5; ++it) {
+    const F2 x2 = x * x;
+    const F2 p = fma2(fma2(x2 + c2, x, c1), x, c0);
+    const F2 dp = fma2(fma2(f2(4.f), x2, f2(2.f) * c2), x, c1);
+    const F2 ddp = fma2(f2(12.f), x2, f2(2.f) * c2);
+    const F2 den = fma2(f2(2.f) * dp, dp, f2(0.f) - p * ddp);
+    const F2 nx = x - div2(f2(2.f) * p * dp, den);
+    x = f2(den.v.x > 0.f ? nx.v.x : x.v.x, den.v.y > 0.f ? nx.v.y : x.v.y);
+  }
+  const F2 b00 = k00 - x, b11 = k11 - x, b22 = k22 - x, b33 = k33 - x;
+  const F2 C0 = b11 * (b22 * b33 - k23 * k23) - k12 * (k12 * b33 - k23 * k13) + k13 * (k12 * k23 - b22 * k13);
+  const F2 C1 = b00 * (b22 * b33 - k23 * k23) - k02 * (k02 * b33 - k23 * k03) + k03 * (k02 * k23 - b22 * k03);
+  const F2 C2 = b00 * (b11 * b33 - k13 * k13) - k01 * (k01 * b33 - k13 * k03) + k03 * (k01 * k13 - b11 * k03);
+  const F2 C3 = b00 * (b11 * b22 - k12 * k12) - k01 * (k01 * b22 - k12 * k02) + k02 * (k01 * k12 - b11 * k02);
+  const F2 r0[4] = {b00, k01, k02, k03}, r1[4] = {k01, b11, k12, k13};
+  const F2 r2[4] = {k02, k12, b22, k23}, r3[4] = {k03, k13, k23, b33};
+  // per pair: the diagonal cofactor of largest magnitude picks the three rows
+  float best[2];
+  F2 sa[4], sb[4], sc[4];
+  {
+    int jj[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const float a0 = fabsf(c ? C0.v.y : C0.v.x), a1 = fabsf(c ? C1.v.y : C1.v.x);
+      const float a2 = fabsf(c ? C2.v.y : C2.v.x), a3 = fabsf(c ? C3.v.y : C3.v.x);
+      int j = 0;
+      float b = a0;
+      if (a1 > b) { b = a1; j = 1; }
+      if (a2 > b) { b = a2; j = 2; }
+      if (a3 > b) { b = a3; j = 3; }
+      best[c] = b;
+      jj[c] = j;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const F2 A = r0[i], B = r1[i], Cc = r2[i], D = r3[i];
+      sa[i] = f2(jj[0] == 0 ? B.v.x : A.v.x, jj[1] == 0 ? B.v.y : A.v.y);
+      sb[i] = f2(jj[0] <= 1 ? Cc.v.x : B.v.x, jj[1] <= 1 ? Cc.v.y : B.v.y);
+      sc[i] = f2(jj[0] <= 2 ? D.v.x : Cc.v.x, jj[1] <= 2 ? D.v.y : Cc.v.y);
+    }
+  }
+  // q = generalised cross product of the three rows (gcross4)
+  F2 q[4];
+  {
+    const F2 m01 = sb[0] * sc[1] - sb[1] * sc[0], m02 = sb[0] * sc[2] - sb[2] * sc[0];
+    const F2 m03 = sb[0] * sc[3] - sb[3] * sc[0], m12 = sb[1] * sc[2] - sb[2] * sc[1];
+    const F2 m13 = sb[1] * sc[3] - sb[3] * sc[1], m23 = sb[2] * sc[3] - sb[3] * sc[2];
+    q[0] = sa[1] * m23 - sa[2] * m13 + sa[3] * m12;
+    q[1] = f2(0.f) - (sa[0] * m23 - sa[2] * m03 + sa[3] * m02);
+    q[2] = sa[0] * m13 - sa[1] * m03 + sa[3] * m01;
+    q[3] = f2(0.f) - (sa[0] * m12 - sa[1] * m02 + sa[2] * m01);
+  }
+  const F2 qsq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  const float gs[2] = {gsum.v.x, gsum.v.y}, qs2[2] = {qsq.v.x, qsq.v.y};
+  bool live[2];
+  float qsc[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    live[c] = gs[c] > 0.f;
+    if (live[c] && (!(qs2[c] > 1e-30f) || !(best[c] > 1e-6f))) {
+      st[c]->flag = 1;
+      live[c] = false;
+    }
+    qsc[c] = rsqrtf(qs2[c]) * 0.99999f;  // unit length (a hair below, so |Q_h|^2 <= 2^34)
+  }
+  const F2 qs = f2(qsc[0], qsc[1]);
+  F2 qn[4], qh[4], ql[4];
+  long long Q[2][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    qn[i] = q[i] * qs;
+    const F2 hs = qn[i] * f2(131072.f);
+    const float h0 = rintf(hs.v.x), h1 = rintf(hs.v.y);
+    Q[0][i] = (long long)(int)h0;
+    Q[1][i] = (long long)(int)h1;
+    qh[i] = f2(h0, h1) * f2(7.62939453125e-6f);  // 2^-17
+    ql[i] = qn[i] - qh[i];
+  }
+  // T(q_h, q_l) and T(q_l) (t_bilinear, t_of_q), packed
+  F2 tb[9], tl[9];
+  {
+    const F2 w = qh[0], xx_ = qh[1], y = qh[2], z = qh[3];
+    const F2 W = ql[0], X = ql[1], Y = ql[2], Z = ql[3];
+    const F2 ww = w * W, xx = xx_ * X, yy = y * Y, zz = z * Z;
+    const F2 xy = fma2(xx_, Y, y * X), wz = fma2(w, Z, z * W), xz = fma2(xx_, Z, z * X);
+    const F2 wy = fma2(w, Y, y * W), yz = fma2(y, Z, z * Y), wx = fma2(w, X, xx_ * W);
+    tb[0] = ww + xx - yy - zz;
+    tb[1] = xy + wz;
+    tb[2] = xz - wy;
+    tb[3] = xy - wz;
+    tb[4] = ww - xx + yy - zz;
+    tb[5] = yz + wx;
+    tb[6] = xz + wy;
+    tb[7] = yz - wx;
+    tb[8] = ww - xx - yy + zz;
+    const F2 lww = W * W, lxx = X * X, lyy = Y * Y, lzz = Z * Z;
+    const F2 lwx = W * X, lwy = W * Y, lwz = W * Z, lxy = X * Y, lxz = X * Z, lyz = Y * Z;
+    const F2 two = f2(2.f);
+    tl[0] = lww + lxx - lyy - lzz;
+    tl[1] = two * (lxy + lwz);
+    tl[2] = two * (lxz - lwy);
+    tl[3] = two * (lxy - lwz);
+    tl[4] = lww - lxx + lyy - lzz;
+    tl[5] = two * (lyz + lwx);
+    tl[6] = two * (lxz + lwy);
+    tl[7] = two * (lyz - lwx);
+    tl[8] = lww - lxx - lyy + lzz;
+  }
+  const F2 dot_hl = qh[0] * ql[0] + qh[1] * ql[1] + qh[2] * ql[2] + qh[3] * ql[3];
+  const F2 dot_ll = ql[0] * ql[0] + ql[1] * ql[1] + ql[2] * ql[2] + ql[3] * ql[3];
+  F2 sbv = f2(0.f), slv = f2(0.f);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    sbv = fma2(tb[i], m[i], sbv);
+    slv = fma2(tl[i], m[i], slv);
+  }
+  const F2 rest = f2(4.f) * (lam0 * dot_hl - sbv) + f2(2.f) * (lam0 * dot_ll - slv);
+  F2 qq = f2(0.f);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) qq = fma2(qn[i], qn[i], qq);
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    if (!live[c]) continue;
+    FastState &t = *st[c];
+    t_of_q<long long>(Q[c], t.T);
+    t.q2 = Q[c][0] * Q[c][0] + Q[c][1] * Q[c][1] + Q[c][2] * Q[c][2] + Q[c][3] * Q[c][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t.qh[i] = c ? qh[i].v.y : qh[i].v.x;
+    t.rest = c ? rest.v.y : rest.v.x;
+    t.qq = c ? qq.v.y : qq.v.x;
+  }
+}
+#endif
 
 BS_HD void fast_level(FastState &st, int level, const float s[9]) {
   if (level < 3) {

@@ -526,20 +526,27 @@ __global__ void __launch_bounds__(kThreads, 1)
         int64_t jj[2];
         bool valid[2];
         SInfo ib[2];
+        {
+          // the lane's two pairs through one packed FP32x2 QCP
+          float m9[2][9], gs[2];
 #pragma unroll
-        for (int sl = 0; sl < 2; ++sl) {
-          const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
-          const int jc = jh < 5 ? jh : 4;
-          const int64_t jg = jg0 + 5 * h + jh;
-          jj[sl] = jg - fb;
-          valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
-          ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
-          float m9[9];
+          for (int sl = 0; sl < 2; ++sl) {
+            const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
+            const int jc = jh < 5 ? jh : 4;
+            const int64_t jg = jg0 + 5 * h + jh;
+            jj[sl] = jg - fb;
+            valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
+            ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
 #pragma unroll
-          for (int xr = 0; xr < 3; ++xr)
+            for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
-          bsm::fast_begin(m9, valid[sl] ? ia.gf + ib[sl].gf : 0.f, st[sl]);
+              for (int y = 0; y < 3; ++y) m9[sl][3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+            gs[sl] = valid[sl] ? ia.gf + ib[sl].gf : 0.f;
+          }
+          bsm::F2 mm[9];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) mm[e] = bsm::f2(m9[0][e], m9[1][e]);
+          bsm::fast_begin2(mm, bsm::f2(gs[0], gs[1]), st[0], st[1]);
         }
         __syncwarp();
         // ---- pass B: exact level sums, one level at a time (levels 0-2 as

@@ -242,76 +242,13 @@ __global__ void k_mixed_pairs(DigitsView dg, const SInfo *__restrict__ info, con
   out[t] = certified_pair(dg, dg, i, j, info[i], info[j], jb, levels_out ? levels_out + t * 36 : nullptr);
 }
 
-// certified_pair with a warp per pair: lanes stride over atoms (coalesced
-// digit loads), the integer level sums are reduced across the warp, and
-// every lane finishes the same pair (lane 0's result is the one stored).
-// Integer sums do not depend on the order of accumulation, so the result is
-// bit-identical to certified_pair's.
-__device__ double certified_pair_warp(const DigitsView &da, const DigitsView &db, int64_t ig, int64_t jg,
-                                      const SInfo &ia, const SInfo &ib, const Job &jb, int lane) {
-  const int L = jb.L;
-  int S[5][9];
-#pragma unroll
-  for (int l = 0; l < 5; ++l)
-#pragma unroll
-    for (int e = 0; e < 9; ++e) S[l][e] = 0;
-  const int64_t ra = digit_row(ig, 0) * da.pitch, rb = digit_row(jg, 0) * db.pitch;
-  for (int k = lane; k < L; k += 32) {
-    int a[3][3], b[3][3];  // [coord][digit]
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int64_t oa = ra + c * da.pitch + k, ob = rb + c * db.pitch + k;
-      a[c][0] = (int)__bfloat162float(da.d0[oa]);
-      a[c][1] = (int)__bfloat162float(da.d1[oa]);
-      a[c][2] = (int)__bfloat162float(da.d2[oa]);
-      b[c][0] = (int)__bfloat162float(db.d0[ob]);
-      b[c][1] = (int)__bfloat162float(db.d1[ob]);
-      b[c][2] = (int)__bfloat162float(db.d2[ob]);
-    }
-#pragma unroll
-    for (int x = 0; x < 3; ++x)
-#pragma unroll
-      for (int y = 0; y < 3; ++y) {
-        const int e = 3 * x + y;
-        S[0][e] += a[x][0] * b[y][0];
-        S[1][e] += a[x][0] * b[y][1] + a[x][1] * b[y][0];
-        S[2][e] += a[x][0] * b[y][2] + a[x][1] * b[y][1] + a[x][2] * b[y][0];
-        S[3][e] += a[x][1] * b[y][2] + a[x][2] * b[y][1];
-        S[4][e] += (a[x][2] >> 4) * (b[y][2] >> 4);
-      }
-  }
-#pragma unroll
-  for (int l = 0; l < 5; ++l)
-#pragma unroll
-    for (int e = 0; e < 9; ++e) S[l][e] = __reduce_add_sync(0xffffffffu, S[l][e]);
-  bsm::EpilogueIn in;
-#pragma unroll
-  for (int e = 0; e < 9; ++e) {
-    in.s0[e] = (float)S[0][e];
-    in.s1[e] = (float)S[1][e];
-    in.s2[e] = (float)S[2][e];
-    in.s3[e] = (float)((double)S[3][e] + 0.5 * (double)S[4][e]);
-  }
-  in.ga = ia.ghat;
-  in.gb = ib.ghat;
-  in.gfa = ia.gf;
-  in.gfb = ib.gf;
-  in.qa = ia.qres;
-  in.qb = ib.qres;
-  int flag = 0;
-  const float r = bsm::pair_rmsd_fast(in, jb.u, jb.d34, L, jb.tol, flag);
-  if (!flag) return (double)r;  // flag is the same in every lane
-  long long mh[9];
-  exact_cov_partial(da, db, ig, jg, L, lane, 32, mh);
-#pragma unroll
-  for (int e = 0; e < 9; ++e)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mh[e] += __shfl_xor_sync(0xffffffffu, mh[e], o);
-  return bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
-}
-
-// Block per query row, a warp per screen candidate: the certified crmsd of
-// each of the row's candidates.
+// Block per query row; the row's candidates are split evenly over the eight
+// warps, and a warp takes its share 32 at a time: for each candidate, all
+// lanes accumulate the integer level sums over strided atoms and reduce
+// them, and the candidate's lane keeps the totals; then every lane finishes
+// its own candidate (the certified epilogue once per pair, not once per
+// lane).  Integer sums do not depend on the order of accumulation, so every
+// value is bit-identical to certified_pair's.
 constexpr int kCandWarps = 8;
 __global__ void __launch_bounds__(kCandWarps * 32)
     k_exact_candidates(DigitsView da, DigitsView db, const SInfo *__restrict__ info_a,
@@ -325,11 +262,82 @@ __global__ void __launch_bounds__(kCandWarps * 32)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ig = row_ig[r];
   const int n = min(cand_n[r], cap);
-  const SInfo ia = info_a[ig];
-  for (int c = warp; c < n; c += kCandWarps) {
-    const int64_t jg = (int64_t)cand_j[r * cap + c] + jb.first_b;
-    const double v = certified_pair_warp(da, db, ig, jg, ia, info_b[jg], jb, lane);
-    if (lane == 0) cand_v[r * cap + c] = (float)v;
+  const int L = jb.L;
+  const int64_t ra = digit_row(ig, 0) * da.pitch;
+  const int share = (n + kCandWarps - 1) / kCandWarps;
+  const int cb = min(n, warp * share), ce = min(n, cb + share);
+  for (int c0 = cb; c0 < ce; c0 += 32) {
+    int mine[5][9];
+#pragma unroll
+    for (int l = 0; l < 5; ++l)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) mine[l][e] = 0;
+    const int cnt = min(32, ce - c0);
+    for (int cc = 0; cc < cnt; ++cc) {
+      const int64_t jg = (int64_t)cand_j[r * cap + c0 + cc] + jb.first_b;
+      const int64_t rb = digit_row(jg, 0) * db.pitch;
+      int S[5][9];
+#pragma unroll
+      for (int l = 0; l < 5; ++l)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) S[l][e] = 0;
+      for (int k = lane; k < L; k += 32) {
+        int a[3][3], b[3][3];  // [coord][digit]
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int64_t oa = ra + c * da.pitch + k, ob = rb + c * db.pitch + k;
+          a[c][0] = (int)__bfloat162float(da.d0[oa]);
+          a[c][1] = (int)__bfloat162float(da.d1[oa]);
+          a[c][2] = (int)__bfloat162float(da.d2[oa]);
+          b[c][0] = (int)__bfloat162float(db.d0[ob]);
+          b[c][1] = (int)__bfloat162float(db.d1[ob]);
+          b[c][2] = (int)__bfloat162float(db.d2[ob]);
+        }
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+          for (int y = 0; y < 3; ++y) {
+            const int e = 3 * x + y;
+            S[0][e] += a[x][0] * b[y][0];
+            S[1][e] += a[x][0] * b[y][1] + a[x][1] * b[y][0];
+            S[2][e] += a[x][0] * b[y][2] + a[x][1] * b[y][1] + a[x][2] * b[y][0];
+            S[3][e] += a[x][1] * b[y][2] + a[x][2] * b[y][1];
+            S[4][e] += (a[x][2] >> 4) * (b[y][2] >> 4);
+          }
+      }
+#pragma unroll
+      for (int l = 0; l < 5; ++l)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+          const int t = __reduce_add_sync(0xffffffffu, S[l][e]);
+          if (lane == cc) mine[l][e] = t;
+        }
+    }
+    if (lane >= cnt) continue;
+    const int64_t jg = (int64_t)cand_j[r * cap + c0 + lane] + jb.first_b;
+    const SInfo ia = info_a[ig], ib = info_b[jg];
+    bsm::EpilogueIn in;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      in.s0[e] = (float)mine[0][e];
+      in.s1[e] = (float)mine[1][e];
+      in.s2[e] = (float)mine[2][e];
+      in.s3[e] = (float)((double)mine[3][e] + 0.5 * (double)mine[4][e]);
+    }
+    in.ga = ia.ghat;
+    in.gb = ib.ghat;
+    in.gfa = ia.gf;
+    in.gfb = ib.gf;
+    in.qa = ia.qres;
+    in.qb = ib.qres;
+    int flag = 0;
+    float v = bsm::pair_rmsd_fast(in, jb.u, jb.d34, L, jb.tol, flag);
+    if (flag) {  // rare: the exact path, on this lane alone
+      long long mh[9];
+      exact_cov_partial(da, db, ig, jg, L, 0, 1, mh);
+      v = (float)bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
+    }
+    cand_v[r * cap + c0 + lane] = v;
   }
 }
 

@@ -19,8 +19,10 @@
 //     (A digits 0-1, B digits 0-1 of one tile).  Strips (chains of up to 128
 //     atoms): a record is a query block and a run of library column blocks;
 //     the query block's digits stay resident in shared memory for the whole
-//     run (64 KB) and four 16 KB stages stream only the library blocks --
-//     a third of the bytes per tile, which is what bounds short tiles.
+//     run and four 16 KB stages stream only the library blocks -- a third of
+//     the bytes per tile, which is what bounds short tiles.  The 64 KB of
+//     resident space hold two query blocks of up to 64 atoms (the next
+//     strip's block loads while this one's MMAs run) or one of up to 128.
 // Roles (one persistent CTA per SM, 640 threads): warp 0 TMA (operands, and a
 // bulk copy of each tile's job and per-structure data), warp 1 MMA issuer,
 // warp 2 TMEM allocation, warp 3 idle, warps 4-19 epilogue.  Every mbarrier
@@ -88,7 +90,7 @@ struct Shared {
   uint64_t tempty[2];
   uint64_t mfull[kMetaSlots];
   uint64_t mempty[kMetaSlots];
-  uint64_t afull, aempty;  // strips: the resident query block loaded / released
+  uint64_t afull[2], aempty[2];  // strips: a resident query block loaded / released
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -142,8 +144,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       ptx::mbar_init(&sh->mfull[b], 1);
       ptx::mbar_init(&sh->mempty[b], kEpiWarps * 32);
     }
-    ptx::mbar_init(&sh->afull, 1);
-    ptx::mbar_init(&sh->aempty, 1);
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(&sh->afull[b], 1);
+      ptx::mbar_init(&sh->aempty[b], 1);
+    }
     ptx::mbar_init(&sh->drain, 1);
     sh->abort = 0;
     ptx::fence_mbar_init();
@@ -174,16 +178,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
         const int rowA = rec.a_blk * kBlockRows;
         if (S) {
-          // the query block, resident for the strip (after the previous
-          // strip's MMAs have read their copy)
-          if (!ptx::mbar_wait(&sh->aempty, (ns & 1u) ^ 1u, abort, kTimeoutNs)) {
+          // the query block, resident for the strip, in buffer ns % nbuf
+          // once the MMAs of the strip that last used that buffer are done
+          const uint32_t nbuf = nchunks == 1 ? 2u : 1u, buf = ns % nbuf, use = ns / nbuf;
+          if (!ptx::mbar_wait(&sh->aempty[buf], (use & 1u) ^ 1u, abort, kTimeoutNs)) {
             fail(sh, a.sc);
             break;
           }
-          ptx::mbar_arrive_expect_tx(&sh->afull, (uint32_t)(nchunks * 2 * kAOpBytes));
+          uint8_t *ab = abuf + buf * 2 * kAOpBytes;
+          ptx::mbar_arrive_expect_tx(&sh->afull[buf], (uint32_t)(nchunks * 2 * kAOpBytes));
           for (int kc = 0; kc < nchunks; ++kc) {
-            ptx::tma_load_2d(abuf + kc * 2 * kAOpBytes, &ta0, kc * kKChunk, rowA, &sh->afull);
-            ptx::tma_load_2d(abuf + kc * 2 * kAOpBytes + kAOpBytes, &ta1, kc * kKChunk, rowA, &sh->afull);
+            ptx::tma_load_2d(ab + kc * 2 * kAOpBytes, &ta0, kc * kKChunk, rowA, &sh->afull[buf]);
+            ptx::tma_load_2d(ab + kc * 2 * kAOpBytes + kAOpBytes, &ta1, kc * kKChunk, rowA, &sh->afull[buf]);
           }
         }
         for (int u = 0; u < count && ok; ++u, ++tt) {
@@ -231,8 +237,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         ptx::mbar_wait(&sh->mfull[d % kMetaSlots], (d / kMetaSlots) & 1u, &no_abort, 100000000ull);
       }
       if (S && ns > 0) {
-        volatile int no_abort = 0;
-        ptx::mbar_wait(&sh->afull, (ns - 1) & 1u, &no_abort, 100000000ull);
+        // the query blocks loaded last (both buffers when two were in use)
+        const Tile rec = a.tiles[blockIdx.x];
+        const int nchunks = ((rec.shape & 0xffff) * 16 + kKChunk - 1) / kKChunk;
+        const uint32_t nbuf = nchunks == 1 ? 2u : 1u;
+        for (uint32_t d = (ns > nbuf ? ns - nbuf : 0); d < ns; ++d) {
+          volatile int no_abort = 0;
+          ptx::mbar_wait(&sh->afull[d % nbuf], (d / nbuf) & 1u, &no_abort, 100000000ull);
+        }
       }
     }
     __syncwarp();
@@ -246,7 +258,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         int nk16, count;
         record_shape<S>(rec, nk16, count);
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
-        if (S && !ptx::mbar_wait(&sh->afull, ns & 1u, abort, kTimeoutNs)) {
+        const uint32_t nbuf = nchunks == 1 ? 2u : 1u, buf = ns % nbuf;
+        if (S && !ptx::mbar_wait(&sh->afull[buf], (ns / nbuf) & 1u, abort, kTimeoutNs)) {
           fail(sh, a.sc);
           break;
         }
@@ -267,7 +280,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             ptx::tc_fence_after();
             const uint32_t base = ptx::smem_u32(smem + (size_t)st * kStageBytes);
-            const uint32_t abase = S ? ptx::smem_u32(abuf + kc * 2 * kAOpBytes) : base;
+            const uint32_t abase = S ? ptx::smem_u32(abuf + (buf + kc) * 2 * kAOpBytes) : base;
             const int ksteps = min(4, nk16 - kc * 4);
             for (int kk = 0; kk < ksteps; ++kk) {
               const uint32_t off = (uint32_t)kk * 32u;
@@ -289,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!ok) break;
           ptx::tc_commit(&sh->tfull[p & 1u]);
         }
-        if (S) ptx::tc_commit(&sh->aempty);  // the resident block is free once these MMAs complete
+        if (S) ptx::tc_commit(&sh->aempty[buf]);  // the block's buffer is free once these MMAs complete
       }
       ptx::tc_commit(&sh->drain);
       volatile int no_abort = 0;
@@ -349,27 +362,44 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int t_L = mj.L;
         uint32_t *sout = static_cast<uint32_t *>(mj.out.ptr);
         const int64_t ld = mj.out.ld;
-        // 10 x 5 pairs over the 32 lanes, two rounds
-#pragma unroll 1
-        for (int rd = 0; rd < 2; ++rd) {
-          const int pp = rd * 32 + lane;
-          const int pc = pp < 50 ? pp : 0;  // pad slots read a valid pair
-          const int ir = pc / 5, jc = pc - 5 * (pc / 5);
-          const int64_t i = i0 + ir, j = j0 + jc;
-          float m9[9];
+        // 10 x 5 pairs over the 32 lanes: lane l takes pairs l and 32 + l,
+        // both through one packed FP32x2 bracket
+        int64_t oi[2];
+        bool okp[2];
+        bsm::F2 m2[9], ga, dr;
+        {
+          float mv[2][9], gv[2], dv[2];
 #pragma unroll
-          for (int xr = 0; xr < 3; ++xr)
+          for (int u = 0; u < 2; ++u) {
+            const int pp = u * 32 + lane;
+            const int pc = pp < 50 ? pp : 0;  // pad slots read a valid pair
+            const int ir = pc / 5, jc = pc - 5 * (pc / 5);
+            const int64_t i = i0 + ir, j = j0 + jc;
+            okp[u] = job_ok && pp < 50 && i < jn && j < jnb;
+            oi[u] = i * ld + j;
 #pragma unroll
-            for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
-          const float2 fa = mt.ta[qd * kGroupStructs + ir], fb = mt.tb[5 * cq + jc];
-          float lo, hi;
-          bsm::screen_bracket(m9, fa.x + fb.x, t_de, fa.y + fb.y, t_u, t_L, lo, hi);
-          if (job_ok && pp < 50 && i < jn && j < jnb) {
-            const uint32_t wlo = __half_as_ushort(__float2half_rd(lo));
-            const uint32_t whi = __half_as_ushort(__float2half_ru(hi));
-            sout[i * ld + j] = (whi << 16) | wlo;
+            for (int xr = 0; xr < 3; ++xr)
+#pragma unroll
+              for (int y = 0; y < 3; ++y) mv[u][3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+            const float2 fa = mt.ta[qd * kGroupStructs + ir], fb = mt.tb[5 * cq + jc];
+            gv[u] = fa.x + fb.x;
+            dv[u] = fa.y + fb.y;
           }
+#pragma unroll
+          for (int e = 0; e < 9; ++e) m2[e] = bsm::f2(mv[0][e], mv[1][e]);
+          ga = bsm::f2(gv[0], gv[1]);
+          dr = bsm::f2(dv[0], dv[1]);
         }
+        bsm::F2 lo, hi;
+        bsm::screen_bracket2(m2, ga, t_de, dr, t_u, t_L, lo, hi);
+        const float los[2] = {lo.v.x, lo.v.y}, his[2] = {hi.v.x, hi.v.y};
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (okp[u]) {
+            const uint32_t wlo = __half_as_ushort(__float2half_rd(los[u]));
+            const uint32_t whi = __half_as_ushort(__float2half_ru(his[u]));
+            sout[oi[u]] = (whi << 16) | wlo;
+          }
         __syncwarp();
         ptx::mbar_arrive(&sh->mempty[slot]);
       }
