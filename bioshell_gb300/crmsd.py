@@ -40,6 +40,7 @@ class CrmsdOptions:
     tolerance: Optional[float] = None
     graph: bool = True  # replay a captured CUDA graph for repeated shapes
     autotune: bool = False  # time the tile shapes per set class (mixed path)
+    flag_queue: int = 0  # capacity of the exact-recomputation queue (0 = default)
 
     def to_c(self) -> _l.bs_opts:
         o = _l.bs_opts()
@@ -49,6 +50,7 @@ class CrmsdOptions:
         o.out_type = _l.OUT_TYPE[self.out_type]
         o.tolerance = float(self.tolerance or 0.0)
         o.flags = (0 if self.graph else _l.FLAG_NO_GRAPH) | (_l.FLAG_AUTOTUNE if self.autotune else 0)
+        o.flag_queue = int(self.flag_queue)
         return o
 
 

@@ -78,6 +78,15 @@ bool is_device_ptr(const void *p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
+bool is_pinned_host(const void *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 }  // namespace bs
 
 namespace {
@@ -85,6 +94,9 @@ namespace {
 constexpr double kDefaultTol = 1e-4;                  // Angstrom, certified total |dRMSD| per pair
 constexpr unsigned long long kFlagCap = 1ull << 24;  // queued exact recomputations
 constexpr size_t kMaxGraphs = 16;
+// banded read-back: results of at least 2^24 pairs, in about 16 bands
+constexpr int64_t kBandMinPairs = 1ll << 24;
+constexpr int kBands = 16;
 
 #define CK(call, what)                                     \
   do {                                                     \
@@ -203,7 +215,8 @@ std::vector<int64_t> plan_key(bs_ctx *ctx, const Plan &plan, unsigned long long 
 
 // Runs the device sequence of a plan (graph replay when possible) and reads
 // back the counters; the caller synchronises and calls finish_mixed.
-bs_status launch_plan(bs_ctx *ctx, const Plan &plan, const MixedBuffers &b, bool use_graph) {
+bs_status launch_plan(bs_ctx *ctx, const Plan &plan, const MixedBuffers &b, bool use_graph,
+                      const Readback *rb = nullptr) {
   const int nj = (int)plan.jobs.size();
   memcpy(ctx->job_stage, plan.jobs.data(), (size_t)nj * sizeof(Job));
   std::string m = get_encoder(&ctx->encode);
@@ -212,9 +225,10 @@ bs_status launch_plan(bs_ctx *ctx, const Plan &plan, const MixedBuffers &b, bool
   m = encode_maps(ctx->encode, b, tm);
   if (!m.empty()) return set_err(ctx, BS_ERR_CUDA, "%s", m.c_str());
   const Job *stage = static_cast<const Job *>(ctx->job_stage);
-  ctx->metrics.main_launches = plan.tiles.empty() ? 5 : 9;
-  if (!use_graph) {
-    CK(enqueue_mixed(plan, b, stage, tm, ctx->num_sms, ctx->stream, &ctx->ev[1], false), "mixed-path launch");
+  ctx->metrics.main_launches = plan.tiles.empty() ? 5 : rb ? 6 + 4 * (int)rb->tile_end.size() : 9;
+  if (!use_graph || rb) {
+    CK(enqueue_mixed(plan, b, stage, tm, ctx->num_sms, ctx->stream, &ctx->ev[1], false, nullptr, rb),
+       "mixed-path launch");
     ctx->metrics.graph = 0;
   } else {
     const std::vector<int64_t> key = plan_key(ctx, plan, b.flag_cap);
@@ -406,6 +420,8 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
   if (out_bytes && (s = ensure(ctx, ctx->out, out_bytes, "result buffer"))) return s;
   CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
   std::vector<JobSpec> specs;
+  Readback rb;
+  bool banded = false;
   for (int k = 0; k < nsets; ++k) {
     const bs_set_desc &d = sets[k];
     if (d.n < 2) continue;
@@ -441,11 +457,34 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     Plan plan;
     const std::string m = make_symmetric_plan(specs, total_tolerance(o), true, plan);
     if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
-    const unsigned long long cap = std::min<unsigned long long>(kFlagCap, std::max<int64_t>(pairs, 4096));
+    unsigned long long cap = std::min<unsigned long long>(kFlagCap, std::max<int64_t>(pairs, 4096));
+    if (o.flag_queue > 0) cap = std::min<unsigned long long>(cap, (unsigned long long)o.flag_queue);
     MixedBuffers b;
     if ((s = prepare_buffers(ctx, plan, cap, b))) return s;
     if ((s = upload_tables(ctx, plan, b, plan_key(ctx, plan, cap)))) return s;
-    if ((s = launch_plan(ctx, plan, b, !(o.flags & BS_FLAG_NO_GRAPH)))) return s;
+    // one large triangle bound for pinned host memory: read back in row
+    // bands while the later bands compute
+    if (nsets == 1 && specs.size() == 1 && io[0].out_off != SIZE_MAX && o.layout == BS_LAYOUT_TRIANGLE &&
+        pairs >= kBandMinPairs && is_pinned_host(sets[0].out)) {
+      if (!ctx->copy_stream) CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream");
+      make_bands(plan, specs[0].n, kBands, rb);
+      while (ctx->band_ev.size() < rb.tile_end.size() + 1) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "band event");
+        ctx->band_ev.push_back(e);
+      }
+      rb.dev = static_cast<const char *>(io[0].out_dev);
+      rb.host = static_cast<char *>(sets[0].out);
+      rb.esz = esz;
+      rb.copy = ctx->copy_stream;
+      rb.ev = ctx->band_ev.data();
+      banded = true;
+    }
+    s = launch_plan(ctx, plan, b, !(o.flags & BS_FLAG_NO_GRAPH), banded ? &rb : nullptr);
+    if (s) {
+      if (banded) cudaStreamSynchronize(ctx->copy_stream);
+      return s;
+    }
   } else {
     for (int k = 1; k <= 4; ++k) CK(cudaEventRecord(ctx->ev[k], ctx->stream), "event");
     memset(ctx->sc_back, 0, sizeof(DevScalars));
@@ -454,7 +493,8 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     const bs_set_desc &d = sets[k];
     if (d.n < 2 || io[k].out_off == SIZE_MAX) continue;
     const size_t bytes = out_elems(d.n, o.layout) * esz;
-    CK(cudaMemcpyAsync(d.out, io[k].out_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy result to host");
+    if (!banded)
+      CK(cudaMemcpyAsync(d.out, io[k].out_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy result to host");
     ctx->metrics.bytes_d2h += (int64_t)bytes;
   }
   CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
@@ -776,6 +816,11 @@ BS_API void bs_ctx_destroy(bs_ctx *ctx) {
   if (ctx->sc_back) cudaFreeHost(ctx->sc_back);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  for (cudaEvent_t e : ctx->band_ev) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

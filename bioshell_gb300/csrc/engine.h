@@ -69,13 +69,34 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
 std::string encode_maps(PFN_cuTensorMapEncodeTiled_v12000 encode, const MixedBuffers &b, CUtensorMap tm[7]);
 std::string get_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out);
 
+// Read-back of one symmetric job's packed triangle in row bands, each band
+// copied to pinned host memory on a second stream while the next computes.
+// Band k is tiles [tile_end[k-1], tile_end[k]) of the plan (whole super-rows
+// of A blocks, so its rows are complete when they and their recomputations
+// are done) and output elements [elem_end[k-1], elem_end[k]).
+struct Readback {
+  std::vector<int64_t> tile_end, elem_end;
+  const char *dev = nullptr;
+  char *host = nullptr;
+  size_t esz = 0;
+  cudaStream_t copy = nullptr;
+  const cudaEvent_t *ev = nullptr;  // tile_end.size() + 1 events
+};
+
+// Band boundaries for a single symmetric job of n structures: whole
+// super-rows, about `bands` bands of equal pair counts.
+void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb);
+
 // Enqueues the mixed-path sequence of a plan whose tables are on the
 // device: counters reset, job table upload from `job_stage` (pinned or
 // pageable; pinned when captured), preparation, tensor-core tiles, exact
 // recomputation.  `ev` (optional, 4 events) marks prep / main / refine
-// boundaries; `capturing` records them as graph event nodes.
+// boundaries; `capturing` records them as graph event nodes.  With `rb`
+// (not captured) the tiles run band by band and each band is read back
+// as soon as it is final; the stream waits for the last copy.
 cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *job_stage, const CUtensorMap tm[7],
-                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg = nullptr);
+                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg = nullptr,
+                          const Readback *rb = nullptr);
 
 // Maps the device error bits of a finished launch to a status and message.
 bs_status collect_errors(const DevScalars &sc, const Job *jobs, int njobs, std::string &msg);
@@ -87,6 +108,9 @@ struct bs_ctx {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[6] = {};
+  // banded read-back of large results: its copy stream and band events
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> band_ev;
   size_t budget = 0;
   size_t used = 0;
   uint64_t gen = 0;  // bumped whenever a workspace moves (graphs hold addresses)
@@ -125,4 +149,5 @@ bs_status cuda_err(bs_ctx *ctx, cudaError_t e, const char *what);
 bs_status ensure(bs_ctx *ctx, DevBuf &b, size_t bytes, const char *what);
 void release(bs_ctx *ctx, DevBuf &b);
 bool is_device_ptr(const void *p);
+bool is_pinned_host(const void *p);
 }  // namespace bs

@@ -135,6 +135,8 @@ struct DevScalars {
   unsigned long long flag_count;  // pairs queued for exact recomputation
   int err;                        // kErr* bits not tied to one job
   int pad;
+  unsigned long long flag_done;   // queue entries already recomputed (banded launches)
+  unsigned long long tile_next;   // next tile of the running k_mixed_tc launch (zero before each)
 };
 constexpr int kErrTimeout = 1;
 constexpr int kErrNonFinite = 2;
@@ -236,6 +238,11 @@ struct RefineArgs {
   const unsigned long long *flags;
   unsigned long long cap;
   int num_sms;
+  // banded launches: queue entries from sc->flag_done on are new; `mark`
+  // advances flag_done afterwards, and the overflow scan covers only the
+  // output elements [scan_lo, scan_hi) of job 0 (scan_hi < 0: everything)
+  bool mark = false;
+  int64_t scan_lo = 0, scan_hi = -1;
 };
 // exact recomputation of the queued pairs; then, only when the queue
 // overflowed (checked on the device), of every sentinel left in the outputs

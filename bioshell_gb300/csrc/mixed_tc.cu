@@ -35,8 +35,12 @@
 //           coordinate x of structure i finishes pairs (i, j) with
 //           j = x mod 3 through the three phases of crmsd_math.cuh, and
 //           writes the result.
-// Tiles come from a table of (A block, B block, job): one launch serves any
-// number of jobs -- the symmetric all-vs-all of one or many structure sets
+// Tiles come from a table of (A block, B block, job), handed out one at a
+// time by a counter (DevScalars::tile_next, zero at launch): the TMA thread
+// takes the next tile and passes its record to the MMA thread and the
+// epilogue through the metadata slot, so all SMs work on a narrow window of
+// the table and its operands stay in L2.  One launch serves any number of
+// jobs -- the symmetric all-vs-all of one or many structure sets
 // (pairs i < j), and query-vs-library blocks (every pair) -- each with its
 // own chain length, grid and output.
 // Every mbarrier wait is bounded; a timeout sets an error bit and all roles
@@ -207,10 +211,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       // ------------------------------------------------------ TMA producer
       uint32_t it = 0, tt = 0;
-      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x, ++tt) {
+      unsigned long long *ctr = &a.sc->tile_next;
+      int64_t t = (int64_t)atomicAdd(ctr, 1ull);
+      Tile next = t < a.ntiles ? a.tiles[t] : Tile{};
+      unsigned long long tn = 0;
+      for (; !*abort; ++tt) {
         const Tile tile = next;
-        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
         {
           // the tile's metadata: record, job, per-structure data
           const uint32_t ms = tt % kMetaSlots;
@@ -219,7 +225,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           TileMeta &mt = meta[ms];
+          if (t >= a.ntiles) {
+            // end of the table: a record with job -1 tells the MMA thread and
+            // the epilogue to stop
+            mt.tile = Tile{0, 0, -1, 0};
+            ptx::mbar_arrive(&sh->mfull[ms]);
+            ++tt;
+            break;
+          }
           mt.tile = tile;
+          tn = atomicAdd(ctr, 1ull);  // used after this tile's loads are issued
           const bool nar = tile_narrow(tile), scr = tile_layout(tile) == kAccScreen;
           const int nbs = nar ? kNarrowStructs : kBStructs;
           const int64_t a0 = (int64_t)tile.a_blk * kBlockStructs, b0 = (int64_t)tile.b_blk * nbs;
@@ -258,6 +273,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           ptx::tma_load_2d(st + 4 * kAOpBytes + 1 * kBOpBytes, &tb1, k0, rowB, &sh->full[s]);
           if (!scr) ptx::tma_load_2d(st + 4 * kAOpBytes + 2 * kBOpBytes, &tb2, k0, rowB, &sh->full[s]);
         }
+        // the next tile: its record loads while this block waits for slots
+        t = (int64_t)tn;
+        if (t < a.ntiles) next = a.tiles[t];
       }
       // let the copies still in flight land before the block can retire
       for (uint32_t d = (it > kStages ? it - kStages : 0); d < it; ++d) {
@@ -277,10 +295,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       // (p >> 1)-th time.  A long-layout tile takes two consecutive slots
       // (eight accumulators: accumulator a lives in slot p + a / 4).
       uint32_t it = 0, p = 0;
-      Tile next = blockIdx.x < a.ntiles ? a.tiles[blockIdx.x] : Tile{};
-      for (int64_t t = blockIdx.x; t < a.ntiles && !*abort; t += gridDim.x) {
-        const Tile tile = next;
-        if (t + gridDim.x < a.ntiles) next = a.tiles[t + gridDim.x];  // in flight during this tile
+      for (uint32_t tt = 0; !*abort; ++tt) {
+        // the tile's record, as the TMA thread took it from the table
+        const uint32_t ms = tt % kMetaSlots;
+        if (!ptx::mbar_wait(&sh->mfull[ms], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) {
+          fail(sh, a.sc);
+          break;
+        }
+        const Tile tile = meta[ms].tile;
+        if (tile.job < 0) break;
         const int nk16 = tile_nk16(tile);
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
         const int lay = tile_layout(tile);
@@ -397,14 +420,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int ilr = il < kGroupStructs ? il : kGroupStructs - 1;  // pad lanes read a valid row
     const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * g;
     uint32_t p = 0;   // TMEM buffer slot, as the MMA issuer counts them
-    uint32_t tt = 0;  // tile sequence number (metadata slot)
-    for (int64_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++tt) {
+    for (uint32_t tt = 0;; ++tt) {  // tile sequence number (metadata slot)
       const uint32_t slot = tt % kMetaSlots;
       if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) {
         fail(sh, a.sc);
         break;
       }
       const TileMeta &mt = meta[slot];
+      if (mt.tile.job < 0) break;  // end of the table
       const Job &mj = mt.job;
       const bool lng = mj.layout == kAccLong;
       bool ok = true;

@@ -105,8 +105,31 @@ std::string encode_maps(PFN_cuTensorMapEncodeTiled_v12000 encode, const MixedBuf
   return "";
 }
 
+void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb) {
+  constexpr int64_t SA = 32;  // A blocks per super-row (make_symmetric_plan)
+  rb.tile_end.clear();
+  rb.elem_end.clear();
+  auto off = [n](int64_t r) { return r * n - r * (r + 1) / 2; };  // packed index of (r, r + 1)
+  const int64_t total = n * (n - 1) / 2, want = std::max<int64_t>(1, total / std::max(1, bands));
+  int64_t last = 0;
+  const int64_t nt = (int64_t)plan.tiles.size();
+  for (int64_t t = 1; t < nt; ++t) {
+    const int64_t s = plan.tiles[t].a_blk / SA;
+    if (s == plan.tiles[t - 1].a_blk / SA) continue;
+    const int64_t e = off(std::min(n, s * SA * kBlockStructs));
+    if (e - last >= want) {
+      rb.tile_end.push_back(t);
+      rb.elem_end.push_back(e);
+      last = e;
+    }
+  }
+  rb.tile_end.push_back(nt);
+  rb.elem_end.push_back(total);
+}
+
 cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *job_stage, const CUtensorMap tm[7],
-                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg) {
+                          int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg,
+                          const Readback *rb) {
   auto rec = [&](int k) -> cudaError_t {
     if (!ev) return cudaSuccess;
     return cudaEventRecordWithFlags(ev[k], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
@@ -151,9 +174,6 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     // launches of screen jobs only run the screen-shaped kernel
     bool all_screen = nj > 0;
     for (const Job &jb : plan.jobs) all_screen = all_screen && jb.screen;
-    if ((e = all_screen ? launch_screen_tc(tm, a, plan.strips, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess)
-      return e;
-    if ((e = rec(2)) != cudaSuccess) return e;
     RefineArgs r{};
     r.da = DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a};
     r.db = DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b};
@@ -165,7 +185,36 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     r.flags = b.flags;
     r.cap = b.flag_cap;
     r.num_sms = num_sms;
-    if ((e = launch_refine(r, st)) != cudaSuccess) return e;
+    if (!rb) {
+      if ((e = all_screen ? launch_screen_tc(tm, a, plan.strips, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess)
+        return e;
+      if ((e = rec(2)) != cudaSuccess) return e;
+      if ((e = launch_refine(r, st)) != cudaSuccess) return e;
+    } else {
+      const size_t nb = rb->tile_end.size();
+      r.mark = true;
+      for (size_t k = 0; k < nb; ++k) {
+        const int64_t t0 = k ? rb->tile_end[k - 1] : 0, e0 = k ? rb->elem_end[k - 1] : 0;
+        a.tiles = b.tiles + t0;
+        a.ntiles = rb->tile_end[k] - t0;
+        // each launch hands out its tiles from a counter at zero
+        if (k > 0 && (e = cudaMemsetAsync(&b.sc->tile_next, 0, sizeof(unsigned long long), st)) != cudaSuccess)
+          return e;
+        if (a.ntiles > 0 && (e = launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
+        if (k + 1 == nb && (e = rec(2)) != cudaSuccess) return e;
+        r.scan_lo = e0;
+        r.scan_hi = rb->elem_end[k];
+        if ((e = launch_refine(r, st)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(rb->ev[k], st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(rb->copy, rb->ev[k], 0)) != cudaSuccess) return e;
+        const size_t bytes = (size_t)(rb->elem_end[k] - e0) * rb->esz;
+        if (bytes && (e = cudaMemcpyAsync(rb->host + (size_t)e0 * rb->esz, rb->dev + (size_t)e0 * rb->esz, bytes,
+                                          cudaMemcpyDeviceToHost, rb->copy)) != cudaSuccess)
+          return e;
+      }
+      if ((e = cudaEventRecord(rb->ev[nb], rb->copy)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(st, rb->ev[nb], 0)) != cudaSuccess) return e;
+    }
   } else {
     if ((e = rec(2)) != cudaSuccess) return e;
   }

@@ -64,6 +64,13 @@ __device__ __forceinline__ int coord(const DigitsView &dg, int64_t s, int c, int
                           (int)__bfloat162float(dg.d2[off]));
 }
 
+// The FP64 finish of the exact path as one compiled function shared by
+// every kernel here: inlined copies may contract multiply-adds differently,
+// and a pair's exact value must not depend on which kernel recomputed it.
+__device__ __noinline__ double exact_finish(const long long mh[9], long long ga, long long gb, int scale_exp, int L) {
+  return bsm::pair_rmsd_exact(mh, ga, gb, scale_exp, L);
+}
+
 // Exact int64 covariance of pair (i on side A, j on side B), partial over
 // atoms k = k0, k0+ks, ...
 __device__ __forceinline__ void exact_cov_partial(const DigitsView &da, const DigitsView &db, int64_t i, int64_t j,
@@ -93,14 +100,16 @@ __device__ __forceinline__ double exact_pair_warp(const RefineArgs &r, const Job
   for (int e = 0; e < 9; ++e)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mh[e] += __shfl_xor_sync(0xffffffffu, mh[e], o);
-  return bsm::pair_rmsd_exact(mh, r.info_a[ig].ghat, r.info_b[jg].ghat, jb.scale_exp, jb.L);
+  return exact_finish(mh, r.info_a[ig].ghat, r.info_b[jg].ghat, jb.scale_exp, jb.L);
 }
 
 __global__ void k_refine_list(RefineArgs r) {
   const unsigned long long cnt = r.sc->flag_count < r.cap ? r.sc->flag_count : r.cap;
+  const int64_t done = (int64_t)r.sc->flag_done;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)cnt; w += warps) {
+  for (int64_t w = done + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < (int64_t)cnt;
+       w += warps) {
     const unsigned long long f = r.flags[w];
     const int job = (int)(f >> 48);
     const int64_t ig = (int64_t)((f >> 24) & 0xffffffull), jg = (int64_t)(f & 0xffffffull);
@@ -108,6 +117,11 @@ __global__ void k_refine_list(RefineArgs r) {
     const double v = exact_pair_warp(r, jb, ig, jg, lane);
     if (lane == 0) store_pair(jb.out, ig - jb.first_a, jg - jb.first_b, v);
   }
+}
+
+// After a band's recomputation: its queue entries are done.
+__global__ void k_refine_mark(DevScalars *sc, unsigned long long cap) {
+  sc->flag_done = sc->flag_count < cap ? sc->flag_count : cap;
 }
 
 // Fallback when the queue overflowed: every negative (sentinel) entry of the
@@ -123,8 +137,13 @@ __global__ void k_refine_scan(RefineArgs r) {
     const OutDesc &out = jb.out;
     const bool sym = jb.mode == 0;
     const int64_t n = jb.n, nb = jb.n_b;
-    const int64_t total = sym ? n * (n - 1) / 2 : n * nb;
-    for (int64_t base = w0 * 32; base < total; base += warps * 32) {
+    int64_t total = sym ? n * (n - 1) / 2 : n * nb, first = 0;
+    if (r.scan_hi >= 0) {
+      if (job > 0) break;
+      first = r.scan_lo;
+      total = r.scan_hi < total ? r.scan_hi : total;
+    }
+    for (int64_t base = first + w0 * 32; base < total; base += warps * 32) {
       const int64_t t = base + lane;
       int64_t i = 0, j = 0;
       bool sent = false;
@@ -220,7 +239,7 @@ __device__ double certified_pair(const DigitsView &da, const DigitsView &db, int
   if (!flag) return (double)r;
   long long mh[9];
   exact_cov_partial(da, db, ig, jg, L, 0, 1, mh);
-  return bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
+  return exact_finish(mh, in.ga, in.gb, jb.scale_exp, L);
 }
 
 // Thread per pair of job 0 (explicit pair lists, and the tensor-core path's
@@ -335,7 +354,7 @@ __global__ void __launch_bounds__(kCandWarps * 32)
     if (flag) {  // rare: the exact path, on this lane alone
       long long mh[9];
       exact_cov_partial(da, db, ig, jg, L, 0, 1, mh);
-      v = (float)bsm::pair_rmsd_exact(mh, in.ga, in.gb, jb.scale_exp, L);
+      v = (float)exact_finish(mh, in.ga, in.gb, jb.scale_exp, L);
     }
     cand_v[r * cap + c0 + lane] = v;
   }
@@ -345,6 +364,7 @@ __global__ void __launch_bounds__(kCandWarps * 32)
 
 cudaError_t launch_refine(const RefineArgs &r, cudaStream_t st) {
   k_refine_list<<<r.num_sms * 4, 256, 0, st>>>(r);
+  if (r.mark) k_refine_mark<<<1, 1, 0, st>>>(r.sc, r.cap);
   k_refine_scan<<<r.num_sms * 4, 256, 0, st>>>(r);
   return cudaGetLastError();
 }

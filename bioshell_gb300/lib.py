@@ -31,7 +31,7 @@ FLAG_AUTOTUNE = 2
 class bs_opts(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("precision", ctypes.c_int32), ("layout", ctypes.c_int32),
                 ("out_type", ctypes.c_int32), ("tolerance", ctypes.c_double), ("flags", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("flag_queue", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
 
 
 class bs_set_desc(ctypes.Structure):

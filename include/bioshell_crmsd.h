@@ -100,7 +100,11 @@ typedef struct {
                          meet it are recomputed exactly.  <= 0 selects the
                          default, 1e-4                                    */
   int32_t flags;      /* BS_FLAG_* bits                                    */
-  int32_t reserved[7];
+  int32_t flag_queue; /* mixed path: capacity of the queue of pairs to
+                         recompute exactly; <= 0 selects the default,
+                         min(2^24, pairs).  Pairs flagged beyond it are
+                         found by a scan of the result for their sentinel  */
+  int32_t reserved[6];
 } bs_opts;
 
 /* bs_opts.flags */
