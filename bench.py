@@ -235,6 +235,40 @@ def run_neighbors(eng, xd, outd, n, torch, eps=1.0, steps=3):
             "dense_f32_bytes": int(4 * n * (n - 1) // 2), "rows_checked_against_dense": len(rows), "match": ok}
 
 
+def run_superpose(eng, xd, x, torch, npairs=1_000_000, steps=3):
+    """Rototranslations of random pairs of the headline set (device-resident
+    coordinates, pair lists and outputs): device time, and a sample checked
+    against the host copy of the same math."""
+    import ctypes
+    n, L = x.shape[0], x.shape[1]
+    rng = np.random.default_rng(31)
+    ii = torch.from_numpy(rng.integers(0, n, npairs)).cuda()
+    jj = torch.from_numpy(rng.integers(0, n, npairs)).cuda()
+    out = (torch.empty((npairs, 3, 3), dtype=torch.float64, device="cuda"),
+           torch.empty((npairs, 3), dtype=torch.float64, device="cuda"),
+           torch.empty(npairs, dtype=torch.float64, device="cuda"))
+    eng.superpose_pairs(xd, ii, jj, out)
+    ms = []
+    for _ in range(steps):
+        eng.superpose_pairs(xd, ii, jj, out)
+        ms.append(eng.metrics()["ms_main"])
+    sel = rng.choice(npairs, 64, replace=False)
+    rot = out[0][torch.from_numpy(sel).cuda()].cpu().numpy()
+    rm = out[2][torch.from_numpy(sel).cuda()].cpu().numpy()
+    si, sj = ii.cpu().numpy()[sel], jj.cpu().numpy()[sel]
+    worst_r = worst_m = 0.0
+    for t in range(len(sel)):
+        hr, ht, hm = np.empty(9), np.empty(3), ctypes.c_double()
+        a, b = np.ascontiguousarray(x[si[t]]), np.ascontiguousarray(x[sj[t]])
+        eng._lib.bs_selftest_superpose(a.ctypes.data, b.ctypes.data, L, hr.ctypes.data, ht.ctypes.data,
+                                       ctypes.byref(hm))
+        worst_r = max(worst_r, float(np.abs(rot[t] - hr.reshape(3, 3)).max()))
+        worst_m = max(worst_m, abs(float(rm[t]) - hm.value))
+    msd = statistics.median(ms)
+    return {"pairs": npairs, "L": L, "ms_device": msd, "pairs_per_s": npairs / (msd * 1e-3),
+            "sample_checked": len(sel), "max_abs_rot_vs_host": worst_r, "max_abs_rmsd_vs_host": worst_m}
+
+
 def run_formats(eng, torch, n_models=1000, L=300, n_tsv=4000):
     """Throughput of the formats either side of the path: multi-model PDB
     ingestion (a synthetic ensemble of n_models x L residues, 4 atoms each,
@@ -616,6 +650,7 @@ def run_ours(a, rank, world, local_rank):
                "tolerance": 1e-4, "pass": bool(d.max() <= 1e-4 and (len(d2) == 0 or d2.max() <= 1e-4))}
 
     neighbors = run_neighbors(eng, xd, outd, n, torch) if rank == 0 else None
+    superpose = run_superpose(eng, xd, x, torch) if rank == 0 else None
 
     pk, pk_kind = peaks()
     achieved = 18.0 * L * npairs / (ms_main * 1e-3) / 1e12
@@ -648,7 +683,7 @@ def run_ours(a, rank, world, local_rank):
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
             "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
-            "formats": formats, "hierarchical": hier,
+            "superpose": superpose, "formats": formats, "hierarchical": hier,
             "batched": batched,
             "serving": serving}
     if rank == 0:

@@ -5,9 +5,10 @@ behind the C ABI of ``include/bioshell_crmsd.h``); this package is the thin
 host-side mirror of the Rust API and the synthetic-workload generator.
 """
 from .crmsd import (CrmsdMatrix, CrmsdOptions, Engine, crmsd, crmsd_all_vs_all, crmsd_batched,  # noqa: F401
-                    default_engine, tri_index)
+                    default_engine, superpose, tri_index)
 from .lib import CrmsdError  # noqa: F401
 from .serving import CrmsdServer  # noqa: F401
+from .superpose import Rototranslation  # noqa: F401
 
 __all__ = ["CrmsdMatrix", "CrmsdOptions", "Engine", "crmsd", "crmsd_all_vs_all", "crmsd_batched", "default_engine", "tri_index",
-           "CrmsdError", "CrmsdServer"]
+           "CrmsdError", "CrmsdServer", "Rototranslation", "superpose"]

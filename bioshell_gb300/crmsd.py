@@ -254,6 +254,52 @@ class Engine:
         self._check(self._lib.bs_pairs(self._h, xp, n, L, ip, jp, npairs, ctypes.byref(o), op))
         return out
 
+    # -- superposition -------------------------------------------------------
+    def superpose(self, a, b):
+        """The superposition of b onto a: (Rototranslation with R b + t ~ a,
+        RMSD of that superposition)."""
+        from .superpose import Rototranslation
+
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        if a.ndim != 2 or a.shape[1] != 3 or a.shape != b.shape:
+            raise ValueError("superpose: both inputs must be [L][3] with the same L")
+        rot = np.empty(9)
+        t = np.empty(3)
+        r = np.empty(1)
+        self._check(self._lib.bs_superpose(self._h, a.ctypes.data, b.ctypes.data, a.shape[0], rot.ctypes.data,
+                                           t.ctypes.data, r.ctypes.data))
+        return Rototranslation(rot.reshape(3, 3), t), float(r[0])
+
+    def superpose_pairs(self, xyz, ii, jj, out=None):
+        """For each pair t: rot[t] (3x3), trans[t] (3) with rot x_jj[t] + trans ~
+        x_ii[t], and the RMSD of that superposition.  xyz ([n][L][3]) and the
+        pair lists may be numpy arrays or CUDA tensors; ``out`` = (rot, trans,
+        rmsd) buffers (numpy or CUDA), allocated on the host when omitted."""
+        if isinstance(xyz, np.ndarray) or not hasattr(xyz, "data_ptr"):
+            xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        if len(xyz.shape) != 3 or xyz.shape[2] != 3:
+            raise ValueError("coordinates must be [n][L][3]")
+        n, L = int(xyz.shape[0]), int(xyz.shape[1])
+        if isinstance(ii, np.ndarray) or not hasattr(ii, "data_ptr"):
+            ii = np.ascontiguousarray(ii, dtype=np.int64)
+            jj = np.ascontiguousarray(jj, dtype=np.int64)
+        if tuple(ii.shape) != tuple(jj.shape) or len(ii.shape) != 1:
+            raise ValueError("pair lists must be 1-D and of equal length")
+        npairs = int(ii.shape[0])
+        if out is None:
+            out = (np.empty((npairs, 3, 3)), np.empty((npairs, 3)), np.empty(npairs))
+        rot, trans, rmsd = out
+        if npairs:
+            xp, _k1 = _ptr(xyz)
+            ip, _k2 = _ptr(ii)
+            jp, _k3 = _ptr(jj)
+            rp, _k4 = _ptr(rot)
+            tp, _k5 = _ptr(trans)
+            mp, _k6 = _ptr(rmsd)
+            self._check(self._lib.bs_superpose_pairs(self._h, xp, n, L, ip, jp, npairs, rp, tp, mp))
+        return rot, trans, rmsd
+
     # -- diagnostics ---------------------------------------------------------
     def debug_tile_levels(self, xyz) -> np.ndarray:
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
@@ -288,6 +334,11 @@ def default_engine() -> Engine:
 def crmsd(a, b) -> float:
     """crmsd of two index-matched [L][3] coordinate sets (on the GPU)."""
     return default_engine().crmsd(a, b)
+
+
+def superpose(a, b):
+    """(Rototranslation moving b onto a, its RMSD), on the GPU."""
+    return default_engine().superpose(a, b)
 
 
 def crmsd_all_vs_all(models, opts: Optional[CrmsdOptions] = None) -> CrmsdMatrix:

@@ -630,7 +630,8 @@ DevBuf *all_buffers(bs_ctx *ctx, std::vector<DevBuf *> &v) {
        &ctx->dig[3],  &ctx->jobs,   &ctx->jobmap, &ctx->tiles, &ctx->flags,  &ctx->y,      &ctx->g,
        &ctx->ctrd,    &ctx->pairs_i, &ctx->pairs_j, &ctx->pout,
        &ctx->nbr_sink, &ctx->nbr_count, &ctx->nbr_ij, &ctx->nbr_d, &ctx->nbr_rows, &ctx->nbr_key, &ctx->nbr_tmp,
-       &ctx->nbr_rowptr, &ctx->nbr_col, &ctx->nbr_dist, &ctx->hier_ws, &ctx->hier_tri, &ctx->hier_out};
+       &ctx->nbr_rowptr, &ctx->nbr_col, &ctx->nbr_dist, &ctx->hier_ws, &ctx->hier_tri, &ctx->hier_out,
+       &ctx->sp_out};
   return nullptr;
 }
 
@@ -985,6 +986,102 @@ BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, 
   return pairs_impl(ctx, xyz, n, L, ii, jj, npairs, o, out, nullptr);
 }
 
+namespace {
+
+// Superposition of a pair list (host or device pointers): staging as in
+// pairs_impl, one warp per pair on the device.
+bs_status superpose_impl(bs_ctx *ctx, const double *xyz, int64_t n, int L, const int64_t *ii, const int64_t *jj,
+                         int64_t np, double *rot, double *trans, double *rmsd) {
+  ctx->metrics = bs_metrics{};
+  bs_status s;
+  CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
+  const double *dxyz = xyz;
+  if (!is_device_ptr(xyz)) {
+    const size_t bytes = (size_t)n * (size_t)L * 3 * sizeof(double);
+    if ((s = ensure(ctx, ctx->xyz, bytes, "coordinates"))) return s;
+    CK(cudaMemcpyAsync(ctx->xyz.p, xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
+    ctx->metrics.bytes_h2d += (int64_t)bytes;
+    dxyz = static_cast<const double *>(ctx->xyz.p);
+  }
+  const int64_t *dii = ii, *djj = jj;
+  if (!is_device_ptr(ii)) {
+    if ((s = ensure(ctx, ctx->pairs_i, (size_t)np * 8, "pair list"))) return s;
+    CK(cudaMemcpyAsync(ctx->pairs_i.p, ii, (size_t)np * 8, cudaMemcpyHostToDevice, ctx->stream), "copy pair list");
+    dii = static_cast<const int64_t *>(ctx->pairs_i.p);
+  }
+  if (!is_device_ptr(jj)) {
+    if ((s = ensure(ctx, ctx->pairs_j, (size_t)np * 8, "pair list"))) return s;
+    CK(cudaMemcpyAsync(ctx->pairs_j.p, jj, (size_t)np * 8, cudaMemcpyHostToDevice, ctx->stream), "copy pair list");
+    djj = static_cast<const int64_t *>(ctx->pairs_j.p);
+  }
+  // device outputs in place; host outputs staged (rot | trans | rmsd)
+  const bool rot_dev = is_device_ptr(rot), trans_dev = is_device_ptr(trans), rmsd_dev = rmsd && is_device_ptr(rmsd);
+  const size_t stage = (size_t)np * ((rot_dev ? 0 : 9) + (trans_dev ? 0 : 3) + (rmsd && !rmsd_dev ? 1 : 0));
+  if (stage && (s = ensure(ctx, ctx->sp_out, stage * sizeof(double), "superposition results"))) return s;
+  double *sp = static_cast<double *>(ctx->sp_out.p);
+  double *drot = rot_dev ? rot : sp;
+  double *dtrans = trans_dev ? trans : (rot_dev ? sp : sp + (size_t)np * 9);
+  double *drmsd = !rmsd ? nullptr : rmsd_dev ? rmsd : sp + stage - (size_t)np;
+  DevScalars *sc = static_cast<DevScalars *>(ctx->scal.p);
+  CK(cudaMemsetAsync(sc, 0, sizeof(DevScalars), ctx->stream), "clear counters");
+  CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
+  CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
+  CK(launch_superpose(dxyz, n, L, dii, djj, np, drot, dtrans, drmsd, &sc->err, ctx->num_sms, ctx->stream),
+     "superposition");
+  CK(cudaEventRecord(ctx->ev[3], ctx->stream), "event");
+  CK(cudaEventRecord(ctx->ev[4], ctx->stream), "event");
+  if (!rot_dev) CK(cudaMemcpyAsync(rot, drot, (size_t)np * 72, cudaMemcpyDeviceToHost, ctx->stream), "copy rotations");
+  if (!trans_dev)
+    CK(cudaMemcpyAsync(trans, dtrans, (size_t)np * 24, cudaMemcpyDeviceToHost, ctx->stream), "copy translations");
+  if (rmsd && !rmsd_dev)
+    CK(cudaMemcpyAsync(rmsd, drmsd, (size_t)np * 8, cudaMemcpyDeviceToHost, ctx->stream), "copy rmsd");
+  CK(cudaMemcpyAsync(ctx->sc_back, sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream), "read counters");
+  CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
+  CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  if (ctx->sc_back->err & kErrBounds) return set_err(ctx, BS_ERR_INVALID_ARG, "a pair index is out of range");
+  if (ctx->sc_back->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
+  ctx->metrics.pairs = np;
+  ctx->metrics.main_launches = 1;
+  ctx->metrics.ms_h2d = elapsed(ctx, 0, 1);
+  ctx->metrics.ms_main = elapsed(ctx, 2, 3);
+  ctx->metrics.ms_d2h = elapsed(ctx, 4, 5);
+  ctx->metrics.ms_total = elapsed(ctx, 0, 5);
+  return BS_OK;
+}
+
+}  // namespace
+
+BS_API bs_status bs_superpose_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
+                                    const int64_t *jj, int64_t npairs, double *rot, double *trans, double *rmsd) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (n < 1 || L < 1 || npairs < 0) return set_err(ctx, BS_ERR_INVALID_ARG, "n >= 1, L >= 1, npairs >= 0 required");
+  if (npairs == 0) return BS_OK;
+  if (!xyz || !ii || !jj || !rot || !trans) return set_err(ctx, BS_ERR_INVALID_ARG, "null pointer argument");
+  if (!is_device_ptr(ii) && !is_device_ptr(jj)) {
+    for (int64_t t = 0; t < npairs; ++t)
+      if (ii[t] < 0 || ii[t] >= n || jj[t] < 0 || jj[t] >= n)
+        return set_err(ctx, BS_ERR_INVALID_ARG, "pair %lld = (%lld, %lld) out of range [0, %lld)", (long long)t,
+                       (long long)ii[t], (long long)jj[t], (long long)n);
+  }
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  return superpose_impl(ctx, xyz, n, L, ii, jj, npairs, rot, trans, rmsd);
+}
+
+BS_API bs_status bs_superpose(bs_ctx *ctx, const double *a, const double *b, int32_t L, double *rot, double *trans,
+                              double *rmsd) {
+  if (!ctx) return BS_ERR_INVALID_ARG;
+  if (!a || !b || !rot || !trans || L < 1) return set_err(ctx, BS_ERR_INVALID_ARG, "null pointer or L < 1");
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
+  const size_t one = (size_t)L * 3 * sizeof(double);
+  bs_status s = ensure(ctx, ctx->xyz, 2 * one, "coordinates");
+  if (s) return s;
+  double *d = static_cast<double *>(ctx->xyz.p);
+  CK(cudaMemcpyAsync(d, a, one, cudaMemcpyDefault, ctx->stream), "copy a");
+  CK(cudaMemcpyAsync(d + (size_t)L * 3, b, one, cudaMemcpyDefault, ctx->stream), "copy b");
+  const int64_t ii = 0, jj = 1;
+  return superpose_impl(ctx, d, 2, L, &ii, &jj, 1, rot, trans, rmsd);
+}
+
 BS_API bs_status bs_crmsd(bs_ctx *ctx, const double *a, const double *b, int32_t L, double *out_rmsd) {
   if (!ctx) return BS_ERR_INVALID_ARG;
   if (!a || !b || !out_rmsd || L < 1) return set_err(ctx, BS_ERR_INVALID_ARG, "null pointer or L < 1");
@@ -1157,6 +1254,35 @@ BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t
       for (int y = 0; y < 3; ++y) mh[3 * x + y] += ax * (long long)nb[y * L + k];
     }
   *rmsd = bsm::pair_rmsd_exact(mh, ga, gb, scale_exp, L);
+  return BS_OK;
+}
+
+BS_API bs_status bs_selftest_superpose(const double *a, const double *b, int32_t L, double *rot, double *trans,
+                                       double *rmsd) {
+  if (!a || !b || !rot || !trans || L < 1) return BS_ERR_INVALID_ARG;
+  double c[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < L; ++k)
+    for (int x = 0; x < 3; ++x) {
+      c[x] += a[3 * k + x];
+      c[3 + x] += b[3 * k + x];
+    }
+  for (int x = 0; x < 6; ++x) c[x] /= (double)L;
+  double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < L; ++k)
+    for (int x = 0; x < 3; ++x)
+      for (int y = 0; y < 3; ++y) m[3 * x + y] += (a[3 * k + x] - c[x]) * (b[3 * k + y] - c[3 + y]);
+  bsm::rotation_from_cov(m, rot);
+  for (int x = 0; x < 3; ++x) trans[x] = c[x] - (rot[3 * x] * c[3] + rot[3 * x + 1] * c[4] + rot[3 * x + 2] * c[5]);
+  if (rmsd) {
+    double ss = 0.0;
+    for (int k = 0; k < L; ++k)
+      for (int x = 0; x < 3; ++x) {
+        const double d = rot[3 * x] * b[3 * k] + rot[3 * x + 1] * b[3 * k + 1] + rot[3 * x + 2] * b[3 * k + 2] +
+                         trans[x] - a[3 * k + x];
+        ss += d * d;
+      }
+    *rmsd = sqrt(ss / (double)L);
+  }
   return BS_OK;
 }
 

@@ -849,4 +849,78 @@ BS_HD void split_digits(int n, int &e0, int &e1, int &e2) {
 // The quantised coordinate back from its stored digits.
 BS_HD int join_digits(int e0, int e1, int e2) { return e0 * 16384 + e1 * 32 + (e2 >> 4); }
 
+// ------------------------------------------------------- superposition
+// The eigenpair of the largest eigenvalue of a symmetric 4x4 matrix k
+// (row-major) by the cyclic Jacobi method (Golub & Van Loan, Matrix
+// Computations, sec. 8.5): sweeps of plane rotations, each zeroing one
+// off-diagonal entry, until the off-diagonal mass is below 1e-30 of the
+// whole (at most 24 sweeps).  Unlike an adjugate column it stays well defined
+// when the top eigenvalue is (nearly) repeated, where any unit vector of its
+// eigenspace is returned.  q is a unit vector.
+BS_HD double sym4_top_eig(const double k[16], double q[4]) {
+  double a[4][4], v[4][4];
+  double total = 0.0;
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      a[r][c] = k[4 * r + c];
+      v[r][c] = r == c ? 1.0 : 0.0;
+      total += a[r][c] * a[r][c];
+    }
+  for (int sweep = 0; sweep < 24; ++sweep) {
+    double off = 0.0;
+    for (int r = 0; r < 4; ++r)
+      for (int c = r + 1; c < 4; ++c) off += a[r][c] * a[r][c];
+    if (!(off > 1e-30 * total)) break;
+    for (int p = 0; p < 3; ++p)
+      for (int r = p + 1; r < 4; ++r) {
+        const double apr = a[p][r];
+        if (apr == 0.0) continue;
+        // rotation J (c at (p,p), (r,r); s at (p,r); -s at (r,p)) with
+        // (J^T A J)_pr = 0: t = tan = sgn(th) / (|th| + sqrt(th^2 + 1))
+        const double th = (a[r][r] - a[p][p]) / (2.0 * apr);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int i = 0; i < 4; ++i) {  // A J
+          const double x = a[i][p], y = a[i][r];
+          a[i][p] = c * x - s * y;
+          a[i][r] = s * x + c * y;
+        }
+        for (int i = 0; i < 4; ++i) {  // J^T (A J)
+          const double x = a[p][i], y = a[r][i];
+          a[p][i] = c * x - s * y;
+          a[r][i] = s * x + c * y;
+        }
+        for (int i = 0; i < 4; ++i) {  // V J
+          const double x = v[i][p], y = v[i][r];
+          v[i][p] = c * x - s * y;
+          v[i][r] = s * x + c * y;
+        }
+      }
+  }
+  int best = 0;
+  for (int i = 1; i < 4; ++i)
+    if (a[i][i] > a[best][best]) best = i;
+  double nn = 0.0;
+  for (int i = 0; i < 4; ++i) nn += v[i][best] * v[i][best];
+  const double inv = 1.0 / sqrt(nn);
+  for (int i = 0; i < 4; ++i) q[i] = v[i][best] * inv;
+  return a[best][best];
+}
+
+// The proper rotation R (row-major) that best superposes b onto a, from the
+// covariance of the centred structures m_xy = sum_k (a_k - ca)_x (b_k - cb)_y:
+// R maximises sum_xy R_xy m_xy = sum_k (a_k - ca) . R (b_k - cb); it is T(q)
+// of the unit top eigenvector q of the QCP key matrix of m.
+BS_HD void rotation_from_cov(const double m[9], double rot[9]) {
+  const double sxx = m[0], sxy = m[1], sxz = m[2], syx = m[3], syy = m[4], syz = m[5], szx = m[6], szy = m[7],
+               szz = m[8];
+  const double k[16] = {sxx + syy + szz, syz - szy,       szx - sxz,        sxy - syx,
+                        syz - szy,       sxx - syy - szz, sxy + syx,        szx + sxz,
+                        szx - sxz,       sxy + syx,       -sxx + syy - szz, syz + szy,
+                        sxy - syx,       szx + sxz,       syz + szy,        -sxx - syy + szz};
+  double q[4];
+  sym4_top_eig(k, q);
+  t_of_q<double>(q, rot);
+}
+
 }  // namespace bsm

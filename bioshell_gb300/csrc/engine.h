@@ -123,6 +123,8 @@ struct bs_ctx {
   int64_t nbr_n = -1, nbr_nnz = 0;
   // hierarchical clustering on the device: workspace, staged triangle, results
   bs::DevBuf hier_ws, hier_tri, hier_out;
+  // superposition results staged for host outputs: rot, trans, rmsd per pair
+  bs::DevBuf sp_out;
   unsigned long long nbr_cap_hint = 0;
   void *job_stage = nullptr;  // pinned host copy of the job table
   size_t job_stage_cap = 0;

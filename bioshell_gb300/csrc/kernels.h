@@ -221,6 +221,12 @@ cudaError_t mixed_tc_prepare();
 // records {query block, first library block, job, nk16 | count << 16} (chains
 // of at most screen_strip_max_nk16() 16-atom steps); else screen tiles.
 cudaError_t launch_screen_tc(const CUtensorMap *tm, const TcArgs &a, bool strips, cudaStream_t st);
+// superpose.cu -- for each pair (pi[p], pj[p]) of xyz[n][L][3]: rot[p] (3x3
+// row-major), trans[p] with rot x_j + trans ~ x_i, and the RMSD of that
+// superposition (rmsd may be null); bad indices set kErrBounds, non-finite
+// input kErrNonFinite in *err.
+cudaError_t launch_superpose(const double *xyz, int64_t n, int L, const int64_t *pi, const int64_t *pj, int64_t np,
+                             double *rot, double *trans, double *rmsd, int *err, int num_sms, cudaStream_t st);
 cudaError_t screen_tc_prepare();
 int screen_strip_max_nk16();
 

@@ -90,6 +90,9 @@ SIGNATURES = [
     ("bs_ctx_trim", ctypes.c_int32, [_vp]),
     ("bs_ctx_stream", ctypes.c_void_p, [_vp]),
     ("bs_crmsd", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _dp]),
+    ("bs_superpose", ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp]),
+    ("bs_superpose_pairs", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp,
+                                            _vp, _vp]),
     ("bs_all_vs_all", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(bs_opts), _vp]),
     ("bs_tune_get", ctypes.c_int32, [_vp, ctypes.c_int32, ctypes.c_int64, _i32p]),
     ("bs_tune_set", ctypes.c_int32, [_vp, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32]),
@@ -135,6 +138,7 @@ SIGNATURES = [
                                               ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, _dp,
                                               _i32p]),
     ("bs_selftest_exact", ctypes.c_int32, [_i32p, _i32p, ctypes.c_int32, ctypes.c_int32, _dp]),
+    ("bs_selftest_superpose", ctypes.c_int32, [_vp, _vp, ctypes.c_int32, _vp, _vp, _vp]),
     ("bs_selftest_screen", ctypes.c_int32, [_fp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                             ctypes.c_int32, _fp, _fp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),

@@ -168,6 +168,25 @@ BS_API void *bs_ctx_stream(const bs_ctx *ctx);
  * (new bioshell_pdb::calc::crmsd; runs on the GPU as a batch of one). */
 BS_API bs_status bs_crmsd(bs_ctx *ctx, const double *a, const double *b, int32_t L, double *out_rmsd);
 
+/* ---- superposition ---------------------------------------------------- */
+/* The optimal superposition of b onto a as a rototranslation: the proper
+ * rotation rot[9] (3x3, row-major) and translation trans[3] with
+ * rot * b_k + trans ~ a_k in the least-squares sense -- the rotation and
+ * translation a bioshell_pdb::calc::Rototranslation carries
+ * (transformation.rs:22-37; applied as R v + t by apply_mut, :171-174).
+ * rmsd (may be NULL) receives the RMSD of that superposition, which is the
+ * crmsd of the pair.  FP64 on the raw coordinates (QCP key matrix, Jacobi
+ * eigenvector); pointers may be host or device memory. */
+BS_API bs_status bs_superpose(bs_ctx *ctx, const double *a, const double *b, int32_t L, double *rot,
+                              double *trans, double *rmsd);
+
+/* The same for an explicit pair list of xyz[n][L][3]: pair t superposes
+ * structure jj[t] onto structure ii[t]; rot[t][9], trans[t][3], rmsd[t]
+ * (rmsd may be NULL).  Out-of-range indices return BS_ERR_INVALID_ARG,
+ * non-finite coordinates BS_ERR_NONFINITE. */
+BS_API bs_status bs_superpose_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
+                                    const int64_t *jj, int64_t npairs, double *rot, double *trans, double *rmsd);
+
 /* All-vs-all crmsd of n structures xyz[n][L][3] into `out` (layout and
  * element type from `opts`, NULL = defaults: mixed precision, packed f64
  * triangle).  Replaces the n(n-1)/2 distance-closure calls of
@@ -435,6 +454,10 @@ BS_API bs_status bs_selftest_screen(const float *m9, double gsum, double de, dou
 /* The exact recomputation from integer coordinates n_a[3][L], n_b[3][L]. */
 BS_API bs_status bs_selftest_exact(const int32_t *na, const int32_t *nb, int32_t L, int32_t scale_exp,
                                    double *rmsd);
+/* The superposition math of bs_superpose on the host (sequential sums):
+ * rot[9], trans[3] with rot b_k + trans ~ a_k, and its RMSD. */
+BS_API bs_status bs_selftest_superpose(const double *a, const double *b, int32_t L, double *rot, double *trans,
+                                       double *rmsd);
 
 /* GPU diagnostics of the mixed path.  bs_debug_tile_levels returns the raw
  * tensor-core level sums of the first two tiles (structures 0..39 against

@@ -132,6 +132,24 @@ def kabsch_pairs(xyz: np.ndarray, ii: np.ndarray, jj: np.ndarray) -> np.ndarray:
     return np.sqrt(np.maximum(e, 0.0))
 
 
+def kabsch_superpose(a: np.ndarray, b: np.ndarray):
+    """Optimal proper superposition of b onto a by SVD-Kabsch, as the
+    (rotation, translation) pair a Rototranslation carries
+    (bioshell-pdb/src/calc/transformation.rs:22-37; applied as R v + t by
+    apply_mut, :171-174): R (3x3) and t with R b_k + t ~ a_k.  Returns
+    (R, t, rmsd of that superposition)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    ca, cb = a.mean(axis=0), b.mean(axis=0)
+    h = (b - cb).T @ (a - ca)  # sum_k (b_k - cb)(a_k - ca)^T
+    u, _, vt = np.linalg.svd(h)
+    d = 1.0 if np.linalg.det(vt.T @ u.T) >= 0 else -1.0
+    r = vt.T @ np.diag([1.0, 1.0, d]) @ u.T
+    t = ca - r @ cb
+    res = b @ r.T + t - a
+    return r, t, float(np.sqrt((res * res).sum() / a.shape[0]))
+
+
 def tri_index(n: int, i, j):
     """Index of pair (i, j), i < j, in the packed row-major upper triangle."""
     i = np.asarray(i, dtype=np.int64)
