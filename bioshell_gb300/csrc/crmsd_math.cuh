@@ -858,9 +858,13 @@ BS_HD int join_digits(int e0, int e1, int e2) { return e0 * 16384 + e1 * 32 + (e
 // when the top eigenvalue is (nearly) repeated, where any unit vector of its
 // eigenspace is returned.  q is a unit vector.
 BS_HD double sym4_top_eig(const double k[16], double q[4]) {
+  // (every index below is a compile-time constant once unrolled, so the
+  // matrices stay in registers)
   double a[4][4], v[4][4];
   double total = 0.0;
+#pragma unroll
   for (int r = 0; r < 4; ++r)
+#pragma unroll
     for (int c = 0; c < 4; ++c) {
       a[r][c] = k[4 * r + c];
       v[r][c] = r == c ? 1.0 : 0.0;
@@ -868,10 +872,14 @@ BS_HD double sym4_top_eig(const double k[16], double q[4]) {
     }
   for (int sweep = 0; sweep < 24; ++sweep) {
     double off = 0.0;
+#pragma unroll
     for (int r = 0; r < 4; ++r)
+#pragma unroll
       for (int c = r + 1; c < 4; ++c) off += a[r][c] * a[r][c];
     if (!(off > 1e-30 * total)) break;
+#pragma unroll
     for (int p = 0; p < 3; ++p)
+#pragma unroll
       for (int r = p + 1; r < 4; ++r) {
         const double apr = a[p][r];
         if (apr == 0.0) continue;
@@ -880,16 +888,19 @@ BS_HD double sym4_top_eig(const double k[16], double q[4]) {
         const double th = (a[r][r] - a[p][p]) / (2.0 * apr);
         const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
         const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+#pragma unroll
         for (int i = 0; i < 4; ++i) {  // A J
           const double x = a[i][p], y = a[i][r];
           a[i][p] = c * x - s * y;
           a[i][r] = s * x + c * y;
         }
+#pragma unroll
         for (int i = 0; i < 4; ++i) {  // J^T (A J)
           const double x = a[p][i], y = a[r][i];
           a[p][i] = c * x - s * y;
           a[r][i] = s * x + c * y;
         }
+#pragma unroll
         for (int i = 0; i < 4; ++i) {  // V J
           const double x = v[i][p], y = v[i][r];
           v[i][p] = c * x - s * y;
@@ -897,14 +908,20 @@ BS_HD double sym4_top_eig(const double k[16], double q[4]) {
         }
       }
   }
-  int best = 0;
-  for (int i = 1; i < 4; ++i)
-    if (a[i][i] > a[best][best]) best = i;
-  double nn = 0.0;
-  for (int i = 0; i < 4; ++i) nn += v[i][best] * v[i][best];
-  const double inv = 1.0 / sqrt(nn);
-  for (int i = 0; i < 4; ++i) q[i] = v[i][best] * inv;
-  return a[best][best];
+  double top = a[0][0];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] = v[i][0];
+#pragma unroll
+  for (int c = 1; c < 4; ++c)
+    if (a[c][c] > top) {
+      top = a[c][c];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) q[i] = v[i][c];
+    }
+  const double inv = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] *= inv;
+  return top;
 }
 
 // The proper rotation R (row-major) that best superposes b onto a, from the
