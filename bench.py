@@ -67,6 +67,7 @@ def args_():
     p.add_argument("--skip-serving", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-inflight", type=int, default=4, help="device slots of the serving benchmark")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--probe-serving", type=int, default=0, metavar="K",
                    help="only run K query batches of 256 structures of the 64-atom bucket through a one-slot "
@@ -449,7 +450,7 @@ def run_serving(a):
         n = int(rng.integers(500, 5001))
         cjobs.append(synth.decoys(bases[L][k], n, rng, (0.3, 4.0)))
     t0 = time.perf_counter()
-    srv = CrmsdServer(lib, top_k=50, max_inflight=4)
+    srv = CrmsdServer(lib, top_k=50, max_inflight=a.serve_inflight)
     build_s = time.perf_counter() - t0
     for L in pools:  # warm-up: first batches of every bucket, both extremes of q
         for n in (1, 512):
@@ -506,7 +507,8 @@ def run_serving(a):
                  "pairs_per_s": st["pairs_per_s"], "wall_s": st["seconds"], "batches": int(st["batches"]),
                  "mean_batch_rows": st["mean_batch_rows"], "plain_fallbacks": int(st["plain_fallbacks"]),
                  "cluster_p50_ms": st["cluster_p50_ms"], "cluster_p99_ms": st["cluster_p99_ms"],
-                 "submit_lag_p99_ms": float(np.percentile(lag, 99)) if lag else None, "submit_s": submit_s}
+                 "submit_lag_p99_ms": float(np.percentile(lag, 99)) if lag else None, "submit_s": submit_s,
+                 "pairs_screened_per_pair": st["pairs_screened"] / max(st["pairs"], 1)}
     cap = _closed_loop(srv, pools, shares, 2.0, rng)
     srv.close()
     # the plain FP64 server on the same library and GPU (closed loop)
@@ -517,7 +519,7 @@ def run_serving(a):
     return {"library": {"structures": int(sum(x.shape[0] for x in lib.values())),
                         "atoms": int(sum(x.shape[0] * x.shape[1] for x in lib.values())),
                         "buckets": {str(L): int(lib[L].shape[0]) for L in lib}, "build_s": build_s},
-            "top_k": 50, "open_loop": open_loop,
+            "top_k": 50, "max_inflight": a.serve_inflight, "open_loop": open_loop,
             "capacity": {"pairs_per_s": cap["pairs_per_s"], "p50_ms": cap["p50_ms"], "p99_ms": cap["p99_ms"],
                          "queries": int(cap["queries_done"])},
             "plain64_capacity": {"pairs_per_s": pcap["pairs_per_s"], "p50_ms": pcap["p50_ms"],

@@ -268,15 +268,16 @@ cudaError_t launch_mixed_pairs(const DigitsView &dg, const SInfo *info, const Jo
                                cudaStream_t st);
 
 // topk.cu -- per row of a dense [rows][ld] f32 block: the k <= kTopkMax
-// smallest of the first n values, ascending by (value, column); columns
-// that do not exist come back as -1.
+// smallest of the first n values, ascending by (value, library index), the
+// library index of column c being perm[c] (perm may be null: c); results
+// report library indices, and entries that do not exist come back as -1.
 constexpr int kTopkMax = 64;
-cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, int64_t *out_idx,
-                        float *out_val, cudaStream_t st);
+cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, const int *perm,
+                        int64_t *out_idx, float *out_val, cudaStream_t st);
 // The same with a per-row count of valid values (row_n[r] <= n) and a map
-// from column to reported index (col_map[r * ld + c]; may be null).
+// from position to column (col_map[r * ld + c]; may be null).
 cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, int64_t ld, int k,
-                             const int *col_map, int64_t *out_idx, float *out_val, cudaStream_t st);
+                             const int *col_map, const int *perm, int64_t *out_idx, float *out_val, cudaStream_t st);
 // Screen candidates from the packed brackets of a screen job (one word per
 // pair: hi rounded up to half precision in the top 16 bits, lo rounded down
 // in the bottom 16).  Per row r: T[r] = an upper bound of the row's k-th

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -51,6 +52,29 @@ struct HostBuf {
   size_t cap = 0;
 };
 
+// The library index of a large bucket.  Every structure is joined to its
+// nearest representative (exact crmsd at build time) and the bucket is
+// stored in cluster order -- clusters contiguous, each sorted by distance
+// to its representative -- so a library block of 20 holds one or two
+// clusters.  The heads of the clusters (each representative and the members
+// nearest to it) form a small set that a batch screens first: the k-th
+// smallest upper bracket over the heads, T(q), bounds q's k-th nearest from
+// above, and with d(x) an upper bound of crmsd(rep(x), x),
+//   crmsd(q, x) >= crmsd(q, rep(x)) - d(x)     (triangle inequality),
+// so a block whose members all have lo(q, rep) - d > T(q) + 2 tol holds
+// none of q's top k, even after the certified per-pair error tol of the
+// values that rank them.
+struct Index {
+  int nrep = 0;                // representatives (= clusters)
+  int nhead = 0;               // head structures (every cluster's first members)
+  DevBuf dig[4], info, tinfo;  // the heads' digit rows and data, on the bucket's grid
+  int64_t rows = 0;            // digit rows of the head set
+  DevBuf rep_slot;             // per cluster: its representative's slot in the head set (int32)
+  DevBuf perm;                 // bucket position -> library index (int32)
+  std::vector<int> c0, c1;     // per library block: first / last cluster (c0 -1: more than two)
+  std::vector<float> d0, d1;   // per block: largest member bound d within c0 / c1
+};
+
 struct Bucket {
   int L = 0, lp = 0, pitch = 0;
   int64_t n = 0, rows = 0;
@@ -60,7 +84,12 @@ struct Bucket {
   DevBuf dig[4], info;  // mixed path
   DevBuf tinfo;         // screen: truncated-structure data per structure
   DevBuf y, g;          // plain path: centred f64 [n][3][lp], squared norms
+  bool indexed = false;
+  Index ix;
 };
+
+// Library index of bucket position c (null: positions are library indices).
+const int *bk_perm(const Bucket &bk) { return bk.indexed ? static_cast<const int *>(bk.ix.perm.p) : nullptr; }
 
 struct Request {
   int64_t id = 0;
@@ -92,11 +121,12 @@ struct Slot {
   int64_t rows = 0;           // query structures in the batch
   int njobs = 0;
   bool screen = false;        // the batch ran the two-stage (screen + exact) top-k
+  std::vector<int64_t> row_of;  // indexed screens: result row of query t of request j at row0[j] + t
   // device
   DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
-  DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab;
+  DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab, pre, prerep;
   // pinned host
-  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n;
+  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n, hpre;
 };
 
 }  // namespace
@@ -125,6 +155,7 @@ struct bs_server {
   // stats
   std::vector<double> lat, clat;
   int64_t qdone = 0, cdone = 0, pairs = 0, batches = 0, fallbacks = 0, rows_batched = 0;
+  std::atomic<int64_t> screened{0};  // updated by launches that run without the lock
   bs::Clock::time_point t0;
 };
 
@@ -180,7 +211,7 @@ void slot_release(bs_server *s, Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
                     &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep};
   for (DevBuf *b : list) sv_release(s, *b);
 }
 
@@ -188,7 +219,7 @@ size_t slot_bytes(Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
                     &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab};
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep};
   size_t t = 0;
   for (DevBuf *b : list) t += b->cap;
   return t;
@@ -314,9 +345,210 @@ bs_status build_bucket(bs_server *s, Bucket &bk, const double *xyz_in) {
 }
 
 // ------------------------------------------------------------ batches
+// Half-precision bits -> float (the packed screen brackets).
+float half_bits_to_float(uint32_t h) {
+  const uint32_t sgn = (h >> 15) & 1u, e = (h >> 10) & 31u, m = h & 1023u;
+  float v;
+  if (e == 0) v = ldexpf((float)m, -24);
+  else if (e == 31) v = m ? NAN : INFINITY;
+  else v = ldexpf((float)(m | 1024u), (int)e - 25);
+  return sgn ? -v : v;
+}
+
+// Tiles of one query batch: query blocks x library column blocks, column
+// block by column block (strips for chains the strip kernel takes).  need
+// (optional) lists the library blocks each query block has to see.
+void batch_tiles(const bs_server *s, const Plan &plan_in, int64_t blk, int64_t nbb, int nk16, bool strips,
+                 const std::vector<std::vector<int64_t>> *need, std::vector<Tile> &tiles) {
+  tiles.clear();
+  if (strips) {
+    const int64_t total = blk * nbb;
+    const int64_t run =
+        std::max<int64_t>(8, std::min<int64_t>(4096, (total + 12 * s->num_sms - 1) / (12 * s->num_sms)));
+    if (!need) {
+      for (int64_t J = 0; J < nbb; J += run)
+        for (int64_t I = 0; I < blk; ++I) {
+          const int64_t cnt = std::min(run, nbb - J);
+          tiles.push_back(Tile{(int)I, (int)J, plan_in.jobmap[I], nk16 | (int)(cnt << 16)});
+        }
+      return;
+    }
+    // runs of consecutive needed blocks, at most `run` long
+    const int64_t prun = std::max<int64_t>(8, std::min<int64_t>(run, 64));
+    for (int64_t I = 0; I < blk; ++I) {
+      const std::vector<int64_t> &v = (*need)[I];
+      for (size_t a = 0; a < v.size();) {
+        size_t e = a + 1;
+        while (e < v.size() && v[e] == v[e - 1] + 1 && (int64_t)(e - a) < prun) ++e;
+        tiles.push_back(Tile{(int)I, (int)v[a], plan_in.jobmap[I], nk16 | (int)((int64_t)(e - a) << 16)});
+        a = e;
+      }
+    }
+    return;
+  }
+  if (!need) {
+    tiles.reserve((size_t)(blk * nbb));
+    for (int64_t J = 0; J < nbb; ++J)
+      for (int64_t I = 0; I < blk; ++I) tiles.push_back(Tile{(int)I, (int)J, plan_in.jobmap[I], 0});
+    return;
+  }
+  for (int64_t I = 0; I < blk; ++I)
+    for (int64_t J : (*need)[I]) tiles.push_back(Tile{(int)I, (int)J, plan_in.jobmap[I], 0});
+}
+
+// Per row r of a [rows][ld] block of packed brackets: the words at the
+// representatives' slots, into out[r][c].
+__global__ void k_gather_cols(const uint32_t *__restrict__ pre, int64_t ld, const int *__restrict__ slot, int R,
+                              int64_t rows, uint32_t *__restrict__ out) {
+  const int64_t r = blockIdx.y;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < R; c += gridDim.x * blockDim.x)
+    out[r * R + c] = pre[r * ld + slot[c]];
+}
+
+// Indexed screens, phase 1: the batch's queries (request order) against the
+// bucket's head set on the tensor cores; the k-th smallest upper bracket of
+// each row (the screen selection's threshold) and the brackets against the
+// representatives are read back.  On the host each request's queries are
+// ordered by nearest representative (so a query block holds similar
+// queries) and each query block gets the library blocks it cannot rule out.
+// Returns false when the index cannot be used for this batch (a job reported
+// an error): the batch then runs unpruned.
+bool index_prescreen(bs_server *s, Slot &sl, const Plan &base, int64_t blk, int64_t rows, const double *dx,
+                     const std::vector<size_t> &xoff, std::vector<std::vector<int>> &order,
+                     std::vector<std::vector<int64_t>> &need) {
+  const Bucket &bk = s->buckets[sl.bucket];
+  const Index &ix = bk.ix;
+  const int nj = (int)base.jobs.size(), R = ix.nrep, H = ix.nhead, nk16 = bk.lp / 16, k = s->top_k;
+  const int64_t ldh = (H + 3) & ~3, nbh = (H + kBStructs - 1) / kBStructs;
+  Plan p1 = base;
+  p1.strips = nk16 <= screen_strip_max_nk16();
+  batch_tiles(s, p1, blk, nbh, nk16, p1.strips, nullptr, p1.tiles);
+  if (!sv_ensure(s, sl.pre, (size_t)rows * ldh * 4) || !sv_ensure(s, sl.prerep, (size_t)rows * (R + 1) * 4) ||
+      !host_ensure(sl.hpre, (size_t)rows * (R + 1) * 4) || !sv_ensure(s, sl.tiles, p1.tiles.size() * sizeof(Tile)) ||
+      !host_ensure(sl.htab, p1.jobmap.size() * 4 + p1.tiles.size() * sizeof(Tile)))
+    return false;
+  uint32_t *pre = static_cast<uint32_t *>(sl.pre.p);
+  for (int j = 0; j < nj; ++j) {
+    p1.jobs[j].xyz = dx + xoff[j];
+    p1.jobs[j].n_b = H;
+    p1.jobs[j].out = OutDesc{pre + sl.row0[j] * ldh, p1.jobs[j].n, ldh, kLayoutRect, 1};
+  }
+  memcpy(sl.hjobs.p, p1.jobs.data(), (size_t)nj * sizeof(Job));
+  char *ht = static_cast<char *>(sl.htab.p);
+  memcpy(ht, p1.jobmap.data(), p1.jobmap.size() * 4);
+  memcpy(ht + p1.jobmap.size() * 4, p1.tiles.data(), p1.tiles.size() * sizeof(Tile));
+  MixedBuffers b{};
+  b.ctr = static_cast<long long *>(sl.ctr.p);
+  b.info_a = static_cast<SInfo *>(sl.info.p);
+  b.info_b = static_cast<const SInfo *>(ix.info.p);
+  b.tinfo_a = static_cast<float2 *>(sl.tinfo.p);
+  b.tinfo_b = static_cast<const float2 *>(ix.tinfo.p);
+  for (int d = 0; d < 4; ++d) b.dig_a[d] = static_cast<__nv_bfloat16 *>(sl.dig[d].p);
+  for (int d = 0; d < 3; ++d) b.dig_b[d] = static_cast<const __nv_bfloat16 *>(ix.dig[d].p);
+  b.pitch_a = b.pitch_b = bk.pitch;
+  b.rows_a = blk * kBlockRows;
+  b.rows_b = ix.rows;
+  b.jobs = static_cast<Job *>(sl.jobs.p);
+  b.jobmap = static_cast<int *>(sl.jobmap.p);
+  b.tiles = static_cast<Tile *>(sl.tiles.p);
+  b.flags = static_cast<unsigned long long *>(sl.flags.p);
+  b.flag_cap = kServerFlagCap;
+  b.sc = static_cast<DevScalars *>(sl.scal.p);
+  CUtensorMap tm[7];
+  if (!encode_maps(s->encode, b, tm).empty()) return false;
+  uint32_t *prerep = static_cast<uint32_t *>(sl.prerep.p);
+  uint32_t *thr = static_cast<uint32_t *>(sl.thr.p);
+  if (cudaMemcpyAsync(b.jobmap, ht, p1.jobmap.size() * 4, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(b.tiles, ht + p1.jobmap.size() * 4, p1.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice,
+                      sl.st) != cudaSuccess ||
+      enqueue_mixed(p1, b, static_cast<const Job *>(sl.hjobs.p), tm, s->num_sms, sl.st, nullptr, false) !=
+          cudaSuccess ||
+      launch_screen_select(pre, rows, H, ldh, k, kCandCap, static_cast<uint32_t *>(sl.hist.p), thr,
+                           static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) != cudaSuccess)
+    return false;
+  k_gather_cols<<<dim3((unsigned)((R + 127) / 128), (unsigned)rows), 128, 0, sl.st>>>(
+      pre, ldh, static_cast<const int *>(ix.rep_slot.p), R, rows, prerep);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(sl.hpre.p, prerep, (size_t)rows * R * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(static_cast<uint32_t *>(sl.hpre.p) + (size_t)rows * R, thr, (size_t)rows * 4,
+                      cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hback.p, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hsc.p, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaStreamSynchronize(sl.st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const Job *back = static_cast<const Job *>(sl.hback.p);
+  for (int j = 0; j < nj; ++j) {
+    std::string msg;
+    if (collect_errors(*static_cast<const DevScalars *>(sl.hsc.p), back + j, 1, msg) != BS_OK) return false;
+  }
+  // per row: nearest representative and the bound of its k-th nearest
+  static const std::vector<float> half_table = [] {
+    std::vector<float> t(65536);
+    for (uint32_t h = 0; h < 65536; ++h) t[h] = half_bits_to_float(h);
+    return t;
+  }();
+  const float *ht16 = half_table.data();
+  const uint32_t *hp = static_cast<const uint32_t *>(sl.hpre.p);
+  const uint32_t *hthr = hp + (size_t)rows * R;
+  std::vector<float> lo((size_t)rows * R), test(rows);
+  std::vector<int> nearest(rows);
+  for (int64_t r = 0; r < rows; ++r) {
+    float best = INFINITY;
+    int arg = 0;
+    for (int c = 0; c < R; ++c) {
+      const float l = ht16[hp[r * R + c] & 0xffffu];
+      lo[(size_t)r * R + c] = l;
+      if (l < best) best = l, arg = c;
+    }
+    // the threshold is the top edge of the bin of the k-th smallest upper
+    // bracket over the heads (0xffff: fewer than k): T >= the k-th nearest
+    const float t = hthr[r] >= 0xffffu ? INFINITY : ht16[hthr[r] & 0xffffu];
+    test[r] = t + 2.f * s->tol * 1.001f;
+    nearest[r] = arg;
+  }
+  order.assign(nj, {});
+  for (int j = 0; j < nj; ++j) {
+    const int64_t q = base.jobs[j].n;
+    std::vector<int> &o = order[j];
+    o.resize(q);
+    for (int64_t t = 0; t < q; ++t) o[t] = (int)t;
+    const int64_t r0 = sl.row0[j];
+    std::stable_sort(o.begin(), o.end(), [&](int a, int c) { return nearest[r0 + a] < nearest[r0 + c]; });
+  }
+  // per query block: need_c = min over its queries of lo - T; library block
+  // b is needed unless every cluster in it has largest bound d < need_c
+  const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
+  need.assign(blk, {});
+  std::vector<float> nc(R);
+  for (int j = 0; j < nj; ++j) {
+    const int64_t q = base.jobs[j].n, b0 = base.jobs[j].first_a / kBlockStructs;
+    for (int64_t I = 0; I * kBlockStructs < q; ++I) {
+      std::fill(nc.begin(), nc.end(), INFINITY);
+      for (int64_t u = I * kBlockStructs; u < std::min<int64_t>(q, (I + 1) * kBlockStructs); ++u) {
+        const int64_t r = sl.row0[j] + order[j][u];
+        const float tr = test[r];
+        const float *lr = &lo[(size_t)r * R];
+        for (int c = 0; c < R; ++c) nc[c] = std::min(nc[c], lr[c] - tr);
+      }
+      std::vector<int64_t> &v = need[b0 + I];
+      for (int64_t lb = 0; lb < nbb; ++lb) {
+        const int a0 = ix.c0[lb], a1 = ix.c1[lb];
+        if (a0 < 0 || ix.d0[lb] >= nc[a0] || (a1 >= 0 && ix.d1[lb] >= nc[a1])) v.push_back(lb);
+      }
+    }
+  }
+  return true;
+}
+
 // Enqueues a query batch on the slot.  screen: the two-stage top-k (bounds
 // from the leading levels on the tensor cores, then the certified crmsd of
-// each row's candidates); otherwise every pair is certified densely.
+// each row's candidates); otherwise every pair is certified densely.  On an
+// indexed bucket a screen first runs against the representatives
+// (index_prescreen) and then only on the library blocks that can hold a
+// query's nearest; each request's queries are then processed in the order of
+// their nearest representative and their results mapped back (row_of).
 bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   const Bucket &bk = s->buckets[sl.bucket];
   const int L = bk.L, k = s->top_k;
@@ -353,38 +585,25 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
     blk += nb;
     rows += r->q;
   }
+  const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
+  const int nk16 = bk.lp / 16;
+  plan.strips = screen && s->precision == BS_PRECISION_MIXED && nk16 <= screen_strip_max_nk16();
+  plan.nblocks = blk;
+  sl.rows = rows;
+  sl.njobs = nj;
+  sl.screen = screen && s->precision == BS_PRECISION_MIXED;
+  sl.row_of.clear();
+  const int64_t ns = blk * kBlockStructs, drows = blk * kBlockRows;
+  const bool plain = s->precision == BS_PRECISION_PLAIN64;
+  // screen batches: one packed bracket word per pair, rows padded to 4 words
+  const int64_t ld = sl.screen ? ((bk.n + 3) & ~int64_t(3)) : bk.n;
   // tiles column block by column block: the persistent blocks sweep the
   // library once, each library block read from HBM once and reused from L2
   // by every query block of the batch.  Screens of chains the strip kernel
   // takes run as strips: a query block against a run of library blocks,
   // the query block's digits resident in shared memory for the run; runs
   // sized for about a dozen per block of the grid.
-  {
-    const int64_t nbb = (bk.n + kBStructs - 1) / kBStructs;
-    const int nk16 = bk.lp / 16;
-    plan.strips = screen && s->precision == BS_PRECISION_MIXED && nk16 <= screen_strip_max_nk16();
-    if (plan.strips) {
-      const int64_t total = blk * nbb;
-      const int64_t run = std::max<int64_t>(8, std::min<int64_t>(4096, (total + 12 * s->num_sms - 1) / (12 * s->num_sms)));
-      for (int64_t J = 0; J < nbb; J += run)
-        for (int64_t I = 0; I < blk; ++I) {
-          const int64_t cnt = std::min(run, nbb - J);
-          plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], nk16 | (int)(cnt << 16)});
-        }
-    } else {
-      plan.tiles.reserve((size_t)(blk * nbb));
-      for (int64_t J = 0; J < nbb; ++J)
-        for (int64_t I = 0; I < blk; ++I) plan.tiles.push_back(Tile{(int)I, (int)J, plan.jobmap[I], 0});
-    }
-  }
-  plan.nblocks = blk;
-  sl.rows = rows;
-  sl.njobs = nj;
-  sl.screen = screen && s->precision == BS_PRECISION_MIXED;
-  const int64_t ns = blk * kBlockStructs, drows = blk * kBlockRows;
-  const bool plain = s->precision == BS_PRECISION_PLAIN64;
-  // screen batches: one packed bracket word per pair, rows padded to 4 words
-  const int64_t ld = sl.screen ? ((bk.n + 3) & ~int64_t(3)) : bk.n;
+  batch_tiles(s, plan, blk, nbb, nk16, plan.strips, nullptr, plan.tiles);
   bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * ld * 4) &&
             sv_ensure(s, sl.topi, (size_t)rows * k * 8) && sv_ensure(s, sl.topv, (size_t)rows * k * 4) &&
             sv_ensure(s, sl.scal, sizeof(DevScalars)) && host_ensure(sl.hxyz, xyz_off * 8) &&
@@ -413,6 +632,29 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   for (int j = 0; j < nj; ++j) memcpy(hx + xoff[j], sl.reqs[j]->xyz.data(), sl.reqs[j]->xyz.size() * 8);
   double *dx = static_cast<double *>(sl.xyz.p);
   if (cudaMemcpyAsync(dx, hx, xyz_off * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess) return BS_ERR_CUDA;
+  bool pruned = false;
+  if (sl.screen && bk.indexed) {
+    std::vector<std::vector<int>> order;
+    std::vector<std::vector<int64_t>> need;
+    if (index_prescreen(s, sl, plan, blk, rows, dx, xoff, order, need)) {
+      pruned = true;
+      // each request's queries in the order of their nearest representative
+      sl.row_of.assign(rows, 0);
+      for (int j = 0; j < nj; ++j) {
+        const size_t one = (size_t)L * 3;
+        const double *src = sl.reqs[j]->xyz.data();
+        for (size_t u = 0; u < order[j].size(); ++u) {
+          memcpy(hx + xoff[j] + u * one, src + (size_t)order[j][u] * one, one * 8);
+          sl.row_of[sl.row0[j] + order[j][u]] = sl.row0[j] + (int64_t)u;
+        }
+      }
+      if (cudaMemcpyAsync(dx, hx, xyz_off * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess) return BS_ERR_CUDA;
+      batch_tiles(s, plan, blk, nbb, nk16, plan.strips, &need, plan.tiles);
+      if (!sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) ||
+          !host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16))
+        return BS_ERR_OOM;
+    }
+  }
   float *dense = static_cast<float *>(sl.dense.p);
   if (plain) {
     if (cudaMemsetAsync(sl.scal.p, 0, sizeof(DevScalars), sl.st) != cudaSuccess) return BS_ERR_CUDA;
@@ -428,6 +670,14 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
         return BS_ERR_CUDA;
     }
   } else {
+    // pruned screens: every pair not screened reads as lo = hi = 61,184 A
+    // (half-precision bits 0x7B7B), above every bound that can matter
+    if (pruned && cudaMemsetAsync(dense, 0x7B, (size_t)rows * ld * 4, sl.st) != cudaSuccess) return BS_ERR_CUDA;
+    if (sl.screen) {
+      int64_t t = 0;
+      for (const Tile &tl : plan.tiles) t += plan.strips ? (tl.shape >> 16) : 1;
+      s->screened += t * kBlockStructs * kBStructs;
+    }
     for (int j = 0; j < nj; ++j) plan.jobs[j].xyz = dx + xoff[j];
     for (int j = 0; j < nj; ++j) plan.jobs[j].out = OutDesc{dense + sl.row0[j] * ld, sl.reqs[j]->q, ld, kLayoutRect, 1};
     memcpy(sl.hjobs.p, plan.jobs.data(), (size_t)nj * sizeof(Job));
@@ -488,13 +738,13 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
                                   DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b}, b.info_a, b.info_b, b.jobs,
                                   drjob, drig, rows, cj, cn, kCandCap, static_cast<float *>(sl.cand_v.p),
                                   sl.st) != cudaSuccess ||
-          launch_topk_rows(static_cast<const float *>(sl.cand_v.p), rows, cn, kCandCap, k, cj,
+          launch_topk_rows(static_cast<const float *>(sl.cand_v.p), rows, cn, kCandCap, k, cj, bk_perm(bk),
                            static_cast<int64_t *>(sl.topi.p), static_cast<float *>(sl.topv.p), sl.st) != cudaSuccess ||
           cudaMemcpyAsync(sl.hcand_n.p, cn, (size_t)rows * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess)
         return BS_ERR_CUDA;
     }
   }
-  if ((!sl.screen && launch_topk(dense, rows, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p),
+  if ((!sl.screen && launch_topk(dense, rows, bk.n, bk.n, k, bk_perm(bk), static_cast<int64_t *>(sl.topi.p),
                                  static_cast<float *>(sl.topv.p), sl.st) != cudaSuccess) ||
       cudaMemcpyAsync(sl.htopi.p, sl.topi.p, (size_t)rows * k * 8, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
       cudaMemcpyAsync(sl.htopv.p, sl.topv.p, (size_t)rows * k * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
@@ -523,7 +773,7 @@ bs_status plain_fallback(bs_server *s, Slot &sl, int j) {
       launch_plain64_rect(static_cast<const double *>(sl.y.p), static_cast<const double *>(sl.g.p), r->q,
                           static_cast<const double *>(bk.y.p), static_cast<const double *>(bk.g.p), bk.n, bk.L, bk.lp,
                           od, sl.st) != cudaSuccess ||
-      launch_topk(dense, r->q, bk.n, bk.n, k, static_cast<int64_t *>(sl.topi.p) + sl.row0[j] * k,
+      launch_topk(dense, r->q, bk.n, bk.n, k, bk_perm(bk), static_cast<int64_t *>(sl.topi.p) + sl.row0[j] * k,
                   static_cast<float *>(sl.topv.p) + sl.row0[j] * k, sl.st) != cudaSuccess ||
       cudaMemcpyAsync(static_cast<int64_t *>(sl.htopi.p) + sl.row0[j] * k,
                       static_cast<int64_t *>(sl.topi.p) + sl.row0[j] * k, (size_t)r->q * k * 8, cudaMemcpyDeviceToHost,
@@ -630,6 +880,201 @@ void complete(bs_server *s, Request *r, bs_status st, const std::string &msg) {
   s->cv_done.notify_all();
 }
 
+// ------------------------------------------------------------ index
+constexpr int64_t kIndexPerRep = 512;  // structures per representative
+constexpr int64_t kIndexMinDefault = 16384;  // buckets indexed by default
+constexpr int kIndexMaxReps = 256;
+
+struct DigitPtrs {
+  const __nv_bfloat16 *src[4];
+  __nv_bfloat16 *dst[4];
+};
+
+// Structure r of a set (bucket position pos[r]): its three digit rows of
+// each digit matrix, its SInfo and its screen data, into slot r of a set
+// laid out like a bucket (one block per structure).
+__global__ void k_gather_reps(DigitPtrs d, int pitch, const int64_t *__restrict__ pos, int R,
+                              const SInfo *__restrict__ info_src, SInfo *__restrict__ info_dst,
+                              const float2 *__restrict__ t_src, float2 *__restrict__ t_dst) {
+  const int r = blockIdx.x;
+  if (r >= R) return;
+  const int64_t p = pos[r];
+  for (int c = 0; c < 3; ++c) {
+    const int64_t rs = digit_row(p, c) * pitch, rd = digit_row(r, c) * pitch;
+    for (int m = 0; m < 4; ++m)
+      for (int k = threadIdx.x; k < pitch; k += blockDim.x) d.dst[m][rd + k] = d.src[m][rs + k];
+  }
+  if (threadIdx.x == 0) {
+    info_dst[r] = info_src[p];
+    t_dst[r] = t_src[p];
+  }
+}
+
+void free_bucket(Bucket &bk) {
+  for (DevBuf *d : {&bk.dig[0], &bk.dig[1], &bk.dig[2], &bk.dig[3], &bk.info, &bk.tinfo, &bk.y, &bk.g, &bk.ix.dig[0],
+                    &bk.ix.dig[1], &bk.ix.dig[2], &bk.ix.dig[3], &bk.ix.info, &bk.ix.tinfo, &bk.ix.perm,
+                    &bk.ix.rep_slot}) {
+    if (d->p) cudaFree(d->p);
+    d->p = nullptr;
+    d->cap = 0;
+  }
+}
+
+// Builds the library index of bucket bi (see Index) from its coordinates in
+// library order on the host, and stores the bucket in cluster order.  The
+// representatives are every (n / R)-th structure; their exact crmsd to every
+// structure comes from the dense certified path on slot 0.
+bs_status build_index(bs_server *s, int bi, const double *xyz) {
+  Bucket &bk = s->buckets[bi];
+  const int64_t n = bk.n;
+  const int L = bk.L, k = s->top_k;
+  const int R = (int)std::min<int64_t>(kIndexMaxReps, std::max<int64_t>(2, n / kIndexPerRep));
+  std::vector<int64_t> rep(R);
+  for (int r = 0; r < R; ++r) rep[r] = (int64_t)r * n / R;
+  Slot &sl = *s->slots[0];
+  sl.bucket = bi;
+  sl.kind = 0;
+  std::vector<float> dist((size_t)R * n);
+  const size_t one = (size_t)L * 3;
+  for (int r0 = 0; r0 < R; r0 += 256) {
+    const int cnt = std::min(256, R - r0);
+    Request rq;
+    rq.kind = 0;
+    rq.bucket = bi;
+    rq.L = L;
+    rq.q = cnt;
+    rq.xyz.resize(cnt * one);
+    for (int u = 0; u < cnt; ++u) memcpy(rq.xyz.data() + u * one, xyz + rep[r0 + u] * one, one * 8);
+    sl.reqs.assign(1, &rq);
+    bs_status st = launch_query_batch(s, sl, false);
+    if (st == BS_OK && cudaStreamSynchronize(sl.st) != cudaSuccess) st = BS_ERR_CUDA;
+    std::string msg;
+    if (st == BS_OK)
+      st = collect_errors(*static_cast<const DevScalars *>(sl.hsc.p), static_cast<const Job *>(sl.hback.p), 1, msg);
+    if (st == BS_OK && cudaMemcpy(dist.data() + (size_t)r0 * n, sl.dense.p, (size_t)cnt * n * 4,
+                                  cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = BS_ERR_CUDA;
+    sl.reqs.clear();
+    if (st) {
+      s->err = "library index: " + (msg.empty() ? std::string("device error") : msg);
+      return st;
+    }
+  }
+  // nearest representative and an upper bound of the distance: the values
+  // are certified to tol; the margin covers their f32 rounding
+  std::vector<int> cl(n);
+  std::vector<float> dd(n);
+  for (int64_t x = 0; x < n; ++x) {
+    int best = 0;
+    float v = dist[x];
+    for (int r = 1; r < R; ++r)
+      if (dist[(size_t)r * n + x] < v) v = dist[(size_t)r * n + x], best = r;
+    cl[x] = best;
+    dd[x] = v + s->tol * 1.01f + v * 1e-6f;
+  }
+  std::vector<int64_t> ord(n);
+  for (int64_t x = 0; x < n; ++x) ord[x] = x;
+  std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) {
+    return cl[a] != cl[b] ? cl[a] < cl[b] : (dd[a] != dd[b] ? dd[a] < dd[b] : a < b);
+  });
+  std::vector<int64_t> pos_of(n);
+  for (int64_t u = 0; u < n; ++u) pos_of[ord[u]] = u;
+  // the bucket again, in cluster order
+  std::vector<double> px(n * one);
+  for (int64_t u = 0; u < n; ++u) memcpy(px.data() + u * one, xyz + ord[u] * one, one * 8);
+  free_bucket(bk);
+  bs_status st = build_bucket(s, bk, px.data());
+  if (st) return st;
+  Index &ix = bk.ix;
+  ix = Index{};
+  ix.nrep = R;
+  // cluster c occupies positions [first[c], first[c + 1])
+  std::vector<int64_t> first(R + 1, n);
+  for (int64_t u = n - 1; u >= 0; --u) first[cl[ord[u]]] = u;
+  for (int r = R - 1; r >= 0; --r)
+    if (first[r] == n || first[r] > first[r + 1]) first[r] = first[r + 1];  // empty clusters
+  // per library block: its clusters and their largest bounds
+  const int64_t nbb = (n + kBStructs - 1) / kBStructs;
+  ix.c0.assign(nbb, -1);
+  ix.c1.assign(nbb, -1);
+  ix.d0.assign(nbb, 0.f);
+  ix.d1.assign(nbb, 0.f);
+  for (int64_t b = 0; b < nbb; ++b) {
+    const int64_t u0 = b * kBStructs, u1 = std::min(n, u0 + kBStructs);
+    const int a = cl[ord[u0]], z = cl[ord[u1 - 1]];
+    int distinct = 1;
+    for (int64_t u = u0 + 1; u < u1; ++u) distinct += cl[ord[u]] != cl[ord[u - 1]];
+    if (distinct > 2) continue;  // c0 = -1: always screened
+    ix.c0[b] = a;
+    ix.c1[b] = z != a ? z : -1;
+    for (int64_t u = u0; u < u1; ++u) {
+      const int c = cl[ord[u]];
+      float &m = c == a ? ix.d0[b] : ix.d1[b];
+      m = std::max(m, dd[ord[u]]);
+    }
+  }
+  // the heads: each cluster's representative and its next k + 10 members
+  // (a representative is its own cluster's nearest member, so it comes
+  // first unless an identical structure ties with it)
+  std::vector<int64_t> hpos;
+  std::vector<int> rep_slot(R, -1);
+  for (int r = 0; r < R; ++r) {
+    const int64_t rp = pos_of[rep[r]];
+    if (cl[rep[r]] == r) {
+      rep_slot[r] = (int)hpos.size();
+      hpos.push_back(rp);
+    }
+    const int64_t m = std::min<int64_t>(first[r + 1] - first[r], (int64_t)k + 10);
+    for (int64_t u = first[r]; u < first[r] + m; ++u)
+      if (u != rp) hpos.push_back(u);
+  }
+  for (int r = 0; r < R; ++r)
+    if (rep_slot[r] < 0) {  // a representative joined to another (identical) one
+      rep_slot[r] = (int)hpos.size();
+      hpos.push_back(pos_of[rep[r]]);
+    }
+  const int H = (int)hpos.size();
+  ix.nhead = H;
+  // library index of each position; the heads' digit rows
+  std::vector<int> perm32(n);
+  for (int64_t u = 0; u < n; ++u) perm32[u] = (int)ord[u];
+  const int64_t hblocks = blocks_for(H);
+  ix.rows = hblocks * kBlockRows;
+  DevBuf dpos;
+  bool ok = cudaMalloc(&ix.perm.p, (size_t)n * 4) == cudaSuccess &&
+            cudaMalloc(&ix.info.p, (size_t)hblocks * kBlockStructs * 16) == cudaSuccess &&
+            cudaMalloc(&ix.tinfo.p, (size_t)hblocks * kBlockStructs * 8) == cudaSuccess &&
+            cudaMalloc(&ix.rep_slot.p, (size_t)R * 4) == cudaSuccess && cudaMalloc(&dpos.p, (size_t)H * 8) == cudaSuccess;
+  for (int d = 0; d < 4 && ok; ++d) ok = cudaMalloc(&ix.dig[d].p, (size_t)ix.rows * bk.pitch * 2) == cudaSuccess;
+  if (ok) {
+    DigitPtrs dp{};
+    for (int d = 0; d < 4; ++d) {
+      dp.src[d] = static_cast<const __nv_bfloat16 *>(bk.dig[d].p);
+      dp.dst[d] = static_cast<__nv_bfloat16 *>(ix.dig[d].p);
+      ok = ok && cudaMemset(ix.dig[d].p, 0, (size_t)ix.rows * bk.pitch * 2) == cudaSuccess;
+    }
+    ok = ok && cudaMemset(ix.info.p, 0, (size_t)hblocks * kBlockStructs * 16) == cudaSuccess &&
+         cudaMemset(ix.tinfo.p, 0, (size_t)hblocks * kBlockStructs * 8) == cudaSuccess &&
+         cudaMemcpy(ix.perm.p, perm32.data(), (size_t)n * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(ix.rep_slot.p, rep_slot.data(), (size_t)R * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dpos.p, hpos.data(), (size_t)H * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) {
+      k_gather_reps<<<H, 128>>>(dp, bk.pitch, static_cast<const int64_t *>(dpos.p), H,
+                                static_cast<const SInfo *>(bk.info.p), static_cast<SInfo *>(ix.info.p),
+                                static_cast<const float2 *>(bk.tinfo.p), static_cast<float2 *>(ix.tinfo.p));
+      ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+    }
+  }
+  if (dpos.p) cudaFree(dpos.p);
+  if (!ok) {
+    cudaGetLastError();
+    s->err = "library index: device memory";
+    return BS_ERR_OOM;
+  }
+  bk.indexed = true;
+  return BS_OK;
+}
+
 // After the slot's event: results to the requests (lock held; released
 // while a clustering job's triangle is copied out of the slot).
 void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
@@ -656,21 +1101,32 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
     const Job *back = static_cast<const Job *>(sl.hback.p);
     const int *hcn = sl.screen ? static_cast<const int *>(sl.hcand_n.p) : nullptr;
     std::vector<int> redo;
-    auto take = [&](Request *r, int64_t row0) {
-      const int64_t *hi = static_cast<const int64_t *>(sl.htopi.p) + row0 * k;
-      const float *hv = static_cast<const float *>(sl.htopv.p) + row0 * k;
-      r->idx.assign(hi, hi + r->q * k);
+    // rows of query t of a request at row0 + t, or where an indexed screen
+    // put it (mapped)
+    auto take = [&](Request *r, int64_t row0, bool mapped) {
+      const int64_t *hi = static_cast<const int64_t *>(sl.htopi.p);
+      const float *hv = static_cast<const float *>(sl.htopv.p);
+      r->idx.resize(r->q * k);
       r->val.resize(r->q * k);
-      for (int64_t t = 0; t < r->q * k; ++t) r->val[t] = (double)hv[t];
+      for (int64_t t = 0; t < r->q; ++t) {
+        const int64_t src = mapped ? sl.row_of[row0 + t] : row0 + t;
+        for (int e = 0; e < k; ++e) {
+          r->idx[t * k + e] = hi[src * k + e];
+          r->val[t * k + e] = (double)hv[src * k + e];
+        }
+      }
       r->pairs = r->q * bk.n;
     };
+    const bool mapped_rows = !sl.row_of.empty();
     for (int j = 0; j < (int)sl.reqs.size(); ++j) {
       Request *r = sl.reqs[j];
       bs_status st = BS_OK;
       std::string msg;
+      bool fell_back = false;
       if (s->precision == BS_PRECISION_MIXED) {
         st = collect_errors(sc, back + j, 1, msg);
         if (st == BS_ERR_UNSUPPORTED) {  // outside the bucket's grid: plain FP64 path
+          fell_back = true;
           st = plain_fallback(s, sl, j);
           if (st == BS_OK) ++s->fallbacks;
           else msg = "plain fallback failed";
@@ -686,7 +1142,7 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
         st = BS_ERR_NONFINITE;
         msg = "input coordinates contain NaN or Inf";
       }
-      if (st == BS_OK) take(r, sl.row0[j]);
+      if (st == BS_OK) take(r, sl.row0[j], mapped_rows && !fell_back);
       complete(s, r, st, msg);
     }
     // rows whose screen band held more candidates than kept: every pair of
@@ -700,7 +1156,7 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
       std::string msg;
       if (st == BS_OK)
         st = collect_errors(*static_cast<const DevScalars *>(sl.hsc.p), static_cast<const Job *>(sl.hback.p), 1, msg);
-      if (st == BS_OK) take(r, 0);
+      if (st == BS_OK) take(r, 0, false);
       complete(s, r, st, msg);
     }
   }
@@ -801,8 +1257,12 @@ void sched_loop(bs_server *s) {
       sl.bucket = r0->bucket;
       ++s->batches;
       if (r0->kind == 0) s->rows_batched += rows;
-      // release the unused part of this slot's buffers before growing others
+      // the launch runs without the lock (an indexed screen waits for its
+      // pre-screen): submits go on meanwhile.  Only this thread launches,
+      // grows slot buffers or touches the slot, so nothing it reads changes.
+      lk.unlock();
       const bs_status st = r0->kind == 0 ? launch_query_batch(s, sl, true) : launch_cluster_batch(s, sl);
+      lk.lock();
       if (st) {
         cudaGetLastError();
         cudaStreamSynchronize(sl.st);
@@ -891,9 +1351,6 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
       return st;
     }
   }
-  size_t free_b = 0, total_b = 0;
-  cudaMemGetInfo(&free_b, &total_b);
-  s->budget = cfg->hbm_budget ? cfg->hbm_budget : free_b / 2;
   for (int i = 0; i < s->max_inflight; ++i) {
     auto sl = std::make_unique<Slot>();
     if (cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -903,6 +1360,30 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
     }
     s->slots.push_back(std::move(sl));
   }
+  // library indexes of the large buckets (mixed precision: they prune screens)
+  const int64_t index_min = cfg->index_min > 0 ? cfg->index_min : (cfg->index_min < 0 ? INT64_MAX : kIndexMinDefault);
+  for (int b = 0; b < cfg->nbuckets && s->precision == BS_PRECISION_MIXED; ++b) {
+    if (cfg->bucket_n[b] < index_min || cfg->bucket_n[b] < 2) continue;
+    const size_t bytes = (size_t)cfg->bucket_n[b] * cfg->bucket_L[b] * 3 * 8;
+    std::vector<double> hx;
+    const double *src = cfg->bucket_xyz[b];
+    if (is_device_ptr(src)) {
+      hx.resize(bytes / 8);
+      if (cudaMemcpy(hx.data(), src, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        bs_server_destroy(s);
+        return BS_ERR_CUDA;
+      }
+      src = hx.data();
+    }
+    const bs_status st = build_index(s, b, src);
+    if (st) {
+      bs_server_destroy(s);
+      return st;
+    }
+  }
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  s->budget = cfg->hbm_budget ? cfg->hbm_budget : free_b / 2;
   s->t0 = Clock::now();
   s->sched = std::thread(sched_loop, s);
   s->clus = std::thread(cluster_loop, s);
@@ -925,14 +1406,13 @@ BS_API void bs_server_destroy(bs_server *s) {
     Slot &sl = *up;
     if (sl.st) cudaStreamSynchronize(sl.st);
     slot_release(s, sl);
-    for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri})
+    for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri,
+                       &sl.hcand_n, &sl.hpre})
       if (h->p) cudaFreeHost(h->p);
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.st) cudaStreamDestroy(sl.st);
   }
-  for (Bucket &bk : s->buckets)
-    for (DevBuf *d : {&bk.dig[0], &bk.dig[1], &bk.dig[2], &bk.dig[3], &bk.info, &bk.tinfo, &bk.y, &bk.g})
-      if (d->p) cudaFree(d->p);
+  for (Bucket &bk : s->buckets) free_bucket(bk);
   for (auto &kv : s->reqs) delete kv.second;
   delete s;
 }
@@ -1056,6 +1536,7 @@ BS_API bs_status bs_server_get_stats(bs_server *s, bs_server_stats *out) {
   out->seconds = ms_between(s->t0, Clock::now()) * 1e-3;
   out->pairs_per_s = out->seconds > 0 ? (double)s->pairs / out->seconds : 0.0;
   out->mean_batch_rows = s->batches ? (double)s->rows_batched / (double)s->batches : 0.0;
+  out->pairs_screened = s->screened;
   return BS_OK;
 }
 
@@ -1065,6 +1546,7 @@ BS_API bs_status bs_server_reset_stats(bs_server *s) {
   s->lat.clear();
   s->clat.clear();
   s->qdone = s->cdone = s->pairs = s->batches = s->fallbacks = s->rows_batched = 0;
+  s->screened = 0;
   s->t0 = Clock::now();
   return BS_OK;
 }

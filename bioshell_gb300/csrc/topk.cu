@@ -1,7 +1,10 @@
 // topk.cu -- the k nearest library structures of each query structure: the
 // k smallest values of each row of a dense [rows][n] f32 crmsd block, in
-// ascending (value, column) order -- a total order, so the result does not
-// depend on how the row is scanned.
+// ascending (value, library index) order -- a total order, so the result
+// does not depend on how the row is scanned or in which order candidates
+// were appended.  The library index of column c is perm[c] when the library
+// is stored in another order (perm), else c; candidate lists map their
+// positions to columns first (col_map).
 //
 // One block of eight warps per row.  Each warp scans a strided share of the
 // row and keeps its best k in a sorted list spread over its lanes (two
@@ -59,17 +62,28 @@ __device__ __forceinline__ void consider(float x, int xi, int lane, int k, float
   }
 }
 
+// The ordering key (library index) of position pos of row r.
+struct KeyMap {
+  const int *col_map;  // [rows][ld] candidate -> column, or null
+  const int *perm;     // column -> library index, or null
+  int64_t ld;
+  __device__ __forceinline__ int key(int64_t r, int pos) const {
+    const int c = col_map ? col_map[r * ld + pos] : pos;
+    return perm ? perm[c] : c;
+  }
+};
+
 // One warp's share of a row: 16-byte loads of four values per lane; a
 // chunk of 128 values costs one compare and one ballot unless some lane
 // holds a value below the warp's current k-th entry.
 __device__ void warp_scan(const float *__restrict__ v, int64_t n, int warp, int lane, int k, float (&lv)[2],
-                          int (&li)[2], float &tv, int &ti) {
+                          int (&li)[2], float &tv, int &ti, const KeyMap &km, int64_t row) {
   const float inf = __int_as_float(0x7f800000);
   const int64_t mis = (int64_t)(((16 - ((uintptr_t)v & 15)) & 15) >> 2);  // values before 16-byte alignment
   const int64_t head = n < mis ? n : mis;
   if (warp == 0) {
     const bool ok = lane < head;
-    consider(ok ? v[lane] : inf, lane, lane, k, lv, li, tv, ti, ok);
+    consider(ok ? v[lane] : inf, ok ? km.key(row, lane) : 0x7fffffff, lane, k, lv, li, tv, ti, ok);
   }
   const float4 *v4 = reinterpret_cast<const float4 *>(v + head);
   const int64_t n4 = (n - head) >> 2;
@@ -79,16 +93,19 @@ __device__ void warp_scan(const float *__restrict__ v, int64_t n, int warp, int 
     const float mn = fminf(fminf(x.x, x.y), fminf(x.z, x.w));
     if (!__any_sync(kFull, qi < n4 && mn <= tv)) continue;
     const int base = (int)(head + 4 * qi);
-    consider(x.x, base + 0, lane, k, lv, li, tv, ti, qi < n4);
-    consider(x.y, base + 1, lane, k, lv, li, tv, ti, qi < n4);
-    consider(x.z, base + 2, lane, k, lv, li, tv, ti, qi < n4);
-    consider(x.w, base + 3, lane, k, lv, li, tv, ti, qi < n4);
+    const bool in = qi < n4;
+    // keys only where a value can enter (the mapping reads global memory)
+    const bool any = in && mn <= tv;
+    consider(x.x, any ? km.key(row, base + 0) : 0x7fffffff, lane, k, lv, li, tv, ti, in);
+    consider(x.y, any ? km.key(row, base + 1) : 0x7fffffff, lane, k, lv, li, tv, ti, in);
+    consider(x.z, any ? km.key(row, base + 2) : 0x7fffffff, lane, k, lv, li, tv, ti, in);
+    consider(x.w, any ? km.key(row, base + 3) : 0x7fffffff, lane, k, lv, li, tv, ti, in);
   }
   const int64_t tail0 = head + 4 * n4;
   if (warp == kTopkWarps - 1) {
     const int64_t j = tail0 + lane;
     const bool ok = j < n;
-    consider(ok ? v[j] : inf, (int)j, lane, k, lv, li, tv, ti, ok);
+    consider(ok ? v[j] : inf, ok ? km.key(row, (int)j) : 0x7fffffff, lane, k, lv, li, tv, ti, ok);
   }
 }
 
@@ -104,8 +121,7 @@ __device__ void merge_lists(float (*sv)[kTopkMax], int (*si)[kTopkMax], int lane
 }
 
 __global__ void __launch_bounds__(kTopkWarps * 32) k_topk(const float *__restrict__ vals, int64_t n_all, int64_t ld,
-                                                          const int *__restrict__ row_n,
-                                                          const int *__restrict__ col_map, int k,
+                                                          const int *__restrict__ row_n, KeyMap km, int k,
                                                           int64_t *__restrict__ out_idx,
                                                           float *__restrict__ out_val) {
   __shared__ float sv[kTopkWarps][kTopkMax];
@@ -118,7 +134,7 @@ __global__ void __launch_bounds__(kTopkWarps * 32) k_topk(const float *__restric
   int li[2] = {0x7fffffff, 0x7fffffff};
   float tv = inf;
   int ti = 0x7fffffff;
-  warp_scan(v, n, warp, lane, k, lv, li, tv, ti);
+  warp_scan(v, n, warp, lane, k, lv, li, tv, ti, km, blockIdx.x);
   sv[warp][2 * lane] = lv[0];
   sv[warp][2 * lane + 1] = lv[1];
   si[warp][2 * lane] = li[0];
@@ -133,9 +149,7 @@ __global__ void __launch_bounds__(kTopkWarps * 32) k_topk(const float *__restric
     const int e = 2 * lane + s;
     if (e < k) {
       const bool real = li[s] != 0x7fffffff;
-      int64_t col = -1;
-      if (real) col = col_map ? (int64_t)col_map[(int64_t)blockIdx.x * ld + li[s]] : (int64_t)li[s];
-      oi[e] = col;
+      oi[e] = real ? (int64_t)li[s] : -1;  // the key is the library index
       ov[e] = real ? lv[s] : -1.0f;
     }
   }
@@ -262,19 +276,21 @@ __global__ void __launch_bounds__(kSelThreads) k_screen_extract(const uint32_t *
 
 }  // namespace
 
-cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, int64_t *out_idx,
-                        float *out_val, cudaStream_t st) {
+cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, const int *perm,
+                        int64_t *out_idx, float *out_val, cudaStream_t st) {
   if (rows <= 0) return cudaSuccess;
   if (k < 1 || k > kTopkMax || n > 0x7ffffffe) return cudaErrorInvalidValue;
-  k_topk<<<(unsigned)rows, kTopkWarps * 32, 0, st>>>(vals, n, ld, nullptr, nullptr, k, out_idx, out_val);
+  k_topk<<<(unsigned)rows, kTopkWarps * 32, 0, st>>>(vals, n, ld, nullptr, KeyMap{nullptr, perm, ld}, k, out_idx,
+                                                      out_val);
   return cudaGetLastError();
 }
 
 cudaError_t launch_topk_rows(const float *vals, int64_t rows, const int *row_n, int64_t ld, int k,
-                             const int *col_map, int64_t *out_idx, float *out_val, cudaStream_t st) {
+                             const int *col_map, const int *perm, int64_t *out_idx, float *out_val, cudaStream_t st) {
   if (rows <= 0) return cudaSuccess;
   if (k < 1 || k > kTopkMax || ld > 0x7ffffffe) return cudaErrorInvalidValue;
-  k_topk<<<(unsigned)rows, kTopkWarps * 32, 0, st>>>(vals, ld, ld, row_n, col_map, k, out_idx, out_val);
+  k_topk<<<(unsigned)rows, kTopkWarps * 32, 0, st>>>(vals, ld, ld, row_n, KeyMap{col_map, perm, ld}, k, out_idx,
+                                                      out_val);
   return cudaGetLastError();
 }
 

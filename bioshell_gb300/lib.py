@@ -57,7 +57,7 @@ class bs_server_config(ctypes.Structure):
                 ("bucket_n", ctypes.POINTER(ctypes.c_int64)), ("bucket_xyz", ctypes.POINTER(ctypes.c_void_p)),
                 ("top_k", ctypes.c_int32), ("max_inflight", ctypes.c_int32), ("hbm_budget", ctypes.c_size_t),
                 ("precision", ctypes.c_int32), ("max_batch_rows", ctypes.c_int32), ("tolerance", ctypes.c_double),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("index_min", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 class bs_server_stats(ctypes.Structure):
@@ -66,7 +66,8 @@ class bs_server_stats(ctypes.Structure):
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
                 ("mean_ms", ctypes.c_double), ("cluster_p50_ms", ctypes.c_double),
                 ("cluster_p99_ms", ctypes.c_double), ("pairs_per_s", ctypes.c_double),
-                ("mean_batch_rows", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("mean_batch_rows", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("pairs_screened", ctypes.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -25,7 +25,7 @@ from . import lib as _l
 class CrmsdServer:
     def __init__(self, library: Dict[int, np.ndarray], device: int = 0, top_k: int = 50, max_inflight: int = 4,
                  hbm_budget: int = 0, precision: str = "mixed", max_batch_rows: int = 0,
-                 tolerance: Optional[float] = None):
+                 tolerance: Optional[float] = None, index_min: int = 0):
         self._lib = _l.load()
         self.top_k = int(top_k)
         lengths = sorted(library)
@@ -48,6 +48,7 @@ class CrmsdServer:
         cfg.precision = _l.PRECISION[precision]
         cfg.max_batch_rows = int(max_batch_rows)
         cfg.tolerance = float(tolerance or 0.0)
+        cfg.index_min = int(index_min)  # buckets this large get a library index (0: 16384, < 0: never)
         h = ctypes.c_void_p()
         st = self._lib.bs_server_create(ctypes.byref(h), int(device), ctypes.byref(cfg))
         if st != _l.BS_OK:

@@ -285,7 +285,12 @@ typedef struct {
   int32_t precision;                 /* BS_PRECISION_MIXED or _PLAIN64       */
   int32_t max_batch_rows;            /* query structures per batch (0 = 4096) */
   double tolerance;                  /* as bs_opts.tolerance (<= 0: 1e-4)    */
-  int32_t reserved[6];
+  int32_t index_min;                 /* mixed precision: buckets of at least
+                                        this many structures get a library
+                                        index that prunes the screen (their
+                                        results are unchanged); 0 = 16384,
+                                        < 0 = never                         */
+  int32_t reserved[5];
 } bs_server_config;
 
 typedef struct {
@@ -305,6 +310,10 @@ typedef struct {
   double pairs_per_s;       /* pairs / wall time since the last reset        */
   double mean_batch_rows;   /* query structures per batch                    */
   double seconds;           /* wall time since the last reset                */
+  int64_t pairs_screened;   /* (query, library) pairs the screens of launched
+                               batches covered, in tiles of 40 x 20; below
+                               the requests' pairs when library indexes
+                               prune                                         */
 } bs_server_stats;
 
 BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_server_config *cfg);

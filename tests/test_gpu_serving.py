@@ -157,3 +157,38 @@ def test_server_errors(server, library):
     assert e.value.status == 6
     idx, _ = server.wait(server.submit(_queries(library, 64, 2, 42)))  # still serving
     assert np.all(idx >= 0)
+
+
+def test_library_index_keeps_results(oracle_mod, enginelib):
+    """A library index prunes the screen but changes no result: an indexed
+    server and an unindexed one return the same indices and values, bit for
+    bit, for single-family and mixed-family requests and with exact
+    duplicates in the library (ties broken by library index)."""
+    from bioshell_gb300 import CrmsdServer
+    rng = np.random.default_rng(91)
+    parts = [synth.decoys(synth.base_chain(64, rng), 480, rng, sigma=(0.3, 3.0)) for _ in range(8)]
+    lib = np.concatenate(parts)
+    lib = np.concatenate([lib, lib[rng.choice(len(lib), 96, replace=False)]])  # exact duplicates
+    plain = CrmsdServer({64: lib}, top_k=TOPK, max_inflight=2, index_min=-1)
+    indexed = CrmsdServer({64: lib}, top_k=TOPK, max_inflight=2, index_min=1)
+    try:
+        reqs = []
+        for f, q in ((0, 45), (3, 1), (5, 120)):
+            base = parts[f][0] - parts[f][0].mean(axis=0)
+            reqs.append(synth.decoys(base, q, rng, sigma=(0.3, 2.0)))
+        # one request mixing families, and library members themselves (ties)
+        reqs.append(np.concatenate([synth.decoys(p[0] - p[0].mean(axis=0), 7, rng, sigma=(0.3, 2.0))
+                                    for p in parts]))
+        reqs.append(lib[rng.choice(len(lib), 30, replace=False)])
+        for x in reqs:
+            a = plain.wait(plain.submit(x))
+            b = indexed.wait(indexed.submit(x))
+            np.testing.assert_array_equal(a[0], b[0])
+            np.testing.assert_array_equal(a[1], b[1])
+        _check_against_oracle(lib, reqs[3][:4], *[v[:4] for v in indexed.wait(indexed.submit(reqs[3]))],
+                              oracle_mod)
+        st = indexed.stats()
+        assert 0 < st["pairs_screened"]
+    finally:
+        plain.close()
+        indexed.close()
