@@ -303,6 +303,19 @@ cudaError_t launch_hierarchical(const void *tri, int out_type, int64_t n, int ru
 cudaError_t launch_neighbors_csr(const int2 *ij, const float *d, int64_t cnt, int64_t n, int num_sms,
                                  int64_t *row_ptr, int32_t *col, float *dist, unsigned long long *scratch_rows,
                                  unsigned long long *key, unsigned long long *tmp, cudaStream_t st);
+// A row-block segment of a pruned screen's brackets: rows r0 .. r0 + nr - 1,
+// columns [c0, c1) (at most screen_select_chunk(), c0 a multiple of 4).
+struct SelSeg {
+  int64_t r0;
+  int nr, pad;
+  int64_t c0, c1;
+};
+int screen_select_chunk();
+// launch_screen_select over the listed segments only (the rest of each row
+// is never read); max_rows bounds nr.
+cudaError_t launch_screen_select_seg(const uint32_t *packed, int64_t rows, int64_t ld, int k, int cap,
+                                     const SelSeg *segs, int64_t nsegs, int max_rows, uint32_t *hist,
+                                     uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st);
 cudaError_t launch_screen_select(const uint32_t *packed, int64_t rows, int64_t n, int64_t ld, int k, int cap,
                                  uint32_t *hist, uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st);
 

@@ -189,7 +189,8 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
       if ((e = all_screen ? launch_screen_tc(tm, a, plan.strips, st) : launch_mixed_tc(tm, a, st)) != cudaSuccess)
         return e;
       if ((e = rec(2)) != cudaSuccess) return e;
-      if ((e = launch_refine(r, st)) != cudaSuccess) return e;
+      // screen tiles flag no pair: nothing to recompute
+      if (!all_screen && (e = launch_refine(r, st)) != cudaSuccess) return e;
     } else {
       const size_t nb = rb->tile_end.size();
       r.mark = true;

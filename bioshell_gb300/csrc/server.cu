@@ -114,6 +114,12 @@ struct Request {
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
+  cudaStream_t pst = nullptr;  // indexed screens: the pre-screen's high-priority stream
+  cudaEvent_t pev = nullptr;
+  // the slot's worker thread and its hand-off from the scheduler (server lock)
+  std::thread worker;
+  std::condition_variable cv;
+  bool has_work = false, quit = false;
   bool busy = false;
   int kind = 0, bucket = -1;
   std::vector<Request *> reqs;
@@ -124,9 +130,9 @@ struct Slot {
   std::vector<int64_t> row_of;  // indexed screens: result row of query t of request j at row0[j] + t
   // device
   DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
-  DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab, pre, prerep;
+  DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab, pre, prerep, segs;
   // pinned host
-  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n, hpre;
+  HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n, hpre, hsegs;
 };
 
 }  // namespace
@@ -140,7 +146,8 @@ struct bs_server {
   int64_t max_rows = 4096;
   int precision = BS_PRECISION_MIXED;
   float tol = 1e-4f;
-  size_t budget = 0, used = 0;  // in-flight device memory of the slots
+  size_t budget = 0;
+  std::atomic<size_t> used{0};  // in-flight device memory of the slots (workers grow their own buffers)
   std::vector<bs::Bucket> buckets;
   std::vector<std::unique_ptr<bs::Slot>> slots;
   std::mutex mu;
@@ -211,7 +218,7 @@ void slot_release(bs_server *s, Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
                     &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep};
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep, &sl.segs};
   for (DevBuf *b : list) sv_release(s, *b);
 }
 
@@ -219,7 +226,7 @@ size_t slot_bytes(Slot &sl) {
   DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
                     &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep};
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep, &sl.segs};
   size_t t = 0;
   for (DevBuf *b : list) t += b->cap;
   return t;
@@ -457,24 +464,28 @@ bool index_prescreen(bs_server *s, Slot &sl, const Plan &base, int64_t blk, int6
   CUtensorMap tm[7];
   if (!encode_maps(s->encode, b, tm).empty()) return false;
   uint32_t *prerep = static_cast<uint32_t *>(sl.prerep.p);
+  // the pre-screen runs on the slot's high-priority stream (its blocks go
+  // ahead of other batches' screens), after the coordinates' copy
+  cudaStream_t ps = sl.pst;
+  if (cudaEventRecord(sl.pev, sl.st) != cudaSuccess || cudaStreamWaitEvent(ps, sl.pev, 0) != cudaSuccess) return false;
   uint32_t *thr = static_cast<uint32_t *>(sl.thr.p);
-  if (cudaMemcpyAsync(b.jobmap, ht, p1.jobmap.size() * 4, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
+  if (cudaMemcpyAsync(b.jobmap, ht, p1.jobmap.size() * 4, cudaMemcpyHostToDevice, ps) != cudaSuccess ||
       cudaMemcpyAsync(b.tiles, ht + p1.jobmap.size() * 4, p1.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice,
-                      sl.st) != cudaSuccess ||
-      enqueue_mixed(p1, b, static_cast<const Job *>(sl.hjobs.p), tm, s->num_sms, sl.st, nullptr, false) !=
+                      ps) != cudaSuccess ||
+      enqueue_mixed(p1, b, static_cast<const Job *>(sl.hjobs.p), tm, s->num_sms, ps, nullptr, false) !=
           cudaSuccess ||
       launch_screen_select(pre, rows, H, ldh, k, kCandCap, static_cast<uint32_t *>(sl.hist.p), thr,
-                           static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) != cudaSuccess)
+                           static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), ps) != cudaSuccess)
     return false;
-  k_gather_cols<<<dim3((unsigned)((R + 127) / 128), (unsigned)rows), 128, 0, sl.st>>>(
+  k_gather_cols<<<dim3((unsigned)((R + 127) / 128), (unsigned)rows), 128, 0, ps>>>(
       pre, ldh, static_cast<const int *>(ix.rep_slot.p), R, rows, prerep);
   if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpyAsync(sl.hpre.p, prerep, (size_t)rows * R * 4, cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hpre.p, prerep, (size_t)rows * R * 4, cudaMemcpyDeviceToHost, ps) != cudaSuccess ||
       cudaMemcpyAsync(static_cast<uint32_t *>(sl.hpre.p) + (size_t)rows * R, thr, (size_t)rows * 4,
-                      cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
-      cudaMemcpyAsync(sl.hback.p, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
-      cudaMemcpyAsync(sl.hsc.p, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, sl.st) != cudaSuccess ||
-      cudaStreamSynchronize(sl.st) != cudaSuccess) {
+                      cudaMemcpyDeviceToHost, ps) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hback.p, b.jobs, (size_t)nj * sizeof(Job), cudaMemcpyDeviceToHost, ps) != cudaSuccess ||
+      cudaMemcpyAsync(sl.hsc.p, b.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, ps) != cudaSuccess ||
+      cudaStreamSynchronize(ps) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
@@ -633,10 +644,12 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   double *dx = static_cast<double *>(sl.xyz.p);
   if (cudaMemcpyAsync(dx, hx, xyz_off * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess) return BS_ERR_CUDA;
   bool pruned = false;
+  std::vector<std::vector<int64_t>> need;  // pruned screens: library blocks per query block
   if (sl.screen && bk.indexed) {
     std::vector<std::vector<int>> order;
-    std::vector<std::vector<int64_t>> need;
-    if (index_prescreen(s, sl, plan, blk, rows, dx, xoff, order, need)) {
+    const bool usable = index_prescreen(s, sl, plan, blk, rows, dx, xoff, order, need);
+    if (!usable) cudaStreamSynchronize(sl.pst);  // nothing of the pre-screen may still run
+    if (usable) {
       pruned = true;
       // each request's queries in the order of their nearest representative
       sl.row_of.assign(rows, 0);
@@ -670,9 +683,33 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
         return BS_ERR_CUDA;
     }
   } else {
-    // pruned screens: every pair not screened reads as lo = hi = 61,184 A
-    // (half-precision bits 0x7B7B), above every bound that can matter
-    if (pruned && cudaMemsetAsync(dense, 0x7B, (size_t)rows * ld * 4, sl.st) != cudaSuccess) return BS_ERR_CUDA;
+    // pruned screens: the selection reads the screened segments only
+    std::vector<SelSeg> segs;
+    if (pruned) {
+      const int64_t chunk = screen_select_chunk();
+      for (int j = 0; j < nj; ++j) {
+        const int64_t q = plan.jobs[j].n, b0 = plan.jobs[j].first_a / kBlockStructs;
+        for (int64_t I = 0; I * kBlockStructs < q; ++I) {
+          const int64_t r0 = sl.row0[j] + I * kBlockStructs;
+          const int nr = (int)std::min<int64_t>(kBlockStructs, q - I * kBlockStructs);
+          const std::vector<int64_t> &v = need[b0 + I];
+          for (size_t a = 0; a < v.size();) {
+            size_t e = a + 1;
+            while (e < v.size() && v[e] == v[e - 1] + 1) ++e;
+            const int64_t c1 = std::min<int64_t>(bk.n, v[e - 1] * kBStructs + kBStructs);
+            for (int64_t c = v[a] * kBStructs; c < c1; c += chunk)
+              segs.push_back(SelSeg{r0, nr, 0, c, std::min(c + chunk, c1)});
+            a = e;
+          }
+        }
+      }
+      if (!sv_ensure(s, sl.segs, segs.size() * sizeof(SelSeg)) || !host_ensure(sl.hsegs, segs.size() * sizeof(SelSeg)))
+        return BS_ERR_OOM;
+      memcpy(sl.hsegs.p, segs.data(), segs.size() * sizeof(SelSeg));
+      if (cudaMemcpyAsync(sl.segs.p, sl.hsegs.p, segs.size() * sizeof(SelSeg), cudaMemcpyHostToDevice, sl.st) !=
+          cudaSuccess)
+        return BS_ERR_CUDA;
+    }
     if (sl.screen) {
       int64_t t = 0;
       for (const Tile &tl : plan.tiles) t += plan.strips ? (tl.shape >> 16) : 1;
@@ -731,9 +768,15 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
       const int *cj = static_cast<const int *>(sl.cand_j.p);
       const int *cn = static_cast<const int *>(sl.cand_n.p);
       if (cudaMemcpyAsync(drjob, rt, jbytes + (size_t)rows * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess ||
-          launch_screen_select(reinterpret_cast<const uint32_t *>(dense), rows, bk.n, ld, k, kCandCap,
-                               static_cast<uint32_t *>(sl.hist.p), static_cast<uint32_t *>(sl.thr.p),
-                               static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p), sl.st) != cudaSuccess ||
+          (pruned ? launch_screen_select_seg(reinterpret_cast<const uint32_t *>(dense), rows, ld, k, kCandCap,
+                                             static_cast<const SelSeg *>(sl.segs.p), (int64_t)segs.size(),
+                                             kBlockStructs, static_cast<uint32_t *>(sl.hist.p),
+                                             static_cast<uint32_t *>(sl.thr.p), static_cast<int *>(sl.cand_j.p),
+                                             static_cast<int *>(sl.cand_n.p), sl.st)
+                  : launch_screen_select(reinterpret_cast<const uint32_t *>(dense), rows, bk.n, ld, k, kCandCap,
+                                         static_cast<uint32_t *>(sl.hist.p), static_cast<uint32_t *>(sl.thr.p),
+                                         static_cast<int *>(sl.cand_j.p), static_cast<int *>(sl.cand_n.p),
+                                         sl.st)) != cudaSuccess ||
           launch_exact_candidates(DigitsView{b.dig_a[0], b.dig_a[1], b.dig_a[2], b.pitch_a},
                                   DigitsView{b.dig_b[0], b.dig_b[1], b.dig_b[2], b.pitch_b}, b.info_a, b.info_b, b.jobs,
                                   drjob, drig, rows, cj, cn, kCandCap, static_cast<float *>(sl.cand_v.p),
@@ -1194,26 +1237,44 @@ void fail_batch(bs_server *s, Slot &sl, bs_status st, const std::string &msg) {
   sl.busy = false;
 }
 
+// A slot's worker: launches the batch the scheduler handed it (without the
+// lock: an indexed screen waits for its pre-screen), waits for it, and
+// completes its requests (with the lock).  Workers run side by side, so the
+// host work of one batch overlaps the device work and host work of others.
+void worker_loop(bs_server *s, Slot *slp) {
+  cudaSetDevice(s->device);
+  Slot &sl = *slp;
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (true) {
+    sl.cv.wait(lk, [&] { return sl.has_work || sl.quit; });
+    if (!sl.has_work) break;
+    sl.has_work = false;
+    const int kind = sl.kind;
+    lk.unlock();
+    bs_status st = kind == 0 ? launch_query_batch(s, sl, true) : launch_cluster_batch(s, sl);
+    cudaError_t e = cudaSuccess;
+    if (st == BS_OK) e = cudaEventSynchronize(sl.ev);
+    lk.lock();
+    if (st) {
+      cudaGetLastError();
+      cudaStreamSynchronize(sl.st);
+      fail_batch(s, sl, st, st == BS_ERR_OOM ? "device memory" : "batch launch failed");
+    } else if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail_batch(s, sl, BS_ERR_CUDA, cudaGetErrorString(e));
+    } else {
+      finish_slot(s, sl, lk);
+    }
+    s->cv_work.notify_one();  // the slot is free again
+  }
+}
+
+// The scheduler: forms batches from the queue and hands them to idle slots.
 void sched_loop(bs_server *s) {
   cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
   while (true) {
-    bool progress = false, inflight = false;
-    for (auto &up : s->slots) {
-      Slot &sl = *up;
-      if (!sl.busy) continue;
-      const cudaError_t q = cudaEventQuery(sl.ev);
-      if (q == cudaSuccess) {
-        finish_slot(s, sl, lk);
-        progress = true;
-      } else if (q == cudaErrorNotReady) {
-        inflight = true;
-      } else {
-        cudaGetLastError();
-        fail_batch(s, sl, BS_ERR_CUDA, cudaGetErrorString(q));
-        progress = true;
-      }
-    }
+    bool progress = false;
     for (auto &up : s->slots) {
       Slot &sl = *up;
       if (sl.busy || s->queue.empty()) continue;
@@ -1257,35 +1318,19 @@ void sched_loop(bs_server *s) {
       sl.bucket = r0->bucket;
       ++s->batches;
       if (r0->kind == 0) s->rows_batched += rows;
-      // the launch runs without the lock (an indexed screen waits for its
-      // pre-screen): submits go on meanwhile.  Only this thread launches,
-      // grows slot buffers or touches the slot, so nothing it reads changes.
-      lk.unlock();
-      const bs_status st = r0->kind == 0 ? launch_query_batch(s, sl, true) : launch_cluster_batch(s, sl);
-      lk.lock();
-      if (st) {
-        cudaGetLastError();
-        cudaStreamSynchronize(sl.st);
-        fail_batch(s, sl, st, st == BS_ERR_OOM ? "device memory" : "batch launch failed");
-      }
+      sl.has_work = true;
+      sl.cv.notify_one();
       progress = true;
-      inflight = true;
     }
     if (s->stop && s->queue.empty()) {
       bool busy = false;
       for (auto &up : s->slots) busy |= up->busy;
       if (!busy) break;
     }
-    if (!progress) {
-      if (inflight) {
-        lk.unlock();
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
-        lk.lock();
-      } else {
-        s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
-      }
-    }
+    if (!progress) s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
   }
+  for (auto &up : s->slots) up->quit = true;
+  for (auto &up : s->slots) up->cv.notify_one();
 }
 
 double percentile(std::vector<double> v, double p) {
@@ -1353,8 +1398,12 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
   }
   for (int i = 0; i < s->max_inflight; ++i) {
     auto sl = std::make_unique<Slot>();
+    int lo_pri = 0, hi_pri = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri);
     if (cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming | cudaEventBlockingSync) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&sl->pst, cudaStreamNonBlocking, hi_pri) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl->pev, cudaEventDisableTiming) != cudaSuccess) {
       bs_server_destroy(s);
       return BS_ERR_CUDA;
     }
@@ -1385,6 +1434,7 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
   cudaMemGetInfo(&free_b, &total_b);
   s->budget = cfg->hbm_budget ? cfg->hbm_budget : free_b / 2;
   s->t0 = Clock::now();
+  for (auto &up : s->slots) up->worker = std::thread(worker_loop, s, up.get());
   s->sched = std::thread(sched_loop, s);
   s->clus = std::thread(cluster_loop, s);
   *out = s;
@@ -1400,6 +1450,14 @@ BS_API void bs_server_destroy(bs_server *s) {
   s->cv_work.notify_all();
   s->cv_clus.notify_all();
   if (s->sched.joinable()) s->sched.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto &up : s->slots) up->quit = true;
+  }
+  for (auto &up : s->slots) {
+    up->cv.notify_one();
+    if (up->worker.joinable()) up->worker.join();
+  }
   if (s->clus.joinable()) s->clus.join();
   cudaSetDevice(s->device);
   for (auto &up : s->slots) {
@@ -1407,10 +1465,15 @@ BS_API void bs_server_destroy(bs_server *s) {
     if (sl.st) cudaStreamSynchronize(sl.st);
     slot_release(s, sl);
     for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri,
-                       &sl.hcand_n, &sl.hpre})
+                       &sl.hcand_n, &sl.hpre, &sl.hsegs})
       if (h->p) cudaFreeHost(h->p);
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.st) cudaStreamDestroy(sl.st);
+    if (sl.pev) cudaEventDestroy(sl.pev);
+    if (sl.pst) {
+      cudaStreamSynchronize(sl.pst);
+      cudaStreamDestroy(sl.pst);
+    }
   }
   for (Bucket &bk : s->buckets) free_bucket(bk);
   for (auto &kv : s->reqs) delete kv.second;

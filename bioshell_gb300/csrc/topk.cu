@@ -274,7 +274,92 @@ __global__ void __launch_bounds__(kSelThreads) k_screen_extract(const uint32_t *
   }
 }
 
+// The same two passes over a list of row-block segments only (pruned
+// screens): segment s covers rows r0 .. r0 + nr - 1 and columns [c0, c1)
+// (at most kSelChunk, c0 a multiple of 4); blockIdx.y picks the row.
+__global__ void __launch_bounds__(kSelThreads) k_screen_hist_seg(const uint32_t *__restrict__ packed, int64_t ld,
+                                                                 const SelSeg *__restrict__ segs,
+                                                                 uint32_t *__restrict__ hist) {
+  __shared__ uint32_t h[kScreenBins];
+  const SelSeg sg = segs[blockIdx.x];
+  if ((int)blockIdx.y >= sg.nr) return;  // the same for the whole block
+  for (int b = threadIdx.x; b < kScreenBins; b += kSelThreads) h[b] = 0;
+  const int64_t r = sg.r0 + blockIdx.y;
+  const int64_t c0 = sg.c0, c1 = sg.c1;
+  uint4 w[kSelPer];
+  load_chunk(packed + r * ld, c0, w, c1);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < kSelPer; ++u) {
+    const int64_t c = c0 + 4 * ((int64_t)u * kSelThreads + threadIdx.x);
+    if (c < c1) atomicAdd(&h[w[u].x >> 20], 1u);
+    if (c + 1 < c1) atomicAdd(&h[w[u].y >> 20], 1u);
+    if (c + 2 < c1) atomicAdd(&h[w[u].z >> 20], 1u);
+    if (c + 3 < c1) atomicAdd(&h[w[u].w >> 20], 1u);
+  }
+  __syncthreads();
+  uint32_t *gh = hist + r * kScreenBins;
+  for (int b = threadIdx.x; b < kScreenBins; b += kSelThreads)
+    if (h[b]) atomicAdd(&gh[b], h[b]);
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_screen_extract_seg(const uint32_t *__restrict__ packed, int64_t ld,
+                                                                    const SelSeg *__restrict__ segs,
+                                                                    const uint32_t *__restrict__ thr, int cap,
+                                                                    int *__restrict__ cand_j,
+                                                                    int *__restrict__ cand_n) {
+  const SelSeg sg = segs[blockIdx.x];
+  if ((int)blockIdx.y >= sg.nr) return;
+  const int64_t r = sg.r0 + blockIdx.y;
+  const int64_t c0 = sg.c0, c1 = sg.c1;
+  uint4 w[kSelPer];
+  load_chunk(packed + r * ld, c0, w, c1);
+  const uint32_t t = thr[r];
+  const int lane = threadIdx.x & 31;
+  int *cj = cand_j + r * (int64_t)cap;
+#pragma unroll
+  for (int u = 0; u < kSelPer; ++u) {
+    const int64_t c = c0 + 4 * ((int64_t)u * kSelThreads + threadIdx.x);
+    const uint32_t v[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const bool hit = c + e < c1 && (v[e] & 0xffffu) <= t;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (!m) continue;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(&cand_n[r], __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (hit) {
+        const int slot = base + __popc(m & ((1u << lane) - 1u));
+        if (slot < cap) cj[slot] = (int)(c + e);
+      }
+    }
+  }
+}
+
 }  // namespace
+
+int screen_select_chunk() { return kSelChunk; }
+
+cudaError_t launch_screen_select_seg(const uint32_t *packed, int64_t rows, int64_t ld, int k, int cap,
+                                     const SelSeg *segs, int64_t nsegs, int max_rows, uint32_t *hist,
+                                     uint32_t *thresholds, int *cand_j, int *cand_n, cudaStream_t st) {
+  if (rows <= 0) return cudaSuccess;
+  if (cap < 1 || k < 1 || (ld & 3) || ((uintptr_t)packed & 15) || max_rows < 1 || max_rows > 65535 ||
+      nsegs > 0x7fffffff)
+    return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(hist, 0, (size_t)rows * kScreenBins * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cand_n, 0, (size_t)rows * 4, st);
+  if (e != cudaSuccess) return e;
+  if (nsegs > 0) k_screen_hist_seg<<<dim3((unsigned)nsegs, (unsigned)max_rows), kSelThreads, 0, st>>>(packed, ld, segs,
+                                                                                                    hist);
+  k_screen_thresh<<<(unsigned)rows, kSelThreads, 0, st>>>(hist, k, thresholds);
+  if (nsegs > 0)
+    k_screen_extract_seg<<<dim3((unsigned)nsegs, (unsigned)max_rows), kSelThreads, 0, st>>>(packed, ld, segs,
+                                                                                          thresholds, cap, cand_j,
+                                                                                          cand_n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_topk(const float *vals, int64_t rows, int64_t n, int64_t ld, int k, const int *perm,
                         int64_t *out_idx, float *out_val, cudaStream_t st) {
