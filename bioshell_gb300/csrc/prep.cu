@@ -188,45 +188,46 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, in
     for (int d = 0; d < 3; ++d) mfull[a][d] = mhalf[a][d] = mquart[a][d] = 0;
   for (int r = 0; r < 3; ++r) {
     const long long C = p.ctr[3 * g + r];
-    unsigned acc[4][4][3];  // [candidate][quarter][digit]
+    // the chain's quarters one after the other: quarter qq holds the 16-atom
+    // steps k16 with acc_part(k16, nk16, 4) == qq, i.e. 4 k16 in
+    // [qq nk16, (qq + 1) nk16)
+    unsigned qsum[4][3][4];  // [candidate][digit][quarter], warp totals
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int qq = 0; qq < 4; ++qq) {
+      const int k_lo = 16 * ((qq * nk16 + 3) / 4), k_hi = min(L, 16 * (((qq + 1) * nk16 + 3) / 4));
+      unsigned acc[4][3];
 #pragma unroll
-      for (int qq = 0; qq < 4; ++qq)
+      for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) acc[a][qq][d] = 0;
-    for (int k = lane; k < L; k += 32) {
-      long long v;
-      to_fix(x[3 * k + r], v);
-      const long long y = v - C;
-      const int qt = acc_part(k >> 4, nk16, 4);
+        for (int d = 0; d < 3; ++d) acc[a][d] = 0;
+      for (int k = k_lo + lane; k < k_hi; k += 32) {
+        long long v;
+        to_fix(x[3 * k + r], v);
+        const long long y = v - C;
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        if (a < ncand) {
-          const int t = t0 + a;
-          const int q = (int)((y + (1ll << (t - 1))) >> t);
-          int e0, e1, e2;
-          bsm::split_digits(q, e0, e1, e2);
-          const unsigned s0 = (unsigned)(e0 * e0), s1 = (unsigned)(e1 * e1), s2 = (unsigned)(e2 * e2);
-#pragma unroll
-          for (int qq = 0; qq < 4; ++qq) {
-            if (qt == qq) {
-              acc[a][qq][0] += s0;
-              acc[a][qq][1] += s1;
-              acc[a][qq][2] += s2;
-            }
+        for (int a = 0; a < 4; ++a) {
+          if (a < ncand) {
+            const int t = t0 + a;
+            const int q = (int)((y + (1ll << (t - 1))) >> t);
+            int e0, e1, e2;
+            bsm::split_digits(q, e0, e1, e2);
+            acc[a][0] += (unsigned)(e0 * e0);
+            acc[a][1] += (unsigned)(e1 * e1);
+            acc[a][2] += (unsigned)(e2 * e2);
           }
         }
       }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) qsum[a][d][qq] = a < ncand ? warp_sum32(acc[a][d]) : 0u;
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       if (a >= ncand) break;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        unsigned v[4];
-#pragma unroll
-        for (int qq = 0; qq < 4; ++qq) v[qq] = warp_sum32(acc[a][qq][d]);
+        const unsigned *v = qsum[a][d];
         const unsigned h0 = v[0] + v[1], h1 = v[2] + v[3], f = h0 + h1;
         mfull[a][d] = f > mfull[a][d] ? f : mfull[a][d];
         mhalf[a][d] = max(mhalf[a][d], max(h0, h1));
