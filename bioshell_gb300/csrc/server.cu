@@ -19,6 +19,8 @@
 // A batch is admitted only when its device memory fits the budget left by
 // the other slots; batches in different slots run concurrently.
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -42,6 +44,10 @@ namespace {
 using Clock = std::chrono::steady_clock;
 constexpr unsigned long long kServerFlagCap = 1ull << 20;
 constexpr int kCandCap = 2048;  // screen candidates kept per query structure
+
+// Growth of the calling thread's buffers during one batch (trace records).
+thread_local int t_grow_dev = 0, t_grow_host = 0;
+thread_local double t_grow_ms = 0.0;
 
 double ms_between(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
@@ -109,6 +115,7 @@ struct Request {
   bool done = false;
   Clock::time_point t_submit, t_done;
   int64_t pairs = 0;
+  int64_t batch = -1;  // the batch that carried it (trace records)
 };
 
 struct Slot {
@@ -128,11 +135,14 @@ struct Slot {
   int njobs = 0;
   bool screen = false;        // the batch ran the two-stage (screen + exact) top-k
   std::vector<int64_t> row_of;  // indexed screens: result row of query t of request j at row0[j] + t
+  int64_t batch_id = -1;        // trace: sequence number of the batch in hand
+  Clock::time_point t_hand;     // trace: when the scheduler handed it over
   // device
   DevBuf xyz, ctr, info, dig[4], jobs, jobmap, tiles, flags, scal, dense, topi, topv, y, g, ctrd;
   DevBuf tinfo, hist, thr, cand_j, cand_n, cand_v, rowtab, pre, prerep, segs;
   // pinned host
   HostBuf hxyz, htab, hjobs, hback, hsc, htopi, htopv, htri, hcand_n, hpre, hsegs;
+  std::vector<void *> retired;  // replaced pinned buffers, freed when the server is destroyed
 };
 
 }  // namespace
@@ -158,9 +168,14 @@ struct bs_server {
   bool stop = false;
   std::thread sched, clus;
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  cudaMemPool_t pool = nullptr;  // the slots' device buffers
   std::string err;
   // stats
   std::vector<double> lat, clat;
+  // optional trace (BS_SERVER_TRACE=<file>): one line per batch and request,
+  // written when the server is destroyed
+  std::string trace_path;
+  std::vector<std::string> trace;
   int64_t qdone = 0, cdone = 0, pairs = 0, batches = 0, fallbacks = 0, rows_batched = 0;
   std::atomic<int64_t> screened{0};  // updated by launches that run without the lock
   bs::Clock::time_point t0;
@@ -170,39 +185,51 @@ namespace bs {
 namespace {
 
 // ------------------------------------------------------------ memory
-bool sv_ensure(bs_server *s, DevBuf &b, size_t bytes) {
+// Slot buffers come from the server's own stream-ordered pool: growing one
+// frees and allocates on the slot's stream, so it never waits for the other
+// slots' batches (cudaFree would synchronise the whole device).  The slot's
+// stream is idle or nearly so when a buffer grows (its previous batch has
+// completed on the host), and it is synchronised after the allocation so the
+// buffer is usable from the slot's other stream too.
+bool sv_ensure(bs_server *s, Slot &sl, DevBuf &b, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (b.cap >= bytes) return true;
+  const Clock::time_point t0 = Clock::now();
   if (b.p) {
-    cudaFree(b.p);
+    cudaFreeAsync(b.p, sl.st);
     s->used -= b.cap;
     b.p = nullptr;
     b.cap = 0;
   }
   bytes = bytes + bytes / 4;  // headroom: batches vary in size
-  if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+  if (cudaMallocFromPoolAsync(&b.p, bytes, s->pool, sl.st) != cudaSuccess || cudaStreamSynchronize(sl.st) != cudaSuccess) {
     cudaGetLastError();
     b.p = nullptr;
     return false;
   }
   s->used += bytes;
   b.cap = bytes;
+  ++t_grow_dev;
+  t_grow_ms += ms_between(t0, Clock::now());
   return true;
 }
 
-void sv_release(bs_server *s, DevBuf &b) {
+void sv_release(bs_server *s, Slot &sl, DevBuf &b) {
   if (b.p) {
-    cudaFree(b.p);
+    cudaFreeAsync(b.p, sl.st);
     s->used -= b.cap;
   }
   b.p = nullptr;
   b.cap = 0;
 }
 
-bool host_ensure(HostBuf &h, size_t bytes) {
+// Pinned host buffers: a replaced buffer is kept until the server is
+// destroyed (cudaFreeHost would synchronise the device).
+bool host_ensure(Slot &sl, HostBuf &h, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (h.cap >= bytes) return true;
-  if (h.p) cudaFreeHost(h.p);
+  const Clock::time_point t0 = Clock::now();
+  if (h.p) sl.retired.push_back(h.p);
   h.p = nullptr;
   h.cap = 0;
   bytes = bytes + bytes / 4;
@@ -211,24 +238,38 @@ bool host_ensure(HostBuf &h, size_t bytes) {
     return false;
   }
   h.cap = bytes;
+  ++t_grow_host;
+  t_grow_ms += ms_between(t0, Clock::now());
   return true;
 }
 
-void slot_release(bs_server *s, Slot &sl) {
-  DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
+template <typename F>
+void each_dev(Slot &sl, F f) {
+  for (DevBuf *b : {&sl.xyz,   &sl.ctr,    &sl.info,   &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
                     &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
-                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep, &sl.segs};
-  for (DevBuf *b : list) sv_release(s, *b);
+                    &sl.topv,  &sl.y,      &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,   &sl.thr,
+                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre,   &sl.prerep, &sl.segs})
+    f(*b);
+}
+
+template <typename F>
+void each_host(Slot &sl, F f) {
+  for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri,
+                     &sl.hcand_n, &sl.hpre, &sl.hsegs})
+    f(*h);
+}
+
+// Frees an idle slot's device buffers (its stream has nothing in flight)
+// and gives the pool's unused memory back to the device.
+void slot_release(bs_server *s, Slot &sl) {
+  each_dev(sl, [&](DevBuf &b) { sv_release(s, sl, b); });
+  cudaStreamSynchronize(sl.st);
+  cudaMemPoolTrimTo(s->pool, 0);
 }
 
 size_t slot_bytes(Slot &sl) {
-  DevBuf *list[] = {&sl.xyz,   &sl.ctr,   &sl.info,    &sl.dig[0], &sl.dig[1], &sl.dig[2], &sl.dig[3],
-                    &sl.jobs,  &sl.jobmap, &sl.tiles,  &sl.flags,  &sl.scal,   &sl.dense,  &sl.topi,
-                    &sl.topv,  &sl.y,     &sl.g,      &sl.ctrd,   &sl.tinfo,  &sl.hist,  &sl.thr,
-                    &sl.cand_j, &sl.cand_n, &sl.cand_v, &sl.rowtab, &sl.pre, &sl.prerep, &sl.segs};
   size_t t = 0;
-  for (DevBuf *b : list) t += b->cap;
+  each_dev(sl, [&](DevBuf &b) { t += b.cap; });
   return t;
 }
 
@@ -430,9 +471,9 @@ bool index_prescreen(bs_server *s, Slot &sl, const Plan &base, int64_t blk, int6
   Plan p1 = base;
   p1.strips = nk16 <= screen_strip_max_nk16();
   batch_tiles(s, p1, blk, nbh, nk16, p1.strips, nullptr, p1.tiles);
-  if (!sv_ensure(s, sl.pre, (size_t)rows * ldh * 4) || !sv_ensure(s, sl.prerep, (size_t)rows * (R + 1) * 4) ||
-      !host_ensure(sl.hpre, (size_t)rows * (R + 1) * 4) || !sv_ensure(s, sl.tiles, p1.tiles.size() * sizeof(Tile)) ||
-      !host_ensure(sl.htab, p1.jobmap.size() * 4 + p1.tiles.size() * sizeof(Tile)))
+  if (!sv_ensure(s, sl, sl.pre, (size_t)rows * ldh * 4) || !sv_ensure(s, sl, sl.prerep, (size_t)rows * (R + 1) * 4) ||
+      !host_ensure(sl, sl.hpre, (size_t)rows * (R + 1) * 4) || !sv_ensure(s, sl, sl.tiles, p1.tiles.size() * sizeof(Tile)) ||
+      !host_ensure(sl, sl.htab, p1.jobmap.size() * 4 + p1.tiles.size() * sizeof(Tile)))
     return false;
   uint32_t *pre = static_cast<uint32_t *>(sl.pre.p);
   for (int j = 0; j < nj; ++j) {
@@ -615,27 +656,27 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
   // the query block's digits resident in shared memory for the run; runs
   // sized for about a dozen per block of the grid.
   batch_tiles(s, plan, blk, nbb, nk16, plan.strips, nullptr, plan.tiles);
-  bool ok = sv_ensure(s, sl.xyz, xyz_off * 8) && sv_ensure(s, sl.dense, (size_t)rows * ld * 4) &&
-            sv_ensure(s, sl.topi, (size_t)rows * k * 8) && sv_ensure(s, sl.topv, (size_t)rows * k * 4) &&
-            sv_ensure(s, sl.scal, sizeof(DevScalars)) && host_ensure(sl.hxyz, xyz_off * 8) &&
-            host_ensure(sl.htopi, (size_t)rows * k * 8) && host_ensure(sl.htopv, (size_t)rows * k * 4) &&
-            host_ensure(sl.hsc, sizeof(DevScalars));
+  bool ok = sv_ensure(s, sl, sl.xyz, xyz_off * 8) && sv_ensure(s, sl, sl.dense, (size_t)rows * ld * 4) &&
+            sv_ensure(s, sl, sl.topi, (size_t)rows * k * 8) && sv_ensure(s, sl, sl.topv, (size_t)rows * k * 4) &&
+            sv_ensure(s, sl, sl.scal, sizeof(DevScalars)) && host_ensure(sl, sl.hxyz, xyz_off * 8) &&
+            host_ensure(sl, sl.htopi, (size_t)rows * k * 8) && host_ensure(sl, sl.htopv, (size_t)rows * k * 4) &&
+            host_ensure(sl, sl.hsc, sizeof(DevScalars));
   if (plain) {
-    ok = ok && sv_ensure(s, sl.y, (size_t)rows * 3 * bk.lp * 8) && sv_ensure(s, sl.g, (size_t)rows * 8) &&
-         sv_ensure(s, sl.ctrd, (size_t)rows * 24);
+    ok = ok && sv_ensure(s, sl, sl.y, (size_t)rows * 3 * bk.lp * 8) && sv_ensure(s, sl, sl.g, (size_t)rows * 8) &&
+         sv_ensure(s, sl, sl.ctrd, (size_t)rows * 24);
   } else {
-    ok = ok && sv_ensure(s, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl.info, (size_t)ns * 16) &&
-         sv_ensure(s, sl.jobs, (size_t)nj * sizeof(Job)) && sv_ensure(s, sl.jobmap, plan.jobmap.size() * 4) &&
-         sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl.flags, kServerFlagCap * 8) &&
-         host_ensure(sl.hjobs, (size_t)nj * sizeof(Job)) && host_ensure(sl.hback, (size_t)nj * sizeof(Job)) &&
-         host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16);
-    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * bk.pitch * 2);
+    ok = ok && sv_ensure(s, sl, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl, sl.info, (size_t)ns * 16) &&
+         sv_ensure(s, sl, sl.jobs, (size_t)nj * sizeof(Job)) && sv_ensure(s, sl, sl.jobmap, plan.jobmap.size() * 4) &&
+         sv_ensure(s, sl, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl, sl.flags, kServerFlagCap * 8) &&
+         host_ensure(sl, sl.hjobs, (size_t)nj * sizeof(Job)) && host_ensure(sl, sl.hback, (size_t)nj * sizeof(Job)) &&
+         host_ensure(sl, sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16);
+    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl, sl.dig[d], (size_t)drows * bk.pitch * 2);
     if (sl.screen)
-      ok = ok && sv_ensure(s, sl.tinfo, (size_t)ns * 8) && sv_ensure(s, sl.hist, (size_t)rows * kScreenBins * 4) &&
-           sv_ensure(s, sl.thr, (size_t)rows * 4) &&
-           sv_ensure(s, sl.cand_j, (size_t)rows * kCandCap * 4) &&
-           sv_ensure(s, sl.cand_n, (size_t)rows * 4) && sv_ensure(s, sl.cand_v, (size_t)rows * kCandCap * 4) &&
-           sv_ensure(s, sl.rowtab, (size_t)rows * 12 + 8) && host_ensure(sl.hcand_n, (size_t)rows * 4);
+      ok = ok && sv_ensure(s, sl, sl.tinfo, (size_t)ns * 8) && sv_ensure(s, sl, sl.hist, (size_t)rows * kScreenBins * 4) &&
+           sv_ensure(s, sl, sl.thr, (size_t)rows * 4) &&
+           sv_ensure(s, sl, sl.cand_j, (size_t)rows * kCandCap * 4) &&
+           sv_ensure(s, sl, sl.cand_n, (size_t)rows * 4) && sv_ensure(s, sl, sl.cand_v, (size_t)rows * kCandCap * 4) &&
+           sv_ensure(s, sl, sl.rowtab, (size_t)rows * 12 + 8) && host_ensure(sl, sl.hcand_n, (size_t)rows * 4);
   }
   if (!ok) return BS_ERR_OOM;
   // coordinates in
@@ -663,8 +704,8 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
       }
       if (cudaMemcpyAsync(dx, hx, xyz_off * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess) return BS_ERR_CUDA;
       batch_tiles(s, plan, blk, nbb, nk16, plan.strips, &need, plan.tiles);
-      if (!sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) ||
-          !host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16))
+      if (!sv_ensure(s, sl, sl.tiles, plan.tiles.size() * sizeof(Tile)) ||
+          !host_ensure(sl, sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile) + (size_t)rows * 12 + 16))
         return BS_ERR_OOM;
     }
   }
@@ -703,7 +744,7 @@ bs_status launch_query_batch(bs_server *s, Slot &sl, bool screen) {
           }
         }
       }
-      if (!sv_ensure(s, sl.segs, segs.size() * sizeof(SelSeg)) || !host_ensure(sl.hsegs, segs.size() * sizeof(SelSeg)))
+      if (!sv_ensure(s, sl, sl.segs, segs.size() * sizeof(SelSeg)) || !host_ensure(sl, sl.hsegs, segs.size() * sizeof(SelSeg)))
         return BS_ERR_OOM;
       memcpy(sl.hsegs.p, segs.data(), segs.size() * sizeof(SelSeg));
       if (cudaMemcpyAsync(sl.segs.p, sl.hsegs.p, segs.size() * sizeof(SelSeg), cudaMemcpyHostToDevice, sl.st) !=
@@ -803,8 +844,8 @@ bs_status plain_fallback(bs_server *s, Slot &sl, int j) {
   const Bucket &bk = s->buckets[sl.bucket];
   const Request *r = sl.reqs[j];
   const int k = s->top_k;
-  if (!sv_ensure(s, sl.y, (size_t)r->q * 3 * bk.lp * 8) || !sv_ensure(s, sl.g, (size_t)r->q * 8) ||
-      !sv_ensure(s, sl.ctrd, (size_t)r->q * 24) || !sv_ensure(s, sl.xyz, r->xyz.size() * 8))
+  if (!sv_ensure(s, sl, sl.y, (size_t)r->q * 3 * bk.lp * 8) || !sv_ensure(s, sl, sl.g, (size_t)r->q * 8) ||
+      !sv_ensure(s, sl, sl.ctrd, (size_t)r->q * 24) || !sv_ensure(s, sl, sl.xyz, r->xyz.size() * 8))
     return BS_ERR_OOM;
   float *dense = static_cast<float *>(sl.dense.p) + sl.row0[j] * bk.n;
   OutDesc od{dense, r->q, bk.n, kLayoutRect, 1};
@@ -835,9 +876,9 @@ bs_status launch_cluster_batch(bs_server *s, Slot &sl) {
   Request *r = sl.reqs[0];
   const int64_t n = r->q;
   const size_t tri = (size_t)(n * (n - 1) / 2);
-  if (!sv_ensure(s, sl.xyz, r->xyz.size() * 8) || !sv_ensure(s, sl.dense, tri * 4) ||
-      !host_ensure(sl.htri, tri * 4) || !host_ensure(sl.hxyz, r->xyz.size() * 8) ||
-      !sv_ensure(s, sl.scal, sizeof(DevScalars)) || !host_ensure(sl.hsc, sizeof(DevScalars)))
+  if (!sv_ensure(s, sl, sl.xyz, r->xyz.size() * 8) || !sv_ensure(s, sl, sl.dense, tri * 4) ||
+      !host_ensure(sl, sl.htri, tri * 4) || !host_ensure(sl, sl.hxyz, r->xyz.size() * 8) ||
+      !sv_ensure(s, sl, sl.scal, sizeof(DevScalars)) || !host_ensure(sl, sl.hsc, sizeof(DevScalars)))
     return BS_ERR_OOM;
   memcpy(sl.hxyz.p, r->xyz.data(), r->xyz.size() * 8);
   if (cudaMemcpyAsync(sl.xyz.p, sl.hxyz.p, r->xyz.size() * 8, cudaMemcpyHostToDevice, sl.st) != cudaSuccess)
@@ -846,8 +887,8 @@ bs_status launch_cluster_batch(bs_server *s, Slot &sl) {
                                      OutDesc{sl.dense.p, n, n, kLayoutTriangle, 1}}};
   if (s->precision == BS_PRECISION_PLAIN64) {
     const int lp = lp_for(r->L);
-    if (!sv_ensure(s, sl.y, (size_t)n * 3 * lp * 8) || !sv_ensure(s, sl.g, (size_t)n * 8) ||
-        !sv_ensure(s, sl.ctrd, (size_t)n * 24))
+    if (!sv_ensure(s, sl, sl.y, (size_t)n * 3 * lp * 8) || !sv_ensure(s, sl, sl.g, (size_t)n * 8) ||
+        !sv_ensure(s, sl, sl.ctrd, (size_t)n * 24))
       return BS_ERR_OOM;
     DevScalars *sc = static_cast<DevScalars *>(sl.scal.p);
     if (cudaMemsetAsync(sc, 0, sizeof(DevScalars), sl.st) != cudaSuccess ||
@@ -861,12 +902,12 @@ bs_status launch_cluster_batch(bs_server *s, Slot &sl) {
     Plan plan;
     if (!make_symmetric_plan(specs, s->tol, true, plan).empty()) return BS_ERR_UNSUPPORTED;
     const int64_t ns = plan.nblocks * kBlockStructs, drows = plan.nblocks * kBlockRows;
-    bool ok = sv_ensure(s, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl.info, (size_t)ns * 16) &&
-              sv_ensure(s, sl.jobs, sizeof(Job)) && sv_ensure(s, sl.jobmap, plan.jobmap.size() * 4) &&
-              sv_ensure(s, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl.flags, kServerFlagCap * 8) &&
-              host_ensure(sl.hjobs, sizeof(Job)) && host_ensure(sl.hback, sizeof(Job)) &&
-              host_ensure(sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile));
-    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl.dig[d], (size_t)drows * plan.pitch * 2);
+    bool ok = sv_ensure(s, sl, sl.ctr, (size_t)ns * 24) && sv_ensure(s, sl, sl.info, (size_t)ns * 16) &&
+              sv_ensure(s, sl, sl.jobs, sizeof(Job)) && sv_ensure(s, sl, sl.jobmap, plan.jobmap.size() * 4) &&
+              sv_ensure(s, sl, sl.tiles, plan.tiles.size() * sizeof(Tile)) && sv_ensure(s, sl, sl.flags, kServerFlagCap * 8) &&
+              host_ensure(sl, sl.hjobs, sizeof(Job)) && host_ensure(sl, sl.hback, sizeof(Job)) &&
+              host_ensure(sl, sl.htab, plan.jobmap.size() * 4 + plan.tiles.size() * sizeof(Tile));
+    for (int d = 0; d < 4 && ok; ++d) ok = sv_ensure(s, sl, sl.dig[d], (size_t)drows * plan.pitch * 2);
     if (!ok) return BS_ERR_OOM;
     MixedBuffers b{};
     b.ctr = static_cast<long long *>(sl.ctr.p);
@@ -904,12 +945,91 @@ bs_status launch_cluster_batch(bs_server *s, Slot &sl) {
   return BS_OK;
 }
 
+// Sizes every slot's buffers for a full batch of each bucket before the
+// server takes requests, so that no buffer grows while requests wait.  Slot
+// 0 runs one batch of max_rows library structures (requests of 64) per
+// bucket and the other slots take the same capacities.  Buckets whose full
+// batch the budget cannot hold in every slot are skipped (their buffers grow
+// on demand), and so is the plain FP64 path (its batches are slow).
+bs_status reserve_slots(bs_server *s, const bs_server_config *cfg) {
+  if (s->precision != BS_PRECISION_MIXED || s->slots.empty()) return BS_OK;
+  Slot &s0 = *s->slots[0];
+  const size_t nslots = s->slots.size();
+  for (int b = 0; b < (int)s->buckets.size(); ++b) {
+    const Bucket &bk = s->buckets[b];
+    const int L = bk.L;
+    const size_t one = (size_t)L * 3;
+    const int64_t take = std::min<int64_t>(bk.n, 64);
+    std::vector<double> src(take * one);
+    if (is_device_ptr(cfg->bucket_xyz[b])) {
+      if (cudaMemcpy(src.data(), cfg->bucket_xyz[b], src.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return BS_ERR_CUDA;
+    } else {
+      memcpy(src.data(), cfg->bucket_xyz[b], src.size() * 8);
+    }
+    std::vector<std::unique_ptr<Request>> reqs;
+    std::vector<Request *> batch;
+    for (int64_t rows = 0; rows < s->max_rows;) {
+      auto r = std::make_unique<Request>();
+      r->bucket = b;
+      r->L = L;
+      r->q = std::min<int64_t>(64, s->max_rows - rows);
+      r->xyz.resize(r->q * one);
+      for (int64_t t = 0; t < r->q; ++t)
+        memcpy(r->xyz.data() + t * one, src.data() + ((rows + t) % take) * one, one * 8);
+      rows += r->q;
+      batch.push_back(r.get());
+      reqs.push_back(std::move(r));
+    }
+    if (s->used + batch_bytes(s, batch) * 5 / 4 * nslots > s->budget) continue;
+    s0.reqs = batch;
+    s0.kind = 0;
+    s0.bucket = b;
+    bs_status st = launch_query_batch(s, s0, true);
+    if (st == BS_OK && cudaEventSynchronize(s0.ev) != cudaSuccess) st = BS_ERR_CUDA;
+    s0.reqs.clear();
+    if (st) {
+      cudaGetLastError();
+      cudaStreamSynchronize(s0.st);
+      return st;
+    }
+  }
+  std::vector<DevBuf *> d0;
+  std::vector<HostBuf *> h0;
+  each_dev(s0, [&](DevBuf &x) { d0.push_back(&x); });
+  each_host(s0, [&](HostBuf &x) { h0.push_back(&x); });
+  for (size_t i = 1; i < nslots; ++i) {
+    Slot &o = *s->slots[i];
+    size_t k = 0;
+    bool ok = true;
+    each_dev(o, [&](DevBuf &x) {
+      const size_t cap = d0[k++]->cap;
+      if (ok && cap > x.cap) ok = sv_ensure(s, o, x, cap * 4 / 5);
+    });
+    k = 0;
+    each_host(o, [&](HostBuf &x) {
+      const size_t cap = h0[k++]->cap;
+      if (ok && cap > x.cap) ok = host_ensure(o, x, cap * 4 / 5);
+    });
+    if (!ok) return BS_ERR_OOM;
+  }
+  s->screened = 0;
+  return BS_OK;
+}
+
 void complete(bs_server *s, Request *r, bs_status st, const std::string &msg) {
   r->status = st;
   r->err = msg;
   r->t_done = Clock::now();
   r->done = true;
   const double ms = ms_between(r->t_submit, r->t_done);
+  if (!s->trace_path.empty()) {
+    char line[160];
+    snprintf(line, sizeof line, "R,%lld,%d,%d,%lld,%.3f,%.3f,%lld,%d", (long long)r->id, r->kind, r->bucket,
+             (long long)r->q, ms_between(s->t0, r->t_submit), ms_between(s->t0, r->t_done), (long long)r->batch,
+             (int)st);
+    s->trace.emplace_back(line);
+  }
   if (st == BS_OK) {
     if (r->kind == 0) {
       s->lat.push_back(ms);
@@ -1250,10 +1370,21 @@ void worker_loop(bs_server *s, Slot *slp) {
     if (!sl.has_work) break;
     sl.has_work = false;
     const int kind = sl.kind;
+    const int64_t rows = kind == 0 ? [&] {
+      int64_t t = 0;
+      for (const Request *r : sl.reqs) t += r->q;
+      return t;
+    }() : sl.reqs[0]->q;
+    const int nreq = (int)sl.reqs.size(), bucket = sl.bucket;
     lk.unlock();
+    t_grow_dev = t_grow_host = 0;
+    t_grow_ms = 0.0;
+    const Clock::time_point t_lb = Clock::now();
     bs_status st = kind == 0 ? launch_query_batch(s, sl, true) : launch_cluster_batch(s, sl);
+    const Clock::time_point t_le = Clock::now();
     cudaError_t e = cudaSuccess;
     if (st == BS_OK) e = cudaEventSynchronize(sl.ev);
+    const Clock::time_point t_ev = Clock::now();
     lk.lock();
     if (st) {
       cudaGetLastError();
@@ -1264,6 +1395,19 @@ void worker_loop(bs_server *s, Slot *slp) {
       fail_batch(s, sl, BS_ERR_CUDA, cudaGetErrorString(e));
     } else {
       finish_slot(s, sl, lk);
+    }
+    if (!s->trace_path.empty()) {
+      char line[256];
+      snprintf(line, sizeof line, "B,%d,%lld,%d,%d,%lld,%d,%.3f,%.3f,%.3f,%.3f,%.3f,%d,%d,%.3f",
+               [&] {
+                 for (size_t i = 0; i < s->slots.size(); ++i)
+                   if (s->slots[i].get() == slp) return (int)i;
+                 return -1;
+               }(),
+               (long long)sl.batch_id, kind, bucket, (long long)rows, nreq, ms_between(s->t0, sl.t_hand),
+               ms_between(s->t0, t_lb), ms_between(s->t0, t_le), ms_between(s->t0, t_ev),
+               ms_between(s->t0, Clock::now()), t_grow_dev, t_grow_host, t_grow_ms);
+      s->trace.emplace_back(line);
     }
     s->cv_work.notify_one();  // the slot is free again
   }
@@ -1311,7 +1455,12 @@ void sched_loop(bs_server *s) {
         progress = true;
         continue;
       }
-      for (Request *r : batch) s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
+      for (Request *r : batch) {
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
+        r->batch = s->batches;
+      }
+      sl.batch_id = s->batches;
+      sl.t_hand = Clock::now();
       sl.busy = true;
       sl.reqs = batch;
       sl.kind = r0->kind;
@@ -1379,11 +1528,25 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
   s->max_rows = cfg->max_batch_rows > 0 ? cfg->max_batch_rows : 4096;
   s->precision = cfg->precision;
   s->tol = (float)(cfg->tolerance > 0 ? cfg->tolerance : 1e-4);
+  if (const char *tp = getenv("BS_SERVER_TRACE")) s->trace_path = tp;
   cudaSetDevice(device);
   if (mixed_tc_prepare() != cudaSuccess || screen_tc_prepare() != cudaSuccess || prep_prepare() != cudaSuccess ||
       !get_encoder(&s->encode).empty()) {
     delete s;
     return BS_ERR_CUDA;
+  }
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    uint64_t keep = UINT64_MAX;  // freed blocks stay in the pool for the next batch
+    if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      cudaGetLastError();
+      bs_server_destroy(s);
+      return BS_ERR_CUDA;
+    }
   }
   s->buckets.resize(cfg->nbuckets);
   for (int b = 0; b < cfg->nbuckets; ++b) {
@@ -1433,6 +1596,10 @@ BS_API bs_status bs_server_create(bs_server **out, int32_t device, const bs_serv
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   s->budget = cfg->hbm_budget ? cfg->hbm_budget : free_b / 2;
+  if (const bs_status st = reserve_slots(s, cfg)) {
+    bs_server_destroy(s);
+    return st;
+  }
   s->t0 = Clock::now();
   for (auto &up : s->slots) up->worker = std::thread(worker_loop, s, up.get());
   s->sched = std::thread(sched_loop, s);
@@ -1462,11 +1629,15 @@ BS_API void bs_server_destroy(bs_server *s) {
   cudaSetDevice(s->device);
   for (auto &up : s->slots) {
     Slot &sl = *up;
-    if (sl.st) cudaStreamSynchronize(sl.st);
-    slot_release(s, sl);
-    for (HostBuf *h : {&sl.hxyz, &sl.htab, &sl.hjobs, &sl.hback, &sl.hsc, &sl.htopi, &sl.htopv, &sl.htri,
-                       &sl.hcand_n, &sl.hpre, &sl.hsegs})
-      if (h->p) cudaFreeHost(h->p);
+    if (sl.pst) cudaStreamSynchronize(sl.pst);
+    if (sl.st) {
+      cudaStreamSynchronize(sl.st);
+      slot_release(s, sl);
+    }
+    each_host(sl, [](HostBuf &h) {
+      if (h.p) cudaFreeHost(h.p);
+    });
+    for (void *p : sl.retired) cudaFreeHost(p);
     if (sl.ev) cudaEventDestroy(sl.ev);
     if (sl.st) cudaStreamDestroy(sl.st);
     if (sl.pev) cudaEventDestroy(sl.pev);
@@ -1475,8 +1646,17 @@ BS_API void bs_server_destroy(bs_server *s) {
       cudaStreamDestroy(sl.pst);
     }
   }
+  if (s->pool) cudaMemPoolDestroy(s->pool);
   for (Bucket &bk : s->buckets) free_bucket(bk);
   for (auto &kv : s->reqs) delete kv.second;
+  if (!s->trace_path.empty()) {
+    if (FILE *f = fopen(s->trace_path.c_str(), "a")) {  // servers of one process append
+      fprintf(f, "# server\n# B,slot,batch,kind,bucket,rows,nreq,hand_ms,launch_begin_ms,launch_end_ms,event_ms,finish_ms,"
+                 "dev_grows,host_grows,grow_ms\n# R,id,kind,bucket,q,submit_ms,done_ms,batch,status\n");
+      for (const std::string &l : s->trace) fprintf(f, "%s\n", l.c_str());
+      fclose(f);
+    }
+  }
   delete s;
 }
 
@@ -1610,6 +1790,7 @@ BS_API bs_status bs_server_reset_stats(bs_server *s) {
   s->clat.clear();
   s->qdone = s->cdone = s->pairs = s->batches = s->fallbacks = s->rows_batched = 0;
   s->screened = 0;
+  if (!s->trace_path.empty()) s->trace.emplace_back("# reset");  // later times count from here
   s->t0 = Clock::now();
   return BS_OK;
 }

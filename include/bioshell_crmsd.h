@@ -269,7 +269,12 @@ BS_API bs_status bs_all_vs_all_static(const double *xyz, int64_t n, int32_t L, d
  * arrive while others are on the GPU are admitted as slots and memory free
  * up, and their work overlaps on the device.  Every query's result depends
  * only on the query and the library: the same alone or in any mix.
- * submit, poll, wait and stats may be called from any thread. */
+ * submit, poll, wait and stats may be called from any thread.
+ * Creation sizes every slot's device and pinned buffers for a full batch of
+ * each bucket (mixed precision, where the budget holds it), so buffers do not
+ * grow while requests wait.  With the environment variable BS_SERVER_TRACE
+ * naming a file, a server appends a per-batch and per-request timing trace
+ * to it when destroyed. */
 typedef struct bs_server bs_server;
 
 typedef struct {
