@@ -21,6 +21,7 @@
 // All of it is integer arithmetic: the FP64 pipe is not used.
 //
 // Plain path: FP64 centring into K-major [n][3][lp] and G.
+#include <limits.h>
 #include <math.h>
 
 #include "crmsd_math.cuh"
@@ -86,57 +87,112 @@ __device__ __forceinline__ Where locate(const PrepArgs &p, int64_t g) {
   return w;
 }
 
+// Each warp takes a run of kRun consecutive structures (usually all of one
+// job) and keeps the job-wide maxima of the run in registers: one atomic per
+// job change instead of one per structure (same-address atomics
+// serialise).  Runs stay short so the block scheduler balances sets of
+// different chain lengths.
+constexpr int kRun = 8;
+struct Run {
+  int64_t g0, g1;
+};
+__device__ __forceinline__ Run warp_run(int64_t nstructs) {
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  Run r;
+  r.g0 = w * kRun;
+  r.g1 = r.g0 + kRun < nstructs ? r.g0 + kRun : nstructs;
+  return r;
+}
+
+__device__ __forceinline__ long long warp_min64s(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ long long warp_max64s(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
 // ------------------------------------------------------------------ center
+// One read of the coordinates: per component the sum (centroid) and the
+// extremes; the largest centred coordinate max|v - C| is max(vmax - C,
+// C - vmin), the same value a second pass over |v - C| would find.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, int64_t nstructs) {
   const int lane = threadIdx.x & 31;
-  const int64_t g = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (g >= nstructs) return;
-  const Where w = locate(p, g);
-  if (!w.valid) return;
-  Job &jb = p.jobs[w.job];
-  const int L = jb.L;
-  const double *x = jb.xyz + w.local * 3 * (int64_t)L;
-  long long s[3] = {0, 0, 0};
-  int bad = 0;
-  int c = lane % 3;
-  for (int i = lane; i < 3 * L; i += 32) {
-    long long v;
-    bad |= to_fix(x[i], v);
-    s[0] += c == 0 ? v : 0;
-    s[1] += c == 1 ? v : 0;
-    s[2] += c == 2 ? v : 0;
-    c = (c + 2) % 3;  // (i + 32) mod 3
-  }
+  const Run run = warp_run(nstructs);
+  int cur = -1;                // job whose maximum is being gathered
+  unsigned long long mrun = 0;  // its largest centred coordinate so far
+  for (int64_t g = run.g0; g < run.g1; ++g) {
+    const Where w = locate(p, g);
+    if (!w.valid) continue;
+    if (w.job != cur) {
+      if (cur >= 0 && lane == 0) atomicMax(&p.jobs[cur].maxabs, mrun);
+      cur = w.job;
+      mrun = 0;
+    }
+    Job &jb = p.jobs[w.job];
+    const int L = jb.L;
+    const double *x = jb.xyz + w.local * 3 * (int64_t)L;
+    long long s[3] = {0, 0, 0};
+    long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+    int bad = 0;
+    int c = lane % 3;
+    // four coalesced loads in flight per lane, then their updates in order
+    for (int i0 = lane; i0 < 3 * L; i0 += 128) {
+      double xv[4];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-  if (bad) {
-    if (lane == 0) atomicOr(&jb.err, bad);
-    return;
-  }
-  long long C[3];
+      for (int u = 0; u < 4; ++u) xv[u] = i0 + 32 * u < 3 * L ? x[i0 + 32 * u] : 0.0;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const long long t = warp_sum64(s[k]);
-    const long long h = L / 2;
-    C[k] = t >= 0 ? (t + h) / L : -((-t + h) / L);
+      for (int u = 0; u < 4; ++u) {
+        if (i0 + 32 * u < 3 * L) {
+          long long v;
+          bad |= to_fix(xv[u], v);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (c == k) {
+              s[k] += v;
+              lo[k] = v < lo[k] ? v : lo[k];
+              hi[k] = v > hi[k] ? v : hi[k];
+            }
+          }
+        }
+        c = (c + 2) % 3;  // (i + 32) mod 3
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    if (bad) {
+      if (lane == 0) atomicOr(&jb.err, bad);
+      continue;
+    }
+    long long C[3];
+    unsigned long long m = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const long long t = warp_sum64(s[k]);
+      const long long h = L / 2;
+      C[k] = t >= 0 ? (t + h) / L : -((-t + h) / L);
+      const long long vlo = warp_min64s(lo[k]), vhi = warp_max64s(hi[k]);
+      const unsigned long long a0 = (unsigned long long)(vhi - C[k]), a1 = (unsigned long long)(C[k] - vlo);
+      m = a0 > m ? a0 : m;
+      m = a1 > m ? a1 : m;
+    }
+    mrun = m > mrun ? m : mrun;
+    if (lane == 0) {
+      p.ctr[3 * g + 0] = C[0];
+      p.ctr[3 * g + 1] = C[1];
+      p.ctr[3 * g + 2] = C[2];
+    }
   }
-  unsigned long long m = 0;
-  c = lane % 3;
-  for (int i = lane; i < 3 * L; i += 32) {
-    long long v;
-    to_fix(x[i], v);
-    const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
-    const unsigned long long a = (unsigned long long)(y < 0 ? -y : y);
-    m = a > m ? a : m;
-    c = (c + 2) % 3;
-  }
-  m = warp_max64(m);
-  if (lane == 0) {
-    p.ctr[3 * g + 0] = C[0];
-    p.ctr[3 * g + 1] = C[1];
-    p.ctr[3 * g + 2] = C[2];
-    atomicMax(&jb.maxabs, m);
-  }
+  if (cur >= 0 && lane == 0) atomicMax(&p.jobs[cur].maxabs, mrun);
 }
 
 // ------------------------------------------------------------------- scale
@@ -167,43 +223,63 @@ __global__ void k_mx_scale(PrepArgs p) {
 // ---------------------------------------------------------------- norms
 // Row norms of the digits per candidate grid, over the whole chain, its two
 // halves and its four quarters (the accumulator parts of a long-layout
-// tile).  The three coordinate rows are done one after another.
+// tile).  Lane group qq (8 lanes) takes quarter qq of the chain, an atom
+// (all three coordinate rows) per lane-step; the 36 (row, grid, digit)
+// sums are reduced within each group, then combined across the groups into
+// half and full sums.  Unsigned sums wrap identically in any order.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, int64_t nstructs) {
   const int lane = threadIdx.x & 31;
-  const int64_t g = (int64_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (g >= nstructs) return;
-  const Where w = locate(p, g);
-  if (!w.valid) return;
-  Job &jb = p.jobs[w.job];
-  if (jb.err) return;
-  const int L = jb.L;
-  const int nk16 = jb.lp / 16;
-  const double *x = jb.xyz + w.local * 3 * (int64_t)L;
-  const int ncand = jb.fixed_scale ? 1 : 4;
-  const int t0 = jb.scale_base + kFixBits;
-  unsigned mfull[4][3], mhalf[4][3], mquart[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; ++a)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) mfull[a][d] = mhalf[a][d] = mquart[a][d] = 0;
-  for (int r = 0; r < 3; ++r) {
-    const long long C = p.ctr[3 * g + r];
-    // the chain's quarters one after the other: quarter qq holds the 16-atom
-    // steps k16 with acc_part(k16, nk16, 4) == qq, i.e. 4 k16 in
-    // [qq nk16, (qq + 1) nk16)
-    unsigned qsum[4][3][4];  // [candidate][digit][quarter], warp totals
-#pragma unroll
-    for (int qq = 0; qq < 4; ++qq) {
-      const int k_lo = 16 * ((qq * nk16 + 3) / 4), k_hi = min(L, 16 * (((qq + 1) * nk16 + 3) / 4));
-      unsigned acc[4][3];
+  const int qq = lane >> 3, u = lane & 7;
+  const Run run = warp_run(nstructs);
+  int cur = -1;
+  unsigned rf[4][3], rh[4][3], rq[4][3];  // the current job's maxima over the run so far
+  auto flush = [&]() {
+    if (cur < 0 || lane != 0) return;
+    Job &jc = p.jobs[cur];
+    const int nc = jc.fixed_scale ? 1 : 4;
+    for (int a = 0; a < nc; ++a)
+      for (int d = 0; d < 3; ++d) {
+        atomicMax(&jc.norm[a][d], (unsigned long long)rf[a][d]);
+        atomicMax(&jc.normh[a][d], (unsigned long long)rh[a][d]);
+        atomicMax(&jc.normq[a][d], (unsigned long long)rq[a][d]);
+      }
+  };
+  for (int64_t g = run.g0; g < run.g1; ++g) {
+    const Where w = locate(p, g);
+    if (!w.valid) continue;
+    Job &jb = p.jobs[w.job];
+    if (jb.err) continue;
+    if (w.job != cur) {
+      flush();
+      cur = w.job;
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) acc[a][d] = 0;
-      for (int k = k_lo + lane; k < k_hi; k += 32) {
+        for (int d = 0; d < 3; ++d) rf[a][d] = rh[a][d] = rq[a][d] = 0;
+    }
+    const int L = jb.L;
+    const int nk16 = jb.lp / 16;
+    const double *x = jb.xyz + w.local * 3 * (int64_t)L;
+    const int ncand = jb.fixed_scale ? 1 : 4;
+    const int t0 = jb.scale_base + kFixBits;
+    const long long C[3] = {p.ctr[3 * g], p.ctr[3 * g + 1], p.ctr[3 * g + 2]};
+    // quarter qq holds the 16-atom steps k16 with acc_part(k16, nk16, 4) ==
+    // qq, i.e. 4 k16 in [qq nk16, (qq + 1) nk16)
+    const int k_lo = 16 * ((qq * nk16 + 3) / 4), k_hi = min(L, 16 * (((qq + 1) * nk16 + 3) / 4));
+    unsigned acc[3][4][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[r][a][d] = 0;
+    for (int k = k_lo + u; k < k_hi; k += 8) {
+      const double xr[3] = {x[3 * k], x[3 * k + 1], x[3 * k + 2]};
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
         long long v;
-        to_fix(x[3 * k + r], v);
-        const long long y = v - C;
+        to_fix(xr[r], v);
+        const long long y = v - C[r];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
           if (a < ncand) {
@@ -211,38 +287,40 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, in
             const int q = (int)((y + (1ll << (t - 1))) >> t);
             int e0, e1, e2;
             bsm::split_digits(q, e0, e1, e2);
-            acc[a][0] += (unsigned)(e0 * e0);
-            acc[a][1] += (unsigned)(e1 * e1);
-            acc[a][2] += (unsigned)(e2 * e2);
+            acc[r][a][0] += (unsigned)(e0 * e0);
+            acc[r][a][1] += (unsigned)(e1 * e1);
+            acc[r][a][2] += (unsigned)(e2 * e2);
           }
         }
       }
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) qsum[a][d][qq] = a < ncand ? warp_sum32(acc[a][d]) : 0u;
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       if (a >= ncand) break;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const unsigned *v = qsum[a][d];
-        const unsigned h0 = v[0] + v[1], h1 = v[2] + v[3], f = h0 + h1;
-        mfull[a][d] = f > mfull[a][d] ? f : mfull[a][d];
-        mhalf[a][d] = max(mhalf[a][d], max(h0, h1));
-        mquart[a][d] = max(mquart[a][d], max(max(v[0], v[1]), max(v[2], v[3])));
+        unsigned f = 0, h = 0, q4 = 0;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          unsigned v = acc[r][a][d];
+          v += __shfl_xor_sync(0xffffffffu, v, 4);
+          v += __shfl_xor_sync(0xffffffffu, v, 2);
+          v += __shfl_xor_sync(0xffffffffu, v, 1);  // quarter qq's sum
+          const unsigned vq = max(v, __shfl_xor_sync(0xffffffffu, v, 8));
+          const unsigned hs = v + __shfl_xor_sync(0xffffffffu, v, 8);  // half sum (quarters 0+1 or 2+3)
+          const unsigned hx = __shfl_xor_sync(0xffffffffu, hs, 16);
+          const unsigned fs = hs + hx;  // the whole chain
+          q4 = max(q4, max(vq, __shfl_xor_sync(0xffffffffu, vq, 16)));
+          h = max(h, max(hs, hx));
+          f = max(f, fs);
+        }
+        rf[a][d] = max(rf[a][d], f);
+        rh[a][d] = max(rh[a][d], h);
+        rq[a][d] = max(rq[a][d], q4);
       }
     }
   }
-  if (lane == 0) {
-    for (int a = 0; a < ncand; ++a)
-      for (int d = 0; d < 3; ++d) {
-        atomicMax(&jb.norm[a][d], (unsigned long long)mfull[a][d]);
-        atomicMax(&jb.normh[a][d], (unsigned long long)mhalf[a][d]);
-        atomicMax(&jb.normq[a][d], (unsigned long long)mquart[a][d]);
-      }
-  }
+  flush();
 }
 
 // ---------------------------------------------------------------- choose
@@ -346,17 +424,27 @@ __global__ void k_mx_digits(PrepArgs p, int64_t nstructs, int wpb) {
   long long gsum = 0;
   float rsum = 0.f;  // |r| < 2^31 units; relative rounding charged below
   int c = lane % 3;
-  for (int i = lane; i < 3 * L; i += 32) {
-    long long v;
-    to_fix(x[i], v);
-    const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
-    const int n = (int)((y + (1ll << (t - 1))) >> t);
-    const long long r = y - ((long long)n << t);
-    gsum += (long long)n * n;
-    const float rf = (float)(int)r;
-    rsum = fmaf(rf, rf, rsum);
-    q[c * p.pitch + i / 3] = n;
-    c = (c + 2) % 3;
+  // four coalesced loads in flight per lane, then their updates in order
+  for (int i0 = lane; i0 < 3 * L; i0 += 128) {
+    double xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) xv[u] = i0 + 32 * u < 3 * L ? x[i0 + 32 * u] : 0.0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + 32 * u;
+      if (i < 3 * L) {
+        long long v;
+        to_fix(xv[u], v);
+        const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
+        const int n = (int)((y + (1ll << (t - 1))) >> t);
+        const long long r = y - ((long long)n << t);
+        gsum += (long long)n * n;
+        const float rf = (float)(int)r;
+        rsum = fmaf(rf, rf, rsum);
+        q[c * p.pitch + i / 3] = n;
+      }
+      c = (c + 2) % 3;
+    }
   }
   for (int i = L + lane; i < lp; i += 32) {
     q[i] = 0;
@@ -494,7 +582,7 @@ __global__ void __launch_bounds__(kPlainThreads)
 cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st) {
   const int64_t nstructs = p.nblocks * kBlockStructs;
   if (nstructs <= 0) return cudaSuccess;
-  const unsigned gw = (unsigned)((nstructs + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const unsigned gw = (unsigned)((nstructs + kRun * kWarpsPerBlock - 1) / (kRun * kWarpsPerBlock));
   k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
   k_mx_scale<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
   k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
