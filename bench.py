@@ -13,6 +13,8 @@ One JSON line on stdout (rank 0):
             copies the coordinates in and the whole f64 triangle out;
   roofline  the tensor-core kernel: algorithmic 18*L flops/pair over its
             event-timed duration, against the measured bf16 peak;
+  streaming_roofline  the preparation pass: 48 L + 40 bytes per structure
+            over its event-timed duration, against the measured HBM rate;
   plain64   the plain FP64 GPU path on the same workload (the denominator);
   serving   a device-resident library of 200,000 decoys bucketed by chain
             length (L 64/128/256/512 at 85/9/4/2%); queries arrive as a
@@ -662,6 +664,15 @@ def run_ours(a, rank, world, local_rank):
             "frac": achieved / peak, "peak_source": f"{pk_kind} bf16 sustained",
             "issued_tflops": issued_flops(n, L) / (ms_main * 1e-3) / 1e12,
             "kernel_ms": ms_main, "traffic": traffic}
+    # the preparation (centring, grid choice, digit rows): a streaming pass;
+    # algorithmic bytes per structure: 24 L read (f64 xyz), 24 L written
+    # (four bf16 digit rows of three coordinates), 40 B of per-structure data
+    prep_bytes = float(n) * (48.0 * L + 40.0)
+    prep_gbs = prep_bytes / (phases["ms_prep"] * 1e-3) / 1e9
+    streaming = {"kernel": "k_mx_center/scale/norms/choose/digits (preparation)", "bound": "hbm",
+                 "achieved": prep_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": prep_gbs / pk["hbm_gbs"],
+                 "peak_source": f"{pk_kind} HBM copy", "bytes": prep_bytes, "ms": phases["ms_prep"],
+                 "traffic": profiled_traffic("prep")}
     cb = cpu_baseline(x, a.cpu_seconds) if rank == 0 else None
     batched = serving = None
     if rank == 0 and not (a.skip_batched and a.skip_serving):
@@ -682,7 +693,8 @@ def run_ours(a, rank, world, local_rank):
             "config": {"workload": w.name, "n": n, "L": L, "pairs": npairs, "precision": "mixed",
                        "output": "f64 packed triangle", "l2": "no flush: inputs (360 MB) and output (10 GB) exceed L2",
                        "replicas": world},
-            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "streaming_roofline": streaming,
+            "cpu_baseline": cb, "clocks": clocks,
             "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
             "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
             "superpose": superpose, "formats": formats, "hierarchical": hier,

@@ -227,22 +227,22 @@ __global__ void k_mx_scale(PrepArgs p) {
 // (all three coordinate rows) per lane-step; the 36 (row, grid, digit)
 // sums are reduced within each group, then combined across the groups into
 // half and full sums.  Unsigned sums wrap identically in any order.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, int64_t nstructs) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_mx_norms(PrepArgs p, int64_t nstructs) {
   const int lane = threadIdx.x & 31;
   const int qq = lane >> 3, u = lane & 7;
   const Run run = warp_run(nstructs);
   int cur = -1;
-  unsigned rf[4][3], rh[4][3], rq[4][3];  // the current job's maxima over the run so far
+  // the current job's maxima over the run so far, lane 3a + d holding those
+  // of grid a, digit d (every lane sees every sum after the reductions)
+  unsigned rf = 0, rh = 0, rq = 0;
   auto flush = [&]() {
-    if (cur < 0 || lane != 0) return;
+    if (cur < 0 || lane >= 12) return;
     Job &jc = p.jobs[cur];
-    const int nc = jc.fixed_scale ? 1 : 4;
-    for (int a = 0; a < nc; ++a)
-      for (int d = 0; d < 3; ++d) {
-        atomicMax(&jc.norm[a][d], (unsigned long long)rf[a][d]);
-        atomicMax(&jc.normh[a][d], (unsigned long long)rh[a][d]);
-        atomicMax(&jc.normq[a][d], (unsigned long long)rq[a][d]);
-      }
+    const int a = lane / 3, d = lane - 3 * (lane / 3);
+    if (a >= (jc.fixed_scale ? 1 : 4)) return;
+    atomicMax(&jc.norm[a][d], (unsigned long long)rf);
+    atomicMax(&jc.normh[a][d], (unsigned long long)rh);
+    atomicMax(&jc.normq[a][d], (unsigned long long)rq);
   };
   for (int64_t g = run.g0; g < run.g1; ++g) {
     const Where w = locate(p, g);
@@ -252,10 +252,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, in
     if (w.job != cur) {
       flush();
       cur = w.job;
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) rf[a][d] = rh[a][d] = rq[a][d] = 0;
+      rf = rh = rq = 0;
     }
     const int L = jb.L;
     const int nk16 = jb.lp / 16;
@@ -314,9 +311,11 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_norms(PrepArgs p, in
           h = max(h, max(hs, hx));
           f = max(f, fs);
         }
-        rf[a][d] = max(rf[a][d], f);
-        rh[a][d] = max(rh[a][d], h);
-        rq[a][d] = max(rq[a][d], q4);
+        if (lane == 3 * a + d) {
+          rf = max(rf, f);
+          rh = max(rh, h);
+          rq = max(rq, q4);
+        }
       }
     }
   }
