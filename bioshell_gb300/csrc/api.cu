@@ -6,8 +6,13 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/mman.h>
+#include <sys/syscall.h>
+#include <unistd.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1102,10 +1107,53 @@ BS_API bs_status bs_crmsd(bs_ctx *ctx, const double *a, const double *b, int32_t
   return BS_OK;
 }
 
+namespace {
+// bs_host_alloc buffers placed with mmap + mbind (their sizes, for the free)
+std::mutex g_near_mu;
+std::map<void *, size_t> g_near;
+
+// Page-locked memory on the host NUMA node of the current GPU: on systems
+// where each CPU socket has its own GPU link (Grace), copies between a GPU
+// and the other socket's memory cross the socket link and run at a fraction
+// of the GPU link's rate.  cudaHostAlloc places the pages on the node of the
+// calling thread, which may be the other socket.  Returns null where the
+// GPU reports no host NUMA node or the placement fails.
+void *alloc_near_gpu(size_t bytes) {
+#if defined(__linux__) && defined(SYS_mbind)
+  int dev = 0, numa = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&numa, cudaDevAttrHostNumaId, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  constexpr int kMaxNodes = 1024;
+  constexpr int kBits = 8 * (int)sizeof(unsigned long);
+  if (numa < 0 || numa >= kMaxNodes) return nullptr;
+  void *p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (p == MAP_FAILED) return nullptr;
+  unsigned long mask[kMaxNodes / kBits] = {};
+  mask[numa / kBits] |= 1ul << (numa % kBits);
+  const long kPreferred = 1;  // MPOL_PREFERRED: that node while it has free pages
+  if (syscall(SYS_mbind, p, bytes, kPreferred, mask, (unsigned long)kMaxNodes + 1, 0ul) != 0 ||
+      cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
+    cudaGetLastError();
+    munmap(p, bytes);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_near_mu);
+  g_near[p] = bytes;
+  return p;
+#else
+  (void)bytes;
+  return nullptr;
+#endif
+}
+}  // namespace
+
 BS_API bs_status bs_host_alloc(size_t bytes, void **out) {
   if (!out) return BS_ERR_INVALID_ARG;
   *out = nullptr;
   if (bytes == 0) return BS_OK;
+  if ((*out = alloc_near_gpu(bytes)) != nullptr) return BS_OK;
   cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1117,6 +1165,20 @@ BS_API bs_status bs_host_alloc(size_t bytes, void **out) {
 
 BS_API bs_status bs_host_free(void *p) {
   if (!p) return BS_OK;
+  size_t bytes = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_near_mu);
+    auto it = g_near.find(p);
+    if (it != g_near.end()) {
+      bytes = it->second;
+      g_near.erase(it);
+    }
+  }
+  if (bytes) {
+    const bool ok = cudaHostUnregister(p) == cudaSuccess;
+    munmap(p, bytes);
+    return ok ? BS_OK : BS_ERR_CUDA;
+  }
   return cudaFreeHost(p) == cudaSuccess ? BS_OK : BS_ERR_CUDA;
 }
 

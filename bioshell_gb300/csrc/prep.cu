@@ -87,20 +87,20 @@ __device__ __forceinline__ Where locate(const PrepArgs &p, int64_t g) {
   return w;
 }
 
-// Each warp takes a run of kRun consecutive structures (usually all of one
-// job) and keeps the job-wide maxima of the run in registers: one atomic per
-// job change instead of one per structure (same-address atomics
-// serialise).  Runs stay short so the block scheduler balances sets of
-// different chain lengths.
-constexpr int kRun = 8;
+// Each warp takes a run of consecutive structures (usually all of one job)
+// and keeps the job-wide maxima of the run in registers: one atomic per job
+// change instead of one per structure (same-address atomics serialise).
+// Runs are at most 8 structures, so the block scheduler balances sets of
+// different chain lengths, and shorter where that leaves fewer than about
+// 32 warps per SM.
 struct Run {
   int64_t g0, g1;
 };
-__device__ __forceinline__ Run warp_run(int64_t nstructs) {
+__device__ __forceinline__ Run warp_run(int64_t nstructs, int run) {
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   Run r;
-  r.g0 = w * kRun;
-  r.g1 = r.g0 + kRun < nstructs ? r.g0 + kRun : nstructs;
+  r.g0 = w * run;
+  r.g1 = r.g0 + run < nstructs ? r.g0 + run : nstructs;
   return r;
 }
 
@@ -125,9 +125,9 @@ __device__ __forceinline__ long long warp_max64s(long long v) {
 // One read of the coordinates: per component the sum (centroid) and the
 // extremes; the largest centred coordinate max|v - C| is max(vmax - C,
 // C - vmin), the same value a second pass over |v - C| would find.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, int64_t nstructs) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, int64_t nstructs, int run_len) {
   const int lane = threadIdx.x & 31;
-  const Run run = warp_run(nstructs);
+  const Run run = warp_run(nstructs, run_len);
   int cur = -1;                // job whose maximum is being gathered
   unsigned long long mrun = 0;  // its largest centred coordinate so far
   for (int64_t g = run.g0; g < run.g1; ++g) {
@@ -227,10 +227,10 @@ __global__ void k_mx_scale(PrepArgs p) {
 // (all three coordinate rows) per lane-step; the 36 (row, grid, digit)
 // sums are reduced within each group, then combined across the groups into
 // half and full sums.  Unsigned sums wrap identically in any order.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_mx_norms(PrepArgs p, int64_t nstructs) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_mx_norms(PrepArgs p, int64_t nstructs, int run_len) {
   const int lane = threadIdx.x & 31;
   const int qq = lane >> 3, u = lane & 7;
-  const Run run = warp_run(nstructs);
+  const Run run = warp_run(nstructs, run_len);
   int cur = -1;
   // the current job's maxima over the run so far, lane 3a + d holding those
   // of grid a, digit d (every lane sees every sum after the reductions)
@@ -581,10 +581,15 @@ __global__ void __launch_bounds__(kPlainThreads)
 cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st) {
   const int64_t nstructs = p.nblocks * kBlockStructs;
   if (nstructs <= 0) return cudaSuccess;
-  const unsigned gw = (unsigned)((nstructs + kRun * kWarpsPerBlock - 1) / (kRun * kWarpsPerBlock));
-  k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t per = nstructs / ((int64_t)nsm * 32);
+  const int run = per < 1 ? 1 : (per > 8 ? 8 : (int)per);
+  const unsigned gw = (unsigned)((nstructs + (int64_t)run * kWarpsPerBlock - 1) / ((int64_t)run * kWarpsPerBlock));
+  k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs, run);
   k_mx_scale<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
-  k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs);
+  k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs, run);
   k_mx_choose<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
   const size_t per_warp = (size_t)3 * p.pitch * sizeof(int);
   int wpb = (int)(196608 / per_warp);

@@ -192,3 +192,32 @@ def test_library_index_keeps_results(oracle_mod, enginelib):
     finally:
         plain.close()
         indexed.close()
+
+
+def test_trace_records_batches_and_requests(library, enginelib, tmp_path, monkeypatch):
+    """BS_SERVER_TRACE: one B line per batch and one R line per request, written
+    when the server is destroyed; results are the same as without the trace."""
+    from bioshell_gb300 import CrmsdServer
+    lib, _, _ = library
+    path = tmp_path / "trace.csv"
+    x = _queries(library, 64, 5, 9)
+    plain = CrmsdServer(lib, top_k=TOPK, max_inflight=2)
+    want = plain.wait(plain.submit(x))
+    plain.close()
+    monkeypatch.setenv("BS_SERVER_TRACE", str(path))
+    s = CrmsdServer(lib, top_k=TOPK, max_inflight=2)
+    monkeypatch.delenv("BS_SERVER_TRACE")
+    tickets = [s.submit(x), s.submit(_queries(library, 128, 3, 10))]
+    got = s.wait(tickets[0])
+    s.wait(tickets[1])
+    s.close()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    lines = path.read_text().splitlines()
+    assert lines[0] == "# server"
+    b = [ln.split(",") for ln in lines if ln.startswith("B,")]
+    r = [ln.split(",") for ln in lines if ln.startswith("R,")]
+    assert len(r) == 2 and {int(f[4]) for f in r} == {5, 3}
+    assert len(b) >= 1 and sum(int(f[5]) for f in b) == 8
+    for f in r:  # submitted before completed, carried by a traced batch, status OK
+        assert float(f[5]) <= float(f[6]) and int(f[8]) == 0
+        assert int(f[7]) in {int(g[2]) for g in b}
