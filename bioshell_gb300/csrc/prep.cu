@@ -394,9 +394,10 @@ __global__ void k_mx_choose(PrepArgs p) {
 }
 
 // ---------------------------------------------------------------- digits
-// Warp per structure.  Pass 1 reads the AoS coordinates coalesced and keeps
-// the quantised values in shared memory (three rows of pitch ints); pass 2
-// writes the digit rows 16 bytes at a time.
+// Warp per structure, in chunks of 256 atoms.  Pass 1 reads a chunk's AoS
+// coordinates coalesced and keeps the quantised values in shared memory
+// (three rows of 256 ints: 3 KB per warp whatever the chain length); pass 2
+// writes the chunk's digit rows 16 bytes at a time.
 __device__ __forceinline__ uint32_t bf16x2(int lo, int hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn((float)lo, (float)hi);
   return *reinterpret_cast<const uint32_t *>(&v);
@@ -406,77 +407,90 @@ __device__ __forceinline__ uint32_t bf16x2s(int lo, int hi) {  // (d2/32) of bot
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-__global__ void k_mx_digits(PrepArgs p, int64_t nstructs, int wpb) {
-  extern __shared__ int qsm[];
+constexpr int kDigitWarps = 8;
+constexpr int kChunkAtoms = 256;  // atoms staged per warp at a time: 768 coordinates, a multiple of 32
+
+__global__ void __launch_bounds__(kDigitWarps * 32) k_mx_digits(PrepArgs p, int64_t nstructs) {
+  __shared__ int qsm[kDigitWarps][3 * kChunkAtoms];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t g = (int64_t)blockIdx.x * wpb + wib;
+  const int64_t g = (int64_t)blockIdx.x * kDigitWarps + wib;
   if (g >= nstructs) return;
   const Where w = locate(p, g);
   if (!w.valid) return;
   Job &jb = p.jobs[w.job];
   if (jb.err) return;
   const int L = jb.L, lp = jb.lp;
-  int *q = qsm + (size_t)wib * 3 * p.pitch;
+  int *q = qsm[wib];
   const double *x = jb.xyz + w.local * 3 * (int64_t)L;
   const long long C[3] = {p.ctr[3 * g], p.ctr[3 * g + 1], p.ctr[3 * g + 2]};
   const int t = jb.scale_exp + kFixBits;
   long long gsum = 0;
   float rsum = 0.f;  // |r| < 2^31 units; relative rounding charged below
-  int c = lane % 3;
-  // four coalesced loads in flight per lane, then their updates in order
-  for (int i0 = lane; i0 < 3 * L; i0 += 128) {
-    double xv[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) xv[u] = i0 + 32 * u < 3 * L ? x[i0 + 32 * u] : 0.0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + 32 * u;
-      if (i < 3 * L) {
-        long long v;
-        to_fix(xv[u], v);
-        const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
-        const int n = (int)((y + (1ll << (t - 1))) >> t);
-        const long long r = y - ((long long)n << t);
-        gsum += (long long)n * n;
-        const float rf = (float)(int)r;
-        rsum = fmaf(rf, rf, rsum);
-        q[c * p.pitch + i / 3] = n;
-      }
-      c = (c + 2) % 3;
-    }
-  }
-  for (int i = L + lane; i < lp; i += 32) {
-    q[i] = 0;
-    q[p.pitch + i] = 0;
-    q[2 * p.pitch + i] = 0;
-  }
-  __syncwarp();
-  // pass 2: 8 atoms of one row per lane-step; also the truncated structure
-  // t = n - d2 that levels 0 and 1 describe (sum of t^2, sum of d2^2)
-  const int chunks = lp / 8;
   long long gt = 0;
   int d2s = 0;
-  for (int u = lane; u < 3 * chunks; u += 32) {
-    const int r = u / chunks, k0 = (u - r * chunks) * 8;
-    int e0[8], e1[8], e2[8];
+  // The structure in chunks of kChunkAtoms atoms (the last one up to lp).  A
+  // chunk's coordinates start at a multiple of 768, so each lane visits its
+  // coordinates lane + 32 j in the same order as over the whole structure.
+  for (int a0 = 0; a0 < lp; a0 += kChunkAtoms) {
+    const int na = min(kChunkAtoms, lp - a0);         // atoms of the chunk, a multiple of 16
+    const int nreal = max(0, min(na, L - a0));        // of which real atoms
+    const double *xc = x + 3 * (int64_t)a0;
+    // pass 1: coalesced reads, four loads in flight per lane; quantised
+    // values staged by coordinate row
+    int c = lane % 3;
+    for (int i0 = lane; i0 < 3 * nreal; i0 += 128) {
+      double xv[4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int nv = q[r * p.pitch + k0 + k];
-      bsm::split_digits(nv, e0[k], e1[k], e2[k]);
-      const int d2 = e2[k] >> 4, tv = nv - d2;
-      gt += (long long)tv * tv;
-      d2s += d2 * d2;
+      for (int u = 0; u < 4; ++u) xv[u] = i0 + 32 * u < 3 * nreal ? xc[i0 + 32 * u] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = i0 + 32 * u;
+        if (i < 3 * nreal) {
+          long long v;
+          to_fix(xv[u], v);
+          const long long y = v - (c == 0 ? C[0] : (c == 1 ? C[1] : C[2]));
+          const int n = (int)((y + (1ll << (t - 1))) >> t);
+          const long long r = y - ((long long)n << t);
+          gsum += (long long)n * n;
+          const float rf = (float)(int)r;
+          rsum = fmaf(rf, rf, rsum);
+          q[c * kChunkAtoms + i / 3] = n;
+        }
+        c = (c + 2) % 3;
+      }
     }
-    const int64_t off = digit_row(g, r) * p.pitch + k0;
-    uint4 v0, v1, v2, v3;
-    v0.x = bf16x2(e0[0], e0[1]); v0.y = bf16x2(e0[2], e0[3]); v0.z = bf16x2(e0[4], e0[5]); v0.w = bf16x2(e0[6], e0[7]);
-    v1.x = bf16x2(e1[0], e1[1]); v1.y = bf16x2(e1[2], e1[3]); v1.z = bf16x2(e1[4], e1[5]); v1.w = bf16x2(e1[6], e1[7]);
-    v2.x = bf16x2(e2[0], e2[1]); v2.y = bf16x2(e2[2], e2[3]); v2.z = bf16x2(e2[4], e2[5]); v2.w = bf16x2(e2[6], e2[7]);
-    v3.x = bf16x2s(e2[0], e2[1]); v3.y = bf16x2s(e2[2], e2[3]); v3.z = bf16x2s(e2[4], e2[5]); v3.w = bf16x2s(e2[6], e2[7]);
-    *reinterpret_cast<uint4 *>(p.dig[0] + off) = v0;
-    *reinterpret_cast<uint4 *>(p.dig[1] + off) = v1;
-    *reinterpret_cast<uint4 *>(p.dig[2] + off) = v2;
-    *reinterpret_cast<uint4 *>(p.dig[3] + off) = v3;
+    for (int i = nreal + lane; i < na; i += 32) {  // padding atoms
+      q[i] = 0;
+      q[kChunkAtoms + i] = 0;
+      q[2 * kChunkAtoms + i] = 0;
+    }
+    __syncwarp();
+    // pass 2: 8 atoms of one row per lane-step; also the truncated structure
+    // t = n - d2 that levels 0 and 1 describe (sum of t^2, sum of d2^2)
+    const int chunks = na / 8;
+    for (int u = lane; u < 3 * chunks; u += 32) {
+      const int r = u / chunks, k0 = (u - r * chunks) * 8;
+      int e0[8], e1[8], e2[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int nv = q[r * kChunkAtoms + k0 + k];
+        bsm::split_digits(nv, e0[k], e1[k], e2[k]);
+        const int d2 = e2[k] >> 4, tv = nv - d2;
+        gt += (long long)tv * tv;
+        d2s += d2 * d2;
+      }
+      const int64_t off = digit_row(g, r) * p.pitch + a0 + k0;
+      uint4 v0, v1, v2, v3;
+      v0.x = bf16x2(e0[0], e0[1]); v0.y = bf16x2(e0[2], e0[3]); v0.z = bf16x2(e0[4], e0[5]); v0.w = bf16x2(e0[6], e0[7]);
+      v1.x = bf16x2(e1[0], e1[1]); v1.y = bf16x2(e1[2], e1[3]); v1.z = bf16x2(e1[4], e1[5]); v1.w = bf16x2(e1[6], e1[7]);
+      v2.x = bf16x2(e2[0], e2[1]); v2.y = bf16x2(e2[2], e2[3]); v2.z = bf16x2(e2[4], e2[5]); v2.w = bf16x2(e2[6], e2[7]);
+      v3.x = bf16x2s(e2[0], e2[1]); v3.y = bf16x2s(e2[2], e2[3]); v3.z = bf16x2s(e2[4], e2[5]); v3.w = bf16x2s(e2[6], e2[7]);
+      *reinterpret_cast<uint4 *>(p.dig[0] + off) = v0;
+      *reinterpret_cast<uint4 *>(p.dig[1] + off) = v1;
+      *reinterpret_cast<uint4 *>(p.dig[2] + off) = v2;
+      *reinterpret_cast<uint4 *>(p.dig[3] + off) = v3;
+    }
+    __syncwarp();  // the next chunk overwrites the staged rows
   }
   gsum = warp_sum64(gsum);
 #pragma unroll
@@ -591,20 +605,17 @@ cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st) {
   k_mx_scale<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
   k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs, run);
   k_mx_choose<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
-  const size_t per_warp = (size_t)3 * p.pitch * sizeof(int);
-  int wpb = (int)(196608 / per_warp);
-  wpb = wpb > 8 ? 8 : (wpb < 1 ? 1 : wpb);
-  k_mx_digits<<<(unsigned)((nstructs + wpb - 1) / wpb), wpb * 32, wpb * per_warp, st>>>(p, nstructs, wpb);
+  k_mx_digits<<<(unsigned)((nstructs + kDigitWarps - 1) / kDigitWarps), kDigitWarps * 32, 0, st>>>(p, nstructs);
   return cudaGetLastError();
 }
 
 // Largest digit-row pitch (atoms) the preparation pass supports.
-int prep_max_pitch() { return 196608 / (3 * (int)sizeof(int)); }
+// The mixed path's longest chain (digit row pitch, atoms).
+int prep_max_pitch() { return 16384; }
 
-// Kernel attributes, set once per device before any launch or capture.
-cudaError_t prep_prepare() {
-  return cudaFuncSetAttribute(k_mx_digits, cudaFuncAttributeMaxDynamicSharedMemorySize, 196608);
-}
+// Kernel attributes, set once per device before any launch or capture (the
+// preparation kernels need none).
+cudaError_t prep_prepare() { return cudaSuccess; }
 
 cudaError_t launch_prep_plain(const double *xyz, int64_t n, int L, int lp, double *ctr, double *y, double *g,
                               int *err, cudaStream_t st) {
