@@ -89,6 +89,23 @@ def test_ragged_shapes(engine, oracle_mod, n, L):
     assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
 
 
+def test_far_and_lopsided_coordinates(engine, oracle_mod):
+    """Structures up to 30,000 A from the origin (inside the fixed-point range
+    of 2^15 A), of different sizes in one set, and lopsided ones whose
+    centroid lies far from the middle of their extent (one atom 200 A out):
+    the centring, the grid choice and the digits must stay within tolerance
+    of the FP64 oracle on every pair."""
+    rng = np.random.default_rng(29)
+    x = synth.decoys(synth.base_chain(270, rng), 48, rng, near_dup_frac=0.1)
+    x += rng.uniform(-30000.0, 30000.0, size=(48, 1, 3))
+    x[3:9, 17] += np.array([200.0, -150.0, 90.0])  # one atom far out in six structures
+    c = x[20:24].mean(axis=1, keepdims=True)
+    x[20:24] = c + 1.5 * (x[20:24] - c)  # larger structures in the same set
+    ref = oracle_mod.crmsd_all_vs_all(x)
+    assert np.abs(engine.all_vs_all(x).values - ref).max() <= TOL_MIXED
+    assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
+
+
 def test_duplicates_and_rigid_copies(engine, oracle_mod):
     rng = np.random.default_rng(5)
     x = synth.decoys(synth.base_chain(300, rng), 60, rng, sigma=(0.2, 2.0))
