@@ -84,7 +84,9 @@ struct Readback {
 };
 
 // Band boundaries for a single symmetric job of n structures: whole
-// super-rows, about `bands` bands of equal pair counts.
+// super-rows, about `bands` bands of equal pair counts, the last two bands'
+// worth split in halves down to a sixteenth of a band (the last band's copy
+// is the part of the read-back that no computation hides).
 void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb);
 
 // Enqueues the mixed-path sequence of a plan whose tables are on the

@@ -117,7 +117,11 @@ void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb) {
     const int64_t s = plan.tiles[t].a_blk / SA;
     if (s == plan.tiles[t - 1].a_blk / SA) continue;
     const int64_t e = off(std::min(n, s * SA * kBlockStructs));
-    if (e - last >= want) {
+    // equal bands, then each half of what is left (down to a sixteenth of a
+    // band): the copy of the last band, which nothing hides, stays short
+    const int64_t rem = total - last;
+    const int64_t target = rem > 2 * want ? want : std::max<int64_t>(rem / 2, std::max<int64_t>(1, want / 16));
+    if (e - last >= target) {
       rb.tile_end.push_back(t);
       rb.elem_end.push_back(e);
       last = e;
