@@ -277,11 +277,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_mx_norms(PrepArgs p,
         long long v;
         to_fix(xr[r], v);
         const long long y = v - C[r];
+        // round-half-up of y / 2^(t0 + a) is ((w >> a) + 1) >> 1 with
+        // w = floor(y / 2^(t0 - 1)); |w| <= 2^23 (the grid bounds every
+        // centred coordinate by 2^22 2^t0), so the candidates are 32-bit
+        const int wv = (int)(y >> (t0 - 1));
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
           if (a < ncand) {
-            const int t = t0 + a;
-            const int q = (int)((y + (1ll << (t - 1))) >> t);
+            const int q = ((wv >> a) + 1) >> 1;
             int e0, e1, e2;
             bsm::split_digits(q, e0, e1, e2);
             acc[r][a][0] += (unsigned)(e0 * e0);
