@@ -1244,6 +1244,19 @@ BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n,
 }
 
 // ------------------------------------------------------------ test hooks
+BS_API bs_status bs_selftest_bands(int64_t n, int32_t bands, int64_t *elem_end, int32_t cap, int32_t *count) {
+  if (n < 2 || bands < 1 || !elem_end || !count || cap < 1) return BS_ERR_INVALID_ARG;
+  std::vector<JobSpec> specs{JobSpec{nullptr, n, 16, OutDesc{nullptr, n, n, kLayoutTriangle, 0, 0.f, 0}}};
+  Plan plan;
+  if (!make_symmetric_plan(specs, (float)kDefaultTol, true, plan).empty()) return BS_ERR_UNSUPPORTED;
+  Readback rb;
+  make_bands(plan, n, bands, rb);
+  *count = (int32_t)rb.elem_end.size();
+  if (*count > cap) return BS_ERR_INVALID_ARG;
+  for (int32_t i = 0; i < *count; ++i) elem_end[i] = rb.elem_end[i];
+  return BS_OK;
+}
+
 BS_API bs_status bs_selftest_digits(const double *xyz, int32_t L, int32_t scale_exp, int32_t *digits,
                                     int64_t *g_exact, double *qres) {
   if (!xyz || !digits || !g_exact || !qres || L < 1) return BS_ERR_INVALID_ARG;

@@ -117,6 +117,7 @@ void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb) {
     const int64_t s = plan.tiles[t].a_blk / SA;
     if (s == plan.tiles[t - 1].a_blk / SA) continue;
     const int64_t e = off(std::min(n, s * SA * kBlockStructs));
+    if (e >= total) break;  // the rest holds no pairs: it joins the last band
     // equal bands, then each half of what is left (down to a sixteenth of a
     // band): the copy of the last band, which nothing hides, stays short
     const int64_t rem = total - last;

@@ -140,6 +140,7 @@ SIGNATURES = [
                                               _i32p]),
     ("bs_selftest_exact", ctypes.c_int32, [_i32p, _i32p, ctypes.c_int32, ctypes.c_int32, _dp]),
     ("bs_selftest_superpose", ctypes.c_int32, [_vp, _vp, ctypes.c_int32, _vp, _vp, _vp]),
+    ("bs_selftest_bands", ctypes.c_int32, [ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32, _vp]),
     ("bs_selftest_screen", ctypes.c_int32, [_fp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                             ctypes.c_int32, _fp, _fp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),

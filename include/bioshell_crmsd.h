@@ -441,6 +441,10 @@ BS_API bs_status bs_host_free(void *p);
  * CPU test-suite can check the exact-digit algebra without a GPU.  They are
  * never used by the compute entry points above. */
 
+/* The row bands of the banded read-back for one set of n structures asked
+ * for in `bands` bands: writes the packed-triangle index at which each band
+ * ends (the last is n(n-1)/2) and their count (at most cap).  Host only. */
+BS_API bs_status bs_selftest_bands(int64_t n, int32_t bands, int64_t *elem_end, int32_t cap, int32_t *count);
 /* Digits of one structure's centred coordinates at grid 2^scale_exp:
  * digits[3][3][L] (digit-major, then coordinate, then atom) as stored, i.e.
  * e0, e1 and e2 = 16 d2 with n = 2^14 e0 + 2^5 e1 + d2, plus the exact
