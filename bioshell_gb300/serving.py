@@ -115,3 +115,57 @@ class CrmsdServer:
 
     def reset_stats(self):
         self._check(self._lib.bs_server_reset_stats(self._h))
+
+
+# ---- the server's timing trace (BS_SERVER_TRACE) ---------------------------
+_B_FIELDS = ("slot", "batch", "kind", "bucket", "rows", "nreq", "hand_ms", "launch_begin_ms", "launch_end_ms",
+             "event_ms", "finish_ms", "dev_grows", "host_grows", "grow_ms")
+_R_FIELDS = ("id", "kind", "bucket", "q", "submit_ms", "done_ms", "batch", "status")
+
+
+def read_trace(path: str):
+    """Parse a trace written by a server created with ``BS_SERVER_TRACE=path``.
+
+    Returns one dict per server in the file (servers of one process append),
+    each with ``segments``: the records between ``reset_stats`` calls (times
+    count from the latest reset), each a dict of ``batches`` and
+    ``requests`` (lists of dicts keyed by the trace's field names).
+    """
+    servers = []
+    with open(path) as fh:
+        for line in fh:
+            line = line.strip()
+            if line == "# server":
+                servers.append({"segments": [{"batches": [], "requests": []}]})
+            elif line == "# reset" and servers:
+                servers[-1]["segments"].append({"batches": [], "requests": []})
+            elif line[:2] in ("B,", "R,") and servers:
+                parts = line.split(",")[1:]
+                names = _B_FIELDS if line[0] == "B" else _R_FIELDS
+                rec = {k: (float(v) if k.endswith("_ms") else int(v)) for k, v in zip(names, parts)}
+                servers[-1]["segments"][-1]["batches" if line[0] == "B" else "requests"].append(rec)
+    return servers
+
+
+def slow_requests(segment: dict, percentile: float = 99.0):
+    """The query requests of one trace segment at or above the given latency
+    percentile, each with where its time went: ``wait`` (submit to hand-off
+    to a slot), ``launch`` (host work of the batch launch), ``device`` (until
+    the batch's work completed), ``finish`` (results to the requests)."""
+    import numpy as np
+    batches = {b["batch"]: b for b in segment["batches"]}
+    reqs = [r for r in segment["requests"] if r["kind"] == 0 and r["status"] == 0]
+    if not reqs:
+        return []
+    lat = np.array([r["done_ms"] - r["submit_ms"] for r in reqs])
+    cut = float(np.percentile(lat, percentile))
+    out = []
+    for r, ms in zip(reqs, lat):
+        b = batches.get(r["batch"])
+        if ms < cut or b is None:
+            continue
+        out.append({"id": r["id"], "latency_ms": float(ms), "rows": b["rows"], "slot": b["slot"],
+                    "wait": b["hand_ms"] - r["submit_ms"], "launch": b["launch_end_ms"] - b["launch_begin_ms"],
+                    "device": b["event_ms"] - b["launch_end_ms"], "finish": b["finish_ms"] - b["event_ms"],
+                    "grows": b["dev_grows"] + b["host_grows"]})
+    return sorted(out, key=lambda d: -d["latency_ms"])
