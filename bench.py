@@ -202,6 +202,15 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def fp64_peak(device):
+    """The GPU's FP64 FMA rate in FLOP/s, measured in-tree (bs_diag_fp64_peak)."""
+    import ctypes
+    from bioshell_gb300 import lib as _l
+    v = ctypes.c_double()
+    st = _l.load().bs_diag_fp64_peak(int(device), ctypes.byref(v))
+    return v.value if st == 0 else None
+
+
 def profiled_traffic(name):
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
@@ -436,38 +445,21 @@ def _closed_loop(srv, pools, shares, seconds, rng, max_inflight=8):
     return srv.stats()
 
 
-def run_serving(a):
-    """Open-loop Poisson load against the resident library, then capacity."""
+def _open_loop(srv, pools, shares, rate, T, rng, q_fixed=None, cjobs=()):
+    """Poisson arrivals at `rate` for `T` seconds: queries of q ~ U{1..512}
+    structures (or exactly q_fixed) of a bucket drawn by library share, with
+    the clustering jobs spread over the run.  Returns the server's stats for
+    the run, the submit lags (ms), the submitting time and the request count."""
     import queue as qmod
     import threading
-    from bioshell_gb300 import CrmsdServer
-    lib, bases = synth.serving_library()
-    pools = synth.serving_queries(bases)
-    shares = list(synth.SERVING_BUCKETS)
-    rng = np.random.default_rng(6)
-    # clustering jobs mixed in: all-vs-all + OPTICS of 500-5000 decoys
-    cjobs = []
-    for k in range(4):
-        L = 64 if k % 2 == 0 else 128
-        n = int(rng.integers(500, 5001))
-        cjobs.append(synth.decoys(bases[L][k], n, rng, (0.3, 4.0)))
-    t0 = time.perf_counter()
-    srv = CrmsdServer(lib, top_k=50, max_inflight=a.serve_inflight)
-    build_s = time.perf_counter() - t0
-    for L in pools:  # warm-up: first batches of every bucket, both extremes of q
-        for n in (1, 512):
-            srv.wait(srv.submit(pools[L][:n]))
-    srv.wait_cluster(srv.submit_cluster(cjobs[0][:500], 3.0, 5))
     srv.reset_stats()
-    # open loop: Poisson arrivals at the offered rate
-    rate, T = a.serve_rate, a.serve_seconds
     gaps = rng.exponential(1.0 / rate, size=int(rate * T * 1.5) + 10)
     times = np.cumsum(gaps)
     times = times[times < T]
     Ls = np.array([L for L, _ in shares])
     ps = np.array([p for _, p in shares])
     bk = rng.choice(Ls, size=len(times), p=ps / ps.sum())
-    qs = rng.integers(1, 513, size=len(times))
+    qs = np.full(len(times), q_fixed) if q_fixed else rng.integers(1, 513, size=len(times))
     offs = [int(rng.integers(0, pools[int(L)].shape[0] - int(n) + 1)) for L, n in zip(bk, qs)]
     ctimes = np.linspace(0.1, T * 0.9, len(cjobs))
     tickets = qmod.Queue()
@@ -501,9 +493,35 @@ def run_serving(a):
     submit_s = time.perf_counter() - start
     tickets.put(None)
     th.join()
-    st = srv.stats()
+    return srv.stats(), lag, submit_s, int(len(times))
+
+
+def run_serving(a):
+    """Open-loop Poisson load against the resident library, then capacity."""
+    from bioshell_gb300 import CrmsdServer
+    lib, bases = synth.serving_library()
+    pools = synth.serving_queries(bases)
+    shares = list(synth.SERVING_BUCKETS)
+    rng = np.random.default_rng(6)
+    # clustering jobs mixed in: all-vs-all + OPTICS of 500-5000 decoys
+    cjobs = []
+    for k in range(4):
+        L = 64 if k % 2 == 0 else 128
+        n = int(rng.integers(500, 5001))
+        cjobs.append(synth.decoys(bases[L][k], n, rng, (0.3, 4.0)))
+    t0 = time.perf_counter()
+    srv = CrmsdServer(lib, top_k=50, max_inflight=a.serve_inflight)
+    build_s = time.perf_counter() - t0
+    for L in pools:  # warm-up: first batches of every bucket, both extremes of q
+        for n in (1, 512):
+            srv.wait(srv.submit(pools[L][:n]))
+    srv.wait_cluster(srv.submit_cluster(cjobs[0][:500], 3.0, 5))
+    rate, T = a.serve_rate, a.serve_seconds
+    st, lag, submit_s, n_req = _open_loop(srv, pools, shares, rate, T, rng, cjobs=cjobs)
+    Ls = np.array([L for L, _ in shares])
+    ps = np.array([p for _, p in shares])
     offered = float(rate * sum(ps[list(Ls).index(L)] * lib[L].shape[0] for L in Ls) * 256.5)
-    open_loop = {"offered_req_per_s": rate, "seconds": T, "requests": int(len(times)),
+    open_loop = {"offered_req_per_s": rate, "seconds": T, "requests": n_req,
                  "cluster_jobs": len(cjobs), "offered_pairs_per_s": offered,
                  "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"], "mean_ms": st["mean_ms"],
                  "pairs_per_s": st["pairs_per_s"], "wall_s": st["seconds"], "batches": int(st["batches"]),
@@ -511,6 +529,12 @@ def run_serving(a):
                  "cluster_p50_ms": st["cluster_p50_ms"], "cluster_p99_ms": st["cluster_p99_ms"],
                  "submit_lag_p99_ms": float(np.percentile(lag, 99)) if lag else None, "submit_s": submit_s,
                  "pairs_screened_per_pair": st["pairs_screened"] / max(st["pairs"], 1)}
+    # the benchmark spec's latency target is quoted for 64-structure queries: the
+    # same Poisson load with every query exactly 64 structures
+    st64, _, _, n64 = _open_loop(srv, pools, shares, rate, min(T, 2.0), rng, q_fixed=64)
+    open_loop_q64 = {"offered_req_per_s": rate, "seconds": min(T, 2.0), "requests": n64, "q": 64,
+                     "p50_ms": st64["p50_ms"], "p99_ms": st64["p99_ms"], "max_ms": st64["max_ms"],
+                     "pairs_per_s": st64["pairs_per_s"]}
     cap = _closed_loop(srv, pools, shares, 2.0, rng)
     srv.close()
     # the plain FP64 server on the same library and GPU (closed loop)
@@ -521,7 +545,7 @@ def run_serving(a):
     return {"library": {"structures": int(sum(x.shape[0] for x in lib.values())),
                         "atoms": int(sum(x.shape[0] * x.shape[1] for x in lib.values())),
                         "buckets": {str(L): int(lib[L].shape[0]) for L in lib}, "build_s": build_s},
-            "top_k": 50, "max_inflight": a.serve_inflight, "open_loop": open_loop,
+            "top_k": 50, "max_inflight": a.serve_inflight, "open_loop": open_loop, "open_loop_q64": open_loop_q64,
             "capacity": {"pairs_per_s": cap["pairs_per_s"], "p50_ms": cap["p50_ms"], "p99_ms": cap["p99_ms"],
                          "queries": int(cap["queries_done"])},
             "plain64_capacity": {"pairs_per_s": pcap["pairs_per_s"], "p50_ms": pcap["p50_ms"],
@@ -623,11 +647,19 @@ def run_ours(a, rank, world, local_rank):
 
     # ---- plain FP64 denominator on the same workload
     plain = None
+    f64_flops = fp64_peak(local_rank) if rank == 0 else None
     if not a.skip_plain:
         step(xd, outd, CrmsdOptions(precision="plain64"))
         m = step(xd, outd, CrmsdOptions(precision="plain64"))
         plain = {"value": npairs / (m["ms_total"] * 1e-3), "unit": UNIT, "ms_per_step": m["ms_total"],
                  "kernel_ms": m["ms_main"]}
+        if f64_flops:
+            # algorithmic FP64 work: the covariance, 18 L flops per pair (the
+            # per-pair QCP solve, ~200 flops, is not counted)
+            ach = 18.0 * L * npairs / (m["ms_main"] * 1e-3)
+            plain["roofline"] = {"kernel": "k_plain64_all", "bound": "fp64", "achieved_tflops": ach / 1e12,
+                                 "peak_tflops": f64_flops / 1e12, "frac": ach / f64_flops,
+                                 "peak_source": "measured in-tree (bs_diag_fp64_peak)"}
         step(xd, outd)  # leave the mixed result in outd
 
     # ---- accuracy against the FP64 oracle
@@ -687,6 +719,9 @@ def run_ours(a, rank, world, local_rank):
         batched = run_batched(a, eng, stream, torch)
     if not a.skip_serving and rank == 0:
         serving = run_serving(a)
+    # The contract keys first, the large sections next, and the short headline
+    # figures (accuracy, the plain FP64 denominator, serving latency) last, so
+    # that the end of the line carries them.
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16", "data": "synthetic",
@@ -694,12 +729,24 @@ def run_ours(a, rank, world, local_rank):
                        "output": "f64 packed triangle", "l2": "no flush: inputs (360 MB) and output (10 GB) exceed L2",
                        "replicas": world},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "streaming_roofline": streaming,
-            "cpu_baseline": cb, "clocks": clocks,
-            "plain64": plain, "speedup_vs_plain64": (value / world / plain["value"]) if plain else None,
-            "accuracy": acc, "pairs_refined": int(refined), "phases": phases, "neighbors": neighbors,
-            "superpose": superpose, "formats": formats, "hierarchical": hier,
-            "batched": batched,
-            "serving": serving}
+            "cpu_baseline": cb, "clocks": clocks, "phases": phases,
+            "neighbors": neighbors, "superpose": superpose, "formats": formats, "hierarchical": hier,
+            "batched": batched, "serving": serving}
+    if batched:
+        line["batched_summary"] = {"value": batched["value"], "e2e": batched["e2e"]["value"],
+                                   "speedup_vs_plain64": batched["speedup_vs_plain64"],
+                                   "optics_identical": f"{batched['optics']['identical_labels']}/{batched['sets']}"}
+    if serving:
+        ol, q64 = serving["open_loop"], serving["open_loop_q64"]
+        line["serving_summary"] = {"req_per_s": ol["offered_req_per_s"], "p50_ms": ol["p50_ms"], "p99_ms": ol["p99_ms"],
+                                   "q64_p50_ms": q64["p50_ms"], "q64_p99_ms": q64["p99_ms"],
+                                   "pairs_per_s": ol["pairs_per_s"],
+                                   "speedup_vs_plain64": serving["speedup_vs_plain64"]}
+    line["fp64_peak_tflops"] = f64_flops / 1e12 if f64_flops else None
+    line["pairs_refined"] = int(refined)
+    line["accuracy"] = acc
+    line["plain64"] = plain
+    line["speedup_vs_plain64"] = (value / world / plain["value"]) if plain else None
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

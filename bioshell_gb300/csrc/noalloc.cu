@@ -18,6 +18,8 @@
 // at once) race on the same scratch and must not be issued.
 #include <string.h>
 
+#include <mutex>
+
 #include "engine.h"
 
 namespace bs {
@@ -44,6 +46,7 @@ static __device__ __align__(256) DevScalars g_scal;
 constexpr int kMaxDevices = 64;
 struct Scratch {
   bool ready = false;
+  bool sm103 = false;  // the device is an sm_103 GPU (checked once, at set-up)
   __nv_bfloat16 *dig[4] = {};
   SInfo *info = nullptr;
   long long *ctr = nullptr;
@@ -56,6 +59,7 @@ struct Scratch {
 };
 Scratch g_scratch[kMaxDevices];
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_setup_mu;  // first calls on different devices may come from different threads
 
 template <typename T>
 bool symbol(T &sym, void **p) {
@@ -63,11 +67,22 @@ bool symbol(T &sym, void **p) {
 }
 
 // Device addresses of the static arrays on the current device (host code may
-// not use the array names as addresses).
+// not use the array names as addresses), and the device's compute capability,
+// looked up once per device.
 bs_status setup(int dev, Scratch **out) {
   if (dev < 0 || dev >= kMaxDevices) return BS_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_setup_mu);
   Scratch &s = g_scratch[dev];
   if (!s.ready) {
+    int major = 0, minor = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+      return BS_ERR_NO_DEVICE;
+    s.sm103 = major == 10 && minor == 3;
+    if (!s.sm103) {
+      s.ready = true;
+      return BS_ERR_NO_DEVICE;
+    }
     void *p = nullptr;
     if (!symbol(g_digits, &p)) return BS_ERR_CUDA;
     for (int d = 0; d < 4; ++d) s.dig[d] = static_cast<__nv_bfloat16 *>(p) + (size_t)d * kDigitElems;
@@ -90,6 +105,7 @@ bs_status setup(int dev, Scratch **out) {
     if (!get_encoder(&g_encode).empty()) return BS_ERR_CUDA;
     s.ready = true;
   }
+  if (!s.sm103) return BS_ERR_NO_DEVICE;
   *out = &s;
   return BS_OK;
 }
@@ -106,9 +122,6 @@ extern "C" BS_API bs_status bs_all_vs_all_static(const double *xyz, int64_t n, i
   if (!xyz || !out || !is_device_ptr(xyz) || !is_device_ptr(out)) return BS_ERR_INVALID_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return BS_ERR_NO_DEVICE;
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || !(prop.major == 10 && prop.minor == 3))
-    return BS_ERR_NO_DEVICE;
   Scratch *sc = nullptr;
   bs_status s = setup(dev, &sc);
   if (s) return s;

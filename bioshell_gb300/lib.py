@@ -146,6 +146,7 @@ SIGNATURES = [
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                               _fp, _dp]),
+    ("bs_diag_fp64_peak", ctypes.c_int32, [ctypes.c_int32, _dp]),
 ]
 
 _lib = None

@@ -488,6 +488,13 @@ BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n,
 BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
                                       const int64_t *jj, int64_t npairs, float *levels, double *rmsd);
 
+/* Measured FP64 FMA rate of GPU `device` in FLOP/s (2 per fused multiply-add):
+ * eight independent chains of fma per thread on 8 blocks of 256 threads per
+ * SM, the best of three ~0.1 s launches.  The denominator of the plain FP64
+ * path's roofline fraction; a diagnostic with no counterpart in the
+ * reference. */
+BS_API bs_status bs_diag_fp64_peak(int32_t device, double *flops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

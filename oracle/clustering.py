@@ -126,24 +126,25 @@ def preorder_leaves(node):
 
 
 def retrieve_clusters(root, max_distance):
+    """The reference's recursion (hierarchical.rs:136-169) with an explicit
+    stack, so that deep trees (single linkage of thousands of items) do not
+    hit Python's recursion limit; clusters come out in the same order."""
     max_distance = F32(max_distance)
     out = []
-
-    def rec(node):
-        if node.is_leaf():
-            out.append(node)
-        elif node.dist > max_distance:
-            for ch in (node.left, node.right):
-                if ch is not None:
-                    if ch.dist <= max_distance:
-                        out.append(ch)
-                    else:
-                        rec(ch)
-
     if root.dist <= max_distance:
         out.append(root)
-    else:
-        rec(root)
+        return out
+    stack = [(False, root)]  # (emit, node): emit a cluster, or recurse into a node
+    while stack:
+        emit, node = stack.pop()
+        if emit:
+            out.append(node)
+        elif node.is_leaf():
+            out.append(node)
+        elif node.dist > max_distance:
+            for ch in (node.right, node.left):  # pushed in reverse: left is handled first
+                if ch is not None:
+                    stack.append((ch.dist <= max_distance, ch))
     return out
 
 
@@ -291,3 +292,159 @@ def optics(n, dist, eps, min_points):
             start = k
     clusters.append(order[start:n])
     return order, reach, clusters
+
+
+# ------------------------------------------- vectorised hierarchical runs
+# The same steps as hierarchical_clustering above (hierarchical.rs:22-80 with
+# clustering_matrix.rs:27-74), one merge at a time with numpy over a float32
+# square matrix, so that the 500-structure workload clusters in about a
+# second per rule.  Each rule evaluates in the reference's operation order,
+# one float32 rounding per operation (numpy does not contract a * b + c).
+def _rule_rows(rule, si, sj, sk, dij, dik, djk):
+    if rule == "single":
+        return np.minimum(dik, djk)
+    if rule == "complete":
+        return np.maximum(dik, djk)
+    if rule == "average":
+        d = F32(1.0) / F32(si + sj)
+        return (d * F32(si)) * dik + (d * F32(sj)) * djk
+    if rule == "median":
+        return (F32(0.5) * dik + F32(0.5) * djk) - F32(0.25) * dij
+    if rule == "centroid":
+        d = F32(1.0) / F32(si + sj)
+        return ((d * F32(si)) * dik + (d * F32(sj)) * djk) - (((F32(si) * F32(sj)) * d) * d) * dij
+    if rule == "ward":
+        d = F32(1.0) / F32(si + sj + sk)
+        return ((d * F32(si + sk)) * dik + (d * F32(sj + sk)) * djk) - (F32(sk) * d) * dij
+    raise ValueError(rule)
+
+
+class HierRun:
+    """One hierarchical_clustering run over a square matrix, advanced merge by
+    merge.  ``merges`` rows are (left id, right id, new id, size) -- leaves
+    are 0..n-1, the s-th merge creates node n + s -- and ``dist`` holds the
+    float32 merging distances."""
+
+    def __init__(self, sq, rule):
+        m = np.array(sq, dtype=F32, copy=True)
+        n = m.shape[0]
+        np.fill_diagonal(m, F32(0.0))
+        self.m, self.n, self.rule = m, n, rule
+        self.sizes = [1] * n           # clustering_matrix.rs sizes (not moved by replace_with_last)
+        self.ids = list(range(n))      # node id at each matrix position
+        self.node_size = {i: 1 for i in range(n)}
+        self.order, self.cur = n, n
+        self.merges, self.dist = [], []
+        self._upper = np.triu(np.ones((n, n), dtype=bool), 1)
+
+    def done(self):
+        return self.order <= 1
+
+    def closest(self):
+        """(i, j, minimum, second smallest candidate): the first minimum of the
+        j-outer, i-inner scan over i < j (clustering_matrix.rs:27-42)."""
+        o = self.order
+        u = np.where(self._upper[:o, :o], self.m[:o, :o], np.inf).T.ravel()
+        k = int(np.argmin(u))
+        mn = u[k]
+        if not mn < F32_MAX:
+            return 0, 0, F32_MAX, np.inf
+        j, i = divmod(k, o)
+        second = np.partition(u, 1)[1] if u.size > 1 else np.inf
+        return i, j, mn, second
+
+    def merge(self, i, j):
+        m, o = self.m, self.order
+        dij = m[i, j]
+        left, right = self.ids[i], self.ids[j]
+        size = self.node_size[left] + self.node_size[right]
+        self.merges.append((left, right, self.cur, size))
+        self.dist.append(F32(dij))
+        self.node_size[self.cur] = size
+        self.ids[i] = self.cur
+        si, sj = self.sizes[i], self.sizes[j]
+        res = _rule_rows(self.rule, si, sj, self.sizes[j], dij, m[i, :o].copy(), m[j, :o].copy()).astype(F32)
+        m[i, :o] = res
+        m[:o, i] = res
+        m[i, i] = F32(0.0)
+        self.sizes[i] = sj + si
+        last = o - 1
+        if j < last:
+            self.ids[j] = self.ids[last]
+            self.order = o - 1
+            o = self.order
+            m[[j, o]] = m[[o, j]]
+            m[:o, j] = m[:o, o]
+        else:
+            self.order = o - 1
+        self.cur += 1
+
+    def run(self):
+        while not self.done():
+            i, j, _, _ = self.closest()
+            self.merge(i, j)
+        return self.result()
+
+    def result(self):
+        n = self.n
+        merges = np.array(self.merges, dtype=np.int64).reshape(max(n - 1, 0), 4)
+        return merges, np.array(self.dist, dtype=F32)
+
+
+def hierarchical_merges(sq, rule):
+    """merges and merging distances of hierarchical_clustering(sq, rule)."""
+    return HierRun(sq, rule).run()
+
+
+def tree_from_merges(n, merges, dist):
+    """The Node tree of a merge list (root: the last merge)."""
+    nodes = {i: Node(i, 1, 0.0) for i in range(n)}
+    for (a, b, c, s), d in zip(merges, dist):
+        nodes[int(c)] = Node(int(c), int(s), d, nodes[int(a)], nodes[int(b)])
+    return nodes[2 * n - 2] if n > 1 else nodes.get(0)
+
+
+def cut_labels(n, merges, dist, cutoff):
+    """Cluster index per item: the k-th cluster retrieve_clusters returns
+    (hierarchical.rs:136-169) is label k."""
+    labels = np.zeros(n, dtype=np.int64)
+    if n == 0:
+        return labels
+    root = tree_from_merges(n, merges, dist)
+    for k, c in enumerate(retrieve_clusters(root, cutoff)):
+        labels[preorder_leaves(c)] = k
+    return labels
+
+
+def lockstep(sq_a, sq_b, rule):
+    """Runs the clustering of two nearby matrices side by side.  While both
+    runs take the same merges, it records per merge the largest difference
+    between their working matrices (delta) and the slack of run b's merge:
+    the least, over every other candidate c, of b[c] - b[min] - |a[c] - b[c]|
+    - |a[min] - b[min]|.  A merge with slack > 0 is taken by run a as well,
+    whatever the two matrices' differences do to the scan; slack <= 0 marks
+    a merge that could go the other way.  Returns both runs' (merges, dist),
+    the index of the first merge where they part (None if never), and the
+    per-merge delta and slack up to that merge."""
+    a, b = HierRun(sq_a, rule), HierRun(sq_b, rule)
+    delta, slack, split = [], [], None
+    while not b.done():
+        o = b.order
+        up = b._upper[:o, :o]
+        bm = b.m[:o, :o].astype(np.float64)
+        d = np.abs(a.m[:o, :o].astype(np.float64) - bm)
+        delta.append(float(d[up].max()) if o > 1 else 0.0)
+        ia, ja, _, _ = a.closest()
+        ib, jb, mn, _ = b.closest()
+        if o > 2:
+            margin = np.where(up, bm - float(mn) - d, np.inf)
+            margin[ib, jb] = np.inf
+            slack.append(float(margin.min()) - float(d[ib, jb]))
+        else:
+            slack.append(np.inf)
+        if (ia, ja) != (ib, jb):
+            split = len(delta) - 1
+            break
+        a.merge(ia, ja)
+        b.merge(ib, jb)
+    return a.run(), b.run(), split, np.array(delta), np.array(slack)

@@ -1,6 +1,6 @@
 """Regenerates the committed golden fixtures of the crmsd tests.
 
-    python tests/golden/make_golden.py [path/to/reference/checkout]
+    BIOSHELL_REFERENCE=path/to/reference/checkout python tests/golden/make_golden.py
 
 * ``decoys_small.npz``   -- a seeded decoy set (32 x 47 atoms, including
   near-duplicates, an exact copy and a rigidly moved copy) with the FP64 QCP
@@ -13,8 +13,10 @@
   bioshell-clustering/tests/test_hierarchical.rs:10-71, read from the test
   source and the d5.tsv fixture it uses.
 
-The reference checkout is only needed for the last two; the script is run
-once on a machine that has it, and its outputs are committed.
+The reference checkout (named by the BIOSHELL_REFERENCE environment variable,
+or the first argument) is needed for the last two; the script is run once on
+a machine that has it, and its outputs are committed.  Without it, only
+the first fixture is regenerated and the script says so.
 """
 from __future__ import annotations
 
@@ -101,8 +103,10 @@ def hierarchical_tests(ref):
 if __name__ == "__main__":
     oracle.build()
     small_decoys()
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if os.path.isdir(ref):
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BIOSHELL_REFERENCE", "")
+    if ref and os.path.isdir(ref):
         models_2jqb(ref)
         hierarchical_tests(ref)
+    else:
+        print("BIOSHELL_REFERENCE names no reference checkout: only decoys_small.npz was regenerated")
     print("golden fixtures written to", HERE)

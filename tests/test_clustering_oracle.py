@@ -5,6 +5,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 from oracle import clustering as C
 
@@ -79,3 +80,54 @@ def test_optics_two_blobs():
     assert sorted(order) == list(range(40))
     sizes = sorted(len(c) for c in clusters)
     assert sizes[-2:] == [20, 20]
+
+
+@pytest.mark.parametrize("rule", list(C.RULES))
+@pytest.mark.parametrize("seed,ties", [(0, False), (1, True)])
+def test_vectorised_runs_equal_the_loop_restatement(rule, seed, ties):
+    """HierRun (numpy, one merge at a time) takes the same merges with the same
+    float32 distances as the loop restatement of hierarchical.rs."""
+    rng = np.random.default_rng(seed)
+    n = 40
+    if ties:
+        sq = rng.integers(1, 6, size=(n, n)).astype(np.float64)
+    else:
+        pts = rng.normal(size=(n, 3))
+        sq = np.linalg.norm(pts[:, None] - pts[None], axis=2)
+    sq = np.triu(sq, 1)
+    sq = sq + sq.T
+    dist = lambda i, j: np.float32(0.0) if i == j else np.float32(sq[i, j])  # noqa: E731
+    root = C.hierarchical_clustering(n, dist, C.RULES[rule])
+    merges, d = C.hierarchical_merges(sq.astype(np.float32), rule)
+
+    def walk(nd, out):
+        if not nd.is_leaf():
+            walk(nd.left, out)
+            walk(nd.right, out)
+            out.append((nd.id, nd.left.id, nd.right.id, nd.size, float(nd.dist)))
+        return out
+
+    assert sorted(walk(root, [])) == sorted(walk(C.tree_from_merges(n, merges, d), []))
+    for cut in (1.5, 2.5, float(np.median(d))):
+        want = np.zeros(n, dtype=np.int64)
+        for k, c in enumerate(C.retrieve_clusters(root, cut)):
+            want[C.preorder_leaves(c)] = k
+        np.testing.assert_array_equal(C.cut_labels(n, merges, d, cut), want)
+
+
+def test_lockstep_reports_where_runs_part():
+    """Two matrices that differ in one entry part exactly where that entry
+    decides a merge, and the slack recorded there is not positive."""
+    rng = np.random.default_rng(4)
+    pts = rng.normal(size=(30, 3))
+    sq = np.linalg.norm(pts[:, None] - pts[None], axis=2).astype(np.float32)
+    (ma, da), (mb, db), split, delta, slack = C.lockstep(sq, sq, "average")
+    assert split is None and np.all(delta == 0.0) and np.all(slack >= 0.0)
+    np.testing.assert_array_equal(ma, mb)
+    iu = np.triu_indices(30, 1)
+    k = int(np.argsort(sq[iu])[1])  # the second closest pair becomes the closest
+    i, j = iu[0][k], iu[1][k]
+    sq2 = sq.copy()
+    sq2[i, j] = sq2[j, i] = np.float32(sq[iu].min() - 1e-3)
+    _, _, split, delta, slack = C.lockstep(sq2, sq, "average")
+    assert split == 0 and slack[0] <= 0.0 and delta[0] > 0.0

@@ -1,6 +1,12 @@
 """eps-neighbour lists on the GPU (bs_neighbors): the sparse form of the
 all-vs-all that OPTICS consumes (NeighborsOf, points_set.rs:29-39).
 
+* Against the FP64 oracle: row i holds every j != i whose oracle distance
+  (rounded to f32, as the reference stores it) is <= eps -- the rule of
+  CartesianPoints::neighbors_of (points_set.rs:150-169) without the point
+  itself -- with distances within the 1e-4 A tolerance, ordered by (d, j).
+  Rows where some distance lies within the tolerance of eps are skipped and
+  counted.
 * The lists equal those read off the dense f32 matrix of the same call path:
   the same (j, d) entries per row, ordered by (d, j), bit for bit.
 * OPTICS over the lists gives the dense matrix's order, reachability and
@@ -31,6 +37,38 @@ def _check_equal(engine, x, eps):
     np.testing.assert_array_equal(col, col2)
     np.testing.assert_array_equal(dist, dist2)
     return rp, col, dist, sq
+
+
+TOL = 1e-4
+
+
+@pytest.mark.parametrize("eps", [0.8, 2.5, 6.0])
+def test_lists_match_the_oracle(engine, oracle_mod, eps):
+    rng = np.random.default_rng(15)
+    x = synth.decoys(synth.base_chain(120, rng), 700, rng, sigma=(0.2, 4.0), near_dup_frac=0.05)
+    x[10] = x[11]  # identical structures: distance 0
+    n = x.shape[0]
+    ref = np.zeros((n, n))
+    ref[np.triu_indices(n, 1)] = oracle_mod.crmsd_all_vs_all(x)
+    ref = ref + ref.T
+    ref32 = ref.astype(np.float32)
+    rp, col, dist = engine.neighbors(x, eps)
+    skipped = 0
+    for i in range(n):
+        others = np.arange(n) != i
+        if np.any(np.abs(ref[i, others] - eps) <= TOL):
+            skipped += 1  # a neighbour decision within tolerance of eps
+            continue
+        want = np.flatnonzero((ref32[i] <= eps) & others)
+        c, d = col[rp[i]:rp[i + 1]], dist[rp[i]:rp[i + 1]]
+        np.testing.assert_array_equal(np.sort(c), want)
+        assert np.all(np.abs(d.astype(np.float64) - ref[i, c]) <= TOL)
+        # ordered by (d, j) on the engine's values
+        o = np.lexsort((c, d))
+        np.testing.assert_array_equal(o, np.arange(c.size))
+    print(f"eps {eps}: {n - skipped} rows compared, {skipped} skipped (a distance within {TOL} A of eps), "
+          f"{rp[-1]} entries")
+    assert skipped <= n // 10
 
 
 @pytest.mark.parametrize("eps", [0.8, 2.5, 6.0])
