@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1,
                const __grid_constant__ CUtensorMap tb2, TcArgs a) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  // 1024-byte aligned (128-byte swizzle atoms); offset arithmetic on the
+  // shared array keeps every access below in the shared address space
+  uint8_t *smem = smem_raw + ((1024u - (ptx::smem_u32(smem_raw) & 1023u)) & 1023u);
   float *stage_epi = reinterpret_cast<float *>(smem + (size_t)kStages * kStageBytes);
   TileMeta *meta = reinterpret_cast<TileMeta *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes);
   Shared *sh = reinterpret_cast<Shared *>(smem + (size_t)kStages * kStageBytes + kEpiStageBytes + kMetaBytes);

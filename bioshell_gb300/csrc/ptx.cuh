@@ -49,20 +49,35 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// The same with a suspend-time hint: a thread whose phase is not complete
+// may be suspended (issuing nothing) for up to `hint_ns` nanoseconds or until
+// the phase completes, whichever comes first.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Waits for the phase with the given parity to complete.  Gives up after
 // `timeout_ns` of wall-clock time, or at once when *abort is set by another
-// role of the block; returns false in both cases.
+// role of the block; returns false in both cases.  After a first test, the
+// waiting thread is suspended between tests (up to 20 us each, woken by the
+// phase's completion), so long waits do not take issue slots from the warps
+// that share its scheduler.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           uint64_t timeout_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
-  uint32_t spins = 0;
   while (true) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((++spins & 63u) == 0u) {
-      if (*abort) return false;
-      if (globaltimer() - t0 > timeout_ns) return false;
-    }
+    if (mbar_try_wait_hint(bar, parity, 20000u)) return true;
+    if (*abort) return false;
+    if (globaltimer() - t0 > timeout_ns) return false;
   }
 }
 

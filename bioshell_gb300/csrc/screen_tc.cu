@@ -124,7 +124,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   constexpr int kStages = F::kStages;
   constexpr int kStageBytes = F::kStageBytes;
   extern __shared__ uint8_t smem_raw[];
-  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  // 1024-byte aligned (128-byte swizzle atoms); offset arithmetic on the
+  // shared array keeps every access below in the shared address space
+  uint8_t *smem = smem_raw + ((1024u - (ptx::smem_u32(smem_raw) & 1023u)) & 1023u);
   uint8_t *abuf = smem + (size_t)kStages * kStageBytes;  // strips: resident query block
   float *stage_epi = reinterpret_cast<float *>(abuf + F::kABytes);
   ScreenMeta *meta = reinterpret_cast<ScreenMeta *>(reinterpret_cast<uint8_t *>(stage_epi) + kEpiStageBytes);
