@@ -12,10 +12,12 @@ namespace bs {
 // ---------------------------------------------------------------- layout
 // Digit matrices: one row per (structure, coordinate), `pitch` bf16 columns
 // (atoms; a job uses the first lp = L rounded up to 16, zero padded).
-// Structures are packed ten to a 32-row group (rows 30 and 31 of each group
-// are zero), four groups to a 128-row block, so that a tensor-core A tile of
-// 128 rows holds 40 whole structures (B tiles: 64 rows, 20 structures) and
-// each structure's three rows sit in one warp's TMEM lanes.  Structures are
+// Structures are packed ten to a 32-row group, four groups to a 128-row
+// block, so that a tensor-core A tile of 128 rows holds 40 whole structures
+// (B tiles: 64 rows, 20 structures) and each structure's three rows sit in
+// one warp's TMEM lanes.  Within a group, structures 0-4 take rows 0-14 and
+// structures 5-9 rows 16-30 (rows 15 and 31 are zero): each half of a group
+// is then one aligned 16-column TMEM load in the epilogue.  Structures are
 // numbered globally across the jobs of one launch; every job starts on a
 // 40-structure block boundary.
 constexpr int kGroupRows = 32;
@@ -25,8 +27,10 @@ constexpr int kBlockStructs = 40;
 constexpr int kBStructs = 20;
 constexpr int kKChunk = 64;  // atoms per 128-byte swizzled TMA box row
 
+// row of coordinate c of structure s (0..9) within its group
+__host__ __device__ inline int group_row(int s, int c) { return 3 * s + (s >= 5 ? 1 : 0) + c; }
 __host__ __device__ inline int64_t digit_row(int64_t s, int c) {
-  return (s / kGroupStructs) * kGroupRows + (s % kGroupStructs) * 3 + c;
+  return (s / kGroupStructs) * kGroupRows + group_row((int)(s % kGroupStructs), c);
 }
 inline int64_t blocks_for(int64_t n) { return (n + kBlockStructs - 1) / kBlockStructs; }
 inline int lp_for(int L) { return ((L + 15) / 16) * 16; }

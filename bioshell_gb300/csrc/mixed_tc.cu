@@ -64,8 +64,13 @@ constexpr int kThreads = 384;
 constexpr int kEpiWarp0 = 4;
 constexpr int kEpiWarps = 8;
 constexpr int kTmemCols = 512;                           // 2 buffers x 4 levels x 64 columns
-constexpr int kPitch = 33;                               // staging pitch in floats
-constexpr int kEpiStageBytes = kEpiWarps * 32 * kPitch * 4;
+// Epilogue staging per warp: two buffers of 32 rows x 16 columns (pitch 17
+// floats), or for screen tiles one area of 32 rows x 32 columns (pitch 33).
+constexpr int kPitch = 17;
+constexpr int kPitchWide = 33;
+constexpr int kEpiStageFloats = 2 * 32 * kPitch;
+static_assert(32 * kPitchWide <= kEpiStageFloats, "screen staging exceeds the warp's area");
+constexpr int kEpiStageBytes = kEpiWarps * kEpiStageFloats * 4;
 constexpr int kBarBytes = 256;
 
 // What the epilogue needs of one tile: its record, its job and the
@@ -417,8 +422,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------------------------------------------------- epilogue
     const int qd = warp & 3;                // TMEM lane quarter of this warp
     const int g = (warp - kEpiWarp0) >> 2;  // column group (10 structures)
-    float *stg = stage_epi + (warp - kEpiWarp0) * 32 * kPitch;
-    const int il = lane / 3, x = lane - 3 * (lane / 3);
+    float *stg = stage_epi + (warp - kEpiWarp0) * kEpiStageFloats;
+    // lane -> (row structure il, coordinate x) of the group layout: lanes
+    // 0-14 hold structures 0-4, lanes 16-30 structures 5-9
+    const int lt = lane - (lane >= 16 ? 1 : 0);
+    const int il = lt / 3, x = lt - 3 * (lt / 3);
+    const bool lane_real = lane != 15 && lane < 31;
     const int ilr = il < kGroupStructs ? il : kGroupStructs - 1;  // pad lanes read a valid row
     const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * g;
     uint32_t p = 0;   // TMEM buffer slot, as the MMA issuer counts them
@@ -459,6 +468,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // truncated structures), stored as one word: hi (rounded up) and lo
         // (rounded down) halves
         uint32_t *sout = static_cast<uint32_t *>(out.ptr);
+        __syncwarp();  // the previous tile's reads of the staging area are done
         {
           // m = L0 + 2^-9 L1 + 2^-18 L11: the covariance of the truncated
           // structures in units of 2^28 grid products
@@ -471,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           ptx::tc_fence_before();
           ptx::mbar_arrive(&sh->tempty[p & 1u]);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
+          for (int c = 0; c < 32; ++c) stg[lane * kPitchWide + c] = fmaf(m[c], 0.001953125f, v[c]);
         }
         __syncwarp();
         // the warp's 10 x 10 pairs over its 32 lanes in four rounds, two
@@ -495,7 +505,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-              for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+              for (int y = 0; y < 3; ++y) m9[3 * xr + y] = stg[group_row(ir, xr) * kPitchWide + group_row(jc, y)];
             const float2 ta = mt.ta[qd * kGroupStructs + ir], tb = mt.tb[g * kGroupStructs + jc];
             bsm::screen_bracket(m9, ta.x + tb.x, t_d34, ta.y + tb.y, t_u, t_L, lo[u], hi[u]);
           }
@@ -507,7 +517,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             sout[oi[u]] = (whi << 16) | wlo;
           }
         }
-        __syncwarp();
         ptx::mbar_arrive(&sh->mempty[slot]);
         p += 1u;
         continue;
@@ -517,17 +526,26 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
       const int64_t ig = (int64_t)t_ablk * kBlockStructs + qd * kGroupStructs + il;
       const int64_t i = ig - fa;
-      const bool row_ok = job_ok && cols_ok && (lane < 30) && (i < jn);
+      const bool row_ok = job_ok && cols_ok && lane_real && (il < kGroupStructs) && (i < jn);
       const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
       const bool dump = (a.dbg != nullptr) && (t_ablk == 0) && (t_bblk < 2) && !lng;
-      // The group's 10 column structures are finished in two halves of five
-      // (columns 15h .. 15h+14), so a lane carries at most two pairs at once.
+      // row of coordinate xr of this lane's row structure in the staging buffers
+      int srow[3];
+#pragma unroll
+      for (int xr = 0; xr < 3; ++xr) srow[xr] = group_row(ilr, xr) * kPitch;
+      // The group's 10 column structures are finished in two halves of five:
+      // half h is TMEM columns 16h .. 16h+14 of the group (one 16-column
+      // load per accumulator), and a lane carries at most two pairs at once.
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
+        const uint32_t hc = 16u * (uint32_t)h;
+        float *bufm = stg + kPitch * 32;  // FP32 covariance rows (buffer 1)
         // ---- pass A: FP32 covariance rows of this half, staged per lane
         {
-          float m[32], v[32];
-          ptx::tmem_ld_32x32b_x32(acc_col(0), m);
+          float m[16], v[16];
+          ptx::tmem_ld2_32x32b_x16(acc_col(0) + hc, acc_col(lng ? 1 : 1) + hc, m, v);
+#pragma unroll
+          for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
 #pragma unroll
           for (int lv = 1; lv < 4; ++lv) {
             const float wl = lv == 1 ? 0.001953125f : (lv == 2 ? 3.814697265625e-6f : 7.450580596923828125e-9f);
@@ -535,22 +553,24 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int part = 0; part < 4; ++part) {
               // normal layout: accumulator lv; long: L1 {1, 2}, L2 {3..6}, L3 {7}
               const int ai = lng ? (lv == 1 ? 1 + part : (lv == 2 ? 3 + part : 7)) : lv;
-              const bool use = part == 0 || (lng && (lv == 2 || (lv == 1 && part < 2)));
+              const bool use = (lv == 1 && lng && part == 1) || (lv > 1 && (part == 0 || (lng && lv == 2)));
               if (use) {
-                ptx::tmem_ld_32x32b_x32(acc_col(ai), v);
+                ptx::tmem_ld_32x32b_x16(acc_col(ai) + hc, v);
 #pragma unroll
-                for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], wl, m[c]);
+                for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], wl, m[c]);
               }
             }
           }
+          __syncwarp();  // every lane is done with the previous half's last level (buffer 1)
 #pragma unroll
-          for (int c = 0; c < 16; ++c) stg[lane * kPitch + c] = h ? m[15 + c] : m[c];
+          for (int c = 0; c < 16; ++c) bufm[lane * kPitch + c] = m[c];
         }
         __syncwarp();
         bsm::FastState st[2];
         int64_t jj[2];
         bool valid[2];
         SInfo ib[2];
+        int scol[2];
         {
           // the lane's two pairs through one packed FP32x2 QCP
           float m9[2][9], gs[2];
@@ -558,6 +578,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int sl = 0; sl < 2; ++sl) {
             const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
             const int jc = jh < 5 ? jh : 4;
+            scol[sl] = 3 * jc;
             const int64_t jg = jg0 + 5 * h + jh;
             jj[sl] = jg - fb;
             valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
@@ -565,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-              for (int y = 0; y < 3; ++y) m9[sl][3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+              for (int y = 0; y < 3; ++y) m9[sl][3 * xr + y] = bufm[srow[xr] + scol[sl] + y];
             gs[sl] = valid[sl] ? ia.gf + ib[sl].gf : 0.f;
           }
           bsm::F2 mm[9];
@@ -573,56 +594,52 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int e = 0; e < 9; ++e) mm[e] = bsm::f2(m9[0][e], m9[1][e]);
           bsm::fast_begin2(mm, bsm::f2(gs[0], gs[1]), st[0], st[1]);
         }
-        __syncwarp();
         // ---- pass B: exact level sums, one level at a time (levels 0-2 as
-        // integers: the parts of a long-layout level add exactly)
+        // integers: the parts of a long-layout level add exactly); level lv
+        // is staged in buffer lv & 1, so one warp synchronisation per level
+        // separates each buffer's writes from the previous reads
 #pragma unroll
         for (int lv = 0; lv < 4; ++lv) {
+          float *buf = stg + (lv & 1) * kPitch * 32;
           const int a0 = lng ? (lv == 0 ? 0 : lv == 1 ? 1 : lv == 2 ? 3 : 7) : lv;
-          float v[32];
-          ptx::tmem_ld_32x32b_x32(acc_col(a0), v);
-          if (dump && h == 0) {
-            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * t_bblk + 32 * g;
+          float v[16];
+          ptx::tmem_ld_32x32b_x16(acc_col(a0) + hc, v);
+          if (dump) {
+            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * t_bblk + 32 * g + hc;
 #pragma unroll
-            for (int c = 0; c < 32; ++c) drow[c] = v[c];
+            for (int c = 0; c < 16; ++c) drow[c] = v[c];
+          }
+          if (h == 1 && lv == 3) {
+            // all TMEM reads of this tile are done: hand its buffers back to the MMA warp
+            ptx::tc_fence_before();
+            ptx::mbar_arrive(&sh->tempty[p & 1u]);
+            if (lng) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
           }
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const float w1 = h ? v[15 + c] : v[c];
-            stg[lane * kPitch + c] = lv < 3 ? __int_as_float(__float2int_rn(w1)) : w1;
-          }
+          for (int c = 0; c < 16; ++c) buf[lane * kPitch + c] = lv < 3 ? __int_as_float(__float2int_rn(v[c])) : v[c];
           if (lng && (lv == 1 || lv == 2)) {
-            // further parts of the level: added into the staged row (integers stay exact)
+            // further parts of the level, added into the staged row (integers stay exact)
 #pragma unroll
             for (int part = 1; part < 4; ++part) {
               if (lv == 1 && part > 1) break;
-              ptx::tmem_ld_32x32b_x32(acc_col(a0 + part), v);
+              ptx::tmem_ld_32x32b_x16(acc_col(a0 + part) + hc, v);
 #pragma unroll
               for (int c = 0; c < 16; ++c) {
-                float &d = stg[lane * kPitch + c];
-                d = __int_as_float(__float_as_int(d) + __float2int_rn(h ? v[15 + c] : v[c]));
+                float &d = buf[lane * kPitch + c];
+                d = __int_as_float(__float_as_int(d) + __float2int_rn(v[c]));
               }
             }
           }
           __syncwarp();
 #pragma unroll
           for (int sl = 0; sl < 2; ++sl) {
-            const int jh = 3 * sl + x;
-            const int jc = jh < 5 ? jh : 4;
             float s9[9];
 #pragma unroll
             for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-              for (int y = 0; y < 3; ++y) s9[3 * xr + y] = stg[(3 * ilr + xr) * kPitch + 3 * jc + y];
+              for (int y = 0; y < 3; ++y) s9[3 * xr + y] = buf[srow[xr] + scol[sl] + y];
             bsm::fast_level_staged(st[sl], lv, s9);
           }
-          __syncwarp();
-        }
-        if (h == 1) {
-          // all TMEM reads of this tile are done: hand its buffers back to the MMA warp
-          ptx::tc_fence_before();
-          ptx::mbar_arrive(&sh->tempty[p & 1u]);
-          if (lng) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
         }
         // ---- finish and store (neighbour layout: flagged pairs are kept or
         // dropped by the exact recomputation)

@@ -314,10 +314,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp >= kEpiWarp0) {
     // ---------------------------------------------------------- epilogue
     // warp (qd, cq): TMEM lanes 32 qd .. +31 (A rows of 10 structures) and
-    // the 5 B structures 5 cq .. 5 cq + 4, i.e. 15 columns at 15 (cq & 1)
-    // within the 32-column group cq >> 1
+    // the 5 B structures 5 cq .. 5 cq + 4, i.e. the 15 columns at 16 (cq & 1)
+    // within the 32-column group cq >> 1 (one 16-column load per accumulator)
     const int qd = warp & 3, cq = (warp - kEpiWarp0) >> 2;
-    const int grp = cq >> 1, off = kCols * (cq & 1);
+    const int grp = cq >> 1;
+    const uint32_t off = 16u * (uint32_t)(cq & 1);
     float *stg = stage_epi + (warp - kEpiWarp0) * 32 * kPitch;
     const uint32_t lane_base = tmem + ((uint32_t)(qd * 32) << 16) + 32u * grp;
     uint32_t tt = 0;
@@ -339,21 +340,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         {
           // m = L0 + 2^-9 L1 + 2^-18 L11: the covariance of the truncated
           // structures in units of 2^28 grid products
-          const uint32_t c0 = lane_base + (tt & 1u) * 256u;
-          float m[32], v[32];
-          ptx::tmem_ld2_32x32b_x32(c0 + 64, c0 + 128, m, v);
+          const uint32_t c0 = lane_base + (tt & 1u) * 256u + off;
+          float m[16], v[16];
+          ptx::tmem_ld2_32x32b_x16(c0 + 64, c0 + 128, m, v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
-          ptx::tmem_ld_32x32b_x32(c0, v);
+          for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+          ptx::tmem_ld_32x32b_x16(c0, v);
           ptx::tc_fence_before();
           ptx::mbar_arrive(&sh->tempty[tt & 1u]);
-          if (off) {
 #pragma unroll
-            for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[kCols + c], 0.001953125f, v[kCols + c]);
-          } else {
-#pragma unroll
-            for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
-          }
+          for (int c = 0; c < kCols; ++c) stg[lane * kPitch + c] = fmaf(m[c], 0.001953125f, v[c]);
         }
         __syncwarp();
         const bool job_ok = mj.err == 0;
@@ -382,7 +378,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int xr = 0; xr < 3; ++xr)
 #pragma unroll
-              for (int y = 0; y < 3; ++y) mv[u][3 * xr + y] = stg[(3 * ir + xr) * kPitch + 3 * jc + y];
+              for (int y = 0; y < 3; ++y) mv[u][3 * xr + y] = stg[group_row(ir, xr) * kPitch + 3 * jc + y];
             const float2 fa = mt.ta[qd * kGroupStructs + ir], fb = mt.tb[5 * cq + jc];
             gv[u] = fa.x + fb.x;
             dv[u] = fa.y + fb.y;

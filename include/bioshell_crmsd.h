@@ -481,7 +481,7 @@ BS_API bs_status bs_selftest_superpose(const double *a, const double *b, int32_t
  * tensor-core level sums of the first two tiles (structures 0..39 against
  * 0..19 and 20..39) as levels[4][128][128] (level, row, column; rows and
  * columns in the digit-matrix order of the engine: structure s, coordinate c
- * at 32*(s/10) + 3*(s%10) + c).  bs_debug_pair_levels returns, for each listed
+ * at 32*(s/10) + 3*(s%10) + c, plus 1 when s%10 >= 5).  bs_debug_pair_levels returns, for each listed
  * pair, the level sums computed with integer CUDA-core arithmetic
  * (levels[npairs][4][9]) and that path's crmsd. */
 BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels);
