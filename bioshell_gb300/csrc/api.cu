@@ -51,6 +51,8 @@ bs_status ensure(bs_ctx *ctx, DevBuf &b, size_t bytes, const char *what) {
     b.cap = 0;
   }
   ++ctx->gen;
+  if (ctx->fail_alloc_after >= 0 && ctx->fail_alloc_after-- == 0)
+    return set_err(ctx, BS_ERR_OOM, "%s: allocation of %zu bytes failed (injected by bs_debug_fail_alloc)", what, bytes);
   if (ctx->used + bytes > ctx->budget)
     return set_err(ctx, BS_ERR_BUDGET, "%s: %zu bytes would exceed the context budget (%zu of %zu in use)", what,
                    bytes, ctx->used, ctx->budget);
@@ -752,6 +754,7 @@ BS_API const char *bs_status_string(bs_status s) {
     case BS_ERR_BUDGET: return "HBM budget exceeded";
     case BS_ERR_NO_DEVICE: return "no usable sm_103 GPU";
     case BS_ERR_INTERNAL: return "internal error";
+    case BS_ERR_CANCELLED: return "cancelled";
     default: return "unknown status";
   }
 }
@@ -925,7 +928,7 @@ BS_API bs_status bs_hierarchical_gpu(bs_ctx *ctx, const void *tri, int64_t n, in
   CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
   int *derr = nullptr;
   CK(launch_hierarchical(dtri, out_type == BS_OUT_F64 ? 0 : 1, n, rule, ctx->hier_ws.p, grid, dm, dd, &derr,
-                         ctx->stream),
+                         ctx->wait_limit_ns, ctx->stream),
      "clustering launch");
   CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
   int herr = 0;
@@ -1180,6 +1183,18 @@ BS_API bs_status bs_host_free(void *p) {
     return ok ? BS_OK : BS_ERR_CUDA;
   }
   return cudaFreeHost(p) == cudaSuccess ? BS_OK : BS_ERR_CUDA;
+}
+
+BS_API bs_status bs_debug_set_wait_limit(bs_ctx *ctx, int64_t ns) {
+  if (!ctx || ns < 0) return BS_ERR_INVALID_ARG;
+  ctx->wait_limit_ns = (uint64_t)ns;
+  return BS_OK;
+}
+
+BS_API bs_status bs_debug_fail_alloc(bs_ctx *ctx, int64_t after) {
+  if (!ctx || after < -1) return BS_ERR_INVALID_ARG;
+  ctx->fail_alloc_after = after;
+  return BS_OK;
 }
 
 BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels) {

@@ -145,6 +145,9 @@ struct bs_ctx {
   PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   // autotuner: shape class (64-atom chain bucket, log2 size) -> narrow tiles
   std::map<int64_t, int> tune;
+  // test hooks (bs_debug_set_wait_limit, bs_debug_fail_alloc)
+  uint64_t wait_limit_ns = 0;     // 0: the kernels' default bounds
+  int64_t fail_alloc_after = -1;  // allocations left before an injected failure (-1: off)
 };
 
 namespace bs {

@@ -49,9 +49,10 @@ struct HierState {
   float *merge_dist;        // [n-1]
   unsigned *bar;            // [2] grid barrier: arrivals, generation (zeroed before the launch)
   int *err;                 // 0, or 1 + the phase that gave up
+  uint64_t wait_ns;         // bound on each barrier wait
 };
 
-constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;
+constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;  // default bound
 
 // Grid-wide barrier with a bounded wait.  Returns false, with *err set, when
 // the other blocks did not arrive in time (or another block gave up).
@@ -69,7 +70,7 @@ __device__ bool grid_barrier(const HierState &s, int phase) {
     } else {
       const uint64_t t0 = ptx::globaltimer();
       while (*gen == g) {
-        if (*(volatile int *)s.err || ptx::globaltimer() - t0 > kBarrierTimeoutNs) {
+        if (*(volatile int *)s.err || ptx::globaltimer() - t0 > s.wait_ns) {
           atomicCAS(s.err, 0, 1 + phase);
           ok = 0;
           break;
@@ -341,7 +342,7 @@ int hier_grid(int num_sms) {
 }
 
 cudaError_t launch_hierarchical(const void *tri, int out_type, int64_t n, int rule, void *ws, int grid,
-                                int64_t *merges, float *merge_dist, int **err_out, cudaStream_t st) {
+                                int64_t *merges, float *merge_dist, int **err_out, uint64_t wait_ns, cudaStream_t st) {
   if (n < 2) return cudaSuccess;
   char *p = static_cast<char *>(ws);
   auto take = [&](size_t bytes) {
@@ -365,6 +366,7 @@ cudaError_t launch_hierarchical(const void *tri, int out_type, int64_t n, int ru
   s.err = static_cast<int *>(take(4));
   s.merges = merges;
   s.merge_dist = merge_dist;
+  s.wait_ns = wait_ns ? wait_ns : kBarrierTimeoutNs;
   *err_out = s.err;
   cudaError_t e = cudaMemsetAsync(s.bar, 0, 8, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.err, 0, 4, st);

@@ -299,7 +299,7 @@ int hier_grid(int num_sms);
 // *err_out: a device int, 0 after a complete run, else 1 + the phase whose
 // grid barrier timed out (100: an inconsistent merge pair)
 cudaError_t launch_hierarchical(const void *tri, int out_type, int64_t n, int rule, void *ws, int grid,
-                                int64_t *merges, float *merge_dist, int **err_out, cudaStream_t st);
+                                int64_t *merges, float *merge_dist, int **err_out, uint64_t wait_ns, cudaStream_t st);
 
 // neighbors.cu -- CSR rows (ordered by (d, j), without i itself) from the
 // cnt entries a neighbour-layout launch appended.  scratch_rows: 2n words;

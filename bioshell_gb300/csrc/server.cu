@@ -177,6 +177,7 @@ struct bs_server {
   std::string trace_path;
   std::vector<std::string> trace;
   int64_t qdone = 0, cdone = 0, pairs = 0, batches = 0, fallbacks = 0, rows_batched = 0;
+  int64_t batch_seq = 0;  // trace: batch ids, never reset (the stats counter above is)
   std::atomic<int64_t> screened{0};  // updated by launches that run without the lock
   bs::Clock::time_point t0;
 };
@@ -1309,17 +1310,21 @@ void finish_slot(bs_server *s, Slot &sl, std::unique_lock<std::mutex> &lk) {
       complete(s, r, st, msg);
     }
     // rows whose screen band held more candidates than kept: every pair of
-    // the request certified densely, synchronously on this slot
+    // the request certified densely, synchronously on this slot -- without
+    // the server lock (the slot stays busy, so nothing else uses its buffers),
+    // so that the scheduler and the other slots' workers keep going
     std::vector<Request *> all = sl.reqs;
     for (int j : redo) {
       Request *r = all[j];
       sl.reqs.assign(1, r);
+      lk.unlock();
       bs_status st = launch_query_batch(s, sl, false);
       if (st == BS_OK && cudaStreamSynchronize(sl.st) != cudaSuccess) st = BS_ERR_CUDA;
       std::string msg;
       if (st == BS_OK)
         st = collect_errors(*static_cast<const DevScalars *>(sl.hsc.p), static_cast<const Job *>(sl.hback.p), 1, msg);
       if (st == BS_OK) take(r, 0, false);
+      lk.lock();
       complete(s, r, st, msg);
     }
   }
@@ -1457,9 +1462,9 @@ void sched_loop(bs_server *s) {
       }
       for (Request *r : batch) {
         s->queue.erase(std::find(s->queue.begin(), s->queue.end(), r));
-        r->batch = s->batches;
+        r->batch = s->batch_seq;
       }
-      sl.batch_id = s->batches;
+      sl.batch_id = s->batch_seq++;
       sl.t_hand = Clock::now();
       sl.busy = true;
       sl.reqs = batch;
@@ -1754,6 +1759,21 @@ BS_API bs_status bs_server_wait_cluster(bs_server *s, int64_t ticket, int64_t *c
     delete r;
   }
   return st;
+}
+
+BS_API bs_status bs_server_cancel(bs_server *s, int64_t ticket, int32_t *cancelled) {
+  if (!s || !cancelled) return BS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return BS_ERR_INVALID_ARG;
+  Request *r = it->second;
+  auto q = std::find(s->queue.begin(), s->queue.end(), r);
+  *cancelled = 0;
+  if (q == s->queue.end() || r->done) return BS_OK;  // running or done: its wait returns its result
+  s->queue.erase(q);
+  complete(s, r, BS_ERR_CANCELLED, "cancelled before it ran");
+  *cancelled = 1;
+  return BS_OK;
 }
 
 BS_API bs_status bs_server_get_stats(bs_server *s, bs_server_stats *out) {

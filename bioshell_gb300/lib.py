@@ -18,7 +18,7 @@ BS_OK = 0
 STATUS_NAMES = {
     0: "BS_OK", 1: "BS_ERR_INVALID_ARG", 2: "BS_ERR_CUDA", 3: "BS_ERR_OOM", 4: "BS_ERR_TIMEOUT",
     5: "BS_ERR_UNSUPPORTED", 6: "BS_ERR_NONFINITE", 7: "BS_ERR_BUDGET", 8: "BS_ERR_NO_DEVICE",
-    9: "BS_ERR_INTERNAL",
+    9: "BS_ERR_INTERNAL", 10: "BS_ERR_CANCELLED",
 }
 PRECISION = {"plain64": 0, "mixed": 1}
 LAYOUT = {"triangle": 0, "square": 1}
@@ -111,6 +111,7 @@ SIGNATURES = [
     ("bs_server_wait", ctypes.c_int32, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_double]),
     ("bs_server_wait_cluster", ctypes.c_int32, [_vp, ctypes.c_int64, _vp, ctypes.c_double]),
     ("bs_server_get_stats", ctypes.c_int32, [_vp, ctypes.POINTER(bs_server_stats)]),
+    ("bs_server_cancel", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]),
     ("bs_server_reset_stats", ctypes.c_int32, [_vp]),
     ("bs_hierarchical", ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _i64p, _fp]),
     ("bs_cut_tree", ctypes.c_int32, [_i64p, _fp, ctypes.c_int64, ctypes.c_float, _i64p]),
@@ -144,6 +145,8 @@ SIGNATURES = [
     ("bs_selftest_screen", ctypes.c_int32, [_fp, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                             ctypes.c_int32, _fp, _fp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
+    ("bs_debug_set_wait_limit", ctypes.c_int32, [_vp, ctypes.c_int64]),
+    ("bs_debug_fail_alloc", ctypes.c_int32, [_vp, ctypes.c_int64]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                               _fp, _dp]),
     ("bs_diag_fp64_peak", ctypes.c_int32, [ctypes.c_int32, _dp]),

@@ -108,6 +108,14 @@ class CrmsdServer:
         self._check(self._lib.bs_server_wait_cluster(self._h, int(ticket), cl.ctypes.data, float(timeout)))
         return cl
 
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a request still in the queue (True); one already on the GPU
+        or done runs to completion (False).  A cancelled request's wait raises
+        CrmsdError with status BS_ERR_CANCELLED."""
+        c = ctypes.c_int32()
+        self._check(self._lib.bs_server_cancel(self._h, int(ticket), ctypes.byref(c)))
+        return bool(c.value)
+
     def stats(self) -> dict:
         s = _l.bs_server_stats()
         self._check(self._lib.bs_server_get_stats(self._h, ctypes.byref(s)))

@@ -63,7 +63,8 @@ enum {
   BS_ERR_NONFINITE = 6,    /* NaN or Inf in the input coordinates            */
   BS_ERR_BUDGET = 7,       /* request exceeds the context's HBM budget       */
   BS_ERR_NO_DEVICE = 8,    /* no usable GPU (or not an sm_103 device)        */
-  BS_ERR_INTERNAL = 9      /* invariant violated inside the library          */
+  BS_ERR_INTERNAL = 9,     /* invariant violated inside the library          */
+  BS_ERR_CANCELLED = 10    /* the request was cancelled before it ran        */
 };
 
 typedef struct bs_ctx bs_ctx;
@@ -342,6 +343,10 @@ BS_API bs_status bs_server_wait(bs_server *s, int64_t ticket, int64_t *hit_index
 /* The same for a clustering job: OPTICS cluster index of every structure. */
 BS_API bs_status bs_server_wait_cluster(bs_server *s, int64_t ticket, int64_t *cluster_of, double timeout_s);
 BS_API bs_status bs_server_get_stats(bs_server *s, bs_server_stats *out);
+/* Cancels a request that is still queued: *cancelled = 1 and its wait
+ * returns BS_ERR_CANCELLED.  A request already handed to the GPU (or done)
+ * is not stopped: *cancelled = 0 and its wait returns its result. */
+BS_API bs_status bs_server_cancel(bs_server *s, int64_t ticket, int32_t *cancelled);
 /* Clears the latency record and restarts the wall clock of the stats. */
 BS_API bs_status bs_server_reset_stats(bs_server *s);
 
@@ -481,12 +486,26 @@ BS_API bs_status bs_selftest_superpose(const double *a, const double *b, int32_t
  * tensor-core level sums of the first two tiles (structures 0..39 against
  * 0..19 and 20..39) as levels[4][128][128] (level, row, column; rows and
  * columns in the digit-matrix order of the engine: structure s, coordinate c
- * at 32*(s/10) + 3*(s%10) + c, plus 1 when s%10 >= 5).  bs_debug_pair_levels returns, for each listed
- * pair, the level sums computed with integer CUDA-core arithmetic
- * (levels[npairs][4][9]) and that path's crmsd. */
+ * at 32*(s/10) + 3*(s%10) + c, plus 1 when s%10 >= 5).  bs_debug_pair_levels
+ * returns, for each listed pair, the level sums computed with integer
+ * CUDA-core arithmetic (levels[npairs][4][9]) and that path's crmsd. */
 BS_API bs_status bs_debug_tile_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, float *levels);
 BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii,
                                       const int64_t *jj, int64_t npairs, float *levels, double *rmsd);
+
+/* Failure-injection hooks for tests (no counterpart in the reference; the
+ * reference reports failures only through Result values,
+ * bioshell-pdb/src/pdb_parsing_error.rs:7).  Both act on the host or through
+ * a kernel argument: nothing here faults or stalls a GPU.
+ *   bs_debug_set_wait_limit: the bound, in nanoseconds, on each grid-barrier
+ *     wait of this context's GPU hierarchical clustering (0 restores the
+ *     default 2 s).  A wait that runs out makes every block of the launch
+ *     return and the call return BS_ERR_TIMEOUT; the context stays usable.
+ *   bs_debug_fail_alloc: the `after`-th device workspace allocation of this
+ *     context from now on (0: the next one) fails as if the GPU were out of
+ *     memory (BS_ERR_OOM, nothing allocated); -1 disarms the hook. */
+BS_API bs_status bs_debug_set_wait_limit(bs_ctx *ctx, int64_t ns);
+BS_API bs_status bs_debug_fail_alloc(bs_ctx *ctx, int64_t after);
 
 /* Measured FP64 FMA rate of GPU `device` in FLOP/s (2 per fused multiply-add):
  * eight independent chains of fma per thread on 8 blocks of 256 threads per
