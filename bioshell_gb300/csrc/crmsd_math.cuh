@@ -180,24 +180,46 @@ BS_HD float qcp_top_eig(const float s[9], float &xout, float q[4]) {
 //
 // P(x), the QCP quartic of t normalised by lambda0 = gsum/2, has four real
 // roots (the eigenvalues of the symmetric key matrix over lambda0) and the
-// top one is x* <= sqrt(G_a G_b) / lambda0 <= 1.  Above its largest root a
-// real-rooted polynomial is increasing and convex, so Newton's method from
-// x = 1 decreases monotonically towards x*: every iterate x satisfies
-// x - P(x)/P'(x) >= x*.  And since P'/P = sum 1 / (x - x_i) over the four
-// roots, the root nearest to x -- here x* -- lies within 4 P(x)/P'(x) of x.
-// In FP32 the quartic is known only to within eP = 2^-18 (the rounding of
-// the normalised covariance, of the coefficients -- c0 = det K is a sum of
-// O(1) products -- and of the evaluation; |x| <= 1 and ||K / lambda0|| <= 1
-// keep every term O(1)): eight times the largest |P(x*)| measured in FP32
-// over 11,000 decoy pairs of 64-300 atoms (2^-21.3).  P' is known to within
-// eD = 2^-18 likewise.  With these, for x >= x*:
-//     x - max(P - eP, 0) / (P' + eD)  >=  x*  >=  x - 4 (P + eP) / (P' - eD),
-// widened by 2^-20 for the rounding of the final steps.  The bracket holds whether or not the iteration
-// has converged: near pairs converge in two or three steps, far pairs only
-// need a loose bracket, and where the top root is nearly double (P' small)
-// the bracket widens instead of failing.  Finally crmsd(t) is within dr =
-// rms(d2_a) + rms(d2_b) (Angstrom) of crmsd(n) (Minkowski: each structure
-// moves by the RMS of its dropped digit).
+// top one is 0 <= x* <= 1.  Above its largest root a real-rooted polynomial is
+// increasing and convex, so Newton's method from x = 1 decreases
+// monotonically towards x*: every iterate x satisfies x - P(x)/P'(x) >= x*.
+// And since P'/P = sum 1 / (x - x_i) over the four roots, the root nearest
+// to x -- here x* -- lies within 4 P(x)/P'(x) of x.  With eP >= |computed P -
+// P| and eD >= |computed P' - P'|, for x >= x*:
+//     x - max(P - eP, 0) / (P' + eD)  >=  x*  >=  x - 4 (P + eP) / (P' - eD).
+// The bracket holds whether or not the iteration has converged: near pairs
+// converge in two or three steps, far pairs only need a loose bracket, and
+// where the top root is nearly double (P' small) the bracket widens instead
+// of failing.
+//
+// The error bounds (u = 2^-24): a forward error analysis of the operations
+// below in the manner of Higham (Accuracy and Stability of Numerical
+// Algorithms, ch. 3), every rounding bounded by u times the magnitude it
+// rounds, with the magnitudes bounded as follows.  Let s = M / lambda0 be the
+// exact normalised covariance of the truncated pair: ||M||_F <= sqrt(Ga Gb)
+// <= lambda0 gives ||s||_F <= 1, and the eigenvalues of K(s) are sign
+// combinations of the singular values of s, so ||K(s)||_2 <= ||s||_* <= 1
+// (nuclear norm of A B^T <= ||A||_F ||B||_F).  Hence every row of K has norm
+// <= 1, the singular values of adj(K) are <= 1 (||adj K||_F <= 2), any two
+// distinct products of a 2x2 minor sum to <= 1/2 (s) or <= 1 (K) in
+// magnitude (AM-GM), the six 2x2 minors of two rows have squares summing to
+// <= 1 (Lagrange's identity), and |c2| <= 2, |c1| <= 8 / 3^1.5, |c0| <= 1.
+//   * input: the computed sn differs from s by at most 8.1u |s_i| + 0.01u
+//     per entry (the two FMAs forming m, gsum_f from two rounded G's, the fast
+//     reciprocal (2 ulp), the product), so ||sn - s||_F <= 8.1u and, by Weyl
+//     with ||K(D)||_2 <= sqrt(3) ||D||_F, the top root moves by at most
+//     14u < 2^-19: the bracket is widened by 2^-19 on both sides;
+//   * coefficients from sn: c2 (a 9-term FMA chain) within 18.1u; c1 = -8
+//     det3 within 8 x 4.35u = 35u; c0 = det4 within 31.5u (15.9u for the
+//     expansion in 2x2 minors, 15.6u for the rounded key-matrix entries,
+//     ||dK||_F <= 7.8u, through the cofactors);
+//   * evaluation by Horner at 0 <= x <= 1: P within 14.1u, P' within 21.5u.
+// So |computed P - P| <= 99u and |computed P' - P'| <= 93u, below the
+// eP = eD = 2^-16 (256u) used.  The final steps' roundings are covered by
+// 2^-20 on x and a relative 2^-20 on the two RMSD bounds.  Finally crmsd(t)
+// is within dr = rms(d2_a) + rms(d2_b) (Angstrom) of crmsd(n) (Minkowski:
+// each structure moves by the RMS of its dropped digit), and the rounding of
+// an inexact S11 enters through de as an error of E.
 BS_HD void screen_bracket(const float m[9], float gsum_f, float de, float dr, float u, int L, float &lo,
                           float &hi) {
   if (!(gsum_f > 0.f)) {
@@ -217,7 +239,8 @@ BS_HD void screen_bracket(const float m[9], float gsum_f, float de, float dr, fl
   const float c2 = -2.f * fro2;
   const float c1 = -8.f * det3f(sn);
   const float c0 = det4_sym(k.k00, k.k01, k.k02, k.k03, k.k11, k.k12, k.k13, k.k22, k.k23, k.k33);
-  constexpr float eP = 3.814697265625e-06f, eD = 3.814697265625e-06f;  // 2^-18
+  constexpr float eP = 1.52587890625e-05f, eD = 1.52587890625e-05f;  // 2^-16 (see above)
+  constexpr float mx = 2.86102294921875e-06f;                        // 2^-19 + 2^-20 on x
   float x = 1.0f, p = 0.f, dp = 0.f;
 #pragma unroll
   for (int it = 0; it < 4; ++it) {
@@ -226,11 +249,11 @@ BS_HD void screen_bracket(const float m[9], float gsum_f, float de, float dr, fl
     dp = fmaf(fmaf(4.f, x2, 2.f * c2), x, c1);
     if (it < 3) x -= BS_FDIV(fmaxf(p - eP, 0.f), fmaxf(dp + eD, eD));  // P' >= 0 for x >= x*
   }
-  const float xhi = fminf(x - BS_FDIV(fmaxf(p - eP, 0.f), fmaxf(dp + eD, eD)) + 9.5367431640625e-07f, 1.0f);  // >= x*
-  const float xlo = dp > eD ? fmaxf(x - BS_FDIV(4.f * (p + eP), dp - eD) - 9.5367431640625e-07f, 0.f) : 0.f;
+  const float xhi = fminf(x - BS_FDIV(fmaxf(p - eP, 0.f), fmaxf(dp + eD, eD)) + mx, 1.0f);  // >= x*
+  const float xlo = dp > eD ? fmaxf(x - BS_FDIV(4.f * (p + eP), dp - eD) - mx, 0.f) : 0.f;
   const float scale = BS_FDIV(u, (float)L);
-  lo = fmaxf(sqrtf(fmaxf(fmaf(gsum_f, 1.0f - xhi, -de), 0.f) * scale) - dr, 0.f);
-  hi = sqrtf(fmaf(gsum_f, 1.0f - xlo, de) * scale) + dr;
+  lo = fmaxf(sqrtf(fmaxf(fmaf(gsum_f, 1.0f - xhi, -de), 0.f) * scale) * 0.99999904632568359375f - dr, 0.f);
+  hi = sqrtf(fmaf(gsum_f, 1.0f - xlo, de) * scale) * 1.00000095367431640625f + dr;
 }
 
 #if defined(__CUDACC__)
@@ -276,7 +299,7 @@ __device__ __forceinline__ void screen_bracket2(const F2 m[9], F2 gsum, float de
   const F2 t23 = k22 * k33 - k23 * k23, t13 = k12 * k33 - k23 * k13, t12 = k12 * k23 - k22 * k13;
   const F2 t03 = k02 * k33 - k23 * k03, t02 = k02 * k23 - k22 * k03, t01 = k02 * k13 - k12 * k03;
   const F2 c0 = s01 * t23 - s02 * t13 + s03 * t12 + s12 * t03 - s13 * t02 + s23 * t01;
-  const F2 eP = f2(3.814697265625e-06f), eD = eP;  // 2^-18
+  const F2 eP = f2(1.52587890625e-05f), eD = eP;  // 2^-16, as screen_bracket
   F2 x = f2(1.0f), p = f2(0.f), dp = f2(0.f);
 #pragma unroll
   for (int it = 0; it < 4; ++it) {
@@ -298,10 +321,10 @@ __device__ __forceinline__ void screen_bracket2(const F2 m[9], F2 gsum, float de
       hx[c] = drs[c];
       continue;
     }
-    const float xhi = fminf(xs[c] - d1s[c] + 9.5367431640625e-07f, 1.0f);                      // >= x*
-    const float xlo = dps[c] > 3.814697265625e-06f ? fmaxf(xs[c] - d4s[c] - 9.5367431640625e-07f, 0.f) : 0.f;
-    lx[c] = fmaxf(sqrtf(fmaxf(fmaf(gs[c], 1.0f - xhi, -de), 0.f) * scale) - drs[c], 0.f);
-    hx[c] = sqrtf(fmaf(gs[c], 1.0f - xlo, de) * scale) + drs[c];
+    const float xhi = fminf(xs[c] - d1s[c] + 2.86102294921875e-06f, 1.0f);  // >= x*
+    const float xlo = dps[c] > 1.52587890625e-05f ? fmaxf(xs[c] - d4s[c] - 2.86102294921875e-06f, 0.f) : 0.f;
+    lx[c] = fmaxf(sqrtf(fmaxf(fmaf(gs[c], 1.0f - xhi, -de), 0.f) * scale) * 0.99999904632568359375f - drs[c], 0.f);
+    hx[c] = sqrtf(fmaf(gs[c], 1.0f - xlo, de) * scale) * 1.00000095367431640625f + drs[c];
   }
   lo = f2(lx[0], lx[1]);
   hi = f2(hx[0], hx[1]);

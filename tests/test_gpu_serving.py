@@ -221,3 +221,42 @@ def test_trace_records_batches_and_requests(library, enginelib, tmp_path, monkey
     for f in r:  # submitted before completed, carried by a traced batch, status OK
         assert float(f[5]) <= float(f[6]) and int(f[8]) == 0
         assert int(f[7]) in {int(g[2]) for g in b}
+
+
+def test_top50_of_a_20000_library_against_oracle(oracle_mod, enginelib):
+    """Top-50 over a 20,000-structure bucket (large enough for the library
+    index: the head-set pre-screen and the pruned screen both run) for 300
+    queries: every returned value within 1e-4 A of the FP64 oracle, and every
+    member of the oracle's top 50 that lies more than 2e-4 A inside the cut
+    returned.  A screen bracket that missed its pair's true crmsd would drop
+    such a member."""
+    from bioshell_gb300 import CrmsdServer
+    rng = np.random.default_rng(31)
+    lib, fams = _family_library(rng, 64, 20000, families=8)
+    srv = CrmsdServer({64: lib}, top_k=50, max_inflight=2)
+    try:
+        qs = []
+        for k in range(300):
+            base = fams[k % 8][0]
+            qs.append(synth.decoys(base - base.mean(axis=0), 1, rng, sigma=(0.3, 2.5))[0])
+        x = np.stack(qs)
+        tickets = [srv.submit(x[o:o + 30]) for o in range(0, 300, 30)]
+        res = [srv.wait(t) for t in tickets]
+        idx = np.concatenate([r[0] for r in res])
+        val = np.concatenate([r[1] for r in res])
+    finally:
+        srv.close()
+    n = lib.shape[0]
+    both = np.concatenate([x, lib])
+    ii = np.repeat(np.arange(300), n)
+    jj = np.tile(np.arange(300, 300 + n), 300)
+    ref = oracle_mod.crmsd_pairs(both, ii, jj).reshape(300, n)
+    missing = 0
+    for r in range(300):
+        np.testing.assert_allclose(val[r], ref[r, idx[r]], rtol=0, atol=TOL)
+        order = np.lexsort((np.arange(n), ref[r]))
+        kth = ref[r, order[49]]
+        want = set(order[:50][ref[r, order[:50]] < kth - 2 * TOL].tolist())
+        missing += len(want - set(idx[r].tolist()))
+        assert np.all(np.diff(val[r]) >= 0)
+    assert missing == 0
