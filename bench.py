@@ -641,8 +641,19 @@ def run_ours(a, rank, world, local_rank):
     ev1.record(stream)
     ev1.synchronize()
     ms_e2e = ev0.elapsed_time(ev1)
+    # the machine's host link as a plain copy of the same triangle into the same
+    # pinned buffer: an end-to-end step cannot take less than that copy
+    ohv = torch.from_numpy(oh)
+    torch.cuda.synchronize()
+    l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0.record()
+    ohv.copy_(outd, non_blocking=True)
+    l1.record()
+    l1.synchronize()
+    link_gbs = npairs * 8 / (l0.elapsed_time(l1) * 1e-3) / 1e9
     e2e = {"value": world * npairs * e_steps / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes),
-           "d2h_bytes_per_step": int(npairs * 8), "steps": e_steps, "ms_per_step": ms_e2e / e_steps}
+           "d2h_bytes_per_step": int(npairs * 8), "steps": e_steps, "ms_per_step": ms_e2e / e_steps,
+           "host_link_d2h_gbs": link_gbs}
     np.testing.assert_array_equal(oh[:1000], outd[:1000].cpu().numpy())
 
     # ---- plain FP64 denominator on the same workload
