@@ -427,6 +427,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
   if (out_bytes && (s = ensure(ctx, ctx->out, out_bytes, "result buffer"))) return s;
   CK(cudaEventRecord(ctx->ev[0], ctx->stream), "event");
   std::vector<JobSpec> specs;
+  std::vector<int> set_of_spec;
   Readback rb;
   bool banded = false;
   for (int k = 0; k < nsets; ++k) {
@@ -446,6 +447,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     if (o.layout == BS_LAYOUT_SQUARE)
       CK(cudaMemset2DAsync(io[k].out_dev, (size_t)(d.n + 1) * esz, 0, esz, (size_t)d.n, ctx->stream), "zero diagonal");
     specs.push_back(JobSpec{io[k].xyz_dev, d.n, d.L, od, narrow[k]});
+    set_of_spec.push_back(k);
     ctx->metrics.narrow_jobs += narrow[k];
   }
   if (o.precision == BS_PRECISION_PLAIN64) {
@@ -486,6 +488,44 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
       rb.copy = ctx->copy_stream;
       rb.ev = ctx->band_ev.data();
       banded = true;
+    } else if (specs.size() > 1 && pairs >= kBandMinPairs) {
+      // many sets with host outputs (all pinned): bands end on set
+      // boundaries, and each band's sets are copied out while the later
+      // bands compute
+      bool pinned = false, pageable = false;
+      for (int j = 0; j < (int)specs.size(); ++j) {
+        const int k = set_of_spec[j];
+        if (io[k].out_off == SIZE_MAX) continue;
+        (is_pinned_host(sets[k].out) ? pinned : pageable) = true;
+      }
+      if (pinned && !pageable) {
+        if (!ctx->copy_stream)
+          CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream");
+        make_set_bands(plan, kBands, rb);
+        while (ctx->band_ev.size() < rb.tile_end.size() + 1) {
+          cudaEvent_t e;
+          CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "band event");
+          ctx->band_ev.push_back(e);
+        }
+        int64_t t0 = 0;
+        for (size_t band = 0; band < rb.tile_end.size(); ++band) {
+          int last = -1;
+          for (int64_t t = t0; t < rb.tile_end[band]; ++t) {
+            const int j = plan.tiles[t].job;
+            if (j == last) continue;
+            last = j;
+            const int k = set_of_spec[j];
+            if (io[k].out_off == SIZE_MAX) continue;
+            rb.copies[band].push_back(Readback::Copy{static_cast<const char *>(io[k].out_dev),
+                                                     static_cast<char *>(sets[k].out),
+                                                     out_elems(sets[k].n, o.layout) * esz});
+          }
+          t0 = rb.tile_end[band];
+        }
+        rb.copy = ctx->copy_stream;
+        rb.ev = ctx->band_ev.data();
+        banded = true;
+      }
     }
     s = launch_plan(ctx, plan, b, !(o.flags & BS_FLAG_NO_GRAPH), banded ? &rb : nullptr);
     if (s) {

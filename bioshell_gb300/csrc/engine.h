@@ -81,7 +81,21 @@ struct Readback {
   size_t esz = 0;
   cudaStream_t copy = nullptr;
   const cudaEvent_t *ev = nullptr;  // tile_end.size() + 1 events
+  // many sets (batched): band k ends at tile_end[k] on a set boundary and
+  // copies the outputs of its sets (copies[k]); elem_end is unused, and the
+  // overflow scan of each band covers every set
+  struct Copy {
+    const char *dev;
+    char *host;
+    size_t bytes;
+  };
+  std::vector<std::vector<Copy>> copies;
 };
+
+// Band boundaries for many symmetric jobs whose tiles lie job by job in the
+// plan (make_symmetric_plan): bands end on job boundaries, about `bands`
+// bands of equal pair counts with the last ones halved, as make_bands does.
+void make_set_bands(const Plan &plan, int bands, Readback &rb);
 
 // Band boundaries for a single symmetric job of n structures: whole
 // super-rows, about `bands` bands of equal pair counts, the last two bands'

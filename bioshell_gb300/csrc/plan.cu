@@ -132,6 +132,31 @@ void make_bands(const Plan &plan, int64_t n, int bands, Readback &rb) {
   rb.elem_end.push_back(total);
 }
 
+void make_set_bands(const Plan &plan, int bands, Readback &rb) {
+  rb.tile_end.clear();
+  rb.elem_end.clear();
+  rb.copies.clear();
+  const int64_t nt = (int64_t)plan.tiles.size();
+  int64_t total = 0;
+  for (const Job &jb : plan.jobs) total += jb.n * (jb.n - 1) / 2;
+  const int64_t want = std::max<int64_t>(1, total / std::max(1, bands));
+  int64_t done = 0, band = 0;
+  for (int64_t t = 0; t < nt; ++t) {
+    if (t + 1 < nt && plan.tiles[t + 1].job == plan.tiles[t].job) continue;
+    const Job &jb = plan.jobs[plan.tiles[t].job];  // the last tile of a job
+    band += jb.n * (jb.n - 1) / 2;
+    const int64_t rem = total - done;
+    const int64_t target = rem > 2 * want ? want : std::max<int64_t>(rem / 2, std::max<int64_t>(1, want / 16));
+    if (band >= target || t + 1 == nt) {
+      rb.tile_end.push_back(t + 1);
+      done += band;
+      band = 0;
+    }
+  }
+  if (rb.tile_end.empty()) rb.tile_end.push_back(nt);
+  rb.copies.resize(rb.tile_end.size());
+}
+
 cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *job_stage, const CUtensorMap tm[7],
                           int num_sms, cudaStream_t st, cudaEvent_t *ev, bool capturing, float *dbg,
                           const Readback *rb) {
@@ -198,9 +223,10 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
       if (!all_screen && (e = launch_refine(r, st)) != cudaSuccess) return e;
     } else {
       const size_t nb = rb->tile_end.size();
+      const bool sets = !rb->copies.empty();
       r.mark = true;
       for (size_t k = 0; k < nb; ++k) {
-        const int64_t t0 = k ? rb->tile_end[k - 1] : 0, e0 = k ? rb->elem_end[k - 1] : 0;
+        const int64_t t0 = k ? rb->tile_end[k - 1] : 0, e0 = sets ? 0 : (k ? rb->elem_end[k - 1] : 0);
         a.tiles = b.tiles + t0;
         a.ntiles = rb->tile_end[k] - t0;
         // each launch hands out its tiles from a counter at zero
@@ -208,11 +234,18 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
           return e;
         if (a.ntiles > 0 && (e = launch_mixed_tc(tm, a, st)) != cudaSuccess) return e;
         if (k + 1 == nb && (e = rec(2)) != cudaSuccess) return e;
-        r.scan_lo = e0;
-        r.scan_hi = rb->elem_end[k];
+        r.scan_lo = sets ? 0 : e0;
+        r.scan_hi = sets ? -1 : rb->elem_end[k];
         if ((e = launch_refine(r, st)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(rb->ev[k], st)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(rb->copy, rb->ev[k], 0)) != cudaSuccess) return e;
+        if (sets) {
+          for (const Readback::Copy &c : rb->copies[k])
+            if (c.bytes && (e = cudaMemcpyAsync(c.host, c.dev, c.bytes, cudaMemcpyDeviceToHost, rb->copy)) !=
+                               cudaSuccess)
+              return e;
+          continue;
+        }
         const size_t bytes = (size_t)(rb->elem_end[k] - e0) * rb->esz;
         if (bytes && (e = cudaMemcpyAsync(rb->host + (size_t)e0 * rb->esz, rb->dev + (size_t)e0 * rb->esz, bytes,
                                           cudaMemcpyDeviceToHost, rb->copy)) != cudaSuccess)

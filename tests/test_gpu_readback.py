@@ -72,3 +72,47 @@ def test_queue_overflow_scan(engine, dup_set, pinned):
         out, m = _device_result(engine, x, opts)
     assert engine.metrics()["pairs_refined"] > 64
     np.testing.assert_array_equal(out, ref)
+
+
+@pytest.fixture(scope="module")
+def many_sets():
+    # 12 sets of 1,000-2,400 structures (about 1.9e7 pairs, above the banding
+    # threshold) with exact copies inside each set, and chain lengths from 24
+    # to 90 atoms so that the tile order (longest chains first) differs from
+    # the set order
+    rng = np.random.default_rng(78)
+    sets = []
+    for k in range(12):
+        L = int(rng.integers(24, 91))
+        n = int(rng.integers(1000, 2401))
+        xs = synth.decoys(synth.base_chain(L, rng), n - 40, rng)
+        sets.append(np.ascontiguousarray(np.concatenate([xs, xs[rng.choice(n - 40, 40, replace=False)]])))
+    return sets
+
+
+@pytest.mark.parametrize("flag_queue", [0, 64])
+def test_batched_banded_readback_equals_device_result(engine, many_sets, flag_queue):
+    """Many sets with pinned host outputs: bands end on set boundaries and each
+    band's sets are copied while later bands compute.  Every set's result
+    equals the one-shot result with pageable outputs bit for bit, also when
+    the recomputation queue overflows (flag_queue=64: the per-band scan)."""
+    opts = CrmsdOptions(flag_queue=flag_queue)
+    ref = [m.values.copy() for m in engine.batched(many_sets, opts)]
+    assert engine.metrics()["main_launches"] == 9  # pageable outputs: one launch sequence
+    hin = []
+    for x in many_sets:
+        h = engine.host_empty(x.shape, np.float64)
+        h[...] = x
+        hin.append(h)
+    houts = []
+    for x in many_sets:
+        o = engine.host_empty((x.shape[0] * (x.shape[0] - 1) // 2,), np.float64)
+        o[...] = -7.0
+        houts.append(o)
+    engine.batched(hin, opts, outs=houts)
+    m = engine.metrics()
+    assert m["main_launches"] > 9  # ran in bands
+    if flag_queue:
+        assert m["pairs_refined"] > flag_queue
+    for got, want in zip(houts, ref):
+        np.testing.assert_array_equal(got, want)
