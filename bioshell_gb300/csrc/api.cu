@@ -369,6 +369,7 @@ struct SetIO {
   const double *xyz_dev;
   void *out_dev;
   size_t in_off, out_off;  // staging offsets (SIZE_MAX: caller's device memory)
+  size_t in_bytes = 0;     // bytes of a host input to upload
 };
 
 bs_status plain_set(bs_ctx *ctx, const double *dxyz, int64_t n, int L, const OutDesc &od) {
@@ -437,9 +438,9 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     if (io[k].in_off != SIZE_MAX) {
       double *dst = reinterpret_cast<double *>(static_cast<char *>(ctx->xyz.p) + io[k].in_off);
       const size_t bytes = (size_t)d.n * d.L * 3 * sizeof(double);
-      CK(cudaMemcpyAsync(dst, d.xyz, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy coordinates to device");
       ctx->metrics.bytes_h2d += (int64_t)bytes;
       io[k].xyz_dev = dst;
+      io[k].in_bytes = bytes;  // copied below: up front, or band by band
     }
     io[k].out_dev = io[k].out_off != SIZE_MAX ? static_cast<char *>(ctx->out.p) + io[k].out_off : d.out;
     const int layout = o.layout == BS_LAYOUT_TRIANGLE ? kLayoutTriangle : kLayoutSquare;
@@ -450,7 +451,17 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     set_of_spec.push_back(k);
     ctx->metrics.narrow_jobs += narrow[k];
   }
+  // the uploads of host inputs, in set order, on the context's stream
+  auto upload_all = [&]() -> bs_status {
+    for (int k = 0; k < nsets; ++k)
+      if (sets[k].n >= 2 && io[k].in_off != SIZE_MAX)
+        CK(cudaMemcpyAsync(const_cast<double *>(io[k].xyz_dev), sets[k].xyz, io[k].in_bytes, cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "copy coordinates to device");
+    return BS_OK;
+  };
   if (o.precision == BS_PRECISION_PLAIN64) {
+    if ((s = upload_all())) return s;
     CK(cudaMemsetAsync(ctx->scal.p, 0, sizeof(DevScalars), ctx->stream), "clear counters");
     CK(cudaEventRecord(ctx->ev[1], ctx->stream), "event");
     CK(cudaEventRecord(ctx->ev[2], ctx->stream), "event");
@@ -525,11 +536,51 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
         rb.copy = ctx->copy_stream;
         rb.ev = ctx->band_ev.data();
         banded = true;
+        // inputs all in pinned host memory: each band's sets are uploaded on
+        // a stream of their own and prepared when they land
+        bool in_pinned = false, in_pageable = false;
+        for (int j = 0; j < (int)specs.size(); ++j) {
+          const int k = set_of_spec[j];
+          if (io[k].in_off == SIZE_MAX) continue;
+          (is_pinned_host(sets[k].xyz) ? in_pinned : in_pageable) = true;
+        }
+        if (in_pinned && !in_pageable) {
+          if (!ctx->upload_stream)
+            CK(cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking), "upload stream");
+          while (ctx->up_ev.size() < rb.tile_end.size()) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "upload event");
+            ctx->up_ev.push_back(e);
+          }
+          rb.uploads.resize(rb.tile_end.size());
+          int64_t u0 = 0;
+          for (size_t band = 0; band < rb.tile_end.size(); ++band) {
+            int last = -1;
+            for (int64_t t = u0; t < rb.tile_end[band]; ++t) {
+              const int j = plan.tiles[t].job;
+              if (j == last) continue;
+              last = j;
+              const int k = set_of_spec[j];
+              if (io[k].in_off != SIZE_MAX)
+                rb.uploads[band].push_back(Readback::Upload{reinterpret_cast<char *>(const_cast<double *>(io[k].xyz_dev)),
+                                                            reinterpret_cast<const char *>(sets[k].xyz),
+                                                            io[k].in_bytes});
+            }
+            const Job &lj = plan.jobs[last];
+            rb.struct_end.push_back(lj.first_a + blocks_for(lj.n) * kBlockStructs);
+            u0 = rb.tile_end[band];
+          }
+          rb.struct_end.back() = plan.nblocks * kBlockStructs;
+          rb.upload = ctx->upload_stream;
+          rb.up_ev = ctx->up_ev.data();
+        }
       }
     }
+    if (rb.struct_end.empty() && (s = upload_all())) return s;
     s = launch_plan(ctx, plan, b, !(o.flags & BS_FLAG_NO_GRAPH), banded ? &rb : nullptr);
     if (s) {
       if (banded) cudaStreamSynchronize(ctx->copy_stream);
+      if (ctx->upload_stream) cudaStreamSynchronize(ctx->upload_stream);
       return s;
     }
   } else {
@@ -870,6 +921,11 @@ BS_API void bs_ctx_destroy(bs_ctx *ctx) {
     cudaStreamDestroy(ctx->copy_stream);
   }
   for (cudaEvent_t e : ctx->band_ev) cudaEventDestroy(e);
+  if (ctx->upload_stream) {
+    cudaStreamSynchronize(ctx->upload_stream);
+    cudaStreamDestroy(ctx->upload_stream);
+  }
+  for (cudaEvent_t e : ctx->up_ev) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

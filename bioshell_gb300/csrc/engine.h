@@ -90,6 +90,19 @@ struct Readback {
     size_t bytes;
   };
   std::vector<std::vector<Copy>> copies;
+  // ... and, when their inputs are in pinned host memory, the uploads of
+  // each band's sets (on `upload`, band k signalling up_ev[k]) and the end
+  // of each band's structure range: each band is prepared after its upload,
+  // so the uploads of later bands overlap the work of earlier ones
+  struct Upload {
+    char *dev;
+    const char *host;
+    size_t bytes;
+  };
+  std::vector<std::vector<Upload>> uploads;
+  std::vector<int64_t> struct_end;
+  cudaStream_t upload = nullptr;
+  const cudaEvent_t *up_ev = nullptr;  // tile_end.size() events
 };
 
 // Band boundaries for many symmetric jobs whose tiles lie job by job in the
@@ -127,6 +140,9 @@ struct bs_ctx {
   // banded read-back of large results: its copy stream and band events
   cudaStream_t copy_stream = nullptr;
   std::vector<cudaEvent_t> band_ev;
+  // banded uploads of many sets' inputs: their stream and band events
+  cudaStream_t upload_stream = nullptr;
+  std::vector<cudaEvent_t> up_ev;
   size_t budget = 0;
   size_t used = 0;
   uint64_t gen = 0;  // bumped whenever a workspace moves (graphs hold addresses)

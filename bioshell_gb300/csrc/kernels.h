@@ -182,6 +182,10 @@ struct PrepArgs {
   // screen's levels 0 and 1 describe, and its distance from the full one
   float2 *tinfo;
   DevScalars *sc;
+  // structures [s_lo, s_hi) only (s_hi < 0: all), and of the per-job
+  // kernels only the jobs whose first structure lies there: the preparation
+  // of one band of a banded call
+  int64_t s_lo = 0, s_hi = -1;
 };
 cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st);
 int prep_max_pitch();

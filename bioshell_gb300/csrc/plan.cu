@@ -16,7 +16,13 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
   int64_t blk = 0;
   int pitch = kKChunk;
   plan.jobs.resize(nj);
-  for (int j = 0; j < nj; ++j) {
+  // structure blocks are laid out job by job in the order the tiles run
+  // (longest chains first, so that long tiles do not trail the launch):
+  // a band of consecutive tiles then covers a contiguous range of blocks
+  std::vector<int> order(nj);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return specs[a].L > specs[b].L; });
+  for (int j : order) {
     const JobSpec &s = specs[j];
     Job &jb = plan.jobs[j];
     jb = Job{};
@@ -48,9 +54,6 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
   plan.nblocks = blk;
   plan.pitch = pitch;
   if (!with_tiles) return "";
-  std::vector<int> order(nj);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return specs[a].L > specs[b].L; });
   constexpr int64_t SA = 32, SB = 64;  // super-block: 32 A blocks x 64 B blocks
   for (int j : order) {
     const Job &jb = plan.jobs[j];
@@ -170,6 +173,18 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
   if ((e = cudaMemcpyAsync(b.jobs, job_stage, (size_t)nj * sizeof(Job), cudaMemcpyHostToDevice, st)) != cudaSuccess)
     return e;
   if ((e = cudaMemsetAsync(b.sc, 0, sizeof(DevScalars), st)) != cudaSuccess) return e;
+  // banded preparation: every band's uploads are queued now on their own
+  // stream; each band is prepared once its uploads have landed
+  const bool band_prep = rb && !rb->struct_end.empty();
+  if (band_prep) {
+    for (size_t k = 0; k < rb->tile_end.size(); ++k) {
+      for (const Readback::Upload &u : rb->uploads[k])
+        if (u.bytes && (e = cudaMemcpyAsync(u.dev, u.host, u.bytes, cudaMemcpyHostToDevice, rb->upload)) !=
+                           cudaSuccess)
+          return e;
+      if ((e = cudaEventRecord(rb->up_ev[k], rb->upload)) != cudaSuccess) return e;
+    }
+  }
   PrepArgs p{};
   p.jobs = b.jobs;
   p.njobs = nj;
@@ -181,11 +196,13 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
   p.info = b.info_a;
   p.tinfo = b.tinfo_a;
   p.sc = b.sc;
-  if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
-  if ((e = rec(1)) != cudaSuccess) return e;
+  if (!band_prep) {
+    if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
+    if ((e = rec(1)) != cudaSuccess) return e;
+  }
   if (!plan.tiles.empty()) {
     // strip records carry their shape; tiles get theirs from the prepared jobs
-    if (!plan.strips &&
+    if (!plan.strips && !band_prep &&
         (e = launch_tile_shapes(b.tiles, (int64_t)plan.tiles.size(), b.jobs, num_sms, st)) != cudaSuccess)
       return e;
     TcArgs a{};
@@ -229,6 +246,16 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
         const int64_t t0 = k ? rb->tile_end[k - 1] : 0, e0 = sets ? 0 : (k ? rb->elem_end[k - 1] : 0);
         a.tiles = b.tiles + t0;
         a.ntiles = rb->tile_end[k] - t0;
+        if (band_prep) {
+          // this band's structures, once uploaded, and its tiles' shapes
+          if ((e = cudaStreamWaitEvent(st, rb->up_ev[k], 0)) != cudaSuccess) return e;
+          p.s_lo = k ? rb->struct_end[k - 1] : 0;
+          p.s_hi = rb->struct_end[k];
+          if ((e = launch_prep_mixed(p, st)) != cudaSuccess) return e;
+          if (k == 0 && (e = rec(1)) != cudaSuccess) return e;
+          if (a.ntiles > 0 && (e = launch_tile_shapes(b.tiles + t0, a.ntiles, b.jobs, num_sms, st)) != cudaSuccess)
+            return e;
+        }
         // each launch hands out its tiles from a counter at zero
         if (k > 0 && (e = cudaMemsetAsync(&b.sc->tile_next, 0, sizeof(unsigned long long), st)) != cudaSuccess)
           return e;

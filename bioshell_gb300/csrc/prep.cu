@@ -96,10 +96,10 @@ __device__ __forceinline__ Where locate(const PrepArgs &p, int64_t g) {
 struct Run {
   int64_t g0, g1;
 };
-__device__ __forceinline__ Run warp_run(int64_t nstructs, int run) {
+__device__ __forceinline__ Run warp_run(int64_t s0, int64_t nstructs, int run) {
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   Run r;
-  r.g0 = w * run;
+  r.g0 = s0 + w * run;
   r.g1 = r.g0 + run < nstructs ? r.g0 + run : nstructs;
   return r;
 }
@@ -127,7 +127,7 @@ __device__ __forceinline__ long long warp_max64s(long long v) {
 // C - vmin), the same value a second pass over |v - C| would find.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, int64_t nstructs, int run_len) {
   const int lane = threadIdx.x & 31;
-  const Run run = warp_run(nstructs, run_len);
+  const Run run = warp_run(p.s_lo, nstructs, run_len);
   int cur = -1;                // job whose maximum is being gathered
   unsigned long long mrun = 0;  // its largest centred coordinate so far
   for (int64_t g = run.g0; g < run.g1; ++g) {
@@ -196,10 +196,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_mx_center(PrepArgs p, i
 }
 
 // ------------------------------------------------------------------- scale
+// a banded launch prepares only the jobs whose structures lie in its range
+__device__ __forceinline__ bool job_in_range(const PrepArgs &p, const Job &jb) {
+  return jb.first_a >= p.s_lo && (p.s_hi < 0 || jb.first_a < p.s_hi);
+}
+
 __global__ void k_mx_scale(PrepArgs p) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.njobs) return;
   Job &jb = p.jobs[j];
+  if (!job_in_range(p, jb)) return;
   // smallest e with every centred coordinate <= (2^22 - 1) 2^e (the range of
   // the three balanced digits); one thread per job, so plain FP64 is fine
   const double m = (double)jb.maxabs * 2.3283064365386963e-10;  // Angstrom
@@ -230,7 +236,7 @@ __global__ void k_mx_scale(PrepArgs p) {
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6) k_mx_norms(PrepArgs p, int64_t nstructs, int run_len) {
   const int lane = threadIdx.x & 31;
   const int qq = lane >> 3, u = lane & 7;
-  const Run run = warp_run(nstructs, run_len);
+  const Run run = warp_run(p.s_lo, nstructs, run_len);
   int cur = -1;
   // the current job's maxima over the run so far, lane 3a + d holding those
   // of grid a, digit d (every lane sees every sum after the reductions)
@@ -330,6 +336,7 @@ __global__ void k_mx_choose(PrepArgs p) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= p.njobs) return;
   Job &jb = p.jobs[j];
+  if (!job_in_range(p, jb)) return;
   if (jb.err) return;
   // Preference, from Cauchy-Schwarz bounds on the row norms: (1) the finest
   // grid whose level sums 0-2 are all exact (below 2^24) while its
@@ -416,7 +423,7 @@ constexpr int kChunkAtoms = 256;  // atoms staged per warp at a time: 768 coordi
 __global__ void __launch_bounds__(kDigitWarps * 32) k_mx_digits(PrepArgs p, int64_t nstructs) {
   __shared__ int qsm[kDigitWarps][3 * kChunkAtoms];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int64_t g = (int64_t)blockIdx.x * kDigitWarps + wib;
+  const int64_t g = p.s_lo + (int64_t)blockIdx.x * kDigitWarps + wib;
   if (g >= nstructs) return;
   const Where w = locate(p, g);
   if (!w.valid) return;
@@ -596,19 +603,21 @@ __global__ void __launch_bounds__(kPlainThreads)
 }  // namespace
 
 cudaError_t launch_prep_mixed(const PrepArgs &p, cudaStream_t st) {
-  const int64_t nstructs = p.nblocks * kBlockStructs;
-  if (nstructs <= 0) return cudaSuccess;
+  const int64_t total = p.nblocks * kBlockStructs;
+  const int64_t hi = p.s_hi < 0 ? total : (p.s_hi < total ? p.s_hi : total);  // structures [s_lo, hi)
+  const int64_t count = hi - p.s_lo;
+  if (count <= 0) return cudaSuccess;
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t per = nstructs / ((int64_t)nsm * 32);
+  const int64_t per = count / ((int64_t)nsm * 32);
   const int run = per < 1 ? 1 : (per > 8 ? 8 : (int)per);
-  const unsigned gw = (unsigned)((nstructs + (int64_t)run * kWarpsPerBlock - 1) / ((int64_t)run * kWarpsPerBlock));
-  k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs, run);
+  const unsigned gw = (unsigned)((count + (int64_t)run * kWarpsPerBlock - 1) / ((int64_t)run * kWarpsPerBlock));
+  k_mx_center<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, hi, run);
   k_mx_scale<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
-  k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, nstructs, run);
+  k_mx_norms<<<gw, kWarpsPerBlock * 32, 0, st>>>(p, hi, run);
   k_mx_choose<<<(p.njobs + 127) / 128, 128, 0, st>>>(p);
-  k_mx_digits<<<(unsigned)((nstructs + kDigitWarps - 1) / kDigitWarps), kDigitWarps * 32, 0, st>>>(p, nstructs);
+  k_mx_digits<<<(unsigned)((count + kDigitWarps - 1) / kDigitWarps), kDigitWarps * 32, 0, st>>>(p, hi);
   return cudaGetLastError();
 }
 

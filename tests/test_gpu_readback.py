@@ -93,7 +93,9 @@ def many_sets():
 @pytest.mark.parametrize("flag_queue", [0, 64])
 def test_batched_banded_readback_equals_device_result(engine, many_sets, flag_queue):
     """Many sets with pinned host outputs: bands end on set boundaries and each
-    band's sets are copied while later bands compute.  Every set's result
+    band's sets are copied while later bands compute (with pinned inputs, each
+    band's sets are also uploaded and prepared while earlier bands compute).
+    Every set's result
     equals the one-shot result with pageable outputs bit for bit, also when
     the recomputation queue overflows (flag_queue=64: the per-band scan)."""
     opts = CrmsdOptions(flag_queue=flag_queue)
@@ -109,10 +111,15 @@ def test_batched_banded_readback_equals_device_result(engine, many_sets, flag_qu
         o = engine.host_empty((x.shape[0] * (x.shape[0] - 1) // 2,), np.float64)
         o[...] = -7.0
         houts.append(o)
-    engine.batched(hin, opts, outs=houts)
-    m = engine.metrics()
-    assert m["main_launches"] > 9  # ran in bands
-    if flag_queue:
-        assert m["pairs_refined"] > flag_queue
-    for got, want in zip(houts, ref):
-        np.testing.assert_array_equal(got, want)
+    # pinned inputs: each band's sets are uploaded and prepared band by band;
+    # pageable inputs: uploaded up front, read back in bands
+    for inputs in (hin, many_sets):
+        for o in houts:
+            o[...] = -7.0
+        engine.batched(inputs, opts, outs=houts)
+        m = engine.metrics()
+        assert m["main_launches"] > 9  # ran in bands
+        if flag_queue:
+            assert m["pairs_refined"] > flag_queue
+        for got, want in zip(houts, ref):
+            np.testing.assert_array_equal(got, want)
