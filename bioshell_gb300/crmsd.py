@@ -41,6 +41,7 @@ class CrmsdOptions:
     graph: bool = True  # replay a captured CUDA graph for repeated shapes
     autotune: bool = False  # time the tile shapes per set class (mixed path)
     flag_queue: int = 0  # capacity of the exact-recomputation queue (0 = default)
+    rows: Optional[tuple] = None  # (row_begin, row_end): only the pairs of those rows (all_vs_all)
 
     def to_c(self) -> _l.bs_opts:
         o = _l.bs_opts()
@@ -51,7 +52,20 @@ class CrmsdOptions:
         o.tolerance = float(self.tolerance or 0.0)
         o.flags = (0 if self.graph else _l.FLAG_NO_GRAPH) | (_l.FLAG_AUTOTUNE if self.autotune else 0)
         o.flag_queue = int(self.flag_queue)
+        if self.rows is not None:
+            o.row_begin, o.row_end = int(self.rows[0]), int(self.rows[1])
         return o
+
+
+def partition_rows(n: int, parts: int):
+    """Row bounds that split the pairs of an n-structure all-vs-all into
+    `parts` ranges of nearly equal pair counts (bs_partition_rows): range p is
+    CrmsdOptions(rows=(b[p], b[p + 1])), e.g. one per GPU."""
+    b = np.zeros(parts + 1, dtype=np.int64)
+    st = _l.load().bs_partition_rows(int(n), int(parts), b.ctypes.data)
+    if st != _l.BS_OK:
+        raise _l.CrmsdError(st, "bs_partition_rows")
+    return b
 
 
 def tri_index(n: int, i, j):

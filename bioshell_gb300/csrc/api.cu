@@ -388,8 +388,15 @@ bs_status plain_set(bs_ctx *ctx, const double *dxyz, int64_t n, int L, const Out
   return BS_OK;
 }
 
+// packed-triangle index of the first pair of row r (pairs (i, j), i < j)
+inline int64_t row_off(int64_t n, int64_t r) { return r * n - r * (r + 1) / 2; }
+
 bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_opts &o) {
   ctx->metrics = bs_metrics{};
+  // a row range (bs_all_vs_all only; validated there): rows [rlo, rhi)
+  const bool ranged = nsets == 1 && (o.row_begin != 0 || o.row_end != 0);
+  const int64_t rlo = ranged ? o.row_begin : 0;
+  const int64_t rhi = ranged ? (o.row_end > 0 ? std::min<int64_t>(o.row_end, sets[0].n) : sets[0].n) : 0;
   const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
   // tile shape per set (autotuner, mixed path), before anything is staged
   std::vector<int> narrow(nsets, 0);
@@ -413,7 +420,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     const bs_set_desc &d = sets[k];
     io[k].in_off = io[k].out_off = SIZE_MAX;
     if (d.n < 2) continue;
-    pairs += d.n * (d.n - 1) / 2;
+    pairs += ranged ? row_off(d.n, rhi) - row_off(d.n, rlo) : d.n * (d.n - 1) / 2;
     if (!is_device_ptr(d.xyz)) {
       io[k].in_off = in_bytes;
       in_bytes = align(in_bytes + (size_t)d.n * d.L * 3 * sizeof(double));
@@ -448,6 +455,10 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     if (o.layout == BS_LAYOUT_SQUARE)
       CK(cudaMemset2DAsync(io[k].out_dev, (size_t)(d.n + 1) * esz, 0, esz, (size_t)d.n, ctx->stream), "zero diagonal");
     specs.push_back(JobSpec{io[k].xyz_dev, d.n, d.L, od, narrow[k]});
+    if (ranged) {
+      specs.back().row_lo = rlo;
+      specs.back().row_hi = rhi;
+    }
     set_of_spec.push_back(k);
     ctx->metrics.narrow_jobs += narrow[k];
   }
@@ -477,6 +488,10 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     Plan plan;
     const std::string m = make_symmetric_plan(specs, total_tolerance(o), true, plan);
     if (!m.empty()) return set_err(ctx, BS_ERR_UNSUPPORTED, "%s", m.c_str());
+    if (ranged) {  // the overflow scan stays inside the range
+      plan.scan_lo = row_off(specs[0].n, rlo);
+      plan.scan_hi = row_off(specs[0].n, rhi);
+    }
     unsigned long long cap = std::min<unsigned long long>(kFlagCap, std::max<int64_t>(pairs, 4096));
     if (o.flag_queue > 0) cap = std::min<unsigned long long>(cap, (unsigned long long)o.flag_queue);
     MixedBuffers b;
@@ -485,7 +500,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
     // one large triangle bound for pinned host memory: read back in row
     // bands while the later bands compute
     if (nsets == 1 && specs.size() == 1 && io[0].out_off != SIZE_MAX && o.layout == BS_LAYOUT_TRIANGLE &&
-        pairs >= kBandMinPairs && is_pinned_host(sets[0].out)) {
+        pairs >= kBandMinPairs && is_pinned_host(sets[0].out) && !ranged) {
       if (!ctx->copy_stream) CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream");
       make_bands(plan, specs[0].n, kBands, rb);
       while (ctx->band_ev.size() < rb.tile_end.size() + 1) {
@@ -590,9 +605,15 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
   for (int k = 0; k < nsets; ++k) {
     const bs_set_desc &d = sets[k];
     if (d.n < 2 || io[k].out_off == SIZE_MAX) continue;
-    const size_t bytes = out_elems(d.n, o.layout) * esz;
+    size_t first = 0, bytes = out_elems(d.n, o.layout) * esz;
+    if (ranged) {  // only the range's elements: the rest of the caller's buffer is left as it was
+      first = (size_t)row_off(d.n, rlo) * esz;
+      bytes = (size_t)(row_off(d.n, rhi) - row_off(d.n, rlo)) * esz;
+    }
     if (!banded)
-      CK(cudaMemcpyAsync(d.out, io[k].out_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy result to host");
+      CK(cudaMemcpyAsync(static_cast<char *>(d.out) + first, static_cast<const char *>(io[k].out_dev) + first, bytes,
+                         cudaMemcpyDeviceToHost, ctx->stream),
+         "copy result to host");
     ctx->metrics.bytes_d2h += (int64_t)bytes;
   }
   CK(cudaEventRecord(ctx->ev[5], ctx->stream), "event");
@@ -959,8 +980,33 @@ BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_
   if (s) return s;
   bs_set_desc d{xyz, n, L, 0, out};
   if ((s = validate_sets(ctx, &d, 1))) return s;
+  if (o.row_begin != 0 || o.row_end != 0) {
+    const int64_t hi = o.row_end > 0 ? o.row_end : n;
+    if (o.row_begin < 0 || o.row_begin % kBlockStructs || hi > n || o.row_begin > hi ||
+        (hi % kBlockStructs && hi != n))
+      return set_err(ctx, BS_ERR_INVALID_ARG,
+                     "row range [%d, %d) of %lld structures: bounds must be multiples of 40 (the end may be n)",
+                     o.row_begin, o.row_end, (long long)n);
+    if (o.precision != BS_PRECISION_MIXED || o.layout != BS_LAYOUT_TRIANGLE)
+      return set_err(ctx, BS_ERR_UNSUPPORTED, "row ranges need the mixed path and the packed triangle");
+  }
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
   return sets_impl(ctx, &d, 1, o);
+}
+
+BS_API bs_status bs_partition_rows(int64_t n, int32_t parts, int64_t *bounds) {
+  if (n < 0 || parts < 1 || !bounds) return BS_ERR_INVALID_ARG;
+  const int64_t total = n > 1 ? n * (n - 1) / 2 : 0;
+  bounds[0] = 0;
+  int64_t r = 0;
+  for (int32_t p = 1; p < parts; ++p) {
+    // the first block boundary at or past p / parts of the pairs
+    const int64_t want = (int64_t)((double)total * p / parts);
+    while (r < n && row_off(n, r) < want) r += kBlockStructs;
+    bounds[p] = std::min(r, n);
+  }
+  bounds[parts] = n;
+  return BS_OK;
 }
 
 BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets, const bs_opts *opts) {
@@ -972,6 +1018,7 @@ BS_API bs_status bs_batched(bs_ctx *ctx, const bs_set_desc *sets, int32_t nsets,
   bs_status s = check_opts(ctx, &o);
   if (s) return s;
   if ((s = validate_sets(ctx, sets, nsets))) return s;
+  if (o.row_begin != 0 || o.row_end != 0) return set_err(ctx, BS_ERR_INVALID_ARG, "row ranges apply to bs_all_vs_all only");
   if (cudaSetDevice(ctx->device) != cudaSuccess) return set_err(ctx, BS_ERR_CUDA, "cudaSetDevice failed");
   return sets_impl(ctx, sets, nsets, o);
 }

@@ -48,9 +48,13 @@ struct JobSpec {
   int L;
   OutDesc out;
   int narrow = 0;
+  int64_t row_lo = 0, row_hi = -1;  // rows of the pairs to compute (multiples of 40, or n); -1: all
 };
 
 struct Plan {
+  // overflow scan of the recomputation (non-banded launches): output
+  // elements [scan_lo, scan_hi) of job 0, or everything (scan_hi < 0)
+  int64_t scan_lo = 0, scan_hi = -1;
   std::vector<Job> jobs;  // host part filled, device part zero
   std::vector<int> jobmap;
   std::vector<Tile> tiles;

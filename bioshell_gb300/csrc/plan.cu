@@ -63,9 +63,12 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
     const int64_t bs = jb.narrow ? kNarrowStructs : kBStructs, r = kBlockStructs / bs;
     const int64_t nba = blocks_for(jb.n), nbb = (jb.n + bs - 1) / bs;
     const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / bs;
+    // a row range keeps the tiles of its A blocks (40-structure multiples)
+    const int64_t ilo = specs[j].row_lo / kBlockStructs;
+    const int64_t ihi = specs[j].row_hi < 0 ? nba : (specs[j].row_hi + kBlockStructs - 1) / kBlockStructs;
     for (int64_t sa = 0; sa < nba; sa += SA)
       for (int64_t sb = r * sa; sb < nbb; sb += SB * r / 2)
-        for (int64_t I = sa; I < std::min(sa + SA, nba); ++I)
+        for (int64_t I = std::max(sa, ilo); I < std::min(std::min(sa + SA, nba), ihi); ++I)
           for (int64_t J = std::max(sb, r * I); J < std::min(sb + SB * r / 2, nbb); ++J)
             plan.tiles.push_back(Tile{(int)(a0 + I), (int)(b0 + J), j, 0});
   }
@@ -237,6 +240,8 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
         return e;
       if ((e = rec(2)) != cudaSuccess) return e;
       // screen tiles flag no pair: nothing to recompute
+      r.scan_lo = plan.scan_lo;
+      r.scan_hi = plan.scan_hi;
       if (!all_screen && (e = launch_refine(r, st)) != cudaSuccess) return e;
     } else {
       const size_t nb = rb->tile_end.size();

@@ -31,7 +31,8 @@ FLAG_AUTOTUNE = 2
 class bs_opts(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("precision", ctypes.c_int32), ("layout", ctypes.c_int32),
                 ("out_type", ctypes.c_int32), ("tolerance", ctypes.c_double), ("flags", ctypes.c_int32),
-                ("flag_queue", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+                ("flag_queue", ctypes.c_int32), ("row_begin", ctypes.c_int32), ("row_end", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 class bs_set_desc(ctypes.Structure):
@@ -146,6 +147,7 @@ SIGNATURES = [
                                             ctypes.c_int32, _fp, _fp]),
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
     ("bs_debug_set_wait_limit", ctypes.c_int32, [_vp, ctypes.c_int64]),
+    ("bs_partition_rows", ctypes.c_int32, [ctypes.c_int64, ctypes.c_int32, _vp]),
     ("bs_debug_fail_alloc", ctypes.c_int32, [_vp, ctypes.c_int64]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                               _fp, _dp]),

@@ -105,7 +105,15 @@ typedef struct {
                          recompute exactly; <= 0 selects the default,
                          min(2^24, pairs).  Pairs flagged beyond it are
                          found by a scan of the result for their sentinel  */
-  int32_t reserved[6];
+  int32_t row_begin;  /* bs_all_vs_all, mixed path, packed triangle: only
+                         the pairs (i, j) with row_begin <= i < row_end are
+                         computed and written; the rest of `out` (which
+                         keeps its full n(n-1)/2 size) is left untouched.
+                         row_begin a multiple of 40; row_end a multiple of
+                         40 or n; both 0 = every row.  The partition of one
+                         all-vs-all over several GPUs (bs_partition_rows)  */
+  int32_t row_end;
+  int32_t reserved[4];
 } bs_opts;
 
 /* bs_opts.flags */
@@ -194,6 +202,14 @@ BS_API bs_status bs_superpose_pairs(bs_ctx *ctx, const double *xyz, int64_t n, i
  * HierarchicalClusteringMatrix::new (clustering_matrix.rs:11-22). */
 BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const bs_opts *opts,
                                void *out);
+
+/* Row ranges that split the n(n-1)/2 pairs of one all-vs-all into `parts`
+ * ranges of nearly equal pair counts (bounds[0] = 0 <= bounds[1] <= ... <=
+ * bounds[parts] = n, inner bounds multiples of 40 or n): part p is the row range
+ * [bounds[p], bounds[p+1]) of bs_opts.row_begin/row_end, e.g. one per GPU,
+ * each with its own context and no exchange between them (the pairs are
+ * independent).  Host only. */
+BS_API bs_status bs_partition_rows(int64_t n, int32_t parts, int64_t *bounds);
 
 /* One structure set of a batched call. */
 typedef struct {

@@ -80,7 +80,9 @@ pub struct BsOpts {
     pub tolerance: f64,
     pub flags: i32,
     pub flag_queue: i32,
-    pub reserved: [i32; 6],
+    pub row_begin: i32,
+    pub row_end: i32,
+    pub reserved: [i32; 4],
 }
 
 /// `bs_metrics`: per-call counters of the last compute call on a context.
@@ -186,6 +188,7 @@ extern "C" {
     pub fn bs_pairs(ctx: *mut BsCtx, xyz: *const f64, n: i64, l: i32, ii: *const i64, jj: *const i64,
                     npairs: i64, opts: *const BsOpts, out: *mut f64) -> BsStatus;
     pub fn bs_all_vs_all_static(xyz: *const f64, n: i64, l: i32, out: *mut f64, stream: *mut c_void) -> BsStatus;
+    pub fn bs_partition_rows(n: i64, parts: i32, bounds: *mut i64) -> BsStatus;
 
     // ---- serving
     pub fn bs_server_create(out: *mut *mut BsServer, device: i32, cfg: *const BsServerConfig) -> BsStatus;

@@ -95,3 +95,19 @@ def test_null_context_is_rejected(enginelib):
     assert enginelib.bs_all_vs_all(None, None, 0, 1, None, None) == 1
     assert enginelib.bs_ctx_create(None, 0, 0) == 1
     assert enginelib.bs_last_error(None) == b"null context"
+
+
+def test_partition_rows_balances_pairs(enginelib):
+    """bs_partition_rows: bounds from 0 to n, inner bounds on 40-structure
+    blocks, and ranges whose pair counts differ by at most one block row."""
+    from bioshell_gb300.crmsd import partition_rows
+    for n, parts in ((50000, 8), (20000, 3), (1000, 4), (39, 2), (0, 1)):
+        b = partition_rows(n, parts)
+        assert b[0] == 0 and b[-1] == n and all(b[k] <= b[k + 1] for k in range(parts))
+        assert all(v % 40 == 0 or v == n for v in b[1:-1])
+        off = [int(r) * n - int(r) * (int(r) + 1) // 2 for r in b]
+        counts = [off[k + 1] - off[k] for k in range(parts)]
+        assert sum(counts) == n * (n - 1) // 2
+        if n >= 1000:  # one block row holds at most 40 (n - 1) pairs
+            assert max(counts) - min(counts) <= 2 * 40 * n
+    assert enginelib.bs_partition_rows(10, 0, None) == 1

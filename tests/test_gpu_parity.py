@@ -179,3 +179,39 @@ def test_device_pointers(engine, golden_small):
     engine.all_vs_all(x, out=out)
     torch.cuda.synchronize()
     assert np.abs(out.cpu().numpy() - golden_small["rmsd"]).max() <= TOL_MIXED
+
+
+def test_row_ranges_partition_the_matrix(engine, oracle_mod):
+    """Row ranges (bs_opts.row_begin/row_end): three ranges from
+    bs_partition_rows, written into one host buffer, give the full call's
+    result bit for bit; a single range leaves every element outside it as it
+    was; bad ranges are rejected.  One range per GPU partitions an
+    all-vs-all with no exchange between them."""
+    from bioshell_gb300.crmsd import partition_rows
+    from bioshell_gb300.lib import CrmsdError
+    rng = np.random.default_rng(55)
+    x = synth.decoys(synth.base_chain(90, rng), 1000, rng, near_dup_frac=0.1)
+    n = x.shape[0]
+    full = engine.all_vs_all(x).values.copy()
+    b = partition_rows(n, 3)
+    out = np.full(n * (n - 1) // 2, -7.0)
+    for p in range(3):
+        engine.all_vs_all(x, CrmsdOptions(rows=(int(b[p]), int(b[p + 1]))), out=out)
+    np.testing.assert_array_equal(out, full)
+    # one range alone: the rest untouched, pinned and device outputs too
+    lo, hi = int(b[1]), int(b[2])
+    e0, e1 = lo * n - lo * (lo + 1) // 2, hi * n - hi * (hi + 1) // 2
+    oh = engine.host_empty((n * (n - 1) // 2,), np.float64)
+    oh[...] = -7.0
+    engine.all_vs_all(x, CrmsdOptions(rows=(lo, hi)), out=oh)
+    assert engine.metrics()["pairs"] == e1 - e0
+    np.testing.assert_array_equal(oh[e0:e1], full[e0:e1])
+    assert np.all(oh[:e0] == -7.0) and np.all(oh[e1:] == -7.0)
+    assert np.abs(full[e0:e1] - oracle_mod.crmsd_all_vs_all(x)[e0:e1]).max() <= TOL_MIXED
+    for bad in ((1, 80), (40, 81), (80, 40), (0, n + 40)):
+        with pytest.raises(CrmsdError) as ei:
+            engine.all_vs_all(x, CrmsdOptions(rows=bad))
+        assert ei.value.status == 1
+    with pytest.raises(CrmsdError) as ei:
+        engine.all_vs_all(x, CrmsdOptions(rows=(0, 80), precision="plain64"))
+    assert ei.value.status == 5
