@@ -378,6 +378,18 @@ def run_batched(a, eng, stream, torch):
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1) / a.steps
     graph = mets[-1]["graph"]
+    # the fixed default (every set on 40 x 20 tiles) against the tuned shapes
+    wide = CrmsdOptions()
+    eng.batched(dev, wide, outs=outs)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        eng.batched(dev, wide, outs=outs)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms_wide = ev0.elapsed_time(ev1) / a.steps
+    tuning = eng.tuning()
+    n_narrow_classes = sum(1 for c in tuning["classes"] if c[2] == "narrow")
     # plain FP64 path on the same sets
     outs64 = [torch.empty_like(o) for o in outs]
     eng.batched(dev, CrmsdOptions(precision="plain64"), outs=outs64)
@@ -415,6 +427,8 @@ def run_batched(a, eng, stream, torch):
             "ms_refine": statistics.mean(m["ms_refine"] for m in mets),
             "pairs_refined": int(mets[-1]["pairs_refined"]),
             "autotune": {"classes_timed": tuned, "narrow_sets": int(mets[-1]["narrow_jobs"]),
+                         "classes_narrow": n_narrow_classes, "classes_wide": len(tuning["classes"]) - n_narrow_classes,
+                         "ms_all_wide_default": ms_wide, "gain_vs_all_wide": ms_wide / ms,
                          "warmup_s_incl_tuning": t_tune},
             "e2e": {"value": pairs / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": int(sum(x.nbytes for x in sets)), "d2h_bytes_per_step": int(pairs * 8)},

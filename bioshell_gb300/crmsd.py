@@ -249,6 +249,36 @@ class Engine:
     def set_tile_shape(self, L: int, n: int, shape: str):
         self._check(self._lib.bs_tune_set(self._h, int(L), int(n), 1 if shape == "narrow" else 0))
 
+    def tuning(self) -> dict:
+        """The autotuner's cache: {"num_sms": N, "classes": [[L, n, "wide"|"narrow"], ...]}
+        with (L, n) a representative chain length and set size of each class."""
+        cnt, sms = ctypes.c_int32(), ctypes.c_int32()
+        self._check(self._lib.bs_tune_list(self._h, None, None, None, 0, ctypes.byref(cnt), ctypes.byref(sms)))
+        k = cnt.value
+        Ls, ns, nw = np.zeros(k, np.int32), np.zeros(k, np.int64), np.zeros(k, np.int32)
+        self._check(self._lib.bs_tune_list(self._h, Ls.ctypes.data, ns.ctypes.data, nw.ctypes.data, k,
+                                           ctypes.byref(cnt), ctypes.byref(sms)))
+        return {"num_sms": int(sms.value),
+                "classes": [[int(a), int(b), "narrow" if c else "wide"] for a, b, c in zip(Ls, ns, nw)]}
+
+    def save_tuning(self, path: str):
+        """Writes the autotuner's cache as JSON, keyed by the GPU's SM count."""
+        import json
+        with open(path, "w") as fh:
+            json.dump(self.tuning(), fh)
+
+    def load_tuning(self, path: str) -> bool:
+        """Restores a cache saved on a GPU with the same SM count (False, and
+        nothing loaded, for another SM count)."""
+        import json
+        with open(path) as fh:
+            t = json.load(fh)
+        if int(t.get("num_sms", -1)) != self.tuning()["num_sms"]:
+            return False
+        for L, n, shape in t["classes"]:
+            self.set_tile_shape(L, n, shape)
+        return True
+
     def pairs(self, xyz, ii, jj, opts: Optional[CrmsdOptions] = None, out=None):
         opts = opts or CrmsdOptions()
         if isinstance(xyz, np.ndarray):

@@ -1116,6 +1116,23 @@ BS_API bs_status bs_tune_set(bs_ctx *ctx, int32_t L, int64_t n, int32_t narrow) 
   return BS_OK;
 }
 
+BS_API bs_status bs_tune_list(bs_ctx *ctx, int32_t *L_class, int64_t *n_class, int32_t *narrow, int32_t cap,
+                              int32_t *count, int32_t *num_sms) {
+  if (!ctx || !count || !num_sms || cap < 0 || (cap > 0 && (!L_class || !n_class || !narrow)))
+    return BS_ERR_INVALID_ARG;
+  *count = (int32_t)ctx->tune.size();
+  *num_sms = ctx->num_sms;
+  int32_t k = 0;
+  for (const auto &kv : ctx->tune) {  // key = (pitch / 64) * 64 + ceil(log2 n)
+    if (k >= cap) break;
+    L_class[k] = (int32_t)(kv.first / 64) * kKChunk;
+    n_class[k] = 1ll << (kv.first % 64);
+    narrow[k] = kv.second;
+    ++k;
+  }
+  return BS_OK;
+}
+
 BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const int64_t *ii, const int64_t *jj,
                           int64_t npairs, const bs_opts *opts, double *out) {
   if (!ctx) return BS_ERR_INVALID_ARG;
@@ -1262,8 +1279,11 @@ std::map<void *, size_t> g_near;
 // where each CPU socket has its own GPU link (Grace), copies between a GPU
 // and the other socket's memory cross the socket link and run at a fraction
 // of the GPU link's rate.  cudaHostAlloc places the pages on the node of the
-// calling thread, which may be the other socket.  Returns null where the
-// GPU reports no host NUMA node or the placement fails.
+// calling thread, which may be the other socket.  The region is aligned to
+// 2 MB and marked for transparent huge pages, so that where the kernel
+// allows them the GPU's copies walk 2 MB pages instead of 4 KB ones.
+// Returns null where the GPU reports no host NUMA node or the placement
+// fails.
 void *alloc_near_gpu(size_t bytes) {
 #if defined(__linux__) && defined(SYS_mbind)
   int dev = 0, numa = -1;
@@ -1273,20 +1293,29 @@ void *alloc_near_gpu(size_t bytes) {
   }
   constexpr int kMaxNodes = 1024;
   constexpr int kBits = 8 * (int)sizeof(unsigned long);
+  constexpr size_t kHuge = size_t(2) << 20;
   if (numa < 0 || numa >= kMaxNodes) return nullptr;
-  void *p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-  if (p == MAP_FAILED) return nullptr;
+  const size_t span = (bytes + kHuge - 1) & ~(kHuge - 1);
+  // reserve one huge page more, keep the 2 MB-aligned part
+  char *raw = static_cast<char *>(mmap(nullptr, span + kHuge, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0));
+  if (raw == MAP_FAILED) return nullptr;
+  char *p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(raw) + kHuge - 1) & ~uintptr_t(kHuge - 1));
+  if (p > raw) munmap(raw, (size_t)(p - raw));
+  if (raw + span + kHuge > p + span) munmap(p + span, (size_t)(raw + span + kHuge - (p + span)));
+#if defined(MADV_HUGEPAGE)
+  madvise(p, span, MADV_HUGEPAGE);  // advice only: a kernel without THP ignores it
+#endif
   unsigned long mask[kMaxNodes / kBits] = {};
   mask[numa / kBits] |= 1ul << (numa % kBits);
   const long kPreferred = 1;  // MPOL_PREFERRED: that node while it has free pages
-  if (syscall(SYS_mbind, p, bytes, kPreferred, mask, (unsigned long)kMaxNodes + 1, 0ul) != 0 ||
-      cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
+  if (syscall(SYS_mbind, p, span, kPreferred, mask, (unsigned long)kMaxNodes + 1, 0ul) != 0 ||
+      cudaHostRegister(p, span, cudaHostRegisterDefault) != cudaSuccess) {
     cudaGetLastError();
-    munmap(p, bytes);
+    munmap(p, span);
     return nullptr;
   }
   std::lock_guard<std::mutex> lk(g_near_mu);
-  g_near[p] = bytes;
+  g_near[p] = span;
   return p;
 #else
   (void)bytes;

@@ -148,6 +148,7 @@ SIGNATURES = [
     ("bs_debug_tile_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _fp]),
     ("bs_debug_set_wait_limit", ctypes.c_int32, [_vp, ctypes.c_int64]),
     ("bs_partition_rows", ctypes.c_int32, [ctypes.c_int64, ctypes.c_int32, _vp]),
+    ("bs_tune_list", ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, _vp, _vp]),
     ("bs_debug_fail_alloc", ctypes.c_int32, [_vp, ctypes.c_int64]),
     ("bs_debug_pair_levels", ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, ctypes.c_int64,
                                               _fp, _dp]),

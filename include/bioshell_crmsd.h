@@ -245,6 +245,13 @@ BS_API bs_status bs_neighbors_get(bs_ctx *ctx, int64_t *row_ptr, int32_t *col, f
  * class's choice (it is then not timed). */
 BS_API bs_status bs_tune_get(bs_ctx *ctx, int32_t L, int64_t n, int32_t *narrow);
 BS_API bs_status bs_tune_set(bs_ctx *ctx, int32_t L, int64_t n, int32_t narrow);
+/* The cache as a list, to persist it: up to `cap` classes, each as
+ * (L_class, n_class, narrow) with L_class atoms and n_class structures a
+ * representative of the class (bs_tune_set(ctx, L_class, n_class, narrow)
+ * restores it); *count is the number of classes cached, *num_sms the
+ * context's SM count (a cache applies to GPUs of that size). */
+BS_API bs_status bs_tune_list(bs_ctx *ctx, int32_t *L_class, int64_t *n_class, int32_t *narrow, int32_t cap,
+                              int32_t *count, int32_t *num_sms);
 
 /* crmsd of an explicit pair list: out[t] = crmsd(xyz[ii[t]], xyz[jj[t]]),
  * f64.  Used for sampled checks and for sparse consumers. */

@@ -185,6 +185,8 @@ extern "C" {
     pub fn bs_neighbors_get(ctx: *mut BsCtx, row_ptr: *mut i64, col: *mut i32, dist: *mut f32) -> BsStatus;
     pub fn bs_tune_get(ctx: *mut BsCtx, l: i32, n: i64, narrow: *mut i32) -> BsStatus;
     pub fn bs_tune_set(ctx: *mut BsCtx, l: i32, n: i64, narrow: i32) -> BsStatus;
+    pub fn bs_tune_list(ctx: *mut BsCtx, l_class: *mut i32, n_class: *mut i64, narrow: *mut i32, cap: i32,
+                        count: *mut i32, num_sms: *mut i32) -> BsStatus;
     pub fn bs_pairs(ctx: *mut BsCtx, xyz: *const f64, n: i64, l: i32, ii: *const i64, jj: *const i64,
                     npairs: i64, opts: *const BsOpts, out: *mut f64) -> BsStatus;
     pub fn bs_all_vs_all_static(xyz: *const f64, n: i64, l: i32, out: *mut f64, stream: *mut c_void) -> BsStatus;

@@ -174,3 +174,32 @@ def test_autotuner_times_each_class_once(engine):
     assert engine.metrics()["tuned_classes"] == 0
     for x, mtx in zip(sets, again):
         np.testing.assert_array_equal(mtx.values, engine.all_vs_all(x).values)
+
+
+def test_tuning_cache_persists_as_json(engine, tmp_path):
+    """The autotuner's cache written as JSON (keyed by the SM count) and read
+    into a fresh context: the same choices, and no class timed again."""
+    from bioshell_gb300.crmsd import Engine
+    sets = _sets(17, [(70, 48), (1300, 120)])
+    engine.batched(sets, CrmsdOptions(autotune=True))
+    path = tmp_path / "tuning.json"
+    engine.save_tuning(str(path))
+    saved = engine.tuning()
+    assert saved["num_sms"] > 0 and len(saved["classes"]) >= 2
+    fresh = Engine(0)
+    try:
+        assert fresh.tuning()["classes"] == []
+        assert fresh.load_tuning(str(path))
+        assert sorted(map(tuple, fresh.tuning()["classes"])) == sorted(map(tuple, saved["classes"]))
+        fresh.batched(sets, CrmsdOptions(autotune=True))
+        assert fresh.metrics()["tuned_classes"] == 0
+        for x in sets:
+            assert fresh.tile_shape(x.shape[1], x.shape[0]) == engine.tile_shape(x.shape[1], x.shape[0])
+        # a cache from a GPU of another size is not applied
+        import json
+        other = json.loads(path.read_text())
+        other["num_sms"] += 1
+        path.write_text(json.dumps(other))
+        assert not Engine(0).load_tuning(str(path))
+    finally:
+        fresh.close()
