@@ -168,6 +168,12 @@ struct bs_ctx {
   bs::DevScalars *sc_back = nullptr;
   // cached tables of the last plan
   std::vector<int64_t> plan_key;
+  // host tile table of the last symmetric plan, reused by a call whose jobs
+  // have the same sizes, chain lengths, tile shapes and row ranges; and the
+  // row bands of its banded read-back
+  std::vector<bs::Tile> tile_cache;
+  std::vector<int64_t> tile_key;
+  std::vector<int64_t> band_key, band_tile_end, band_elem_end;
   // graph cache
   struct Graph {
     std::vector<int64_t> key;

@@ -55,22 +55,33 @@ std::string make_symmetric_plan(const std::vector<JobSpec> &specs, float tol, bo
   plan.pitch = pitch;
   if (!with_tiles) return "";
   constexpr int64_t SA = 32, SB = 64;  // super-block: 32 A blocks x 64 B blocks
-  for (int j : order) {
-    const Job &jb = plan.jobs[j];
-    if (jb.n < 2) continue;
-    // B blocks of bs structures; tile (I, J) holds a pair i < j iff
-    // bs J + bs - 1 > 40 I, i.e. J >= r I with r = 40 / bs
-    const int64_t bs = jb.narrow ? kNarrowStructs : kBStructs, r = kBlockStructs / bs;
-    const int64_t nba = blocks_for(jb.n), nbb = (jb.n + bs - 1) / bs;
-    const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / bs;
-    // a row range keeps the tiles of its A blocks (40-structure multiples)
-    const int64_t ilo = specs[j].row_lo / kBlockStructs;
-    const int64_t ihi = specs[j].row_hi < 0 ? nba : (specs[j].row_hi + kBlockStructs - 1) / kBlockStructs;
-    for (int64_t sa = 0; sa < nba; sa += SA)
-      for (int64_t sb = r * sa; sb < nbb; sb += SB * r / 2)
-        for (int64_t I = std::max(sa, ilo); I < std::min(std::min(sa + SA, nba), ihi); ++I)
-          for (int64_t J = std::max(sb, r * I); J < std::min(sb + SB * r / 2, nbb); ++J)
-            plan.tiles.push_back(Tile{(int)(a0 + I), (int)(b0 + J), j, 0});
+  // two passes over the same loops: the count (per A block and super-block),
+  // then the tiles into a table of exactly that size
+  for (int pass = 0; pass < 2; ++pass) {
+    int64_t count = 0;
+    for (int j : order) {
+      const Job &jb = plan.jobs[j];
+      if (jb.n < 2) continue;
+      // B blocks of bs structures; tile (I, J) holds a pair i < j iff
+      // bs J + bs - 1 > 40 I, i.e. J >= r I with r = 40 / bs
+      const int64_t bs = jb.narrow ? kNarrowStructs : kBStructs, r = kBlockStructs / bs;
+      const int64_t nba = blocks_for(jb.n), nbb = (jb.n + bs - 1) / bs;
+      const int64_t a0 = jb.first_a / kBlockStructs, b0 = jb.first_a / bs;
+      // a row range keeps the tiles of its A blocks (40-structure multiples)
+      const int64_t ilo = specs[j].row_lo / kBlockStructs;
+      const int64_t ihi = specs[j].row_hi < 0 ? nba : (specs[j].row_hi + kBlockStructs - 1) / kBlockStructs;
+      for (int64_t sa = 0; sa < nba; sa += SA)
+        for (int64_t sb = r * sa; sb < nbb; sb += SB * r / 2)
+          for (int64_t I = std::max(sa, ilo); I < std::min(std::min(sa + SA, nba), ihi); ++I) {
+            const int64_t jlo = std::max(sb, r * I), jhi = std::min(sb + SB * r / 2, nbb);
+            if (pass == 0) {
+              count += std::max<int64_t>(0, jhi - jlo);
+              continue;
+            }
+            for (int64_t J = jlo; J < jhi; ++J) plan.tiles.push_back(Tile{(int)(a0 + I), (int)(b0 + J), j, 0});
+          }
+    }
+    if (pass == 0) plan.tiles.reserve((size_t)count);
   }
   return "";
 }

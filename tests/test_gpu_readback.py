@@ -56,6 +56,50 @@ def test_banded_readback_equals_device_result(engine, dup_set):
     np.testing.assert_array_equal(op, ref)
 
 
+def test_reused_tile_table_and_bands(engine, dup_set):
+    """A context keeps the last call's tile table and read-back bands and
+    reuses them for a call of the same shapes.  Calls that alternate shapes,
+    row ranges and neighbour lists, and repeat a shape with other
+    coordinates, must equal a fresh context's results bit for bit."""
+    from bioshell_gb300.crmsd import Engine
+    x = dup_set
+    n = x.shape[0]
+    y = np.ascontiguousarray(x[::-1])  # the same shape, other coordinates in every position
+    small = np.ascontiguousarray(x[:777])
+    fresh = Engine(0)
+    try:
+        def ref(z, opts=None):
+            return fresh.all_vs_all(z, opts).values.copy()
+
+        ref_x, ref_y, ref_s = ref(x), ref(y), ref(small)
+        ref_r = ref(x, CrmsdOptions(rows=(400, 1200)))
+        xh = engine.host_empty(x.shape, np.float64)
+        oh = engine.host_empty((n * (n - 1) // 2,), np.float64)
+        for z, want in ((x, ref_x), (y, ref_y), (small, ref_s), (x, ref_x), (y, ref_y)):
+            if z.shape[0] == n:  # pinned in and out: the banded path
+                xh[...] = z
+                oh[...] = -7.0
+                engine.all_vs_all(xh, CrmsdOptions(), out=oh)
+                assert engine.metrics()["main_launches"] > 9
+                np.testing.assert_array_equal(oh, want)
+            else:
+                np.testing.assert_array_equal(engine.all_vs_all(z).values, want)
+        # a row range of the same n: its own tile table, then the full one again
+        e0, e1 = 400 * n - 400 * 401 // 2, 1200 * n - 1200 * 1201 // 2
+        xh[...] = x
+        oh[...] = -7.0
+        engine.all_vs_all(xh, CrmsdOptions(rows=(400, 1200)), out=oh)
+        np.testing.assert_array_equal(oh[e0:e1], ref_r[e0:e1])
+        engine.all_vs_all(small, CrmsdOptions(rows=(0, 80)))
+        engine.neighbors(small, 2.0)
+        np.testing.assert_array_equal(engine.all_vs_all(small).values, ref_s)
+        xh[...] = y
+        engine.all_vs_all(xh, CrmsdOptions(), out=oh)
+        np.testing.assert_array_equal(oh, ref_y)
+    finally:
+        fresh.close()
+
+
 @pytest.mark.parametrize("pinned", [False, True])
 def test_queue_overflow_scan(engine, dup_set, pinned):
     x = dup_set
