@@ -119,13 +119,19 @@ extern "C" BS_API bs_status bs_all_vs_all_static(const double *xyz, int64_t n, i
   if (n < 0 || L < 1) return BS_ERR_INVALID_ARG;
   if (n > kMaxN || L > kMaxL) return BS_ERR_UNSUPPORTED;  // beyond the static scratch
   if (n < 2) return BS_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the call copies tables from host memory, reads its counters back and
+  // synchronises, none of which a stream capture allows: refuse before any
+  // other CUDA call, so the caller's capture stays valid
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return BS_ERR_CUDA;
+  if (cap != cudaStreamCaptureStatusNone) return BS_ERR_UNSUPPORTED;
   if (!xyz || !out || !is_device_ptr(xyz) || !is_device_ptr(out)) return BS_ERR_INVALID_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return BS_ERR_NO_DEVICE;
   Scratch *sc = nullptr;
   bs_status s = setup(dev, &sc);
   if (s) return s;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   std::vector<JobSpec> specs{JobSpec{xyz, n, L, OutDesc{out, n, n, kLayoutTriangle, 0}}};
   Plan plan;

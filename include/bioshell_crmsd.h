@@ -271,8 +271,10 @@ BS_API bs_status bs_pairs(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, 
  *     BS_ERR_UNSUPPORTED without touching the GPU.
  *   - Scratch lives in static device arrays of the library (about 7.4 MB,
  *     held by every GPU that loads the library until the process exits).
- *   - The first call on a device looks up the arrays' device addresses; make
- *     it before capturing the stream into a CUDA graph.
+ *   - The call cannot be captured into a CUDA graph: it copies its tables
+ *     from host memory, reads its counters back and synchronises `stream`.
+ *     On a stream that is being captured it returns BS_ERR_UNSUPPORTED
+ *     before any other CUDA call, and the capture stays valid.
  *   - All calls share the scratch: each call clears what must start at zero,
  *     but calls whose work overlaps on the GPU (e.g. on two streams at once)
  *     race and must not be issued. */

@@ -62,3 +62,26 @@ def test_static_rejects_sizes_beyond_its_scratch(enginelib):
     host = np.zeros((4, 8, 3))
     assert enginelib.bs_all_vs_all_static(host.ctypes.data_as(ctypes.c_void_p), 4, 8,
                                           ctypes.c_void_p(out.data_ptr()), None) == 1  # host memory: invalid
+
+
+def test_static_refuses_a_capturing_stream(enginelib):
+    """The entry point copies from host memory and synchronises, which stream
+    capture forbids: on a capturing stream it returns BS_ERR_UNSUPPORTED
+    without a CUDA call that would invalidate the capture, and the captured
+    graph still runs."""
+    torch = pytest.importorskip("torch")
+    n, L = 40, 16
+    x = torch.zeros((n, L, 3), dtype=torch.float64, device="cuda")
+    out = torch.zeros(n * (n - 1) // 2, dtype=torch.float64, device="cuda")
+    y = torch.zeros(4, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        st = enginelib.bs_all_vs_all_static(ctypes.c_void_p(x.data_ptr()), n, L, ctypes.c_void_p(out.data_ptr()),
+                                            ctypes.c_void_p(s.cuda_stream))
+        y.add_(1.0)
+    assert st == 5  # BS_ERR_UNSUPPORTED
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(y[0]) == 1.0
