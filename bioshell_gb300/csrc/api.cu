@@ -433,6 +433,35 @@ bs_status plain_set(bs_ctx *ctx, const double *dxyz, int64_t n, int L, const Out
 // packed-triangle index of the first pair of row r (pairs (i, j), i < j)
 inline int64_t row_off(int64_t n, int64_t r) { return r * n - r * (r + 1) / 2; }
 
+// After a mixed launch: structure sets that no coordinate grid fits (the
+// digit-1 products of chains beyond ~3,000 atoms exceed the exact range even
+// in quarters of the chain; coordinates beyond +-32768 A) are computed on the
+// plain FP64 path instead, into the same output, and their error is cleared.
+// The mixed kernels wrote nothing of those sets.  A row-ranged call keeps
+// the error: the plain path writes every row.
+bs_status plain_fallback(bs_ctx *ctx, const std::vector<JobSpec> &specs, const std::vector<int> &set_of_spec,
+                         const bs_set_desc *sets, const std::vector<SetIO> &io, const bs_opts &o, bool ranged) {
+  Job *jobs = static_cast<Job *>(ctx->job_back);
+  if (ctx->sc_back->err || ranged) return BS_OK;  // reported as they are
+  const size_t esz = o.out_type == BS_OUT_F64 ? 8 : 4;
+  bool any = false;
+  for (size_t j = 0; j < specs.size(); ++j) {
+    if ((jobs[j].err & kErrNonFinite) || !(jobs[j].err & kErrUnsupported)) continue;
+    bs_status s = plain_set(ctx, specs[j].xyz, specs[j].n, specs[j].L, specs[j].out);
+    if (s) return s;
+    const int k = set_of_spec[j];
+    if (io[k].out_off != SIZE_MAX)
+      CK(cudaMemcpyAsync(sets[k].out, io[k].out_dev, out_elems(sets[k].n, o.layout) * esz, cudaMemcpyDeviceToHost,
+                         ctx->stream),
+         "copy result to host");
+    jobs[j].err &= ~kErrUnsupported;
+    ctx->metrics.pairs_plain += specs[j].n * (specs[j].n - 1) / 2;
+    any = true;
+  }
+  if (any) CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+  return BS_OK;
+}
+
 bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_opts &o) {
   ctx->metrics = bs_metrics{};
   // a row range (bs_all_vs_all only; validated there): rows [rlo, rhi)
@@ -676,6 +705,7 @@ bs_status sets_impl(bs_ctx *ctx, const bs_set_desc *sets, int nsets, const bs_op
   if (o.precision == BS_PRECISION_PLAIN64) {
     if (ctx->sc_back->err & kErrNonFinite) return set_err(ctx, BS_ERR_NONFINITE, "input coordinates contain NaN or Inf");
   } else if (!specs.empty()) {
+    if ((s = plain_fallback(ctx, specs, set_of_spec, sets, io, o, ranged))) return s;
     if ((s = finish_mixed(ctx, (int)specs.size()))) return s;
   }
   // single structures: their one square entry is the zero diagonal

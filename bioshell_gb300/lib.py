@@ -47,7 +47,7 @@ class bs_metrics(ctypes.Structure):
                 ("main_launches", ctypes.c_int32), ("jobs", ctypes.c_int32), ("graph", ctypes.c_int32),
                 ("quant_bound", ctypes.c_double),
                 ("bytes_h2d", ctypes.c_int64), ("bytes_d2h", ctypes.c_int64), ("narrow_jobs", ctypes.c_int32),
-                ("tuned_classes", ctypes.c_int32)]
+                ("tuned_classes", ctypes.c_int32), ("pairs_plain", ctypes.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -151,6 +151,10 @@ typedef struct {
   int64_t bytes_d2h;
   int32_t narrow_jobs;     /* structure sets run with 40 x 10 tiles          */
   int32_t tuned_classes;   /* shape classes the autotuner timed in this call */
+  int64_t pairs_plain;     /* mixed path: pairs of structure sets that no
+                              coordinate grid fits (chains beyond ~3,000
+                              atoms, coordinates beyond +-32768 A), computed
+                              on the plain FP64 GPU path instead            */
 } bs_metrics;
 
 /* ---- version / errors -------------------------------------------------- */
@@ -199,7 +203,11 @@ BS_API bs_status bs_superpose_pairs(bs_ctx *ctx, const double *xyz, int64_t n, i
 /* All-vs-all crmsd of n structures xyz[n][L][3] into `out` (layout and
  * element type from `opts`, NULL = defaults: mixed precision, packed f64
  * triangle).  Replaces the n(n-1)/2 distance-closure calls of
- * HierarchicalClusteringMatrix::new (clustering_matrix.rs:11-22). */
+ * HierarchicalClusteringMatrix::new (clustering_matrix.rs:11-22).
+ * Chains of up to 16,384 atoms.  On the mixed path a structure set that no
+ * coordinate grid fits (chains beyond ~3,000 atoms, or coordinates beyond
+ * +-32768 A) is computed on the plain FP64 GPU path instead
+ * (bs_metrics.pairs_plain); with a row range it returns BS_ERR_UNSUPPORTED. */
 BS_API bs_status bs_all_vs_all(bs_ctx *ctx, const double *xyz, int64_t n, int32_t L, const bs_opts *opts,
                                void *out);
 

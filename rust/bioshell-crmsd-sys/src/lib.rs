@@ -106,6 +106,7 @@ pub struct BsMetrics {
     pub bytes_d2h: i64,
     pub narrow_jobs: i32,
     pub tuned_classes: i32,
+    pub pairs_plain: i64,
 }
 
 /// `bs_set_desc`: one structure set of a batched call.

@@ -135,18 +135,24 @@ def test_per_set_optics_against_fp64_path(engine):
     assert agree >= len(shapes) - 1
 
 
-def test_batched_rejects_bad_sets(engine):
+def test_batched_rejects_bad_sets(engine, oracle_mod):
     from bioshell_gb300.lib import CrmsdError
     x = np.zeros((3, 4, 3))
     x[1, 0, 0] = np.nan
     with pytest.raises(CrmsdError) as e:
         engine.batched([np.ones((5, 6, 3)) * np.arange(6)[None, :, None], x])
     assert e.value.status == 6  # BS_ERR_NONFINITE
-    far = np.zeros((3, 4, 3))
-    far[0, 0, 0] = 40000.0  # beyond the fixed-point range
-    with pytest.raises(CrmsdError) as e:
-        engine.batched([far])
-    assert e.value.status == 5  # BS_ERR_UNSUPPORTED
+    # a set beyond the fixed-point range (|x| >= 32768 A) runs on the plain
+    # FP64 path; the other sets of the call stay on the mixed path
+    rng = np.random.default_rng(21)
+    far = synth.decoys(synth.base_chain(12, rng), 5, rng)
+    far[0] += 40000.0
+    near = _sets(11, [(30, 20)])[0]
+    res = engine.batched([near, far])
+    assert engine.metrics()["pairs_plain"] == 10
+    assert np.abs(res[1].values - oracle_mod.crmsd_all_vs_all(far)).max() <= 1e-6
+    alone = engine.batched([near])[0].values
+    np.testing.assert_array_equal(res[0].values, alone)
     # the context stays usable
     ok = engine.batched(_sets(11, [(10, 20)]))
     assert np.all(ok[0].values >= 0)

@@ -89,6 +89,37 @@ def test_ragged_shapes(engine, oracle_mod, n, L):
     assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
 
 
+@pytest.mark.parametrize("L", [1500, 4096, 16384])
+def test_very_long_chains(engine, oracle_mod, L):
+    """Chains up to the limit of 16,384 atoms (the preparation's 32-bit
+    digit-norm sums cannot overflow below it).  At 1,500 atoms the mixed path
+    runs in its long layout (levels 1 and 2 accumulated in parts).  Beyond
+    ~3,000 atoms the digit-1 products exceed the exact range even in quarters
+    of the chain, no coordinate grid fits, and the set is computed on the
+    plain FP64 GPU path instead (metrics: pairs_plain).  A row-ranged call of
+    such a set reports BS_ERR_UNSUPPORTED (the plain path writes every row);
+    one atom beyond the limit is rejected before any GPU work."""
+    from bioshell_gb300.lib import CrmsdError
+    rng = np.random.default_rng(L)
+    x = synth.decoys(synth.base_chain(L, rng), 41, rng, near_dup_frac=0.1)
+    got = engine.all_vs_all(x).values
+    ref = oracle_mod.crmsd_all_vs_all(x)
+    plain = engine.metrics()["pairs_plain"]
+    if L == 1500:
+        assert plain == 0
+        assert np.abs(got - ref).max() <= TOL_MIXED
+    else:
+        assert plain == 41 * 40 // 2
+        assert plain_close(got, ref)
+        with pytest.raises(CrmsdError) as ei:
+            engine.all_vs_all(x, CrmsdOptions(rows=(0, 40)))
+        assert ei.value.status == 5
+    if L == 16384:
+        with pytest.raises(CrmsdError) as ei:
+            engine.all_vs_all(np.zeros((2, L + 1, 3)))
+        assert ei.value.status == 5
+
+
 def test_far_and_lopsided_coordinates(engine, oracle_mod):
     """Structures up to 30,000 A from the origin (inside the fixed-point range
     of 2^15 A), of different sizes in one set, and lopsided ones whose
