@@ -110,7 +110,9 @@ def test_very_long_chains(engine, oracle_mod, L):
         assert np.abs(got - ref).max() <= TOL_MIXED
     else:
         assert plain == 41 * 40 // 2
-        assert plain_close(got, ref)
+        # FP64 against FP64: the cancellation floor of G_a + G_b - 2 lambda
+        # grows with the chain's extent (coordinates up to ~1,200 A here)
+        assert np.abs(got - ref).max() <= 1e-6
         with pytest.raises(CrmsdError) as ei:
             engine.all_vs_all(x, CrmsdOptions(rows=(0, 40)))
         assert ei.value.status == 5
