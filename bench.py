@@ -55,6 +55,19 @@ METRIC = "crmsd pairs/s (all-vs-all, mixed precision)"
 UNIT = "pairs/s"
 
 
+def whole_job_rate(ms, units_per_rank, steps, world, dist=None, device="cuda"):
+    """The slowest rank's time over `steps` steps (max over ranks) and the
+    whole job's rate: each of the `world` ranks processes `units_per_rank`
+    units per step (weak scaling: independent replicas or disjoint row
+    ranges, no exchange between ranks)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * units_per_rank * steps / (ms * 1e-3)
+
+
 def args_():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -628,12 +641,7 @@ def run_ours(a, rank, world, local_rank):
         ev1.record(stream)
         ev1.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * npairs * a.steps / (ms * 1e-3)
+    ms, value = whole_job_rate(ev0.elapsed_time(ev1), npairs, a.steps, world, dist)
     clocks = clk.summary()
     ms_main = statistics.mean(m["ms_main"] for m in mets)
     launches = int(sum(m["main_launches"] for m in mets))
@@ -654,7 +662,7 @@ def run_ours(a, rank, world, local_rank):
         step(xh, oh)
     ev1.record(stream)
     ev1.synchronize()
-    ms_e2e = ev0.elapsed_time(ev1)
+    ms_e2e, e2e_value = whole_job_rate(ev0.elapsed_time(ev1), npairs, e_steps, world, dist)
     # the machine's host link as a plain copy of the same triangle into the same
     # pinned buffer: an end-to-end step cannot take less than that copy
     ohv = torch.from_numpy(oh)
@@ -665,7 +673,7 @@ def run_ours(a, rank, world, local_rank):
     l1.record()
     l1.synchronize()
     link_gbs = npairs * 8 / (l0.elapsed_time(l1) * 1e-3) / 1e9
-    e2e = {"value": world * npairs * e_steps / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes),
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes),
            "d2h_bytes_per_step": int(npairs * 8), "steps": e_steps, "ms_per_step": ms_e2e / e_steps,
            "host_link_d2h_gbs": link_gbs}
     np.testing.assert_array_equal(oh[:1000], outd[:1000].cpu().numpy())
