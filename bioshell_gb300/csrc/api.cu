@@ -191,6 +191,7 @@ bs_status prepare_buffers(bs_ctx *ctx, const Plan &plan, unsigned long long cap,
   b.flags = static_cast<unsigned long long *>(ctx->flags.p);
   b.flag_cap = cap;
   b.sc = static_cast<DevScalars *>(ctx->scal.p);
+  b.wait_ns = ctx->wait_limit_ns;
   return BS_OK;
 }
 
@@ -252,8 +253,9 @@ std::string cached_symmetric_plan(bs_ctx *ctx, const std::vector<JobSpec> &specs
 }
 
 std::vector<int64_t> plan_key(bs_ctx *ctx, const Plan &plan, unsigned long long cap) {
+  // the wait bound is a kernel argument captured into the graph
   std::vector<int64_t> k = {(int64_t)ctx->gen, (int64_t)plan.jobs.size(), plan.nblocks, plan.pitch,
-                            (int64_t)plan.tiles.size(), (int64_t)cap};
+                            (int64_t)plan.tiles.size(), (int64_t)cap, (int64_t)ctx->wait_limit_ns};
   for (const Job &j : plan.jobs) {
     k.push_back(j.n);
     k.push_back(j.L);

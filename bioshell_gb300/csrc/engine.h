@@ -38,6 +38,7 @@ struct MixedBuffers {
   unsigned long long *flags = nullptr;
   unsigned long long flag_cap = 0;
   DevScalars *sc = nullptr;
+  uint64_t wait_ns = 0;  // bound of the tensor-core kernels' pipeline waits (0: their default)
 };
 
 // A symmetric job as the host describes it (device coordinates and output;

@@ -217,6 +217,7 @@ struct TcArgs {
   unsigned long long flag_cap;
   float *dbg;  // optional dump of the raw level sums of tiles (0,0) and (0,1)
   int num_sms;
+  uint64_t wait_ns;  // bound of each pipeline wait (0: the kernel's default); a test hook
 };
 cudaError_t launch_mixed_tc(const CUtensorMap *tm /* [7]: A digits e0 e1 e2 d2/32, B digits e0 e1 e2 */,
                             const TcArgs &a, cudaStream_t st);

@@ -213,6 +213,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   ptx::tc_fence_after();
   const uint32_t tmem = sh->tmem_base;
   volatile int *abort = &sh->abort;
+  // bound of the producer's and the MMA issuer's pipeline waits; the
+  // epilogue keeps the default and leaves when they give up (abort)
+  const uint64_t tmo = a.wait_ns ? a.wait_ns : kTimeoutNs;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         {
           // the tile's metadata: record, job, per-structure data
           const uint32_t ms = tt % kMetaSlots;
-          if (!ptx::mbar_wait(&sh->mempty[ms], ((tt / kMetaSlots) & 1u) ^ 1u, abort, kTimeoutNs)) {
+          if (!ptx::mbar_wait(&sh->mempty[ms], ((tt / kMetaSlots) & 1u) ^ 1u, abort, tmo)) {
             fail(sh, a.sc);
             break;
           }
@@ -263,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
-          if (!ptx::mbar_wait(&sh->empty[s], ph ^ 1u, abort, kTimeoutNs)) {
+          if (!ptx::mbar_wait(&sh->empty[s], ph ^ 1u, abort, tmo)) {
             fail(sh, a.sc);
             break;
           }
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t tt = 0; !*abort; ++tt) {
         // the tile's record, as the TMA thread took it from the table
         const uint32_t ms = tt % kMetaSlots;
-        if (!ptx::mbar_wait(&sh->mfull[ms], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) {
+        if (!ptx::mbar_wait(&sh->mfull[ms], (tt / kMetaSlots) & 1u, abort, tmo)) {
           fail(sh, a.sc);
           break;
         }
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         for (uint32_t u = 0; u < need && ok; ++u) {
           const uint32_t q = p + u;
-          if (!ptx::mbar_wait(&sh->tempty[q & 1u], ((q >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
+          if (!ptx::mbar_wait(&sh->tempty[q & 1u], ((q >> 1) & 1u) ^ 1u, abort, tmo)) {
             fail(sh, a.sc);
             ok = false;
           }
@@ -330,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
-          if (!ptx::mbar_wait(&sh->full[s], ph, abort, kTimeoutNs)) {
+          if (!ptx::mbar_wait(&sh->full[s], ph, abort, tmo)) {
             fail(sh, a.sc);
             ok = false;
             break;
@@ -433,7 +436,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t p = 0;   // TMEM buffer slot, as the MMA issuer counts them
     for (uint32_t tt = 0;; ++tt) {  // tile sequence number (metadata slot)
       const uint32_t slot = tt % kMetaSlots;
-      if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) {
+      // every lane waits (and so acquires what the phase publishes), and the
+      // warp takes one decision: lanes must not part at a timeout, since
+      // the tile's work below is warp-collective
+      if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs))) {
         fail(sh, a.sc);
         break;
       }
@@ -444,7 +450,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool ok = true;
       for (uint32_t u = 0; u < (lng ? 2u : 1u) && ok; ++u) {
         const uint32_t q = p + u;
-        if (!ptx::mbar_wait(&sh->tfull[q & 1u], (q >> 1) & 1u, abort, kTimeoutNs)) {
+        if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->tfull[q & 1u], (q >> 1) & 1u, abort, kTimeoutNs))) {
           fail(sh, a.sc);
           ok = false;
         }

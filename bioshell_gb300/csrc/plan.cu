@@ -232,6 +232,7 @@ cudaError_t enqueue_mixed(const Plan &plan, const MixedBuffers &b, const Job *jo
     a.flag_cap = b.flag_cap;
     a.dbg = dbg;
     a.num_sms = num_sms;
+    a.wait_ns = b.wait_ns;
     // launches of screen jobs only run the screen-shaped kernel
     bool all_screen = nj > 0;
     for (const Job &jb : plan.jobs) all_screen = all_screen && jb.screen;

@@ -67,15 +67,16 @@ __device__ __forceinline__ bool mbar_try_wait_hint(uint64_t *bar, uint32_t parit
 // Waits for the phase with the given parity to complete.  Gives up after
 // `timeout_ns` of wall-clock time, or at once when *abort is set by another
 // role of the block; returns false in both cases.  After a first test, the
-// waiting thread is suspended between tests (up to 20 us each, woken by the
-// phase's completion), so long waits do not take issue slots from the warps
-// that share its scheduler.
+// waiting thread is suspended between tests (up to 20 us each, or the bound
+// itself when that is shorter; woken by the phase's completion), so long
+// waits do not take issue slots from the warps that share its scheduler.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           uint64_t timeout_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
+  const uint32_t hint = timeout_ns < 20000u ? (uint32_t)timeout_ns : 20000u;
   while (true) {
-    if (mbar_try_wait_hint(bar, parity, 20000u)) return true;
+    if (mbar_try_wait_hint(bar, parity, hint)) return true;
     if (*abort) return false;
     if (globaltimer() - t0 > timeout_ns) return false;
   }

@@ -328,8 +328,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       record_shape<S>(a.tiles[r], nk16, count);
       for (int u = 0; u < count; ++u, ++tt) {
         const uint32_t slot = tt % kMetaSlots;
-        if (!ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs) ||
-            !ptx::mbar_wait(&sh->tfull[tt & 1u], (tt >> 1) & 1u, abort, kTimeoutNs)) {
+        // one decision per warp (the tile's work is warp-collective)
+        if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->mfull[slot], (tt / kMetaSlots) & 1u, abort, kTimeoutNs)) ||
+            !__all_sync(0xffffffffu, ptx::mbar_wait(&sh->tfull[tt & 1u], (tt >> 1) & 1u, abort, kTimeoutNs))) {
           fail(sh, a.sc);
           ok = false;
           break;

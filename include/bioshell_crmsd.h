@@ -531,9 +531,12 @@ BS_API bs_status bs_debug_pair_levels(bs_ctx *ctx, const double *xyz, int64_t n,
  * bioshell-pdb/src/pdb_parsing_error.rs:7).  Both act on the host or through
  * a kernel argument: nothing here faults or stalls a GPU.
  *   bs_debug_set_wait_limit: the bound, in nanoseconds, on each grid-barrier
- *     wait of this context's GPU hierarchical clustering (0 restores the
- *     default 2 s).  A wait that runs out makes every block of the launch
- *     return and the call return BS_ERR_TIMEOUT; the context stays usable.
+ *     wait of this context's GPU hierarchical clustering and on each
+ *     pipeline (mbarrier) wait of the copy and MMA threads of its all-vs-all
+ *     tensor-core kernel (0 restores the defaults, 2 s and 4 s).  A wait that runs out makes every
+ *     block of the launch stop (the tensor-core kernel first lets its copies
+ *     and MMAs in flight complete and frees its tensor memory) and the call
+ *     return BS_ERR_TIMEOUT; the context stays usable.
  *   bs_debug_fail_alloc: the `after`-th device workspace allocation of this
  *     context from now on (0: the next one) fails as if the GPU were out of
  *     memory (BS_ERR_OOM, nothing allocated); -1 disarms the hook. */

@@ -6,7 +6,13 @@ comes back and that the context (or server) computes correctly afterwards.
   hierarchical clustering get a 1 ns bound (bs_debug_set_wait_limit, a
   kernel argument); the first barrier wait that outlasts it makes every
   block return, the call returns BS_ERR_TIMEOUT, and with the default bound
-  restored the same context clusters correctly.
+  restored the same context clusters correctly.  The same bound on the
+  mbarrier waits of the all-vs-all tensor-core kernel's copy and MMA
+  threads: the first such wait that is not already complete runs out, every
+  role of every block
+  stops (copies and MMAs in flight are let complete, tensor memory is
+  freed), the call returns BS_ERR_TIMEOUT, and the next call of the same
+  context, default bound restored, gives the same matrix bit for bit.
 * A failed device allocation: bs_debug_fail_alloc makes a chosen workspace
   allocation of a fresh context fail as out of memory (BS_ERR_OOM); the next
   call, hook disarmed, completes.
@@ -50,6 +56,25 @@ def test_barrier_wait_runs_out_and_context_recovers(engine, enginelib):
     host = K.hierarchical_clustering(m, "average")
     np.testing.assert_array_equal(dev.merges, host.merges)
     np.testing.assert_array_equal(dev.dist, host.dist)
+
+
+def test_pipeline_wait_runs_out_and_context_recovers(engine, enginelib, oracle_mod):
+    rng = np.random.default_rng(13)
+    x = synth.decoys(synth.base_chain(64, rng), 1500, rng, near_dup_frac=0.05)
+    before = engine.all_vs_all(x).values.copy()  # a graph captured with the default bound
+    assert enginelib.bs_debug_set_wait_limit(engine._h, 1) == 0
+    try:
+        for _ in range(2):  # graph captured with the 1 ns bound, then replayed
+            with pytest.raises(CrmsdError) as ei:
+                engine.all_vs_all(x)
+            assert ei.value.status == BS_ERR_TIMEOUT
+            assert "timed out" in str(ei.value)
+    finally:
+        assert enginelib.bs_debug_set_wait_limit(engine._h, 0) == 0
+    after = engine.all_vs_all(x).values
+    np.testing.assert_array_equal(after, before)
+    assert engine.metrics()["graph"] == 2  # the default-bound graph, replayed
+    assert np.abs(after - oracle_mod.crmsd_all_vs_all(x)).max() <= 1e-4
 
 
 def test_injected_allocation_failure(enginelib, oracle_mod):
