@@ -124,10 +124,20 @@ constexpr int kAccLong = 1;
 // 16-atom step, digits 0 and 1 of each side) and an FP32 epilogue writing
 // crmsd bounds -- the first stage of top-k queries.
 constexpr int kAccScreen = 2;
+// Half (chains up to about twice the normal layout's reach): the four levels
+// accumulated separately over each half of the chain (16-atom steps split
+// evenly), [L0 | L1 | L2 | L3] of the first half in one TMEM buffer and of
+// the second half in the other.  Each half's sums stay below 2^24 where the
+// whole chain's would not, and each half keeps the normal layout's column
+// order, so one MMA still covers several levels.
+constexpr int kAccHalf = 3;
 __host__ __device__ inline int acc_part(int k16, int nk16, int parts) { return (k16 * parts) / nk16; }
+// layouts whose tile takes both TMEM buffers
+__host__ __device__ inline bool acc_two_buffers(int layout) { return layout == kAccLong || layout == kAccHalf; }
 // accumulator index (0..7) of level `lv` at 16-atom step k16
 __host__ __device__ inline int acc_index(int layout, int lv, int k16, int nk16) {
   if (layout == kAccNormal) return lv;
+  if (layout == kAccHalf) return 4 * acc_part(k16, nk16, 2) + lv;
   if (lv == 0) return 0;
   if (lv == 1) return 1 + acc_part(k16, nk16, 2);
   if (lv == 2) return 3 + acc_part(k16, nk16, 4);

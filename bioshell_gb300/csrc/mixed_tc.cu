@@ -47,6 +47,8 @@
 // leave their loops so the block always reaches TMEM deallocation.
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "crmsd_math.cuh"
 #include "kernels.h"
 #include "ptx.cuh"
@@ -318,7 +320,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
         const int lay = tile_layout(tile);
         const uint32_t idesc = tile_narrow(tile) ? kIdescNarrow : kIdesc;
-        const uint32_t need = lay == kAccLong ? 2u : 1u;
+        const uint32_t need = acc_two_buffers(lay) ? 2u : 1u;
+        // half layout: the first 16-atom step of the second half
+        // (acc_part(k, nk16, 2) == 1 from there on); never reached otherwise
+        const int khalf = lay == kAccHalf ? (nk16 + 1) / 2 : 1 << 30;
         bool ok = true;
         for (uint32_t u = 0; u < need && ok; ++u) {
           const uint32_t q = p + u;
@@ -366,10 +371,11 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
               continue;
             }
-            if (lay == kAccNormal && !tile_narrow(tile)) {
-              // [L0 | L1 | L2 | L3] in columns c0 .. c0 + 255
-              const uint32_t c0 = acc_col(0);
-              if (k == 0) {
+            if ((lay == kAccNormal || lay == kAccHalf) && !tile_narrow(tile)) {
+              // [L0 | L1 | L2 | L3] in columns c0 .. c0 + 255 (half layout:
+              // of the step's half of the chain, in that half's buffer)
+              const uint32_t c0 = acc_col(k >= khalf ? 4 : 0);
+              if (k == 0 || k == khalf) {
                 ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
                 ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
                 ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
@@ -447,8 +453,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (mt.tile.job < 0) break;  // end of the table
       const Job &mj = mt.job;
       const bool lng = mj.layout == kAccLong;
+      const bool hlf = mj.layout == kAccHalf;
+      const bool two = lng || hlf;  // the tile holds both TMEM buffers
       bool ok = true;
-      for (uint32_t u = 0; u < (lng ? 2u : 1u) && ok; ++u) {
+      for (uint32_t u = 0; u < (two ? 2u : 1u) && ok; ++u) {
         const uint32_t q = p + u;
         if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->tfull[q & 1u], (q >> 1) & 1u, abort, kTimeoutNs))) {
           fail(sh, a.sc);
@@ -528,13 +536,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         continue;
       }
       // accumulators of level lv: normal layout {lv}; long layout L0 {0},
-      // L1 {1, 2}, L2 {3..6}, L3 {7}; accumulator ai sits in slot p + ai / 4
+      // L1 {1, 2}, L2 {3..6}, L3 {7}; half layout {lv, lv + 4};
+      // accumulator ai sits in slot p + ai / 4
       auto acc_col = [&](int ai) -> uint32_t { return lane_base + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
       const int64_t ig = (int64_t)t_ablk * kBlockStructs + qd * kGroupStructs + il;
       const int64_t i = ig - fa;
       const bool row_ok = job_ok && cols_ok && lane_real && (il < kGroupStructs) && (i < jn);
       const SInfo ia = mt.ia[qd * kGroupStructs + ilr];
-      const bool dump = (a.dbg != nullptr) && (t_ablk == 0) && (t_bblk < 2) && !lng;
+      const bool dump = (a.dbg != nullptr) && (t_ablk == 0) && (t_bblk < 2) && !two;
       // row of coordinate xr of this lane's row structure in the staging buffers
       int srow[3];
 #pragma unroll
@@ -542,136 +551,167 @@ __global__ void __launch_bounds__(kThreads, 1)
       // The group's 10 column structures are finished in two halves of five:
       // half h is TMEM columns 16h .. 16h+14 of the group (one 16-column
       // load per accumulator), and a lane carries at most two pairs at once.
-#pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
-        const uint32_t hc = 16u * (uint32_t)h;
-        float *bufm = stg + kPitch * 32;  // FP32 covariance rows (buffer 1)
-        // ---- pass A: FP32 covariance rows of this half, staged per lane
-        {
-          float m[16], v[16];
-          ptx::tmem_ld2_32x32b_x16(acc_col(0) + hc, acc_col(lng ? 1 : 1) + hc, m, v);
-#pragma unroll
-          for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
-#pragma unroll
-          for (int lv = 1; lv < 4; ++lv) {
-            const float wl = lv == 1 ? 0.001953125f : (lv == 2 ? 3.814697265625e-6f : 7.450580596923828125e-9f);
-#pragma unroll
-            for (int part = 0; part < 4; ++part) {
-              // normal layout: accumulator lv; long: L1 {1, 2}, L2 {3..6}, L3 {7}
-              const int ai = lng ? (lv == 1 ? 1 + part : (lv == 2 ? 3 + part : 7)) : lv;
-              const bool use = (lv == 1 && lng && part == 1) || (lv > 1 && (part == 0 || (lng && lv == 2)));
-              if (use) {
-                ptx::tmem_ld_32x32b_x16(acc_col(ai) + hc, v);
-#pragma unroll
-                for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], wl, m[c]);
+      // The halves' work, compiled once per accumulator layout (the layout
+      // is uniform over the tile): runtime layout branches inside it cost
+      // the normal layout 10% in an A/B run.
+      auto finish_halves = [&](auto layout_tag) {
+        constexpr int kLay = decltype(layout_tag)::value;
+        constexpr bool lng = kLay == kAccLong;
+        constexpr bool hlf = kLay == kAccHalf;
+        constexpr bool two = lng || hlf;
+  #pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t hc = 16u * (uint32_t)h;
+          float *bufm = stg + kPitch * 32;  // FP32 covariance rows (buffer 1)
+          // ---- pass A: FP32 covariance rows of this half, staged per lane
+          {
+            float m[16], v[16];
+            ptx::tmem_ld2_32x32b_x16(acc_col(0) + hc, acc_col(1) + hc, m, v);
+            if (hlf) {  // level 0 of the second half
+              float w[16];
+              ptx::tmem_ld_32x32b_x16(acc_col(4) + hc, w);
+  #pragma unroll
+              for (int c = 0; c < 16; ++c) m[c] += w[c];
+            }
+  #pragma unroll
+            for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], 0.001953125f, m[c]);
+  #pragma unroll
+            for (int lv = 1; lv < 4; ++lv) {
+              const float wl = lv == 1 ? 0.001953125f : (lv == 2 ? 3.814697265625e-6f : 7.450580596923828125e-9f);
+  #pragma unroll
+              for (int part = 0; part < 4; ++part) {
+                // normal layout: accumulator lv; long: L1 {1, 2}, L2 {3..6},
+                // L3 {7}; half: {lv, lv + 4}
+                const int ai = lng ? (lv == 1 ? 1 + part : (lv == 2 ? 3 + part : 7)) : lv + 4 * part;
+                const bool use = (lv == 1 && two && part == 1) ||
+                                 (lv > 1 && (part == 0 || (lng && lv == 2) || (hlf && part == 1)));
+                if (use) {
+                  ptx::tmem_ld_32x32b_x16(acc_col(ai) + hc, v);
+  #pragma unroll
+                  for (int c = 0; c < 16; ++c) m[c] = fmaf(v[c], wl, m[c]);
+                }
               }
             }
-          }
-          __syncwarp();  // every lane is done with the previous half's last level (buffer 1)
-#pragma unroll
-          for (int c = 0; c < 16; ++c) bufm[lane * kPitch + c] = m[c];
-        }
-        __syncwarp();
-        bsm::FastState st[2];
-        int64_t jj[2];
-        bool valid[2];
-        SInfo ib[2];
-        int scol[2];
-        {
-          // the lane's two pairs through one packed FP32x2 QCP
-          float m9[2][9], gs[2];
-#pragma unroll
-          for (int sl = 0; sl < 2; ++sl) {
-            const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
-            const int jc = jh < 5 ? jh : 4;
-            scol[sl] = 3 * jc;
-            const int64_t jg = jg0 + 5 * h + jh;
-            jj[sl] = jg - fb;
-            valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
-            ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
-#pragma unroll
-            for (int xr = 0; xr < 3; ++xr)
-#pragma unroll
-              for (int y = 0; y < 3; ++y) m9[sl][3 * xr + y] = bufm[srow[xr] + scol[sl] + y];
-            gs[sl] = valid[sl] ? ia.gf + ib[sl].gf : 0.f;
-          }
-          bsm::F2 mm[9];
-#pragma unroll
-          for (int e = 0; e < 9; ++e) mm[e] = bsm::f2(m9[0][e], m9[1][e]);
-          bsm::fast_begin2(mm, bsm::f2(gs[0], gs[1]), st[0], st[1]);
-        }
-        // ---- pass B: exact level sums, one level at a time (levels 0-2 as
-        // integers: the parts of a long-layout level add exactly); level lv
-        // is staged in buffer lv & 1, so one warp synchronisation per level
-        // separates each buffer's writes from the previous reads
-#pragma unroll
-        for (int lv = 0; lv < 4; ++lv) {
-          float *buf = stg + (lv & 1) * kPitch * 32;
-          const int a0 = lng ? (lv == 0 ? 0 : lv == 1 ? 1 : lv == 2 ? 3 : 7) : lv;
-          float v[16];
-          ptx::tmem_ld_32x32b_x16(acc_col(a0) + hc, v);
-          if (dump) {
-            float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * t_bblk + 32 * g + hc;
-#pragma unroll
-            for (int c = 0; c < 16; ++c) drow[c] = v[c];
-          }
-          if (h == 1 && lv == 3) {
-            // all TMEM reads of this tile are done: hand its buffers back to the MMA warp
-            ptx::tc_fence_before();
-            ptx::mbar_arrive(&sh->tempty[p & 1u]);
-            if (lng) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
-          }
-#pragma unroll
-          for (int c = 0; c < 16; ++c) buf[lane * kPitch + c] = lv < 3 ? __int_as_float(__float2int_rn(v[c])) : v[c];
-          if (lng && (lv == 1 || lv == 2)) {
-            // further parts of the level, added into the staged row (integers stay exact)
-#pragma unroll
-            for (int part = 1; part < 4; ++part) {
-              if (lv == 1 && part > 1) break;
-              ptx::tmem_ld_32x32b_x16(acc_col(a0 + part) + hc, v);
-#pragma unroll
-              for (int c = 0; c < 16; ++c) {
-                float &d = buf[lane * kPitch + c];
-                d = __int_as_float(__float_as_int(d) + __float2int_rn(v[c]));
-              }
-            }
+            __syncwarp();  // every lane is done with the previous half's last level (buffer 1)
+  #pragma unroll
+            for (int c = 0; c < 16; ++c) bufm[lane * kPitch + c] = m[c];
           }
           __syncwarp();
-#pragma unroll
-          for (int sl = 0; sl < 2; ++sl) {
-            float s9[9];
-#pragma unroll
-            for (int xr = 0; xr < 3; ++xr)
-#pragma unroll
-              for (int y = 0; y < 3; ++y) s9[3 * xr + y] = buf[srow[xr] + scol[sl] + y];
-            bsm::fast_level_staged(st[sl], lv, s9);
+          bsm::FastState st[2];
+          int64_t jj[2];
+          bool valid[2];
+          SInfo ib[2];
+          int scol[2];
+          {
+            // the lane's two pairs through one packed FP32x2 QCP
+            float m9[2][9], gs[2];
+  #pragma unroll
+            for (int sl = 0; sl < 2; ++sl) {
+              const int jh = 3 * sl + x;  // owned structure within the half (0..5, valid < 5)
+              const int jc = jh < 5 ? jh : 4;
+              scol[sl] = 3 * jc;
+              const int64_t jg = jg0 + 5 * h + jh;
+              jj[sl] = jg - fb;
+              valid[sl] = row_ok && (jh < 5) && (jj[sl] < jnb) && (!sym || jj[sl] > i);
+              ib[sl] = mt.ib[g * kGroupStructs + 5 * h + jc];
+  #pragma unroll
+              for (int xr = 0; xr < 3; ++xr)
+  #pragma unroll
+                for (int y = 0; y < 3; ++y) m9[sl][3 * xr + y] = bufm[srow[xr] + scol[sl] + y];
+              gs[sl] = valid[sl] ? ia.gf + ib[sl].gf : 0.f;
+            }
+            bsm::F2 mm[9];
+  #pragma unroll
+            for (int e = 0; e < 9; ++e) mm[e] = bsm::f2(m9[0][e], m9[1][e]);
+            bsm::fast_begin2(mm, bsm::f2(gs[0], gs[1]), st[0], st[1]);
           }
-        }
-        // ---- finish and store (neighbour layout: flagged pairs are kept or
-        // dropped by the exact recomputation)
-        const bool nbr = out.layout == kLayoutNeighbors;  // the same for the whole warp
-#pragma unroll
-        for (int sl = 0; sl < 2; ++sl) {
-          const int64_t j = jj[sl];
-          int flag = 0;
-          float r = 0.f;
-          if (valid[sl]) {
-            r = bsm::fast_finish(st[sl], ia.ghat + ib[sl].ghat, ia.gf + ib[sl].gf, ia.qres + ib[sl].qres, t_d34,
-                                 t_u, t_L, t_tol, flag);
-            if (flag) {
-              if (!nbr) store_pair(out, i, j, -1.0f);
-              const unsigned long long q = atomicAdd(&a.sc->flag_count, 1ull);
-              if (q < a.flag_cap) a.flags[q] = flag_pack(t_job, ig, j + fb);
-            } else if (!nbr) {
-              store_pair(out, i, j, r);
+          // ---- pass B: exact level sums, one level at a time (levels 0-2 as
+          // integers: the parts of a long-layout level add exactly); level lv
+          // is staged in buffer lv & 1, so one warp synchronisation per level
+          // separates each buffer's writes from the previous reads
+  #pragma unroll
+          for (int lv = 0; lv < 4; ++lv) {
+            float *buf = stg + (lv & 1) * kPitch * 32;
+            const int a0 = lng ? (lv == 0 ? 0 : lv == 1 ? 1 : lv == 2 ? 3 : 7) : lv;
+            float v[16];
+            if (hlf) {
+              // the level over both halves of the chain: levels 0-2 added as
+              // integers (exact; v then holds their bit patterns), level 3 in FP32
+              float w[16];
+              ptx::tmem_ld2_32x32b_x16(acc_col(a0) + hc, acc_col(a0 + 4) + hc, v, w);
+  #pragma unroll
+              for (int c = 0; c < 16; ++c)
+                v[c] = lv < 3 ? __int_as_float(__float2int_rn(v[c]) + __float2int_rn(w[c])) : v[c] + w[c];
+            } else {
+              ptx::tmem_ld_32x32b_x16(acc_col(a0) + hc, v);
+            }
+            if (dump) {
+              float *drow = a.dbg + ((size_t)(lv * 128 + qd * 32 + lane)) * 128 + 64 * t_bblk + 32 * g + hc;
+  #pragma unroll
+              for (int c = 0; c < 16; ++c) drow[c] = v[c];
+            }
+            if (h == 1 && lv == 3) {
+              // all TMEM reads of this tile are done: hand its buffers back to the MMA warp
+              ptx::tc_fence_before();
+              ptx::mbar_arrive(&sh->tempty[p & 1u]);
+              if (two) ptx::mbar_arrive(&sh->tempty[(p + 1u) & 1u]);
+            }
+  #pragma unroll
+            for (int c = 0; c < 16; ++c)
+              buf[lane * kPitch + c] = (lv < 3 && !hlf) ? __int_as_float(__float2int_rn(v[c])) : v[c];
+            if (lng && (lv == 1 || lv == 2)) {
+              // further parts of the level, added into the staged row (integers stay exact)
+  #pragma unroll
+              for (int part = 1; part < 4; ++part) {
+                if (lv == 1 && part > 1) break;
+                ptx::tmem_ld_32x32b_x16(acc_col(a0 + part) + hc, v);
+  #pragma unroll
+                for (int c = 0; c < 16; ++c) {
+                  float &d = buf[lane * kPitch + c];
+                  d = __int_as_float(__float_as_int(d) + __float2int_rn(v[c]));
+                }
+              }
+            }
+            __syncwarp();
+  #pragma unroll
+            for (int sl = 0; sl < 2; ++sl) {
+              float s9[9];
+  #pragma unroll
+              for (int xr = 0; xr < 3; ++xr)
+  #pragma unroll
+                for (int y = 0; y < 3; ++y) s9[3 * xr + y] = buf[srow[xr] + scol[sl] + y];
+              bsm::fast_level_staged(st[sl], lv, s9);
             }
           }
-          if (nbr) nbr_append(out, valid[sl] && !flag && r <= out.eps, i, j, r, lane);
+          // ---- finish and store (neighbour layout: flagged pairs are kept or
+          // dropped by the exact recomputation)
+          const bool nbr = out.layout == kLayoutNeighbors;  // the same for the whole warp
+  #pragma unroll
+          for (int sl = 0; sl < 2; ++sl) {
+            const int64_t j = jj[sl];
+            int flag = 0;
+            float r = 0.f;
+            if (valid[sl]) {
+              r = bsm::fast_finish(st[sl], ia.ghat + ib[sl].ghat, ia.gf + ib[sl].gf, ia.qres + ib[sl].qres, t_d34,
+                                   t_u, t_L, t_tol, flag);
+              if (flag) {
+                if (!nbr) store_pair(out, i, j, -1.0f);
+                const unsigned long long q = atomicAdd(&a.sc->flag_count, 1ull);
+                if (q < a.flag_cap) a.flags[q] = flag_pack(t_job, ig, j + fb);
+              } else if (!nbr) {
+                store_pair(out, i, j, r);
+              }
+            }
+            if (nbr) nbr_append(out, valid[sl] && !flag && r <= out.eps, i, j, r, lane);
+          }
         }
-      }
+      };
+      if (hlf) finish_halves(std::integral_constant<int, kAccHalf>{});
+      else if (lng) finish_halves(std::integral_constant<int, kAccLong>{});
+      else finish_halves(std::integral_constant<int, kAccNormal>{});
       // the tile's metadata is no longer read: release its slot
       ptx::mbar_arrive(&sh->mempty[slot]);
-      p += lng ? 2u : 1u;
+      p += two ? 2u : 1u;
     }
   }
   __syncthreads();

@@ -341,13 +341,13 @@ __global__ void k_mx_choose(PrepArgs p) {
   // Preference, from Cauchy-Schwarz bounds on the row norms: (1) the finest
   // grid whose level sums 0-2 are all exact (below 2^24) while its
   // quantisation (about 2^e per pair) leaves a quarter of the budget to the
-  // arithmetic; (2) the same with the long accumulator layout (level 1 in
-  // halves, level 2 in quarters of the chain; long chains); (3) the finest
-  // grid with levels 0-1 exact and level 2 below 2^26, its rounding charged
-  // to the budget.
+  // arithmetic; (2) the same with the half layout (every level in halves of
+  // the chain); (3) the same with the long layout (level 1 in halves, level
+  // 2 in quarters; longer chains); (4) the finest grid with levels 0-1 exact
+  // and level 2 below 2^26, its rounding charged to the budget.
   const int ncand = jb.fixed_scale ? 1 : 4;
   const bool can_long = jb.mode == 0 && jb.allow_long && jb.lp / 16 >= 4;
-  int pick = -1, relaxed = -1, pick_long = -1;
+  int pick = -1, relaxed = -1, pick_long = -1, pick_half = -1;
   double bb2[4], bb34[4];
   for (int a = 0; a < ncand; ++a) {
     double f[3], hh[3], qq[3], nb[3];
@@ -366,13 +366,20 @@ __global__ void k_mx_choose(PrepArgs p) {
       pick = a;
       break;
     }
+    if (grid_ok && can_long && pick_half < 0 && hh[0] * hh[0] < 16777216.0 && 2.0 * hh[0] * hh[1] < 16777216.0 &&
+        2.0 * hh[0] * hh[2] + hh[1] * hh[1] < 16777216.0)
+      pick_half = a;
     if (grid_ok && can_long && pick_long < 0 && b0 < 16777216.0 && 2.0 * hh[0] * hh[1] < 16777216.0 &&
         2.0 * qq[0] * qq[2] + qq[1] * qq[1] < 16777216.0)
       pick_long = a;
     if (b0 < 16777216.0 && b1 < 16777216.0 && b2 < 67108864.0 && relaxed < 0) relaxed = a;
   }
   jb.layout = kAccNormal;
-  if (pick < 0 && pick_long >= 0) {
+  if (pick < 0 && pick_half >= 0) {
+    pick = pick_half;
+    bb2[pick] = 0.0;  // both halves of level 2 are exact
+    jb.layout = kAccHalf;
+  } else if (pick < 0 && pick_long >= 0) {
     pick = pick_long;
     bb2[pick] = 0.0;  // every part of level 2 is exact
     jb.layout = kAccLong;

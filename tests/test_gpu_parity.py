@@ -89,6 +89,26 @@ def test_ragged_shapes(engine, oracle_mod, n, L):
     assert plain_close(engine.all_vs_all(x, CrmsdOptions(precision="plain64")).values, ref)
 
 
+@pytest.mark.parametrize("L", [420, 560, 700, 900, 1200])
+def test_mid_length_chains(engine, oracle_mod, L):
+    """Chains where the whole chain's level sums no longer fit the exact
+    range: the half layout (every level accumulated per half of the chain,
+    both TMEM buffers, one MMA for several levels) and, beyond its reach, the
+    long layout.  Near-duplicates included; every pair within the tolerance
+    of the oracle and the same matrix from the batched call.  Up to 900 atoms
+    few pairs are recomputed exactly; at 1,200 atoms level 1 no longer fits
+    in halves of the chain, the coarser relaxed grid is chosen, and its
+    quantisation leaves the pairs to the exact recomputation."""
+    rng = np.random.default_rng(L + 7)
+    x = synth.decoys(synth.base_chain(L, rng), 81, rng, near_dup_frac=0.1)
+    got = engine.all_vs_all(x).values.copy()
+    assert engine.metrics()["pairs_plain"] == 0
+    if L <= 900:
+        assert engine.metrics()["pairs_refined"] <= 0.05 * got.size
+    assert np.abs(got - oracle_mod.crmsd_all_vs_all(x)).max() <= TOL_MIXED
+    np.testing.assert_array_equal(engine.batched([x])[0].values, got)
+
+
 @pytest.mark.parametrize("L", [1500, 4096, 16384])
 def test_very_long_chains(engine, oracle_mod, L):
     """Chains up to the limit of 16,384 atoms (the preparation's 32-bit
