@@ -113,7 +113,8 @@ def test_mid_length_chains(engine, oracle_mod, L):
 def test_very_long_chains(engine, oracle_mod, L):
     """Chains up to the limit of 16,384 atoms (the preparation's 32-bit
     digit-norm sums cannot overflow below it).  At 1,500 atoms the mixed path
-    runs in its long layout (levels 1 and 2 accumulated in parts).  Beyond
+    still runs (on a grid coarse enough for its exact levels, with exact
+    recomputation where the certified bound does not fit).  Beyond
     ~3,000 atoms the digit-1 products exceed the exact range even in quarters
     of the chain, no coordinate grid fits, and the set is computed on the
     plain FP64 GPU path instead (metrics: pairs_plain).  A row-ranged call of
