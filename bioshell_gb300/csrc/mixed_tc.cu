@@ -335,6 +335,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!ok) break;
         ptx::tc_fence_after();
         auto acc_col = [&](int ai) -> uint32_t { return tmem + ((p + (uint32_t)(ai >> 2)) & 1u) * 256u + (ai & 3) * 64u; };
+        // the common tiles (normal or half layout, 20 B structures): four
+        // side-by-side MMAs per step into [L0 | L1 | L2 | L3] at c_lo (the
+        // half layout's second half at c_hi), the tile's columns fixed here
+        const bool wide4 = (lay == kAccNormal || lay == kAccHalf) && !tile_narrow(tile);
+        const uint32_t c_lo = acc_col(0), c_hi = acc_col(4);
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
@@ -347,6 +352,33 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t base = ptx::smem_u32(smem + (size_t)s * kStageBytes);
           const uint32_t bbase = base + 4 * kAOpBytes;
           const int ksteps = min(4, nk16 - kc * 4);
+          if (wide4) {
+            // descriptors of the stage's boxes at step 0; a step, a digit
+            // box or the B boxes are whole multiples of 16 bytes further on,
+            // and the 14-bit address field cannot carry (shared addresses
+            // stay below 2^18), so each descriptor is one addition away
+            const uint64_t dA = ptx::smem_desc_sw128(base), dB = ptx::smem_desc_sw128(bbase);
+            constexpr uint64_t kA16 = kAOpBytes >> 4, kB16 = kBOpBytes >> 4;
+            for (int kk = 0; kk < ksteps; ++kk) {
+              const int k = kc * 4 + kk;
+              const uint64_t o = (uint64_t)kk * 2u;  // 32 bytes per 16-atom step
+              const uint64_t da0 = dA + o, da1 = dA + kA16 + o, da2 = dA + 2 * kA16 + o, da3 = dA + 3 * kA16 + o;
+              const uint64_t db0 = dB + o, db1 = dB + kB16 + o, db2 = dB + 2 * kB16 + o;
+              const uint32_t c0 = k >= khalf ? c_hi : c_lo;
+              if (k == 0 || k == khalf) {  // each accumulator's first write overwrites
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
+                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
+              } else {
+                ptx::tc_mma_f16(c0, da0, db0, kIdesc192, 1u);        // L0 += e0e0, L1 += e0e1, L2 += e0e2
+                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 1u);   // L1 += e1e0, L2 += e1e1, L3 += e1e2
+              }
+              ptx::tc_mma_f16(c0 + 128, da2, db0, kIdesc128, 1u);    // L2 += e2e0, L3 += e2e1
+              ptx::tc_mma_f16(c0 + 192, da3, db2, kIdesc, 1u);       // L3 += (e2/512) e2
+            }
+            ptx::tc_commit(&sh->empty[s]);
+            continue;
+          }
           for (int kk = 0; kk < ksteps; ++kk) {
             const int k = kc * 4 + kk;
             const uint32_t off = (uint32_t)kk * 32u;
@@ -369,22 +401,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);        // L0 += e0e0, L1 += e0e1
                 ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);   // L1 += e1e0, L11 += e1e1
               }
-              continue;
-            }
-            if ((lay == kAccNormal || lay == kAccHalf) && !tile_narrow(tile)) {
-              // [L0 | L1 | L2 | L3] in columns c0 .. c0 + 255 (half layout:
-              // of the step's half of the chain, in that half's buffer)
-              const uint32_t c0 = acc_col(k >= khalf ? 4 : 0);
-              if (k == 0 || k == khalf) {
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
-                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
-              } else {
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc192, 1u);        // L0 += e0e0, L1 += e0e1, L2 += e0e2
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 1u);   // L1 += e1e0, L2 += e1e1, L3 += e1e2
-              }
-              ptx::tc_mma_f16(c0 + 128, da2, db0, kIdesc128, 1u);    // L2 += e2e0, L3 += e2e1
-              ptx::tc_mma_f16(c0 + 192, da3, db2, kIdesc, 1u);       // L3 += (e2/512) e2
               continue;
             }
             uint32_t col[4], acc[4];  // per level: accumulator column, accumulate (vs overwrite)
