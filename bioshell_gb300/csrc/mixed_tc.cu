@@ -23,10 +23,11 @@
 //           digit boxes (64 rows x 64 atoms), 128-byte swizzle, 2 stages;
 //           and per tile a bulk copy of its job and per-structure data
 //           (kMetaSlots tiles ahead);
-//   warp 1  MMA issuer (one thread), tcgen05.mma kind::f16, M = 128,
-//           N = 64 to 192: one instruction per A digit covers the adjacent
-//           level accumulators its products go to (4 instructions per
-//           16-atom step instead of 9);
+//   warp 1  MMA issuer: the whole warp runs the loop (its values stay
+//           warp-uniform) and one elected lane issues tcgen05.mma kind::f16,
+//           M = 128, N = 64 to 192: one instruction per A digit covers the
+//           adjacent level accumulators its products go to (4 instructions
+//           per 16-atom step instead of 9);
 //   warp 2  TMEM allocation (512 columns);
 //   warp 3  idle (keeps the epilogue warps on TMEM lane quarters w % 4);
 //   warps 4-11  epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 (10 row
@@ -301,8 +302,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncwarp();
   } else if (warp == 1) {
-    if (lane == 0) {
+    {
       // ------------------------------------------------------- MMA issuer
+      // The whole warp runs the loop, so its values stay warp-uniform; one
+      // elected lane issues the tensor-core instructions and their commits
+      // (a commit tracks the MMAs of the thread that issues it).
+      const bool leader = ptx::elect_one();
       // TMEM buffer slots are used in order: slot p is buffer p & 1 for the
       // (p >> 1)-th time.  A long-layout tile takes two consecutive slots
       // (eight accumulators: accumulator a lives in slot p + a / 4).
@@ -310,7 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t tt = 0; !*abort; ++tt) {
         // the tile's record, as the TMA thread took it from the table
         const uint32_t ms = tt % kMetaSlots;
-        if (!ptx::mbar_wait(&sh->mfull[ms], (tt / kMetaSlots) & 1u, abort, tmo)) {
+        if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->mfull[ms], (tt / kMetaSlots) & 1u, abort, tmo))) {
           fail(sh, a.sc);
           break;
         }
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool ok = true;
         for (uint32_t u = 0; u < need && ok; ++u) {
           const uint32_t q = p + u;
-          if (!ptx::mbar_wait(&sh->tempty[q & 1u], ((q >> 1) & 1u) ^ 1u, abort, tmo)) {
+          if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->tempty[q & 1u], ((q >> 1) & 1u) ^ 1u, abort, tmo))) {
             fail(sh, a.sc);
             ok = false;
           }
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int kc = 0; kc < nchunks; ++kc, ++it) {
           const int s = it % kStages;
           const uint32_t ph = (it / kStages) & 1u;
-          if (!ptx::mbar_wait(&sh->full[s], ph, abort, tmo)) {
+          if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->full[s], ph, abort, tmo))) {
             fail(sh, a.sc);
             ok = false;
             break;
@@ -366,17 +371,17 @@ __global__ void __launch_bounds__(kThreads, 1)
               const uint64_t db0 = dB + o, db1 = dB + kB16 + o, db2 = dB + 2 * kB16 + o;
               const uint32_t c0 = k >= khalf ? c_hi : c_lo;
               if (k == 0 || k == khalf) {  // each accumulator's first write overwrites
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
-                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
+                if (leader) ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
+                if (leader) ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 0u);   // L1 = e1e0, L2 = e1e1, L3 = e1e2
+                if (leader) ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc128, 1u);   // L1 += e0e1, L2 += e0e2
               } else {
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc192, 1u);        // L0 += e0e0, L1 += e0e1, L2 += e0e2
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 1u);   // L1 += e1e0, L2 += e1e1, L3 += e1e2
+                if (leader) ptx::tc_mma_f16(c0, da0, db0, kIdesc192, 1u);        // L0 += e0e0, L1 += e0e1, L2 += e0e2
+                if (leader) ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc192, 1u);   // L1 += e1e0, L2 += e1e1, L3 += e1e2
               }
-              ptx::tc_mma_f16(c0 + 128, da2, db0, kIdesc128, 1u);    // L2 += e2e0, L3 += e2e1
-              ptx::tc_mma_f16(c0 + 192, da3, db2, kIdesc, 1u);       // L3 += (e2/512) e2
+              if (leader) ptx::tc_mma_f16(c0 + 128, da2, db0, kIdesc128, 1u);    // L2 += e2e0, L3 += e2e1
+              if (leader) ptx::tc_mma_f16(c0 + 192, da3, db2, kIdesc, 1u);       // L3 += (e2/512) e2
             }
-            ptx::tc_commit(&sh->empty[s]);
+            if (leader) ptx::tc_commit(&sh->empty[s]);
             continue;
           }
           for (int kk = 0; kk < ksteps; ++kk) {
@@ -394,12 +399,12 @@ __global__ void __launch_bounds__(kThreads, 1)
               // e1e1], the exact covariance of the structures without digit 2
               const uint32_t c0 = acc_col(0);
               if (k == 0) {  // each accumulator's first write overwrites
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);   // L1 = e1e0, L11 = e1e1
-                ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc, 1u);      // L1 += e0e1
+                if (leader) ptx::tc_mma_f16(c0, da0, db0, kIdesc, 0u);           // L0 = e0e0
+                if (leader) ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);   // L1 = e1e0, L11 = e1e1
+                if (leader) ptx::tc_mma_f16(c0 + 64, da0, db1, kIdesc, 1u);      // L1 += e0e1
               } else {
-                ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);        // L0 += e0e0, L1 += e0e1
-                ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);   // L1 += e1e0, L11 += e1e1
+                if (leader) ptx::tc_mma_f16(c0, da0, db0, kIdesc128, 1u);        // L0 += e0e0, L1 += e0e1
+                if (leader) ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);   // L1 += e1e0, L11 += e1e1
               }
               continue;
             }
@@ -421,24 +426,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                 acc[lv] = (k > 0 && acc_index(lay, lv, k - 1, nk16) == ai) ? 1u : 0u;
               }
             }
-            ptx::tc_mma_f16(col[0], da0, db0, idesc, acc[0]);
-            ptx::tc_mma_f16(col[1], da0, db1, idesc, acc[1]);
-            ptx::tc_mma_f16(col[1], da1, db0, idesc, 1u);
-            ptx::tc_mma_f16(col[2], da0, db2, idesc, acc[2]);
-            ptx::tc_mma_f16(col[2], da1, db1, idesc, 1u);
-            ptx::tc_mma_f16(col[2], da2, db0, idesc, 1u);
-            ptx::tc_mma_f16(col[3], da1, db2, idesc, acc[3]);
-            ptx::tc_mma_f16(col[3], da2, db1, idesc, 1u);
-            ptx::tc_mma_f16(col[3], da3, db2, idesc, 1u);
+            if (leader) ptx::tc_mma_f16(col[0], da0, db0, idesc, acc[0]);
+            if (leader) ptx::tc_mma_f16(col[1], da0, db1, idesc, acc[1]);
+            if (leader) ptx::tc_mma_f16(col[1], da1, db0, idesc, 1u);
+            if (leader) ptx::tc_mma_f16(col[2], da0, db2, idesc, acc[2]);
+            if (leader) ptx::tc_mma_f16(col[2], da1, db1, idesc, 1u);
+            if (leader) ptx::tc_mma_f16(col[2], da2, db0, idesc, 1u);
+            if (leader) ptx::tc_mma_f16(col[3], da1, db2, idesc, acc[3]);
+            if (leader) ptx::tc_mma_f16(col[3], da2, db1, idesc, 1u);
+            if (leader) ptx::tc_mma_f16(col[3], da3, db2, idesc, 1u);
           }
-          ptx::tc_commit(&sh->empty[s]);
+          if (leader) ptx::tc_commit(&sh->empty[s]);
         }
         if (!ok) break;
-        for (uint32_t u = 0; u < need; ++u) ptx::tc_commit(&sh->tfull[(p + u) & 1u]);
+        for (uint32_t u = 0; u < need; ++u) if (leader) ptx::tc_commit(&sh->tfull[(p + u) & 1u]);
         p += need;
       }
       // all MMAs of this thread complete before teardown
-      ptx::tc_commit(&sh->drain);
+      if (leader) ptx::tc_commit(&sh->drain);
       volatile int no_abort = 0;
       ptx::mbar_wait(&sh->drain, 0, &no_abort, 1000000000ull);
     }
