@@ -251,8 +251,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncwarp();
   } else if (warp == 1) {
-    if (lane == 0) {
+    {
       // ------------------------------------------------------- MMA issuer
+      // The whole warp runs the loop, so its values stay warp-uniform; one
+      // elected lane issues the tensor-core instructions and their commits
+      // (a commit tracks the MMAs of the thread that issues it).
+      const bool leader = ptx::elect_one();
       uint32_t it = 0, p = 0, ns = 0;
       bool ok = true;
       for (int64_t r = blockIdx.x; r < a.ntiles && ok && !*abort; r += gridDim.x, ++ns) {
@@ -261,12 +265,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         record_shape<S>(rec, nk16, count);
         const int nchunks = (nk16 * 16 + kKChunk - 1) / kKChunk;
         const uint32_t nbuf = nchunks == 1 ? 2u : 1u, buf = ns % nbuf;
-        if (S && !ptx::mbar_wait(&sh->afull[buf], (ns / nbuf) & 1u, abort, kTimeoutNs)) {
+        if (S && !__all_sync(0xffffffffu, ptx::mbar_wait(&sh->afull[buf], (ns / nbuf) & 1u, abort, kTimeoutNs))) {
           fail(sh, a.sc);
           break;
         }
         for (int u = 0; u < count && ok; ++u, ++p) {
-          if (!ptx::mbar_wait(&sh->tempty[p & 1u], ((p >> 1) & 1u) ^ 1u, abort, kTimeoutNs)) {
+          if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->tempty[p & 1u], ((p >> 1) & 1u) ^ 1u, abort, kTimeoutNs))) {
             fail(sh, a.sc);
             ok = false;
             break;
@@ -275,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t c0 = tmem + (p & 1u) * 256u;
           for (int kc = 0; kc < nchunks; ++kc, ++it) {
             const int st = it % kStages;
-            if (!ptx::mbar_wait(&sh->full[st], (it / kStages) & 1u, abort, kTimeoutNs)) {
+            if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sh->full[st], (it / kStages) & 1u, abort, kTimeoutNs))) {
               fail(sh, a.sc);
               ok = false;
               break;
@@ -284,12 +288,17 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t base = ptx::smem_u32(smem + (size_t)st * kStageBytes);
             const uint32_t abase = S ? ptx::smem_u32(abuf + (buf + kc) * 2 * kAOpBytes) : base;
             const int ksteps = min(4, nk16 - kc * 4);
+            // descriptors of the boxes at step 0; a step or a digit box is a
+            // whole multiple of 16 bytes further on, and the 14-bit address
+            // field cannot carry (shared addresses stay below 2^18), so each
+            // descriptor is one addition away
+            const uint64_t dA = ptx::smem_desc_sw128(abase), dB = ptx::smem_desc_sw128(base + F::kBOff);
+            constexpr uint64_t kA16 = kAOpBytes >> 4, kB16 = kBOpBytes >> 4;
             for (int kk = 0; kk < ksteps; ++kk) {
-              const uint32_t off = (uint32_t)kk * 32u;
-              const uint64_t da0 = ptx::smem_desc_sw128(abase + off);
-              const uint64_t da1 = ptx::smem_desc_sw128(abase + kAOpBytes + off);
-              const uint64_t db0 = ptx::smem_desc_sw128(base + F::kBOff + off);
-              const uint64_t db1 = ptx::smem_desc_sw128(base + F::kBOff + kBOpBytes + off);
+              const uint64_t o = (uint64_t)kk * 2u;  // 32 bytes per 16-atom step
+              const uint64_t da0 = dA + o, da1 = dA + kA16 + o;
+              const uint64_t db0 = dB + o, db1 = dB + kB16 + o;
+              if (!leader) continue;
               if (kc == 0 && kk == 0) {  // each accumulator's first write overwrites
                 ptx::tc_mma_f16(c0, da0, db0, kIdesc64, 0u);          // L0 = e0e0
                 ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 0u);    // L1 = e1e0, L11 = e1e1
@@ -299,14 +308,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ptx::tc_mma_f16(c0 + 64, da1, db0, kIdesc128, 1u);    // L1 += e1e0, L11 += e1e1
               }
             }
-            ptx::tc_commit(&sh->empty[st]);
+            if (leader) ptx::tc_commit(&sh->empty[st]);
           }
           if (!ok) break;
-          ptx::tc_commit(&sh->tfull[p & 1u]);
+          if (leader) ptx::tc_commit(&sh->tfull[p & 1u]);
         }
-        if (S) ptx::tc_commit(&sh->aempty[buf]);  // the block's buffer is free once these MMAs complete
+        if (S && leader) ptx::tc_commit(&sh->aempty[buf]);  // the block's buffer is free once these MMAs complete
       }
-      ptx::tc_commit(&sh->drain);
+      if (leader) ptx::tc_commit(&sh->drain);
       volatile int no_abort = 0;
       ptx::mbar_wait(&sh->drain, 0, &no_abort, 1000000000ull);
     }
