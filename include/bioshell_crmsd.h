@@ -49,7 +49,7 @@ extern "C" {
 
 #define BS_API __attribute__((visibility("default")))
 
-#define BS_ABI_VERSION 2
+#define BS_ABI_VERSION 3
 #define BS_OPTS_VERSION 1
 
 typedef int32_t bs_status;

@@ -18,7 +18,7 @@
 use std::os::raw::{c_char, c_void};
 
 // ---------------------------------------------------------------- constants
-pub const BS_ABI_VERSION: i32 = 2;
+pub const BS_ABI_VERSION: i32 = 3;
 pub const BS_OPTS_VERSION: i32 = 1;
 
 pub type BsStatus = i32;

@@ -36,7 +36,7 @@ def test_ctypes_signatures_cover_header():
 
 
 def test_abi_version_and_status_strings(enginelib):
-    assert enginelib.bs_abi_version() == 2
+    assert enginelib.bs_abi_version() == 3
     assert enginelib.bs_status_string(0) == b"ok"
     assert enginelib.bs_status_string(8).startswith(b"no usable")
     assert enginelib.bs_status_string(1234) == b"unknown status"
