@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // (a commit tracks the MMAs of the thread that issues it).
       const bool leader = ptx::elect_one();
       // TMEM buffer slots are used in order: slot p is buffer p & 1 for the
-      // (p >> 1)-th time.  A long-layout tile takes two consecutive slots
-      // (eight accumulators: accumulator a lives in slot p + a / 4).
+      // (p >> 1)-th time.  A long- or half-layout tile takes two consecutive
+      // slots (eight accumulators: accumulator a lives in slot p + a / 4).
       uint32_t it = 0, p = 0;
       for (uint32_t tt = 0; !*abort; ++tt) {
         // the tile's record, as the TMA thread took it from the table
