@@ -566,8 +566,8 @@ def run_serving(a):
                  "cluster_p50_ms": st["cluster_p50_ms"], "cluster_p99_ms": st["cluster_p99_ms"],
                  "submit_lag_p99_ms": float(np.percentile(lag, 99)) if lag else None, "submit_s": submit_s,
                  "pairs_screened_per_pair": st["pairs_screened"] / max(st["pairs"], 1)}
-    # the benchmark spec's latency target is quoted for 64-structure queries: the
-    # same Poisson load with every query exactly 64 structures
+    # the serving latency target is quoted for 64-structure queries: the same
+    # Poisson load with every query exactly 64 structures
     st64, _, _, n64 = _open_loop(srv, pools, shares, rate, min(T, 2.0), rng, q_fixed=64)
     open_loop_q64 = {"offered_req_per_s": rate, "seconds": min(T, 2.0), "requests": n64, "q": 64,
                      "p50_ms": st64["p50_ms"], "p99_ms": st64["p99_ms"], "max_ms": st64["max_ms"],

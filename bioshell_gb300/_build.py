@@ -4,7 +4,7 @@ Every ``csrc/*.cu`` translation unit is compiled in parallel with
 ``-gencode arch=compute_103a,code=sm_103a`` (host-only ``csrc/*.cpp`` with the
 host compiler, no FMA contraction) and linked into
 ``bioshell_gb300/lib/libbioshell_crmsd.so`` (CUDA runtime linked
-statically; the driver's tensor-map encoder is resolved at run time, so no
+statically; the CUDA driver's tensor-map encoder is resolved at run time, so no
 libcuda is needed at link time).
 """
 from __future__ import annotations

@@ -93,7 +93,7 @@ std::string get_encoder(PFN_cuTensorMapEncodeTiled_v12000 *out) {
   if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
       q != cudaDriverEntryPointSuccess || !fn) {
     cudaGetLastError();
-    return "cuTensorMapEncodeTiled unavailable in the driver";
+    return "cuTensorMapEncodeTiled unavailable in the CUDA driver";
   }
   *out = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   return "";
