@@ -67,9 +67,12 @@ constexpr int kThreads = 384;
 constexpr int kEpiWarp0 = 4;
 constexpr int kEpiWarps = 8;
 constexpr int kTmemCols = 512;                           // 2 buffers x 4 levels x 64 columns
-// Epilogue staging per warp: two buffers of 32 rows x 16 columns (pitch 17
-// floats), or for screen tiles one area of 32 rows x 32 columns (pitch 33).
-constexpr int kPitch = 17;
+// Epilogue staging per warp: two buffers of 32 rows x 16 columns, or for
+// screen tiles one area of 32 rows x 32 columns (pitch 33).  Pitch 19: a
+// lane's pair reads rows 3 il + [il >= 5] + xr at columns 3 x + c, and with
+// 19 floats per row the 30 (il, x) of a warp fall in 30 different banks (17
+// made 3-way conflicts); the per-lane row writes stay conflict-free (odd).
+constexpr int kPitch = 19;
 constexpr int kPitchWide = 33;
 constexpr int kEpiStageFloats = 2 * 32 * kPitch;
 static_assert(32 * kPitchWide <= kEpiStageFloats, "screen staging exceeds the warp's area");
